@@ -1,0 +1,219 @@
+"""Python mirror of the reference's operator interface over the C ABI.
+
+`Maps` and `aMatFree` keep the names, argument meaning and call order of
+par::Maps (include/maps.hpp:279-302) and par::aMatFree / par::aMat
+(include/aMat.hpp:75-242, include/aMatFree.hpp:113-238), with numpy arrays in
+place of jagged C arrays and PETSc Vecs. Every call goes through libafm.so
+(include/afm.h); the product runs on the GB300 only.
+"""
+import ctypes as C
+import enum
+
+import numpy as np
+
+from ._native import AfmInfo, AfmSolveStats, check, libafm
+
+
+class BC_METH(enum.IntEnum):
+    """par::BC_METH (include/enums.hpp:20-21)"""
+    BC_IMATRIX = 0
+    BC_PENALTY = 1
+
+
+class MATFREE_TYPE(enum.IntEnum):
+    """par::MATFREE_TYPE (include/enums.hpp:56); 1 and 3 run the stored-Ke device operator."""
+    QUASI_FREE = 1
+    GPU_PURE = 3
+
+
+class PRECISION(enum.IntEnum):
+    FP64 = 0
+    FP64_SPLIT = 1
+    FP32 = 2
+    AUTO = 3
+
+
+class CG_NORM(enum.IntEnum):
+    UNPRECONDITIONED = 0
+    PRECONDITIONED = 1
+
+
+def _ptr(a):
+    return C.c_void_p(a.ctypes.data) if a is not None else None
+
+
+class Maps:
+    """par::Maps for one rank: element -> DoF map and boundary conditions."""
+
+    def __init__(self, comm=None):
+        self._map = None
+        self._bdr = None
+
+    def set_map(self, n_elements_on_rank, element_to_rank_map, dofs_per_element, n_all_dofs_on_rank,
+                rank_to_global_map=None, owned_global_dof_range_begin=0, owned_global_dof_range_end=None,
+                n_global_dofs=None):
+        """Maps::set_map (include/maps.hpp:279-286, 399-451).
+
+        element_to_rank_map: (n_elem, n) array, or a flat array with
+        dofs_per_element an array of per-element counts. owned range end is
+        inclusive, as in the reference.
+        """
+        n_global = int(n_global_dofs if n_global_dofs is not None else n_all_dofs_on_rank)
+        end = int(owned_global_dof_range_end if owned_global_dof_range_end is not None else n_global - 1)
+        m = np.ascontiguousarray(element_to_rank_map, dtype=np.uint32).reshape(-1)
+        dpe = np.asarray(dofs_per_element)
+        if dpe.ndim == 0:
+            offsets = None
+            n_uniform = int(dpe)
+        else:
+            dpe = dpe.astype(np.uint32)
+            offsets = np.zeros(len(dpe) + 1, dtype=np.uint32)
+            np.cumsum(dpe, out=offsets[1:])
+            n_uniform = 0
+            if np.all(dpe == dpe[0]):
+                offsets, n_uniform = None, int(dpe[0])
+        l2g = None if rank_to_global_map is None else np.ascontiguousarray(rank_to_global_map, dtype=np.uint64)
+        self._map = dict(n_elem=int(n_elements_on_rank), offsets=offsets, n_uniform=n_uniform, map=m,
+                         n_all=int(n_all_dofs_on_rank), l2g=l2g, begin=int(owned_global_dof_range_begin), end=end,
+                         n_global=n_global)
+
+    def set_bdr_map(self, constrained_dofs, prescribed_values, num_constraints=None):
+        """Maps::set_bdr_map (include/maps.hpp:829-880)."""
+        c = np.ascontiguousarray(constrained_dofs, dtype=np.uint64).reshape(-1)
+        v = np.ascontiguousarray(prescribed_values, dtype=np.float64).reshape(-1)
+        n = len(c) if num_constraints is None else int(num_constraints)
+        self._bdr = (c[:n].copy(), v[:n].copy())
+
+    @property
+    def n_dofs(self):
+        return self._map["n_global"]
+
+
+class aMatFree:
+    """par::aMatFree on one GB300: stored element matrices, device matvec."""
+
+    def __init__(self, maps, bc_method=BC_METH.BC_IMATRIX, device=-1):
+        lib = libafm()
+        h = C.c_void_p()
+        check(lib.afm_create(C.byref(h), int(bc_method), int(device)), "afm_create")
+        self._h = h
+        self._lib = lib
+        self.maps = maps
+        self.bc_method = BC_METH(bc_method)
+        mp = maps._map
+        if mp is None:
+            raise ValueError("Maps.set_map has not been called")
+        check(lib.afm_set_map(h, mp["n_elem"], _ptr(mp["offsets"]), mp["n_uniform"], _ptr(mp["map"]), mp["n_all"],
+                              _ptr(mp["l2g"]), mp["begin"], mp["end"], mp["n_global"]), "afm_set_map")
+        if maps._bdr is not None:
+            c, v = maps._bdr
+            check(lib.afm_set_bdr_map(h, _ptr(c), _ptr(v), len(c)), "afm_set_bdr_map")
+        self.n_dofs = mp["n_global"]
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.afm_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- set-up ----------------------------------------------------------
+    def set_matfree_type(self, t):
+        check(self._lib.afm_set_matfree_type(self._h, int(t)), "afm_set_matfree_type")
+
+    def set_precision(self, p):
+        check(self._lib.afm_set_precision(self._h, int(p)), "afm_set_precision")
+
+    def set_element_matrix(self, eid, e_mat, block_i=0, block_j=0, blocks_dim=1):
+        """aMatFree::set_element_matrix (include/aMatFree.hpp:856-880)."""
+        k = np.ascontiguousarray(e_mat, dtype=np.float64)
+        check(self._lib.afm_set_element_matrix(self._h, int(eid), _ptr(k), int(block_i), int(block_j),
+                                               int(blocks_dim)), "afm_set_element_matrix")
+
+    def set_element_matrices(self, first_eid, ke):
+        k = np.ascontiguousarray(ke, dtype=np.float64)
+        count = k.shape[0] if k.ndim == 3 else None
+        if count is None:
+            raise ValueError("ke must be (count, n, n)")
+        check(self._lib.afm_set_element_matrices(self._h, int(first_eid), count, _ptr(k)),
+              "afm_set_element_matrices")
+
+    def finalize(self):
+        check(self._lib.afm_finalize(self._h), "afm_finalize")
+
+    # ---- operator --------------------------------------------------------
+    def matvec(self, v, u, isGhosted=True):
+        """aMatFree::matvec(v, u, isGhosted): v = K u on host arrays."""
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        assert v.dtype == np.float64 and v.flags.c_contiguous
+        check(self._lib.afm_matvec(self._h, _ptr(v), _ptr(u), int(bool(isGhosted))), "afm_matvec")
+        return v
+
+    def matmult_bc(self, v, u):
+        """MatMult_mf (include/aMatFree.hpp:3894-3941)."""
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        check(self._lib.afm_matmult_bc(self._h, _ptr(v), _ptr(u)), "afm_matmult_bc")
+        return v
+
+    def matvec_device(self, v_ptr, u_ptr, stream=None):
+        check(self._lib.afm_matvec_device(self._h, C.c_void_p(v_ptr), C.c_void_p(u_ptr),
+                                          C.c_void_p(stream) if stream else None), "afm_matvec_device")
+
+    def matvec_device_f32(self, v_ptr, u_ptr, stream=None):
+        check(self._lib.afm_matvec_device_f32(self._h, C.c_void_p(v_ptr), C.c_void_p(u_ptr),
+                                              C.c_void_p(stream) if stream else None), "afm_matvec_device_f32")
+
+    def matmult_bc_device(self, v_ptr, u_ptr, stream=None):
+        check(self._lib.afm_matmult_bc_device(self._h, C.c_void_p(v_ptr), C.c_void_p(u_ptr),
+                                              C.c_void_p(stream) if stream else None), "afm_matmult_bc_device")
+
+    def get_diagonal(self):
+        """MatGetDiagonal_mf with apply_bc_diagonal (include/aMatFree.hpp:3945-3975, 4310-4338)."""
+        d = np.empty(self.n_dofs, dtype=np.float64)
+        check(self._lib.afm_get_diagonal(self._h, _ptr(d)), "afm_get_diagonal")
+        return d
+
+    def apply_bc(self, rhs):
+        """aMatFree::apply_bc (include/aMatFree.hpp:957-969): rhs updated in place."""
+        assert rhs.dtype == np.float64 and rhs.flags.c_contiguous
+        check(self._lib.afm_apply_bc_rhs(self._h, _ptr(rhs)), "afm_apply_bc_rhs")
+        return rhs
+
+    def get_trace(self):
+        t = C.c_double()
+        check(self._lib.afm_get_trace(self._h, C.byref(t)), "afm_get_trace")
+        return t.value
+
+    def solve(self, rhs, x=None, rtol=1e-12, atol=1e-12, maxit=10000, norm=CG_NORM.UNPRECONDITIONED,
+              raise_on_fail=True):
+        """par::solve (examples/include/solve.hpp:75-127): Jacobi PCG on the MatMult_mf operator."""
+        b = np.ascontiguousarray(rhs, dtype=np.float64)
+        x = np.zeros(self.n_dofs) if x is None else np.ascontiguousarray(x, dtype=np.float64).copy()
+        st = AfmSolveStats()
+        s = self._lib.afm_solve_cg(self._h, _ptr(b), _ptr(x), float(rtol), float(atol), int(maxit), int(norm),
+                                   C.byref(st))
+        if raise_on_fail:
+            check(s, "afm_solve_cg")
+        return x, st
+
+    def info(self):
+        i = AfmInfo()
+        check(self._lib.afm_get_info(self._h, C.byref(i)), "afm_get_info")
+        return {f: getattr(i, f) for f, _ in AfmInfo._fields_}
+
+    def colors(self):
+        c = np.empty(self.info()["n_elements"], dtype=np.uint32)
+        check(self._lib.afm_get_colors(self._h, _ptr(c)), "afm_get_colors")
+        return c
+
+    def stream(self):
+        s = C.c_void_p()
+        check(self._lib.afm_get_stream(self._h, C.byref(s)), "afm_get_stream")
+        return s.value
+
+    def synchronize(self):
+        check(self._lib.afm_synchronize(self._h), "afm_synchronize")

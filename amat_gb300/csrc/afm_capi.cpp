@@ -1,0 +1,897 @@
+// Host runtime of the GB300 AFM operator: the C ABI of include/afm.h.
+//
+// Set-up mirrors par::Maps / par::aMatFree on one rank; finalize colours the
+// elements (the reference's greedy first-fit, include/meshGraph.hpp:59-193),
+// sorts them by (colour, n, element id), lays the DoF map and element
+// matrices out for the device kernels and uploads them once. Every matvec is
+// then one launch per (colour, n) segment, in colour order, on the operator's
+// stream: no host round trip, no atomics.
+#include <cuda_runtime.h>
+#include <stdarg.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "afm_internal.hpp"
+#include "afm_solver.hpp"
+
+namespace afm {
+cudaError_t launch_segment_fp64(const Segment& s, const SegArgs& a, int sm_count, bool dup, cudaStream_t st);
+cudaError_t launch_segment_split(const Segment& s, const SegArgs& a, int sm_count, bool dup, cudaStream_t st);
+cudaError_t launch_segment_fp32(const Segment& s, const SegArgs& a, int sm_count, bool dup, cudaStream_t st);
+size_t segment_smem_fp64(const Segment& s);
+size_t segment_smem_split(const Segment& s);
+size_t segment_smem_fp32(const Segment& s);
+
+cudaError_t launch_segment(const Segment& s, int prec, const SegArgs& a, int sm_count, bool dup,
+                           cudaStream_t stream) {
+    switch (prec) {
+        case AFM_PREC_FP64: return launch_segment_fp64(s, a, sm_count, dup, stream);
+        case AFM_PREC_FP64_SPLIT: return launch_segment_split(s, a, sm_count, dup, stream);
+        default: return launch_segment_fp32(s, a, sm_count, dup, stream);
+    }
+}
+
+size_t segment_smem_bytes(const Segment& s, int prec) {
+    switch (prec) {
+        case AFM_PREC_FP64: return segment_smem_fp64(s);
+        case AFM_PREC_FP64_SPLIT: return segment_smem_split(s);
+        default: return segment_smem_fp32(s);
+    }
+}
+}  // namespace afm
+
+using namespace afm;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int status, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return status;
+}
+
+int ok() {
+    g_last_error.clear();
+    return AFM_SUCCESS;
+}
+
+#define AFM_CUDA(call)                                                                                    \
+    do {                                                                                                  \
+        cudaError_t e_ = (call);                                                                          \
+        if (e_ != cudaSuccess)                                                                            \
+            return fail(e_ == cudaErrorMemoryAllocation ? AFM_ERR_OOM : AFM_ERR_CUDA, "%s: %s (%s:%d)", #call, \
+                        cudaGetErrorString(e_), __FILE__, __LINE__);                                      \
+    } while (0)
+
+#define AFM_CHECK_OP(op)                                                                    \
+    do {                                                                                    \
+        if (!(op)) return fail(AFM_ERR_INVALID_ARG, "null operator");                       \
+    } while (0)
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        cudaGetDevice(&prev);
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        cudaGetDevice(&cur);
+        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+size_t entry_bytes(int prec) { return prec == AFM_PREC_FP32 ? 4 : 8; }
+
+uint64_t round16(uint64_t b) { return (b + 15) / 16 * 16; }
+
+void free_device(afm_operator* op) {
+    cudaFree(op->d_ke);
+    cudaFree(op->d_map);
+    cudaFree(op->d_diag);
+    cudaFree(op->d_bc_idx);
+    cudaFree(op->d_bc_val);
+    cudaFree(op->d_work);
+    cudaFree(op->d_work32);
+    op->d_ke = nullptr;
+    op->d_map = nullptr;
+    op->d_diag = nullptr;
+    op->d_bc_idx = nullptr;
+    op->d_bc_val = nullptr;
+    op->d_work = nullptr;
+    op->d_work32 = nullptr;
+    op->work_elems = 0;
+    op->work32_elems = 0;
+}
+
+// Greedy first-fit colouring in element order (include/meshGraph.hpp:59-109)
+// of the graph "elements sharing a DoF" (mesh2Graph, 132-155). Integer work,
+// identical result to the reference for the same map.
+uint32_t color_elements(uint32_t n_dofs, uint32_t n_elem, const std::vector<uint32_t>& offs,
+                        const std::vector<uint32_t>& map, std::vector<uint32_t>& colors) {
+    std::vector<uint32_t> cnt((size_t)n_dofs + 1, 0);
+    for (uint32_t e = 0; e < n_elem; e++)
+        for (uint32_t k = offs[e]; k < offs[e + 1]; k++) cnt[map[k] + 1]++;
+    for (uint32_t d = 0; d < n_dofs; d++) cnt[d + 1] += cnt[d];
+    std::vector<uint32_t> fill(cnt.begin(), cnt.end() - 1);
+    std::vector<uint32_t> d2e(offs[n_elem]);
+    for (uint32_t e = 0; e < n_elem; e++)
+        for (uint32_t k = offs[e]; k < offs[e + 1]; k++) d2e[fill[map[k]]++] = e;
+    colors.assign(n_elem, UINT32_MAX);
+    std::vector<uint32_t> used(64, 0);
+    uint32_t ncol = n_elem ? 1 : 0;
+    for (uint32_t e = 0; e < n_elem; e++) {
+        for (uint32_t k = offs[e]; k < offs[e + 1]; k++) {
+            const uint32_t d = map[k];
+            for (uint32_t j = cnt[d]; j < cnt[d + 1]; j++) {
+                const uint32_t f = d2e[j];
+                if (f != e && colors[f] != UINT32_MAX) {
+                    if (colors[f] >= used.size()) used.resize(colors[f] * 2 + 2, 0);
+                    used[colors[f]] = e + 1;
+                }
+            }
+        }
+        uint32_t c = 0;
+        while (c < used.size() && used[c] == e + 1) c++;
+        if (c >= used.size()) used.resize(c * 2 + 2, 0);
+        colors[e] = c;
+        if (c + 1 > ncol) ncol = c + 1;
+    }
+    return ncol;
+}
+
+template <typename KT>
+inline void put_entry(unsigned char* base, size_t idx, double x);
+template <>
+inline void put_entry<double>(unsigned char* base, size_t idx, double x) {
+    reinterpret_cast<double*>(base)[idx] = x;
+}
+template <>
+inline void put_entry<float>(unsigned char* base, size_t idx, double x) {
+    reinterpret_cast<float*>(base)[idx] = (float)x;
+}
+struct SplitPair { float hi, lo; };
+template <>
+inline void put_entry<SplitPair>(unsigned char* base, size_t idx, double x) {
+    const float h = (float)x;
+    const float l = (float)(x - (double)h);
+    reinterpret_cast<SplitPair*>(base)[idx] = {h, l};
+}
+
+// Writes element e (at offset `rel` inside segment s) into the host image of
+// the segment's arena chunk starting at chunk_base (unit index u0).
+template <typename KT>
+void layout_element(const afm_operator* op, const Segment& s, uint32_t e, uint64_t rel, uint64_t u0,
+                    unsigned char* chunk) {
+    const uint32_t n = s.n;
+    const double* k = op->ke.data() + op->kofs[e];
+    if (s.regime == REG_WPE) {
+        unsigned char* dst = chunk + (rel - u0) * s.unit_bytes;
+        for (uint32_t c = 0; c < n; c++)
+            for (uint32_t r = 0; r < n; r++) put_entry<KT>(dst, (size_t)c * n + r, k[(size_t)r * n + c]);
+    } else {
+        const uint64_t unit = rel / kTpeWidth, lane = rel % kTpeWidth;
+        unsigned char* dst = chunk + (unit - u0) * s.unit_bytes;
+        for (uint32_t r = 0; r < n; r++)
+            for (uint32_t c = 0; c < n; c++)
+                put_entry<KT>(dst, ((size_t)r * n + c) * kTpeWidth + lane, k[(size_t)r * n + c]);
+    }
+}
+
+int upload_arena(afm_operator* op) {
+    // staging in pinned memory, chunks of ~256 MB of whole units
+    const size_t kChunk = 256ull << 20;
+    unsigned char* stage = nullptr;
+    AFM_CUDA(cudaMallocHost((void**)&stage, kChunk));
+    int status = AFM_SUCCESS;
+    for (const Segment& s : op->segs) {
+        if (s.units == 0) continue;
+        const uint64_t units_per_chunk = std::max<uint64_t>(1, kChunk / s.unit_bytes);
+        if (s.unit_bytes > kChunk) {
+            status = fail(AFM_ERR_INVALID_ARG, "element matrix larger than staging chunk");
+            break;
+        }
+        for (uint64_t u0 = 0; u0 < s.units; u0 += units_per_chunk) {
+            const uint64_t u1 = std::min<uint64_t>(s.units, u0 + units_per_chunk);
+            const size_t bytes = (size_t)((u1 - u0) * s.unit_bytes);
+            // the previous chunk's copy must finish before the buffer is reused
+            cudaError_t e = cudaStreamSynchronize(op->stream);
+            if (e != cudaSuccess) {
+                status = fail(AFM_ERR_CUDA, "upload: %s", cudaGetErrorString(e));
+                break;
+            }
+            memset(stage, 0, bytes);
+            const uint64_t el0 = (s.regime == REG_WPE) ? u0 : u0 * kTpeWidth;
+            const uint64_t el1 = std::min<uint64_t>(s.count, (s.regime == REG_WPE) ? u1 : u1 * kTpeWidth);
+#pragma omp parallel for schedule(static)
+            for (int64_t rel = (int64_t)el0; rel < (int64_t)el1; rel++) {
+                const uint32_t e = op->perm[s.first_pos + rel];
+                if (op->precision == AFM_PREC_FP64)
+                    layout_element<double>(op, s, e, rel, u0, stage);
+                else if (op->precision == AFM_PREC_FP64_SPLIT)
+                    layout_element<SplitPair>(op, s, e, rel, u0, stage);
+                else
+                    layout_element<float>(op, s, e, rel, u0, stage);
+            }
+            e = cudaMemcpyAsync(op->d_ke + s.ke_offset + u0 * s.unit_bytes, stage, bytes, cudaMemcpyHostToDevice,
+                                op->stream);
+            if (e != cudaSuccess) {
+                status = fail(AFM_ERR_CUDA, "upload: %s", cudaGetErrorString(e));
+                break;
+            }
+        }
+        if (status != AFM_SUCCESS) break;
+    }
+    cudaStreamSynchronize(op->stream);
+    cudaFreeHost(stage);
+    return status;
+}
+
+int ensure_work(afm_operator* op, size_t vectors) {
+    const size_t need = vectors * (size_t)std::max<uint32_t>(op->n_dofs, 1);
+    if (op->work_elems >= need) return AFM_SUCCESS;
+    cudaFree(op->d_work);
+    op->d_work = nullptr;
+    op->work_elems = 0;
+    AFM_CUDA(cudaMalloc((void**)&op->d_work, need * sizeof(double)));
+    op->work_elems = need;
+    return AFM_SUCCESS;
+}
+
+int check_device_error(afm_operator* op) {
+    int h = 0;
+    AFM_CUDA(cudaMemcpyAsync(&h, op->d_err, sizeof(int), cudaMemcpyDeviceToHost, op->stream));
+    AFM_CUDA(cudaStreamSynchronize(op->stream));
+    if (h & kErrTimeout) {
+        cudaMemsetAsync(op->d_err, 0, sizeof(int), op->stream);
+        return fail(AFM_ERR_TIMEOUT, "a device wait exceeded its time limit");
+    }
+    return AFM_SUCCESS;
+}
+
+// v = K u (bc_mode 0) or the product of MatMult_mf without the final v_c = u_c
+// (bc_mode 1: constrained columns of u read as zero), device arrays.
+int enqueue_matvec(afm_operator* op, void* d_v, const void* d_u, int bc_mode, cudaStream_t st) {
+    const size_t vbytes = (size_t)op->n_dofs * (op->precision == AFM_PREC_FP32 ? 4 : 8);
+    AFM_CUDA(cudaMemsetAsync(d_v, 0, vbytes, st));
+    for (const Segment& s : op->segs) {
+        if (s.units == 0) continue;
+        SegArgs a;
+        a.ke = op->d_ke + s.ke_offset;
+        a.map = op->d_map + s.map_offset;
+        a.u = d_u;
+        a.v = d_v;
+        a.units = s.units;
+        a.count = s.count;
+        a.unit_bytes = s.unit_bytes;
+        a.bc_mode = bc_mode;
+        a.err = op->d_err;
+        AFM_CUDA(launch_segment(s, op->precision, a, op->sm_count, op->dup_in_element, st));
+    }
+    return AFM_SUCCESS;
+}
+
+cudaStream_t pick_stream(afm_operator* op, void* stream) {
+    return stream ? (cudaStream_t)stream : op->stream;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* afm_last_error(void) { return g_last_error.c_str(); }
+
+const char* afm_status_string(int s) {
+    switch (s) {
+        case AFM_SUCCESS: return "SUCCESS";
+        case AFM_INDEX_OUT_OF_BOUNDS: return "INDEX_OUT_OF_BOUNDS";
+        case AFM_UNKNOWN_ELEMENT_TYPE: return "UNKNOWN_ELEMENT_TYPE";
+        case AFM_UNKNOWN_ELEMENT_STATUS: return "UNKNOWN_ELEMENT_STATUS";
+        case AFM_NULL_L2G_MAP: return "NULL_L2G_MAP";
+        case AFM_GHOST_NODE_NOT_FOUND: return "GHOST_NODE_NOT_FOUND";
+        case AFM_UNKNOWN_MAT_TYPE: return "UNKNOWN_MAT_TYPE";
+        case AFM_WRONG_COMMUNICATION: return "WRONG_COMMUNICATION";
+        case AFM_UNKNOWN_DOF_TYPE: return "UNKNOWN_DOF_TYPE";
+        case AFM_UNKNOWN_CONSTRAINT: return "UNKNOWN_CONSTRAINT";
+        case AFM_UNKNOWN_BC_METH: return "UNKNOWN_BC_METH";
+        case AFM_NOT_IMPLEMENTED: return "NOT_IMPLEMENTED";
+        case AFM_GLOBAL_DOF_ID_NOT_FOUND: return "GLOBAL_DOF_ID_NOT_FOUND";
+        case AFM_ERR_CUDA: return "ERR_CUDA";
+        case AFM_ERR_OOM: return "ERR_OOM";
+        case AFM_ERR_TIMEOUT: return "ERR_TIMEOUT";
+        case AFM_ERR_BREAKDOWN: return "ERR_BREAKDOWN";
+        case AFM_ERR_STATE: return "ERR_STATE";
+        case AFM_ERR_INVALID_ARG: return "ERR_INVALID_ARG";
+        case AFM_ERR_MAXIT: return "ERR_MAXIT";
+        default: return "UNKNOWN_STATUS";
+    }
+}
+
+int afm_create(afm_operator** out, int bc_method, int device) {
+    if (!out) return fail(AFM_ERR_INVALID_ARG, "out is null");
+    *out = nullptr;
+    if (bc_method != AFM_BC_IMATRIX && bc_method != AFM_BC_PENALTY)
+        return fail(AFM_UNKNOWN_BC_METH, "unknown BC method %d", bc_method);
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0)
+        return fail(AFM_ERR_CUDA, "no CUDA device: %s", e != cudaSuccess ? cudaGetErrorString(e) : "count 0");
+    if (device < 0) AFM_CUDA(cudaGetDevice(&device));
+    if (device >= ndev) return fail(AFM_ERR_INVALID_ARG, "device %d of %d", device, ndev);
+    cudaDeviceProp prop;
+    AFM_CUDA(cudaGetDeviceProperties(&prop, device));
+    if (!(prop.major == 10 && prop.minor == 3))
+        return fail(AFM_ERR_CUDA, "device %d is sm_%d%d; this library is built for sm_103a only", device,
+                    prop.major, prop.minor);
+    DeviceGuard g(device);
+    auto* op = new afm_operator();
+    op->device = device;
+    op->bc_method = bc_method;
+    op->sm_count = prop.multiProcessorCount;
+    if (cudaStreamCreateWithFlags(&op->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMalloc((void**)&op->d_err, sizeof(int)) != cudaSuccess ||
+        cudaMalloc((void**)&op->d_scalars, sizeof(double) * (kScalarSlots + kPartialSlots)) != cudaSuccess ||
+        cudaMallocHost((void**)&op->h_scalars, sizeof(double) * kScalarSlots) != cudaSuccess) {
+        afm_destroy(op);
+        return fail(AFM_ERR_CUDA, "afm_create: stream or buffer allocation failed");
+    }
+    cudaMemsetAsync(op->d_err, 0, sizeof(int), op->stream);
+    cudaStreamSynchronize(op->stream);
+    *out = op;
+    return ok();
+}
+
+int afm_destroy(afm_operator* op) {
+    if (!op) return ok();
+    {
+        DeviceGuard g(op->device);
+        if (op->stream) cudaStreamSynchronize(op->stream);
+        free_device(op);
+        cudaFree(op->d_err);
+        cudaFree(op->d_scalars);
+        if (op->h_scalars) cudaFreeHost(op->h_scalars);
+        if (op->stream) cudaStreamDestroy(op->stream);
+    }
+    delete op;
+    return ok();
+}
+
+int afm_set_matfree_type(afm_operator* op, int t) {
+    AFM_CHECK_OP(op);
+    if (t != 1 && t != 3) return fail(AFM_UNKNOWN_MAT_TYPE, "MATFREE_TYPE %d not provided (1 or 3)", t);
+    op->matfree_type = t;
+    return ok();
+}
+
+int afm_set_precision(afm_operator* op, int p) {
+    AFM_CHECK_OP(op);
+    if (p < AFM_PREC_FP64 || p > AFM_PREC_AUTO) return fail(AFM_ERR_INVALID_ARG, "precision %d", p);
+    op->precision_req = p;
+    op->finalized = false;
+    return ok();
+}
+
+int afm_set_map(afm_operator* op, uint32_t n_elements, const uint32_t* dof_offsets, uint32_t dofs_per_element,
+                const uint32_t* e2r, uint32_t n_all_dofs, const uint64_t* r2g, uint64_t owned_begin,
+                uint64_t owned_end, uint64_t n_global) {
+    AFM_CHECK_OP(op);
+    if (n_elements > 0 && !e2r) return fail(AFM_ERR_INVALID_ARG, "element_to_rank_map is null");
+    if (n_global == 0 || n_global > kDofMask) return fail(AFM_ERR_INVALID_ARG, "n_global_dofs %llu", (unsigned long long)n_global);
+    // one rank owns [0, n_global-1]; the reference's m_uiNumDofs = end - begin + 1 (include/maps.hpp:413)
+    if (owned_begin != 0 || owned_end + 1 != n_global || n_all_dofs != n_global)
+        return fail(AFM_WRONG_COMMUNICATION, "maps need ghost exchange: owned [%llu, %llu], %u local of %llu global",
+                    (unsigned long long)owned_begin, (unsigned long long)owned_end, n_all_dofs,
+                    (unsigned long long)n_global);
+    std::vector<uint32_t> offs((size_t)n_elements + 1, 0);
+    for (uint32_t e = 0; e < n_elements; e++) {
+        const uint32_t n = dof_offsets ? dof_offsets[e + 1] - dof_offsets[e] : dofs_per_element;
+        if (dof_offsets && dof_offsets[e + 1] < dof_offsets[e])
+            return fail(AFM_ERR_INVALID_ARG, "dof_offsets not monotone at element %u", e);
+        if (n == 0 || n > kMaxN) return fail(AFM_NOT_IMPLEMENTED, "element %u has %u DoFs (1..%u supported)", e, n, kMaxN);
+        if ((uint64_t)offs[e] + n > 0xffffffffull) return fail(AFM_ERR_INVALID_ARG, "map too large");
+        offs[e + 1] = offs[e] + n;
+    }
+    const uint32_t base = dof_offsets ? dof_offsets[0] : 0;
+    std::vector<uint32_t> map(offs[n_elements]);
+    for (uint32_t k = 0; k < offs[n_elements]; k++) {
+        const uint32_t l = e2r[base + k];
+        if (l >= n_all_dofs) return fail(AFM_INDEX_OUT_OF_BOUNDS, "local DoF %u >= %u", l, n_all_dofs);
+        const uint64_t gid = r2g ? r2g[l] : l;
+        if (gid >= n_global) return fail(AFM_GLOBAL_DOF_ID_NOT_FOUND, "global DoF %llu >= %llu", (unsigned long long)gid, (unsigned long long)n_global);
+        map[k] = (uint32_t)gid;
+    }
+    op->n_elem = n_elements;
+    op->n_dofs = (uint32_t)n_global;
+    op->offsets.swap(offs);
+    op->map.swap(map);
+    op->nmax = 0;
+    op->dup_in_element = false;
+    op->kofs.assign((size_t)n_elements + 1, 0);
+    std::vector<uint32_t> tmp;
+    for (uint32_t e = 0; e < n_elements; e++) {
+        const uint32_t n = op->offsets[e + 1] - op->offsets[e];
+        op->nmax = std::max(op->nmax, n);
+        op->kofs[e + 1] = op->kofs[e] + (uint64_t)n * n;
+        tmp.assign(op->map.begin() + op->offsets[e], op->map.begin() + op->offsets[e + 1]);
+        std::sort(tmp.begin(), tmp.end());
+        if (std::adjacent_find(tmp.begin(), tmp.end()) != tmp.end()) op->dup_in_element = true;
+    }
+    try {
+        op->ke.assign(op->kofs[n_elements], 0.0);
+    } catch (...) {
+        return fail(AFM_ERR_OOM, "host element-matrix store of %llu entries", (unsigned long long)op->kofs[n_elements]);
+    }
+    op->have_map = true;
+    op->finalized = false;
+    op->ke_dirty = true;
+    return ok();
+}
+
+int afm_set_bdr_map(afm_operator* op, const uint64_t* constrained, const double* values, uint32_t n) {
+    AFM_CHECK_OP(op);
+    if (!op->have_map) return fail(AFM_ERR_STATE, "set_bdr_map before set_map");
+    if (n > 0 && (!constrained || !values)) return fail(AFM_ERR_INVALID_ARG, "null constraint arrays");
+    for (uint32_t i = 0; i < n; i++)
+        if (constrained[i] >= op->n_dofs)
+            return fail(AFM_GLOBAL_DOF_ID_NOT_FOUND, "constrained DoF %llu >= %u", (unsigned long long)constrained[i], op->n_dofs);
+    op->constrained.assign(constrained, constrained + n);
+    op->values.assign(values, values + n);
+    op->bc_unique.assign(constrained, constrained + n);
+    std::sort(op->bc_unique.begin(), op->bc_unique.end());
+    op->bc_unique.erase(std::unique(op->bc_unique.begin(), op->bc_unique.end()), op->bc_unique.end());
+    op->finalized = false;
+    return ok();
+}
+
+int afm_set_element_matrix(afm_operator* op, uint32_t eid, const double* e_mat, uint32_t bi, uint32_t bj,
+                           uint32_t bd) {
+    AFM_CHECK_OP(op);
+    if (!op->have_map) return fail(AFM_ERR_STATE, "set_element_matrix before set_map");
+    if (eid >= op->n_elem) return fail(AFM_INDEX_OUT_OF_BOUNDS, "element %u >= %u", eid, op->n_elem);
+    if (!e_mat || bd == 0 || bi >= bd || bj >= bd) return fail(AFM_ERR_INVALID_ARG, "bad block (%u,%u) of %u", bi, bj, bd);
+    const uint32_t n = op->offsets[eid + 1] - op->offsets[eid];
+    if (n % bd) return fail(AFM_ERR_INVALID_ARG, "element %u: %u DoFs not divisible into %u blocks", eid, n, bd);
+    const uint32_t nb = n / bd;
+    double* k = op->ke.data() + op->kofs[eid];
+    for (uint32_t r = 0; r < nb; r++)
+        for (uint32_t c = 0; c < nb; c++) k[(size_t)(bi * nb + r) * n + (bj * nb + c)] = e_mat[(size_t)r * nb + c];
+    op->ke_dirty = true;
+    op->finalized = false;
+    return ok();
+}
+
+int afm_set_element_matrices(afm_operator* op, uint32_t first, uint32_t count, const double* ke) {
+    AFM_CHECK_OP(op);
+    if (!op->have_map) return fail(AFM_ERR_STATE, "set_element_matrices before set_map");
+    if ((uint64_t)first + count > op->n_elem) return fail(AFM_INDEX_OUT_OF_BOUNDS, "elements %u+%u > %u", first, count, op->n_elem);
+    if (count && !ke) return fail(AFM_ERR_INVALID_ARG, "ke is null");
+    const uint64_t a = op->kofs[first], b = op->kofs[(size_t)first + count];
+    memcpy(op->ke.data() + a, ke, (size_t)(b - a) * sizeof(double));
+    op->ke_dirty = true;
+    op->finalized = false;
+    return ok();
+}
+
+int afm_finalize(afm_operator* op) {
+    AFM_CHECK_OP(op);
+    if (!op->have_map) return fail(AFM_ERR_STATE, "finalize before set_map");
+    DeviceGuard g(op->device);
+    AFM_CUDA(cudaStreamSynchronize(op->stream));
+    free_device(op);
+    op->finalized = false;
+
+    // precision
+    int prec = op->precision_req;
+    if (prec == AFM_PREC_AUTO) {
+        bool fits = true;
+        for (double x : op->ke) {
+            const double a = std::fabs(x);
+            if (a != 0.0 && (a < 1e-30 || a > 1e30 || !std::isfinite(x))) {
+                fits = false;
+                break;
+            }
+        }
+        prec = fits ? AFM_PREC_FP64_SPLIT : AFM_PREC_FP64;
+    }
+    op->precision = prec;
+
+    // colouring and colour-sorted order
+    op->n_colors = color_elements(op->n_dofs, op->n_elem, op->offsets, op->map, op->colors);
+    op->perm.resize(op->n_elem);
+    std::iota(op->perm.begin(), op->perm.end(), 0u);
+    std::stable_sort(op->perm.begin(), op->perm.end(), [&](uint32_t a, uint32_t b) {
+        if (op->colors[a] != op->colors[b]) return op->colors[a] < op->colors[b];
+        const uint32_t na = op->offsets[a + 1] - op->offsets[a], nb = op->offsets[b + 1] - op->offsets[b];
+        return na < nb;
+    });
+
+    // segments and their arena / map offsets
+    op->segs.clear();
+    const size_t eb = entry_bytes(prec);
+    uint64_t ke_off = 0, map_off = 0;
+    for (uint32_t p = 0; p < op->n_elem;) {
+        const uint32_t e = op->perm[p];
+        Segment s;
+        s.color = op->colors[e];
+        s.n = op->offsets[e + 1] - op->offsets[e];
+        s.regime = (s.n <= kTpeMaxN) ? REG_TPE : REG_WPE;
+        s.first_pos = p;
+        uint32_t q = p;
+        while (q < op->n_elem) {
+            const uint32_t f = op->perm[q];
+            if (op->colors[f] != s.color || op->offsets[f + 1] - op->offsets[f] != s.n) break;
+            q++;
+        }
+        s.count = q - p;
+        if (s.regime == REG_TPE) {
+            s.units = (s.count + kTpeWidth - 1) / kTpeWidth;
+            s.unit_bytes = round16((uint64_t)s.n * s.n * eb * kTpeWidth);
+        } else {
+            s.units = s.count;
+            s.unit_bytes = round16((uint64_t)s.n * s.n * eb);
+        }
+        s.ke_offset = ke_off;
+        s.map_offset = map_off;
+        ke_off += s.unit_bytes * s.units;
+        map_off += (uint64_t)s.units * (s.regime == REG_TPE ? kTpeWidth : 1) * s.n;
+        map_off = (map_off + 3) / 4 * 4;  // keep 16-byte alignment of each segment's map
+        op->segs.push_back(s);
+        p = q;
+    }
+    op->ke_bytes = ke_off;
+    op->map_bytes = map_off * sizeof(uint32_t);
+
+    // device map with constrained columns flagged
+    std::vector<uint8_t> is_bc(op->n_dofs, 0);
+    for (uint32_t d : op->bc_unique) is_bc[d] = 1;
+    std::vector<uint32_t> hmap(map_off, 0);
+    for (const Segment& s : op->segs) {
+        for (uint32_t rel = 0; rel < s.count; rel++) {
+            const uint32_t e = op->perm[s.first_pos + rel];
+            for (uint32_t i = 0; i < s.n; i++) {
+                uint32_t d = op->map[op->offsets[e] + i];
+                if (is_bc[d]) d |= kBcFlag;
+                size_t at;
+                if (s.regime == REG_WPE)
+                    at = s.map_offset + (size_t)rel * s.n + i;
+                else
+                    at = s.map_offset + ((size_t)(rel / kTpeWidth) * s.n + i) * kTpeWidth + rel % kTpeWidth;
+                hmap[at] = d;
+            }
+        }
+    }
+
+    // Jacobi diagonal in element order (mat_get_diagonal_ghosted,
+    // include/aMatFree.hpp:998-1056), trace (749-785), BC rows (4310-4338)
+    op->diag_host.assign(op->n_dofs, 0.0);
+    op->trace = 0.0;
+    for (uint32_t e = 0; e < op->n_elem; e++) {
+        const uint32_t n = op->offsets[e + 1] - op->offsets[e];
+        const double* k = op->ke.data() + op->kofs[e];
+        for (uint32_t r = 0; r < n; r++) {
+            op->diag_host[op->map[op->offsets[e] + r]] += k[(size_t)r * n + r];
+            op->trace += k[(size_t)r * n + r];
+        }
+    }
+    // apply_bc_diagonal reaches constrained DoFs through the elements, so a
+    // constrained DoF of no element keeps its (zero) sum
+    const double bc_diag = (op->bc_method == AFM_BC_PENALTY) ? 100.0 * op->trace : 1.0;
+    for (uint32_t d : op->map)
+        if (is_bc[d]) op->diag_host[d] = bc_diag;
+
+    // uploads
+    AFM_CUDA(cudaMalloc((void**)&op->d_ke, std::max<size_t>(op->ke_bytes, 16)));
+    AFM_CUDA(cudaMalloc((void**)&op->d_map, std::max<size_t>(op->map_bytes, 16)));
+    AFM_CUDA(cudaMalloc((void**)&op->d_diag, sizeof(double) * std::max<uint32_t>(op->n_dofs, 1)));
+    op->n_bc = (uint32_t)op->constrained.size();
+    AFM_CUDA(cudaMalloc((void**)&op->d_bc_idx, sizeof(uint32_t) * std::max<uint32_t>(op->n_bc, 1)));
+    AFM_CUDA(cudaMalloc((void**)&op->d_bc_val, sizeof(double) * std::max<uint32_t>(op->n_bc, 1)));
+    std::vector<uint32_t> bci(op->constrained.begin(), op->constrained.end());
+    AFM_CUDA(cudaMemcpyAsync(op->d_map, hmap.data(), op->map_bytes, cudaMemcpyHostToDevice, op->stream));
+    AFM_CUDA(cudaMemcpyAsync(op->d_diag, op->diag_host.data(), sizeof(double) * op->n_dofs, cudaMemcpyHostToDevice,
+                             op->stream));
+    if (op->n_bc) {
+        AFM_CUDA(cudaMemcpyAsync(op->d_bc_idx, bci.data(), sizeof(uint32_t) * op->n_bc, cudaMemcpyHostToDevice,
+                                 op->stream));
+        AFM_CUDA(cudaMemcpyAsync(op->d_bc_val, op->values.data(), sizeof(double) * op->n_bc,
+                                 cudaMemcpyHostToDevice, op->stream));
+    }
+    AFM_CUDA(cudaStreamSynchronize(op->stream));
+    int st = upload_arena(op);
+    if (st != AFM_SUCCESS) return st;
+    op->ke_dirty = false;
+    op->finalized = true;
+    return ok();
+}
+
+int afm_matvec_device(afm_operator* op, double* d_v, const double* d_u, void* stream) {
+    AFM_CHECK_OP(op);
+    if (!op->finalized) return fail(AFM_ERR_STATE, "matvec before finalize");
+    if (op->precision == AFM_PREC_FP32) return fail(AFM_ERR_STATE, "FP32 operator: use afm_matvec_device_f32");
+    if (!d_v || !d_u) return fail(AFM_ERR_INVALID_ARG, "null vector");
+    if (d_v == (double*)d_u) return fail(AFM_ERR_INVALID_ARG, "v and u must not alias");
+    DeviceGuard g(op->device);
+    int s = enqueue_matvec(op, d_v, d_u, 0, pick_stream(op, stream));
+    return s == AFM_SUCCESS ? ok() : s;
+}
+
+int afm_matvec_device_f32(afm_operator* op, float* d_v, const float* d_u, void* stream) {
+    AFM_CHECK_OP(op);
+    if (!op->finalized) return fail(AFM_ERR_STATE, "matvec before finalize");
+    if (op->precision != AFM_PREC_FP32) return fail(AFM_ERR_STATE, "operator is not FP32");
+    if (!d_v || !d_u || (void*)d_v == (const void*)d_u) return fail(AFM_ERR_INVALID_ARG, "bad vectors");
+    DeviceGuard g(op->device);
+    int s = enqueue_matvec(op, d_v, d_u, 0, pick_stream(op, stream));
+    return s == AFM_SUCCESS ? ok() : s;
+}
+
+int afm_matvec(afm_operator* op, double* v, const double* u, int is_ghosted) {
+    (void)is_ghosted;
+    AFM_CHECK_OP(op);
+    if (!op->finalized) return fail(AFM_ERR_STATE, "matvec before finalize");
+    if (!v || !u) return fail(AFM_ERR_INVALID_ARG, "null vector");
+    if (op->precision == AFM_PREC_FP32) return fail(AFM_ERR_STATE, "FP32 operator: use afm_matvec_device_f32");
+    DeviceGuard g(op->device);
+    int s = ensure_work(op, 2);
+    if (s) return s;
+    double* du = op->d_work;
+    double* dv = op->d_work + op->n_dofs;
+    const size_t bytes = sizeof(double) * op->n_dofs;
+    AFM_CUDA(cudaMemcpyAsync(du, u, bytes, cudaMemcpyHostToDevice, op->stream));
+    s = enqueue_matvec(op, dv, du, 0, op->stream);
+    if (s) return s;
+    AFM_CUDA(cudaMemcpyAsync(v, dv, bytes, cudaMemcpyDeviceToHost, op->stream));
+    s = check_device_error(op);
+    return s == AFM_SUCCESS ? ok() : s;
+}
+
+int afm_matmult_bc_device(afm_operator* op, double* d_v, const double* d_u, void* stream) {
+    AFM_CHECK_OP(op);
+    if (!op->finalized) return fail(AFM_ERR_STATE, "matmult before finalize");
+    if (op->precision == AFM_PREC_FP32) return fail(AFM_ERR_STATE, "FP32 operator");
+    if (!d_v || !d_u || d_v == (double*)d_u) return fail(AFM_ERR_INVALID_ARG, "bad vectors");
+    DeviceGuard g(op->device);
+    cudaStream_t st = pick_stream(op, stream);
+    int s = enqueue_matvec(op, d_v, d_u, 1, st);
+    if (s) return s;
+    AFM_CUDA(launch_set_constrained(d_v, d_u, op->d_bc_idx, op->n_bc, st));
+    return ok();
+}
+
+int afm_matmult_bc(afm_operator* op, double* v, const double* u) {
+    AFM_CHECK_OP(op);
+    if (!op->finalized) return fail(AFM_ERR_STATE, "matmult before finalize");
+    if (!v || !u) return fail(AFM_ERR_INVALID_ARG, "null vector");
+    DeviceGuard g(op->device);
+    int s = ensure_work(op, 2);
+    if (s) return s;
+    double* du = op->d_work;
+    double* dv = op->d_work + op->n_dofs;
+    const size_t bytes = sizeof(double) * op->n_dofs;
+    AFM_CUDA(cudaMemcpyAsync(du, u, bytes, cudaMemcpyHostToDevice, op->stream));
+    s = afm_matmult_bc_device(op, dv, du, op->stream);
+    if (s) return s;
+    AFM_CUDA(cudaMemcpyAsync(v, dv, bytes, cudaMemcpyDeviceToHost, op->stream));
+    s = check_device_error(op);
+    return s == AFM_SUCCESS ? ok() : s;
+}
+
+int afm_get_diagonal(afm_operator* op, double* diag) {
+    AFM_CHECK_OP(op);
+    if (!op->finalized) return fail(AFM_ERR_STATE, "get_diagonal before finalize");
+    if (!diag) return fail(AFM_ERR_INVALID_ARG, "null diag");
+    memcpy(diag, op->diag_host.data(), sizeof(double) * op->n_dofs);
+    return ok();
+}
+
+int afm_get_trace(afm_operator* op, double* trace) {
+    AFM_CHECK_OP(op);
+    if (!op->finalized) return fail(AFM_ERR_STATE, "get_trace before finalize");
+    if (!trace) return fail(AFM_ERR_INVALID_ARG, "null trace");
+    *trace = op->trace;
+    return ok();
+}
+
+int afm_apply_bc_rhs(afm_operator* op, double* rhs) {
+    AFM_CHECK_OP(op);
+    if (!op->finalized) return fail(AFM_ERR_STATE, "apply_bc before finalize");
+    if (!rhs) return fail(AFM_ERR_INVALID_ARG, "null rhs");
+    if (op->bc_method == AFM_BC_PENALTY) {
+        const double pen = 100.0 * op->trace;
+        for (size_t i = 0; i < op->constrained.size(); i++) rhs[op->constrained[i]] = pen * op->values[i];
+        return ok();
+    }
+    if (op->precision == AFM_PREC_FP32) return fail(AFM_ERR_STATE, "FP32 operator");
+    // K_fc U_c as K g with g = U_c on constrained DoFs and 0 elsewhere (the
+    // assembled operator's route, include/aMatBased.hpp:366-410)
+    std::vector<double> g(op->n_dofs, 0.0), kg(op->n_dofs);
+    std::vector<uint8_t> is_bc(op->n_dofs, 0);
+    for (size_t i = 0; i < op->constrained.size(); i++) {
+        g[op->constrained[i]] = op->values[i];
+        is_bc[op->constrained[i]] = 1;
+    }
+    int s = afm_matvec(op, kg.data(), g.data(), 1);
+    if (s) return s;
+    for (size_t i = 0; i < op->constrained.size(); i++) rhs[op->constrained[i]] = op->values[i];
+    for (uint32_t d = 0; d < op->n_dofs; d++)
+        if (!is_bc[d]) rhs[d] = -kg[d] + rhs[d];
+    return ok();
+}
+
+int afm_solve_cg_device(afm_operator* op, const double* d_b, double* d_x, double rtol, double atol, int maxit,
+                        int norm_type, afm_solve_stats* stats) {
+    AFM_CHECK_OP(op);
+    if (!op->finalized) return fail(AFM_ERR_STATE, "solve before finalize");
+    if (op->precision == AFM_PREC_FP32) return fail(AFM_ERR_STATE, "FP32 operator: use the mixed-precision solve");
+    if (!d_b || !d_x) return fail(AFM_ERR_INVALID_ARG, "null vector");
+    if (norm_type != AFM_CG_NORM_UNPRECONDITIONED && norm_type != AFM_CG_NORM_PRECONDITIONED)
+        return fail(AFM_ERR_INVALID_ARG, "norm type %d", norm_type);
+    DeviceGuard g(op->device);
+    int s = ensure_work(op, 8);
+    if (s) return s;
+    const size_t n = op->n_dofs;
+    double* r = op->d_work + 2 * n;
+    double* z = op->d_work + 3 * n;
+    double* p = op->d_work + 4 * n;
+    double* q = op->d_work + 5 * n;
+    double* dinv = op->d_work + 6 * n;
+    double* sc = op->d_scalars;
+    double* part = op->d_scalars + kScalarSlots;
+    cudaStream_t st = op->stream;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, st);
+    AFM_CUDA(launch_invert(dinv, op->d_diag, n, st));
+    s = afm_matmult_bc_device(op, q, d_x, st);
+    if (s) return s;
+    AFM_CUDA(launch_cg_init(d_b, q, dinv, r, z, p, n, sc, part, st));
+    AFM_CUDA(cudaMemcpyAsync(op->h_scalars, sc, sizeof(double) * kScalarSlots, cudaMemcpyDeviceToHost, st));
+    AFM_CUDA(cudaStreamSynchronize(st));
+    const double bn = std::sqrt(op->h_scalars[S_BB]);
+    const double ref = (norm_type == AFM_CG_NORM_UNPRECONDITIONED) ? bn : std::sqrt(op->h_scalars[S_DB]);
+    const double tol = std::max(rtol * ref, atol);
+    int it = 0, status = AFM_ERR_MAXIT;
+    double rn = 0.0;
+    for (;;) {
+        const double* h = op->h_scalars;
+        rn = std::sqrt(norm_type == AFM_CG_NORM_UNPRECONDITIONED ? h[S_RR] : h[S_ZZ]);
+        if (h[S_FLAG] != 0.0 || std::isnan(rn)) {
+            status = AFM_ERR_BREAKDOWN;
+            break;
+        }
+        if (rn <= tol) {
+            status = AFM_SUCCESS;
+            break;
+        }
+        if (it >= maxit) break;
+        s = afm_matmult_bc_device(op, q, p, st);
+        if (s) return s;
+        AFM_CUDA(launch_cg_alpha(p, q, n, sc, part, st));
+        AFM_CUDA(launch_cg_update(d_x, r, z, p, q, dinv, n, sc, part, st));
+        AFM_CUDA(cudaMemcpyAsync(op->h_scalars, sc, sizeof(double) * kScalarSlots, cudaMemcpyDeviceToHost, st));
+        AFM_CUDA(cudaStreamSynchronize(st));
+        it++;
+    }
+    cudaEventRecord(e1, st);
+    // true residual in FP64
+    s = afm_matmult_bc_device(op, q, d_x, st);
+    if (s) return s;
+    AFM_CUDA(launch_axpby(q, d_b, 1.0, -1.0, n, st));  // q = b - A x
+    AFM_CUDA(launch_dots(q, q, n, part, st));
+    std::vector<double> hp(kRedBlocks);
+    AFM_CUDA(cudaMemcpyAsync(hp.data(), part, sizeof(double) * kRedBlocks, cudaMemcpyDeviceToHost, st));
+    AFM_CUDA(cudaStreamSynchronize(st));
+    double rr = 0.0;
+    for (double t : hp) rr += t;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    s = check_device_error(op);
+    if (s) return s;
+    if (stats) {
+        stats->iterations = it;
+        stats->status = status;
+        stats->rel_residual = bn > 0 ? std::sqrt(rr) / bn : std::sqrt(rr);
+        stats->residual_norm = rn;
+        stats->seconds = ms * 1e-3;
+        stats->refinements = 0;
+    }
+    if (status != AFM_SUCCESS)
+        return fail(status, status == AFM_ERR_MAXIT ? "CG reached maxit=%d" : "CG breakdown after %d iterations", it);
+    return ok();
+}
+
+int afm_solve_cg(afm_operator* op, const double* b, double* x, double rtol, double atol, int maxit, int norm_type,
+                 afm_solve_stats* stats) {
+    AFM_CHECK_OP(op);
+    if (!op->finalized) return fail(AFM_ERR_STATE, "solve before finalize");
+    if (!b || !x) return fail(AFM_ERR_INVALID_ARG, "null vector");
+    DeviceGuard g(op->device);
+    int s = ensure_work(op, 8);
+    if (s) return s;
+    double* db = op->d_work;
+    double* dx = op->d_work + op->n_dofs;
+    const size_t bytes = sizeof(double) * op->n_dofs;
+    AFM_CUDA(cudaMemcpyAsync(db, b, bytes, cudaMemcpyHostToDevice, op->stream));
+    AFM_CUDA(cudaMemcpyAsync(dx, x, bytes, cudaMemcpyHostToDevice, op->stream));
+    const int st = afm_solve_cg_device(op, db, dx, rtol, atol, maxit, norm_type, stats);
+    const std::string msg = g_last_error;
+    AFM_CUDA(cudaMemcpyAsync(x, dx, bytes, cudaMemcpyDeviceToHost, op->stream));
+    AFM_CUDA(cudaStreamSynchronize(op->stream));
+    if (st != AFM_SUCCESS) return fail(st, "%s", msg.c_str());
+    return ok();
+}
+
+int afm_get_info(afm_operator* op, afm_info* info) {
+    AFM_CHECK_OP(op);
+    if (!info) return fail(AFM_ERR_INVALID_ARG, "null info");
+    memset(info, 0, sizeof(*info));
+    info->n_elements = op->n_elem;
+    info->n_dofs = op->n_dofs;
+    info->n_colors = op->n_colors;
+    info->max_dofs_per_element = op->nmax;
+    info->precision = op->finalized ? op->precision : op->precision_req;
+    info->ke_bytes = op->ke_bytes;
+    info->map_bytes = op->map_bytes;
+    const size_t eb = entry_bytes(op->finalized ? op->precision : AFM_PREC_FP64);
+    const size_t vb = (op->finalized && op->precision == AFM_PREC_FP32) ? 4 : 8;
+    uint64_t alg = 0;
+    double fl = 0;
+    for (uint32_t e = 0; e < op->n_elem; e++) {
+        const uint64_t n = op->offsets[e + 1] - op->offsets[e];
+        alg += n * n * eb + 4 * n;
+        fl += 2.0 * (double)(n * n);
+    }
+    info->algorithmic_bytes = alg + 2 * vb * (uint64_t)op->n_dofs;
+    info->algorithmic_flops = fl;
+    uint32_t launches = 1;  // the zero fill of v
+    for (const Segment& s : op->segs)
+        if (s.units) launches++;
+    info->n_launches = launches;
+    info->device = op->device;
+    return ok();
+}
+
+int afm_get_colors(afm_operator* op, uint32_t* colors) {
+    AFM_CHECK_OP(op);
+    if (!op->finalized) return fail(AFM_ERR_STATE, "colours before finalize");
+    if (!colors) return fail(AFM_ERR_INVALID_ARG, "null colors");
+    memcpy(colors, op->colors.data(), sizeof(uint32_t) * op->n_elem);
+    return ok();
+}
+
+int afm_get_stream(afm_operator* op, void** stream) {
+    AFM_CHECK_OP(op);
+    if (!stream) return fail(AFM_ERR_INVALID_ARG, "null stream");
+    *stream = (void*)op->stream;
+    return ok();
+}
+
+int afm_synchronize(afm_operator* op) {
+    AFM_CHECK_OP(op);
+    DeviceGuard g(op->device);
+    int s = check_device_error(op);
+    return s == AFM_SUCCESS ? ok() : s;
+}
+
+}  // extern "C"

@@ -1,0 +1,123 @@
+// Internal types shared by the host runtime (afm_capi.cpp) and the CUDA
+// kernels (afm_kernels.cu, afm_solver.cu) of the GB300 AFM operator.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/afm.h"
+
+namespace afm {
+
+// Kernel regimes, picked per element size n.
+//   TPE (thread per element, n <= kTpeMaxN): 32 elements of one colour form a
+//       unit; the unit's Ke is stored entry-major [k][32] so that lane l reads
+//       entry k of element l; map [i][32].
+//   WPE (warp per element, n > kTpeMaxN): one element per unit; its Ke is
+//       stored column-major so lane r reads row r of column c; map [i].
+enum Regime : int { REG_TPE = 0, REG_WPE = 1 };
+constexpr uint32_t kTpeMaxN = 16;
+constexpr uint32_t kTpeWidth = 32;
+constexpr uint32_t kMaxN = 96;           // largest element supported (3 rows per lane)
+constexpr uint32_t kBcFlag = 0x80000000u;  // map bit: DoF is constrained
+constexpr uint32_t kDofMask = 0x7fffffffu;
+
+// Device error flags (bit set in *err).
+constexpr int kErrTimeout = 1;
+
+// One launch of the matvec: the elements of one colour that share n.
+struct Segment {
+    uint32_t color = 0;
+    uint32_t n = 0;
+    int regime = REG_WPE;
+    uint64_t first_pos = 0;   // first element position (colour-sorted order)
+    uint32_t count = 0;       // elements
+    uint32_t units = 0;       // work units (TPE: ceil(count/32), WPE: count)
+    uint64_t ke_offset = 0;   // byte offset of the first unit in the Ke arena
+    uint64_t unit_bytes = 0;  // arena bytes per unit (16-byte multiple)
+    uint64_t map_offset = 0;  // uint32 offset of the first unit in the map
+};
+
+// Arguments of one segment launch.
+struct SegArgs {
+    const unsigned char* ke;  // arena + segment offset
+    const uint32_t* map;      // map + segment offset
+    const void* u;            // double* or float*
+    void* v;                  // double* or float*
+    uint32_t units;
+    uint32_t count;           // elements (TPE: last unit may be partial)
+    uint64_t unit_bytes;
+    int bc_mode;              // 1: constrained columns read as zero (MatMult_mf)
+    int* err;
+};
+
+// Launches one segment on stream. prec: afm_precision (FP64, FP64_SPLIT, FP32).
+cudaError_t launch_segment(const Segment& s, int prec, const SegArgs& a, int sm_count, bool dup_in_element,
+                           cudaStream_t stream);
+// Dynamic shared memory the launch of segment s uses (for reporting).
+size_t segment_smem_bytes(const Segment& s, int prec);
+// Sets the kernels' shared-memory attributes once per device.
+cudaError_t configure_kernels();
+
+// Small vector kernels (afm_solver.cu).
+cudaError_t launch_set_constrained(double* v, const double* u, const uint32_t* idx, uint32_t n, cudaStream_t st);
+cudaError_t launch_scatter_values(double* v, const double* vals, const uint32_t* idx, uint32_t n, cudaStream_t st);
+
+}  // namespace afm
+
+// The operator handle.
+struct afm_operator {
+    int device = 0;
+    int bc_method = AFM_BC_IMATRIX;
+    int matfree_type = 1;
+    int precision_req = AFM_PREC_AUTO;
+    int precision = AFM_PREC_FP64;
+    cudaStream_t stream = nullptr;
+    int sm_count = 0;
+
+    // maps (single rank: local == global)
+    bool have_map = false;
+    uint32_t n_elem = 0, n_dofs = 0, nmax = 0;
+    std::vector<uint32_t> offsets;  // n_elem + 1
+    std::vector<uint32_t> map;      // global DoF ids
+    bool dup_in_element = false;    // some element lists a DoF twice
+
+    // boundary conditions
+    std::vector<uint64_t> constrained;
+    std::vector<double> values;
+    std::vector<uint32_t> bc_unique;  // sorted unique constrained ids
+
+    // element matrices, host copy (row-major, reference layout)
+    std::vector<uint64_t> kofs;     // n_elem + 1, entries
+    std::vector<double> ke;
+    bool ke_dirty = true;
+
+    // finalize products
+    bool finalized = false;
+    std::vector<uint32_t> colors;
+    uint32_t n_colors = 0;
+    std::vector<uint32_t> perm;     // position -> element id
+    std::vector<afm::Segment> segs;
+    double trace = 0.0;
+    std::vector<double> diag_host;  // Jacobi diagonal with BC rows
+
+    // device state
+    unsigned char* d_ke = nullptr;
+    size_t ke_bytes = 0;
+    uint32_t* d_map = nullptr;       // DoF map, constrained DoFs carry kBcFlag
+    size_t map_bytes = 0;
+    double* d_diag = nullptr;
+    uint32_t* d_bc_idx = nullptr;    // constrained ids in reference order
+    double* d_bc_val = nullptr;
+    uint32_t n_bc = 0;
+    int* d_err = nullptr;
+    double* d_work = nullptr;        // host-API staging and solver vectors
+    size_t work_elems = 0;
+    double* d_scalars = nullptr;     // solver scalars / reduction partials
+    double* h_scalars = nullptr;     // pinned mirror
+    float* d_work32 = nullptr;       // mixed-precision inner vectors
+    size_t work32_elems = 0;
+};

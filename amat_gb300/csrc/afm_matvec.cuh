@@ -1,0 +1,442 @@
+// AFM matvec kernels for sm_103a: v += sum over the elements of one colour of
+// P_e^T Ke P_e u, with Ke streamed from HBM by bulk TMA copies
+// (cp.async.bulk) into a shared-memory ring.
+//
+// CTA = NW consumer warps + 1 producer warp, one persistent CTA per SM. The
+// CTA owns a contiguous range of work units of the segment. The producer's
+// elected lane copies unit i's Ke (one contiguous chunk of the arena) into
+// ring slot i % S and signals full[slot] through the copy's transaction count;
+// consumer warp i % NW waits on full[slot], multiplies, and releases the slot
+// on empty[slot]. Gather of u_e and of the old v_e run two units ahead in
+// registers so their L2 latency hides behind the product. Elements of one
+// colour share no DoF, so the scatter is a plain v = v_old + ve store: no
+// atomics, and each v entry receives its element contributions in colour
+// order, independent of scheduling (bit-reproducible).
+//
+// Every mbarrier wait is bounded by wall time (globaltimer); on expiry the
+// warp sets kErrTimeout in *err and leaves its loop, and the host reports
+// AFM_ERR_TIMEOUT.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "afm_internal.hpp"
+
+namespace afm {
+
+constexpr unsigned long long kWaitLimitNs = 4000000000ull;  // 4 s per wait
+constexpr uint32_t kSmemBudget = 200 * 1024;
+constexpr uint32_t kSlotAlign = 128;
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait for the phase with the given parity; false on timeout.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const unsigned long long t0 = globaltimer_ns();
+    for (;;) {
+        for (int k = 0; k < 64; k++)
+            if (mbar_try_wait(bar, parity)) return true;
+        if (globaltimer_ns() - t0 > kWaitLimitNs) return false;
+    }
+}
+
+__device__ __forceinline__ uint64_t l2_evict_first_policy() {
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+
+// 1-D bulk copy global -> shared, completion counted on bar. dst, src 16-byte
+// aligned, bytes a multiple of 16 (guaranteed by the arena layout).
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar,
+                                          uint64_t policy) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], "
+        "%4;" ::"r"(smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar)), "l"(policy)
+        : "memory");
+}
+
+// ---- arithmetic policies ----------------------------------------------------
+// KT: stored Ke entry, UT: staged u entry, VT: vector entry, Acc: accumulator.
+
+struct ArithF64 {
+    using KT = double;
+    using UT = double;
+    using VT = double;
+    struct Acc { double s; };
+    static __device__ __forceinline__ Acc zero() { return {0.0}; }
+    static __device__ __forceinline__ UT stage(VT x) { return x; }
+    static __device__ __forceinline__ void fma(Acc& a, KT k, UT u) { a.s = __fma_rn(k, u, a.s); }
+    static __device__ __forceinline__ VT finish(const Acc& a) { return a.s; }
+};
+
+// Double-float product: Ke entry and u entry are unevaluated float pairs.
+// p + e = kh*uh exactly (TwoProduct by FMA); the cross terms kh*ul + kl*uh
+// are rounded once; s_hi collects the leading parts with the error of each
+// addition recovered by TwoSum (Knuth), s_lo the rest (Ogita, Rump & Oishi,
+// "Accurate sum and dot product", SIAM J. Sci. Comput. 26(6), 2005, Dot2).
+// The _rn intrinsics keep the compiler from fusing the steps.
+struct ArithSplit {
+    using KT = float2;
+    using UT = float2;
+    using VT = double;
+    struct Acc { float hi, lo; };
+    static __device__ __forceinline__ Acc zero() { return {0.0f, 0.0f}; }
+    static __device__ __forceinline__ UT stage(VT x) {
+        const float h = __double2float_rn(x);
+        const float l = __double2float_rn(x - (double)h);
+        return make_float2(h, l);
+    }
+    static __device__ __forceinline__ void fma(Acc& a, KT k, UT u) {
+        const float p = __fmul_rn(k.x, u.x);
+        const float e = __fmaf_rn(k.x, u.x, -p);
+        const float t = __fmaf_rn(k.x, u.y, __fmaf_rn(k.y, u.x, e));
+        const float s = __fadd_rn(a.hi, p);
+        const float bp = __fsub_rn(s, a.hi);
+        const float err = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bp)), __fsub_rn(p, bp));
+        a.hi = s;
+        a.lo = __fadd_rn(a.lo, __fadd_rn(err, t));
+    }
+    static __device__ __forceinline__ VT finish(const Acc& a) { return (double)a.hi + (double)a.lo; }
+};
+
+struct ArithF32 {
+    using KT = float;
+    using UT = float;
+    using VT = float;
+    struct Acc { float s; };
+    static __device__ __forceinline__ Acc zero() { return {0.0f}; }
+    static __device__ __forceinline__ UT stage(VT x) { return x; }
+    static __device__ __forceinline__ void fma(Acc& a, KT k, UT u) { a.s = __fmaf_rn(k, u, a.s); }
+    static __device__ __forceinline__ VT finish(const Acc& a) { return a.s; }
+};
+
+template <typename VT>
+__device__ __forceinline__ VT load_u(const VT* u, uint32_t m, int bc_mode) {
+    const uint32_t d = m & kDofMask;
+    VT x = __ldg(u + d);
+    if (bc_mode && (m & kBcFlag)) x = VT(0);
+    return x;
+}
+
+// Shared-memory layout of one CTA: S slots, then 2*S mbarriers, then the
+// per-warp u staging buffers (WPE only).
+struct RingLayout {
+    uint32_t slot_bytes, stages, warps, ubuf_bytes;
+    __host__ __device__ uint32_t bars_offset() const { return slot_bytes * stages; }
+    __host__ __device__ uint32_t ubuf_offset() const { return bars_offset() + 16 * stages; }
+    __host__ __device__ uint32_t total() const { return ubuf_offset() + ubuf_bytes * warps; }
+};
+
+// ---- warp per element (n > 16) --------------------------------------------
+// Ke of one element: column-major, entry (r, c) at c*n + r. Lane l owns rows
+// l, l+32, l+64 (R = ceil(n/32) rows).
+template <int NT, typename A, bool DUP>
+__global__ void __launch_bounds__(9 * 32, 1) afm_wpe_kernel(SegArgs a, RingLayout L, uint32_t n_rt) {
+    using KT = typename A::KT;
+    using UT = typename A::UT;
+    using VT = typename A::VT;
+    constexpr int RMAX = NT ? (NT + 31) / 32 : 3;
+    const uint32_t n = NT ? NT : n_rt;
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + L.bars_offset());
+    uint64_t* empty = full + L.stages;
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t NW = L.warps, S = L.stages;
+
+    const uint32_t per = a.units / gridDim.x, rem = a.units % gridDim.x;
+    const uint32_t begin = blockIdx.x * per + min(blockIdx.x, rem);
+    const uint32_t cnt = per + (blockIdx.x < rem ? 1u : 0u);
+
+    if (threadIdx.x == 0) {
+        for (uint32_t s = 0; s < S; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+
+    if (warp == NW) {  // producer
+        if (lane == 0) {
+            const uint64_t pol = l2_evict_first_policy();
+            for (uint32_t i = 0; i < cnt; i++) {
+                const uint32_t s = i % S;
+                if (i >= S && !mbar_wait(&empty[s], ((i / S) - 1) & 1)) {
+                    atomicOr(a.err, kErrTimeout);
+                    break;
+                }
+                mbar_arrive_expect_tx(&full[s], (uint32_t)a.unit_bytes);
+                bulk_load(smem + (size_t)s * L.slot_bytes, a.ke + (size_t)(begin + i) * a.unit_bytes,
+                          (uint32_t)a.unit_bytes, &full[s], pol);
+            }
+        }
+        return;
+    }
+
+    const VT* __restrict__ u = static_cast<const VT*>(a.u);
+    VT* __restrict__ v = static_cast<VT*>(a.v);
+    UT* us = reinterpret_cast<UT*>(smem + L.ubuf_offset() + warp * L.ubuf_bytes);
+
+    uint32_t dof_c[RMAX], dof_n[RMAX], dof_nn[RMAX];
+    VT vold_c[RMAX], vold_n[RMAX], u_n[RMAX];
+#pragma unroll
+    for (int t = 0; t < RMAX; t++) {
+        dof_c[t] = dof_n[t] = dof_nn[t] = 0u;
+        vold_c[t] = vold_n[t] = u_n[t] = VT(0);
+    }
+    auto load_map = [&](uint32_t i, uint32_t* d) {
+        const uint32_t* mp = a.map + (size_t)(begin + i) * n;
+#pragma unroll
+        for (int t = 0; t < RMAX; t++) {
+            const uint32_t r = lane + 32 * t;
+            d[t] = (r < n) ? __ldg(mp + r) : 0u;
+        }
+    };
+    auto load_uv = [&](const uint32_t* d, VT* uu, VT* vv) {
+#pragma unroll
+        for (int t = 0; t < RMAX; t++) {
+            const uint32_t r = lane + 32 * t;
+            uu[t] = VT(0);
+            vv[t] = VT(0);
+            if (r < n) {
+                uu[t] = load_u(u, d[t], a.bc_mode);
+                if (!DUP) vv[t] = v[d[t] & kDofMask];
+            }
+        }
+    };
+
+    uint32_t i = warp;
+    if (i < cnt) {
+        VT u_c[RMAX];
+        load_map(i, dof_c);
+        load_uv(dof_c, u_c, vold_c);
+#pragma unroll
+        for (int t = 0; t < RMAX; t++)
+            if (lane + 32 * t < n) us[lane + 32 * t] = A::stage(u_c[t]);
+        if (i + NW < cnt) load_map(i + NW, dof_n);
+    }
+    for (; i < cnt; i += NW) {
+        if (i + NW < cnt) load_uv(dof_n, u_n, vold_n);
+        if (i + 2 * NW < cnt) load_map(i + 2 * NW, dof_nn);
+        __syncwarp();
+
+        const uint32_t s = i % S;
+        if (!mbar_wait(&full[s], (i / S) & 1)) {
+            if (lane == 0) atomicOr(a.err, kErrTimeout);
+            break;
+        }
+        const KT* ks = reinterpret_cast<const KT*>(smem + (size_t)s * L.slot_bytes);
+        typename A::Acc acc[RMAX];
+#pragma unroll
+        for (int t = 0; t < RMAX; t++) acc[t] = A::zero();
+#pragma unroll(NT ? (NT < 64 ? NT : 16) : 4)
+        for (uint32_t c = 0; c < n; c++) {
+            const UT uc = us[c];
+            const KT* col = ks + (size_t)c * n;
+#pragma unroll
+            for (int t = 0; t < RMAX; t++) {
+                const uint32_t r = lane + 32 * t;
+                if (r < n) A::fma(acc[t], col[r], uc);
+            }
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[s]);
+
+        if (!DUP) {
+#pragma unroll
+            for (int t = 0; t < RMAX; t++) {
+                const uint32_t r = lane + 32 * t;
+                if (r < n) v[dof_c[t] & kDofMask] = vold_c[t] + A::finish(acc[t]);
+            }
+        } else {
+            // an element lists a DoF more than once: add row by row in order
+            for (uint32_t r = 0; r < n; r++) {
+                if ((r & 31) == lane) {
+                    const uint32_t d = dof_c[r >> 5] & kDofMask;
+                    v[d] = v[d] + A::finish(acc[r >> 5]);
+                }
+                __syncwarp();
+            }
+        }
+        // rotate the pipeline
+#pragma unroll
+        for (int t = 0; t < RMAX; t++) {
+            dof_c[t] = dof_n[t];
+            vold_c[t] = vold_n[t];
+            dof_n[t] = dof_nn[t];
+        }
+        if (i + NW < cnt) {
+#pragma unroll
+            for (int t = 0; t < RMAX; t++)
+                if (lane + 32 * t < n) us[lane + 32 * t] = A::stage(u_n[t]);
+        }
+    }
+}
+
+// ---- thread per element (n <= 16) ------------------------------------------
+// A unit is 32 elements; its Ke is entry-major: entry k = r*n + c of element
+// lane at k*32 + lane; its map entry i of element lane at i*32 + lane.
+template <int NT, typename A, bool DUP>
+__global__ void __launch_bounds__(9 * 32, 1) afm_tpe_kernel(SegArgs a, RingLayout L, uint32_t n_rt) {
+    using KT = typename A::KT;
+    using UT = typename A::UT;
+    using VT = typename A::VT;
+    constexpr int NM = NT ? NT : 16;
+    const uint32_t n = NT ? NT : n_rt;
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + L.bars_offset());
+    uint64_t* empty = full + L.stages;
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t NW = L.warps, S = L.stages;
+
+    const uint32_t per = a.units / gridDim.x, rem = a.units % gridDim.x;
+    const uint32_t begin = blockIdx.x * per + min(blockIdx.x, rem);
+    const uint32_t cnt = per + (blockIdx.x < rem ? 1u : 0u);
+
+    if (threadIdx.x == 0) {
+        for (uint32_t s = 0; s < S; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+
+    if (warp == NW) {
+        if (lane == 0) {
+            const uint64_t pol = l2_evict_first_policy();
+            for (uint32_t i = 0; i < cnt; i++) {
+                const uint32_t s = i % S;
+                if (i >= S && !mbar_wait(&empty[s], ((i / S) - 1) & 1)) {
+                    atomicOr(a.err, kErrTimeout);
+                    break;
+                }
+                mbar_arrive_expect_tx(&full[s], (uint32_t)a.unit_bytes);
+                bulk_load(smem + (size_t)s * L.slot_bytes, a.ke + (size_t)(begin + i) * a.unit_bytes,
+                          (uint32_t)a.unit_bytes, &full[s], pol);
+            }
+        }
+        return;
+    }
+
+    const VT* __restrict__ u = static_cast<const VT*>(a.u);
+    VT* __restrict__ v = static_cast<VT*>(a.v);
+    uint32_t dof_c[NM], dof_n[NM];
+    VT u_c[NM], vold_c[NM];
+
+    auto valid = [&](uint32_t i) { return (size_t)(begin + i) * kTpeWidth + lane < a.count; };
+    auto load_map = [&](uint32_t i, uint32_t* d) {
+        const uint32_t* mp = a.map + (size_t)(begin + i) * n * kTpeWidth + lane;
+#pragma unroll
+        for (int c = 0; c < NM; c++) d[c] = (c < (int)n) ? __ldg(mp + (size_t)c * kTpeWidth) : 0u;
+    };
+    auto load_uv = [&](const uint32_t* d, VT* uu, VT* vv, bool ok) {
+#pragma unroll
+        for (int c = 0; c < NM; c++) {
+            uu[c] = VT(0);
+            vv[c] = VT(0);
+            if (c < (int)n && ok) {
+                uu[c] = load_u(u, d[c], a.bc_mode);
+                if (!DUP) vv[c] = v[d[c] & kDofMask];
+            }
+        }
+    };
+
+    uint32_t i = warp;
+    if (i < cnt) {
+        load_map(i, dof_c);
+        load_uv(dof_c, u_c, vold_c, valid(i));
+        if (i + NW < cnt) load_map(i + NW, dof_n);
+    }
+    for (; i < cnt; i += NW) {
+        const bool ok = valid(i);
+        VT u_n[NM], vold_n[NM];
+        uint32_t dof_nn[NM];
+#pragma unroll
+        for (int c = 0; c < NM; c++) dof_nn[c] = 0u;
+        const bool has_n = i + NW < cnt;
+        if (has_n) load_uv(dof_n, u_n, vold_n, valid(i + NW));
+        if (i + 2 * NW < cnt) load_map(i + 2 * NW, dof_nn);
+
+        const uint32_t s = i % S;
+        if (!mbar_wait(&full[s], (i / S) & 1)) {
+            if (lane == 0) atomicOr(a.err, kErrTimeout);
+            break;
+        }
+        const KT* ks = reinterpret_cast<const KT*>(smem + (size_t)s * L.slot_bytes) + lane;
+        UT us[NM];
+#pragma unroll
+        for (int c = 0; c < NM; c++) us[c] = A::stage(u_c[c]);
+        typename A::Acc acc[NM];
+#pragma unroll
+        for (int r = 0; r < NM; r++) {
+            acc[r] = A::zero();
+            if (r < (int)n) {
+#pragma unroll
+                for (int c = 0; c < NM; c++)
+                    if (c < (int)n) A::fma(acc[r], ks[(size_t)(r * n + c) * kTpeWidth], us[c]);
+            }
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[s]);
+
+        if (ok) {
+#pragma unroll
+            for (int r = 0; r < NM; r++) {
+                if (r < (int)n) {
+                    const uint32_t d = dof_c[r] & kDofMask;
+                    if (!DUP)
+                        v[d] = vold_c[r] + A::finish(acc[r]);
+                    else
+                        v[d] = v[d] + A::finish(acc[r]);
+                }
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < NM; c++) {
+            dof_c[c] = dof_n[c];
+            dof_n[c] = dof_nn[c];
+            if (has_n) {
+                u_c[c] = u_n[c];
+                vold_c[c] = vold_n[c];
+            }
+        }
+    }
+}
+
+}  // namespace afm

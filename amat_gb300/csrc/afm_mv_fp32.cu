@@ -1,0 +1,5 @@
+// Matvec kernels, ArithF32 instances.
+#define ARITH ArithF32
+#define LAUNCH_FN launch_segment_fp32
+#define SMEM_FN segment_smem_fp32
+#include "afm_mv_launch.inl"

@@ -1,0 +1,5 @@
+// Matvec kernels, ArithF64 instances.
+#define ARITH ArithF64
+#define LAUNCH_FN launch_segment_fp64
+#define SMEM_FN segment_smem_fp64
+#include "afm_mv_launch.inl"

@@ -1,0 +1,328 @@
+"""Benchmark of the GB300 AFM matvec (v = K u, stored element matrices).
+
+Workload (default): 3-D linear elasticity on a structured 64^3 mesh of 20-node
+serendipity hexahedra (262,144 elements, 1,085,825 nodes, 3,257,475 DoF),
+60x60 FP64 element matrices from 3x3x3 Gauss quadrature, E = 1, nu = 0.3,
+vertex coordinates jittered by uniform +-0.1 h (seed 1). One step = one
+matvec over the whole mesh with u resident in HBM. The inputs (7.66 GB) are
+~60x the 129 MB L2, so no L2 flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`--impl reference` times the CPU implementation of the reference's method-1
+loop (the oracle's port of matvec_ghosted_OMP: OpenMP parallel-for over
+elements, row-major GEMV, atomic scatter) on all host cores, on a bounded
+sample of the same workload. One JSON line on stdout (rank 0).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "hex20_elastic_64": dict(kind=2, n=64, ngt=3, jitter=0.1, seed=1,
+                             desc="hex20 elasticity 64^3, 60x60 FP64 Ke, 3x3x3 Gauss, jitter 0.1h"),
+    "hex8_poisson_32": dict(kind=0, n=32, ngt=2, jitter=0.0, seed=0,
+                            desc="hex8 Poisson 32^3, 8x8 FP64 Ke, 2x2x2 Gauss"),
+    "hex8_elastic_48": dict(kind=1, n=48, ngt=2, jitter=0.1, seed=3,
+                            desc="hex8 elasticity 48^3, 24x24 FP64 Ke"),
+    "tet10_poisson_96": dict(kind=3, n=96, ngt=2, jitter=0.15, seed=2,
+                             desc="tet10 Poisson 96^3 x 6 (5.3M tets), 10x10 Ke"),
+}
+PREC_NAMES = {"fp64": 0, "fp64_split": 1, "fp32": 2, "auto": 3}
+PREC_DTYPE = {0: "f64", 1: "f64 (double-float split, 2^-48 per entry)", 2: "f32"}
+CHUNK = 16384  # elements per generated block
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(key):
+    """DRAM bytes per matvec of the dominant kernel from the committed ncu summary, or None."""
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        return json.load(f).get(key)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.t.join(timeout=2)
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, val in zip(names, f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def build_problem(w, prec, device_index):
+    """Mesh, element matrices (generated in blocks straight into the operator), operator."""
+    from amat_gb300 import Maps, aMatFree
+    from amat_gb300 import problems as P
+    t0 = time.time()
+    m = P.Mesh(w["kind"], w["n"], jitter=w["jitter"], seed=w["seed"])
+    dmap = m.dof_map()
+    maps = Maps()
+    maps.set_map(m.n_elem, dmap, m.ndpe, m.n_dofs)
+    A = aMatFree(maps, 0, device_index)
+    A.set_precision(prec)
+    buf = np.empty((CHUNK, m.ndpe, m.ndpe))
+    for e0 in range(0, m.n_elem, CHUNK):
+        c = min(CHUNK, m.n_elem - e0)
+        m.element_matrices(e0, c, ngt=w["ngt"], out=buf[:c])
+        A.set_element_matrices(e0, buf[:c])
+    t1 = time.time()
+    A.finalize()
+    t2 = time.time()
+    log("setup: mesh+Ke %.1fs finalize %.1fs, %d elements, %d DoF" % (t1 - t0, t2 - t1, m.n_elem, m.n_dofs))
+    return m, dmap, A
+
+
+def cpu_sample(w, m, dmap, max_elems):
+    """Reference CPU loop on the first max_elems elements (oracle port, all host threads)."""
+    import oracle
+    from amat_gb300 import problems as P
+    ne = min(m.n_elem, max_elems)
+    ke = m.element_matrices(0, ne, ngt=w["ngt"])
+    pr = oracle.Problem(m.n_dofs, dmap[:ne], ke)
+    u = np.random.default_rng(0).uniform(-1, 1, m.n_dofs)
+    v = np.empty(m.n_dofs)
+    pr.matvec_omp(u, v)  # warm-up
+    n = m.ndpe
+    sample_bytes = ne * (n * n * 8 + 4 * n) + 16 * m.n_dofs
+    return pr, u, v, ne, sample_bytes
+
+
+def time_cpu(pr, u, v, reps):
+    ts = []
+    threads = 1
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        _, threads = pr.matvec_omp(u, v)
+        ts.append(time.perf_counter() - t0)
+    return ts, threads
+
+
+def run_reference(args, w, rank):
+    from amat_gb300 import problems as P
+    if rank != 0:
+        return None
+    m = P.Mesh(w["kind"], w["n"], jitter=w["jitter"], seed=w["seed"])
+    dmap = m.dof_map()
+    pr, u, v, ne, sbytes = cpu_sample(w, m, dmap, args.cpu_sample_elems)
+    time_cpu(pr, u, v, args.warmup)
+    ts, threads = time_cpu(pr, u, v, args.steps)
+    t = sum(ts)
+    value = sbytes * args.steps / t / 1e9
+    sample = "%d of %d elements (%s), %d matvecs" % (ne, m.n_elem, w["desc"], args.steps)
+    return {
+        "impl": "reference", "metric": "AFM matvec GB/s", "value": value, "unit": "GB/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": w["desc"], "method": "method 1 (QUASI_FREE), OpenMP + atomic scatter, CPU"},
+        "cpu_baseline": {"value": value, "unit": "GB/s", "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def run_ours(args, w, rank, world, local_rank):
+    import torch
+    dev = local_rank
+    torch.cuda.set_device(dev)
+    prec = PREC_NAMES[args.precision]
+    m, dmap, A = build_problem(w, prec, dev)
+    info = A.info()
+    stream_ptr = A.stream()
+    stream = torch.cuda.ExternalStream(stream_ptr)
+    n = m.n_dofs
+    rng = np.random.default_rng(1234 + rank)
+    u_host = rng.uniform(-1, 1, n)
+    u = torch.tensor(u_host, dtype=torch.float64, device="cuda")
+    v = torch.empty_like(u)
+    torch.cuda.synchronize()
+
+    def step():
+        A.matvec_device(v.data_ptr(), u.data_ptr(), stream_ptr)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    # timed region: K matvecs bracketed by barrier + synchronize, CUDA events on the operator's stream
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev) as clk:
+        with torch.cuda.stream(stream):
+            ev0.record(stream)
+            for _ in range(args.steps):
+                step()
+            ev1.record(stream)
+        torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    A.synchronize()
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    alg = info["algorithmic_bytes"]
+    value = alg * world * args.steps / (ms * 1e-3) / 1e9
+
+    # e2e: the reference-facing host call (copies u in, v out every step)
+    u_pin = torch.from_numpy(u_host).pin_memory()
+    v_pin = torch.empty(n, dtype=torch.float64).pin_memory()
+    from amat_gb300.afm import _ptr  # noqa: F401
+    import ctypes as C
+    lib = A._lib
+    up, vp = C.c_void_p(u_pin.data_ptr()), C.c_void_p(v_pin.data_ptr())
+    for _ in range(2):
+        lib.afm_matvec(A._h, vp, up, 1)
+    if world > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        st = lib.afm_matvec(A._h, vp, up, 1)
+        assert st == 0
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = alg * world * args.steps / e2e_s / 1e9
+    # the host call and the device call agree
+    assert np.array_equal(v_pin.numpy(), v.cpu().numpy())
+
+    if rank != 0:
+        return None
+    peak, peak_kind = measured_peak()
+    achieved = alg / (ms_step * 1e-3) / 1e9
+    key = "%s_%s" % (args.workload, args.precision)
+    traffic = ncu_traffic(key)
+    out = {
+        "metric": "AFM matvec GB/s", "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+        "scaling": "weak" if world > 1 else "weak", "vs_baseline": None,
+        "dtype": PREC_DTYPE[info["precision"]], "data": "synthetic",
+        "config": {"workload": w["desc"], "n_elements": m.n_elem, "n_dofs": n, "colors": info["n_colors"],
+                   "precision": args.precision, "parallelism": "replicas x%d" % world,
+                   "l2": "no flush: inputs %.2f GB > 129 MB L2" % (alg / 1e9)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                     "kernel": "afm matvec (one launch per colour + v zero fill), %d launches/step"
+                               % info["n_launches"],
+                     "algorithmic_bytes_per_step": alg},
+        "e2e": {"value": e2e, "unit": "GB/s", "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n},
+        "gpu_launches": (info["n_launches"] - 1) * args.steps,
+    }
+    clk_sum = clk.summary()
+    if clk_sum:
+        out["clocks"] = clk_sum
+    if args.cpu_sample_elems > 0:
+        pr, uc, vc, ne, sbytes = cpu_sample(w, m, dmap, args.cpu_sample_elems)
+        ts, threads = time_cpu(pr, uc, vc, 5)
+        out["cpu_baseline"] = {"value": sbytes * len(ts) / sum(ts) / 1e9, "unit": "GB/s", "cores": threads,
+                               "kind": "port",
+                               "sample": "%d of %d elements, 5 matvecs, oracle port of matvec_ghosted_OMP"
+                                         % (ne, m.n_elem)}
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="hex20_elastic_64", choices=sorted(WORKLOADS))
+    ap.add_argument("--precision", default="fp64", choices=sorted(PREC_NAMES))
+    ap.add_argument("--cpu-sample-elems", type=int, default=32768)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    w = WORKLOADS[args.workload]
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        out = run_reference(args, w, rank)
+    else:
+        if world > 1:
+            import torch
+            torch.cuda.set_device(local_rank)
+            torch.distributed.init_process_group("nccl")
+        out = run_ours(args, w, rank, world, local_rank)
+        if world > 1:
+            import torch
+            torch.distributed.destroy_process_group()
+    if out is not None:
+        print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()

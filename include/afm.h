@@ -1,0 +1,219 @@
+/* afm.h - C ABI of the GB300 assembly-free (AFM) finite-element operator.
+ *
+ * Drop-in for the single-rank, stored-element-matrix path of paralab/aMat:
+ * the operator v = sum_e P_e^T Ke P_e u of par::aMatFree with
+ * MATFREE_TYPE::QUASI_FREE (include/enums.hpp:56), plus the calls a solver
+ * makes around it. Each entry point below names the reference interface it
+ * replaces (paths relative to the aMat checkout).
+ *
+ * Conventions
+ *  - Every function returns an int status (afm_status). Values 0..12 are the
+ *    reference's par::Error codes (include/enums.hpp:24-36); codes >= 100 are
+ *    new. afm_last_error() gives a message for the calling thread.
+ *  - Indices: local DoF ids are uint32 (the reference's LI), global ids
+ *    uint64 (GI). One rank: global == local after set_map, no ghosts.
+ *  - Host pointers are copied; nothing passed in is retained after the call
+ *    returns (unlike Maps::set_map, which keeps dofs_per_element,
+ *    include/maps.hpp:423).
+ *  - All work for one operator is serialised on that operator's CUDA stream.
+ *    Calls on one operator are not re-entrant (same as aMatFree,
+ *    include/aMatFree.hpp:75-84); different operators may be used from
+ *    different threads.
+ *  - The device path has no CPU fallback: without a usable GB300 (sm_103)
+ *    afm_create fails with AFM_ERR_CUDA.
+ */
+#ifndef AFM_GB300_AFM_H
+#define AFM_GB300_AFM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum afm_status {
+    AFM_SUCCESS = 0,                 /* par::Error::SUCCESS */
+    AFM_INDEX_OUT_OF_BOUNDS = 1,     /* par::Error::INDEX_OUT_OF_BOUNDS */
+    AFM_UNKNOWN_ELEMENT_TYPE = 2,
+    AFM_UNKNOWN_ELEMENT_STATUS = 3,
+    AFM_NULL_L2G_MAP = 4,
+    AFM_GHOST_NODE_NOT_FOUND = 5,
+    AFM_UNKNOWN_MAT_TYPE = 6,        /* unsupported MATFREE_TYPE */
+    AFM_WRONG_COMMUNICATION = 7,     /* maps that need ghost exchange (more than one rank) */
+    AFM_UNKNOWN_DOF_TYPE = 8,
+    AFM_UNKNOWN_CONSTRAINT = 9,
+    AFM_UNKNOWN_BC_METH = 10,
+    AFM_NOT_IMPLEMENTED = 11,
+    AFM_GLOBAL_DOF_ID_NOT_FOUND = 12,
+    AFM_ERR_CUDA = 100,              /* CUDA runtime error or no sm_103 device */
+    AFM_ERR_OOM = 101,               /* device or host allocation failed */
+    AFM_ERR_TIMEOUT = 102,           /* a bounded device wait gave up */
+    AFM_ERR_BREAKDOWN = 103,         /* CG breakdown: p.Ap <= 0, r.z < 0 or NaN */
+    AFM_ERR_STATE = 104,             /* call out of order (e.g. matvec before finalize) */
+    AFM_ERR_INVALID_ARG = 105,       /* null pointer, bad size, unsupported option */
+    AFM_ERR_MAXIT = 106              /* CG stopped at maxit without converging */
+} afm_status;
+
+/* par::BC_METH (include/enums.hpp:20-21) */
+typedef enum afm_bc_method { AFM_BC_IMATRIX = 0, AFM_BC_PENALTY = 1 } afm_bc_method;
+
+/* Arithmetic of the stored element matrices and of the matvec.
+ *  AFM_PREC_FP64        Ke stored as double, native FP64 multiply-add.
+ *  AFM_PREC_FP64_SPLIT  Ke stored as an unevaluated pair of floats (hi, lo)
+ *                       taking the same 8 bytes per entry; the product runs
+ *                       in double-float arithmetic (error-free TwoProduct and
+ *                       TwoSum, Ogita, Rump & Oishi 2005) with FP64 gather and
+ *                       scatter. About 2^-48 relative per entry; for Ke
+ *                       entries whose magnitude lies within 1e-30..1e30.
+ *  AFM_PREC_FP32        Ke stored as float, FP32 multiply and accumulate, on
+ *                       float vectors (afm_matvec_device_f32).
+ * AFM_PREC_AUTO picks FP64_SPLIT when every Ke entry is in its range, FP64
+ * otherwise. */
+typedef enum afm_precision {
+    AFM_PREC_FP64 = 0,
+    AFM_PREC_FP64_SPLIT = 1,
+    AFM_PREC_FP32 = 2,
+    AFM_PREC_AUTO = 3
+} afm_precision;
+
+/* CG stopping norm (afm_solve_cg) */
+typedef enum afm_cg_norm {
+    AFM_CG_NORM_UNPRECONDITIONED = 0, /* ||b - A x||_2 <= max(rtol ||b||_2, atol) */
+    AFM_CG_NORM_PRECONDITIONED = 1    /* ||D^-1 r||_2 <= max(rtol ||D^-1 b||_2, atol): PETSc KSPCG default */
+} afm_cg_norm;
+
+typedef struct afm_operator afm_operator;
+
+typedef struct afm_info {
+    uint32_t n_elements;
+    uint32_t n_dofs;
+    uint32_t n_colors;          /* colours of the element conflict graph */
+    uint32_t max_dofs_per_element;
+    int precision;              /* effective afm_precision after finalize */
+    uint64_t ke_bytes;          /* device bytes of the element-matrix arena */
+    uint64_t map_bytes;         /* device bytes of the DoF map */
+    uint64_t algorithmic_bytes; /* per matvec: sum_e (n_e^2 * entry + 4 n_e) + 16 n_dofs */
+    double algorithmic_flops;   /* per matvec: sum_e 2 n_e^2 */
+    uint32_t n_launches;        /* kernel launches per matvec */
+    int device;
+} afm_info;
+
+typedef struct afm_solve_stats {
+    int iterations;
+    int status;                 /* afm_status of the solve */
+    double rel_residual;        /* ||b - A x||_2 / ||b||_2 at exit, computed in FP64 */
+    double residual_norm;       /* the monitored norm at exit */
+    double seconds;             /* device time of the solve */
+    int refinements;            /* outer FP64 steps (mixed-precision solve only) */
+} afm_solve_stats;
+
+/* ---- lifetime ---------------------------------------------------------- */
+
+/* aMatFree(Maps&, BC_METH) (include/aMatFree.hpp:113, 406-442). device < 0
+ * means the current device. */
+int afm_create(afm_operator** out, int bc_method, int device);
+/* ~aMatFree */
+int afm_destroy(afm_operator* op);
+
+/* aMat::set_matfree_type (include/aMat.hpp:184-187). Accepts QUASI_FREE (1)
+ * and GPU_PURE (3): both select the stored-Ke device operator here. */
+int afm_set_matfree_type(afm_operator* op, int matfree_type);
+/* Arithmetic of the stored Ke; call before afm_finalize. Default AUTO. */
+int afm_set_precision(afm_operator* op, int precision);
+
+/* ---- maps (par::Maps) --------------------------------------------------- */
+
+/* Maps::set_map (include/maps.hpp:279-286, 399-451), flattened:
+ * element e owns DoFs element_to_rank_map[dof_offsets[e] .. dof_offsets[e+1])
+ * (dof_offsets NULL: every element has dofs_per_element DoFs). Local ids are
+ * mapped through rank_to_global_map (NULL: identity). owned_global_dof_end is
+ * inclusive, as in the reference. One rank owns everything:
+ * owned range [0, n_global_dofs-1] and n_all_dofs_on_rank == n_global_dofs,
+ * else AFM_WRONG_COMMUNICATION. */
+int afm_set_map(afm_operator* op, uint32_t n_elements, const uint32_t* dof_offsets, uint32_t dofs_per_element,
+                const uint32_t* element_to_rank_map, uint32_t n_all_dofs_on_rank, const uint64_t* rank_to_global_map,
+                uint64_t owned_global_dof_begin, uint64_t owned_global_dof_end, uint64_t n_global_dofs);
+
+/* Maps::set_bdr_map (include/maps.hpp:829-880): constrained global DoFs and
+ * their prescribed values. */
+int afm_set_bdr_map(afm_operator* op, const uint64_t* constrained_dofs, const double* prescribed_values,
+                    uint32_t n_constraints);
+
+/* ---- element matrices --------------------------------------------------- */
+
+/* aMatFree::set_element_matrix(eid, e_mat, block_i, block_j, blocks_dim)
+ * (include/aMat.hpp:134-141, include/aMatFree.hpp:856-953): e_mat is the
+ * (n/blocks_dim)^2 block (block_i, block_j) of element eid's matrix,
+ * row-major. Blocks never set are zero (the reference's nullptr blocks). */
+int afm_set_element_matrix(afm_operator* op, uint32_t eid, const double* e_mat, uint32_t block_i, uint32_t block_j,
+                           uint32_t blocks_dim);
+/* Bulk form: count whole element matrices, row-major, back to back, for
+ * elements first_eid .. first_eid+count-1. */
+int afm_set_element_matrices(afm_operator* op, uint32_t first_eid, uint32_t count, const double* ke);
+
+/* aMatFree::finalize (include/aMatFree.hpp:151-155, 657-785): colours the
+ * elements, lays out and uploads the DoF map and element matrices, builds the
+ * Jacobi diagonal and tr(K). */
+int afm_finalize(afm_operator* op);
+
+/* ---- operator ----------------------------------------------------------- */
+
+/* aMatFree::matvec(v, u, isGhosted) (include/aMatFree.hpp:226, 1682-1775):
+ * v = K u on host arrays of n_dofs doubles; copies in, runs, copies out,
+ * returns when v is written. is_ghosted is accepted for signature parity
+ * (one rank: ghosted and local layouts coincide). */
+int afm_matvec(afm_operator* op, double* v, const double* u, int is_ghosted);
+/* v = K u on device arrays, enqueued on stream (NULL: the operator's stream)
+ * and returned without waiting. */
+int afm_matvec_device(afm_operator* op, double* d_v, const double* d_u, void* stream);
+/* FP32 operator on float device vectors (needs AFM_PREC_FP32 Ke). */
+int afm_matvec_device_f32(afm_operator* op, float* d_v, const float* d_u, void* stream);
+
+/* aMatFree::MatMult_mf (include/aMatFree.hpp:3894-3941): u_c taken as zero
+ * in the product, then v_c = u_c. Host arrays. */
+int afm_matmult_bc(afm_operator* op, double* v, const double* u);
+int afm_matmult_bc_device(afm_operator* op, double* d_v, const double* d_u, void* stream);
+
+/* MatGetDiagonal_mf (include/aMatFree.hpp:3945-3975): sum of element
+ * diagonals, constrained rows 1 (identity) or 100 tr(K) (penalty,
+ * apply_bc_diagonal 4310-4338). Host array of n_dofs. */
+int afm_get_diagonal(afm_operator* op, double* diag);
+
+/* aMatFree::apply_bc (include/aMatFree.hpp:957-969, apply_bc_rhs 4537-4700):
+ * identity: rhs_f -= K_fc U_c, rhs_c = U_c; penalty: rhs_c = 100 tr(K) U_c.
+ * Host array of n_dofs, updated in place. */
+int afm_apply_bc_rhs(afm_operator* op, double* rhs);
+
+/* tr(K) as computed by finalize_end (include/aMatFree.hpp:749-785). */
+int afm_get_trace(afm_operator* op, double* trace);
+
+/* ---- solver --------------------------------------------------------------- */
+
+/* par::solve (examples/include/solve.hpp:75-127): Jacobi-preconditioned CG on
+ * the MatMult_mf operator, entirely on the device in FP64. b and x are host
+ * arrays of n_dofs; x holds the initial guess on entry and the solution on
+ * return. stats may be NULL. */
+int afm_solve_cg(afm_operator* op, const double* b, double* x, double rtol, double atol, int maxit, int norm_type,
+                 afm_solve_stats* stats);
+/* Same on device arrays (synchronous; returns when x is written). */
+int afm_solve_cg_device(afm_operator* op, const double* d_b, double* d_x, double rtol, double atol, int maxit,
+                        int norm_type, afm_solve_stats* stats);
+
+/* ---- introspection ------------------------------------------------------ */
+
+int afm_get_info(afm_operator* op, afm_info* info);
+/* Colour of each element (n_elements entries), for checking determinism. */
+int afm_get_colors(afm_operator* op, uint32_t* colors);
+/* The operator's CUDA stream (cudaStream_t). */
+int afm_get_stream(afm_operator* op, void** stream);
+/* Waits for the operator's stream and reports a device-side error flag. */
+int afm_synchronize(afm_operator* op);
+const char* afm_status_string(int status);
+/* Message of the last failing call on this thread ("" if none). */
+const char* afm_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

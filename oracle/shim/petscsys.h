@@ -1,0 +1,2 @@
+/* oracle shim: everything lives in petsc.h */
+#include "petsc.h"

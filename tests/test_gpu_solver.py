@@ -1,0 +1,87 @@
+"""Device Jacobi-PCG (the example drivers' par::solve, KSPCG + PCJACOBI on the
+MatMult_mf shell) against the oracle PCG and the examples' analytic solution."""
+import numpy as np
+import pytest
+
+import oracle
+from amat_gb300 import BC_METH, CG_NORM, PRECISION, AfmError, Maps, aMatFree
+from amat_gb300 import problems as P
+from helpers import load, make_operator, rel
+
+pytestmark = pytest.mark.gpu
+
+
+def poisson(n, jitter=0.0, seed=0, prec=PRECISION.AUTO, bc=BC_METH.BC_IMATRIX):
+    m = P.Mesh(P.HEX8_POISSON, n, jitter=jitter, seed=seed)
+    ke = m.element_matrices()
+    dofs, vals = m.boundary_conditions()
+    maps = Maps()
+    maps.set_map(m.n_elem, m.dof_map(), m.ndpe, m.n_dofs)
+    maps.set_bdr_map(dofs, vals)
+    A = aMatFree(maps, bc)
+    A.set_precision(prec)
+    A.set_element_matrices(0, ke)
+    A.finalize()
+    return m, ke, dofs, vals, A
+
+
+@pytest.mark.parametrize("prec", [PRECISION.FP64, PRECISION.FP64_SPLIT])
+def test_cg_matches_oracle_pcg(gpu, prec):
+    m, ke, dofs, vals, A = poisson(8, jitter=0.1, seed=3, prec=prec)
+    rhs = A.apply_bc(m.load())
+    x, st = A.solve(rhs, rtol=1e-10, atol=0.0, maxit=2000)
+    pr = oracle.Problem(m.n_dofs, m.dof_map(), ke, dofs, vals)
+    xo, it, res = pr.pcg(rhs, rtol=1e-10, atol=0.0, maxit=2000)
+    assert st.status == 0 and st.rel_residual <= 1e-10 * 1.01
+    assert abs(st.iterations - it) <= 1
+    assert rel(x, xo) < 1e-8
+
+
+def test_cg_poisson_analytic_solution(gpu):
+    """example03a: u = sin(2 pi x) sin(2 pi y) sin(2 pi z) / (12 pi^2) on the unit cube."""
+    errs = []
+    for n in (8, 16):
+        m, ke, dofs, vals, A = poisson(n)
+        rhs = A.apply_bc(m.load(ngt=3))
+        x, st = A.solve(rhs, rtol=1e-10, atol=0.0)
+        c = m.coords
+        exact = np.sin(2 * np.pi * c[:, 0]) * np.sin(2 * np.pi * c[:, 1]) * np.sin(2 * np.pi * c[:, 2]) / (12 * np.pi ** 2)
+        errs.append(np.abs(x - exact).max() / np.abs(exact).max())
+    assert errs[1] < 0.05 and errs[1] < errs[0] / 3  # second-order convergence
+
+
+def test_cg_golden_problem_and_penalty(gpu):
+    g = load("hex8_poisson_4")
+    for bc in (BC_METH.BC_IMATRIX, BC_METH.BC_PENALTY):
+        A = make_operator(g, bc, PRECISION.FP64)
+        rhs = g["rhs"].copy()
+        A.apply_bc(rhs)
+        x, st = A.solve(rhs, rtol=1e-12, atol=0.0)
+        pr = oracle.Problem(int(g["n_dofs"]), g["map"].reshape(-1, 8), g["ke"].reshape(-1, 8, 8),
+                            g["constrained"], g["values"])
+        xo, it, _ = pr.pcg(rhs, rtol=1e-12, atol=0.0, bc_method=int(bc))
+        assert it >= 0 and rel(x, xo) < 1e-9
+
+
+def test_cg_preconditioned_norm_option(gpu):
+    m, ke, dofs, vals, A = poisson(6)
+    rhs = A.apply_bc(m.load())
+    x, st = A.solve(rhs, rtol=1e-10, atol=0.0, norm=CG_NORM.PRECONDITIONED)
+    pr = oracle.Problem(m.n_dofs, m.dof_map(), ke, dofs, vals)
+    xo, it, _ = pr.pcg(rhs, rtol=1e-10, atol=0.0, norm_type=1)
+    assert abs(st.iterations - it) <= 1 and rel(x, xo) < 1e-8
+
+
+def test_cg_breakdown_and_maxit_are_reported(gpu):
+    m, ke, dofs, vals, A = poisson(6)
+    rhs = A.apply_bc(m.load())
+    bad = rhs.copy()
+    bad[7] = np.nan
+    with pytest.raises(AfmError) as e:
+        A.solve(bad, rtol=1e-10)
+    assert e.value.name == "ERR_BREAKDOWN"
+    x, st = A.solve(rhs, rtol=1e-14, atol=0.0, maxit=3, raise_on_fail=False)
+    assert st.status == 106 and st.iterations == 3
+    # the operator stays usable after both
+    x, st = A.solve(rhs, rtol=1e-10, atol=0.0)
+    assert st.status == 0
