@@ -26,7 +26,7 @@
 namespace afm {
 
 constexpr unsigned long long kWaitLimitNs = 4000000000ull;  // 4 s per wait
-constexpr uint32_t kSmemBudget = 200 * 1024;
+constexpr uint32_t kSmemBudget = 220 * 1024;
 constexpr uint32_t kSlotAlign = 128;
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -73,6 +73,27 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
     }
 }
 
+// Bounded wait that also gives up as soon as another warp of the CTA has set
+// *abort (after a timeout), so that the whole CTA drains quickly and keeps
+// meeting its named barriers.
+__device__ __forceinline__ bool mbar_wait_abortable(uint64_t* bar, uint32_t parity, volatile int* abort) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const unsigned long long t0 = globaltimer_ns();
+    for (;;) {
+        for (int k = 0; k < 64; k++)
+            if (mbar_try_wait(bar, parity)) return true;
+        if (*abort) return false;
+        if (globaltimer_ns() - t0 > kWaitLimitNs) {
+            *abort = 1;
+            return false;
+        }
+    }
+}
+
+__device__ __forceinline__ void named_barrier(uint32_t id, uint32_t threads) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(threads) : "memory");
+}
+
 __device__ __forceinline__ uint64_t l2_evict_first_policy() {
     uint64_t p;
     asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
@@ -102,6 +123,7 @@ struct ArithF64 {
     static __device__ __forceinline__ UT stage(VT x) { return x; }
     static __device__ __forceinline__ void fma(Acc& a, KT k, UT u) { a.s = __fma_rn(k, u, a.s); }
     static __device__ __forceinline__ VT finish(const Acc& a) { return a.s; }
+    static __device__ __forceinline__ void combine(Acc& a, const Acc& b) { a.s += b.s; }
 };
 
 // Double-float product: Ke entry and u entry are unevaluated float pairs.
@@ -132,6 +154,14 @@ struct ArithSplit {
         a.lo = __fadd_rn(a.lo, __fadd_rn(err, t));
     }
     static __device__ __forceinline__ VT finish(const Acc& a) { return (double)a.hi + (double)a.lo; }
+    // a += b, both double-float: TwoSum of the leading parts, the rest into lo
+    static __device__ __forceinline__ void combine(Acc& a, const Acc& b) {
+        const float s = __fadd_rn(a.hi, b.hi);
+        const float bp = __fsub_rn(s, a.hi);
+        const float err = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bp)), __fsub_rn(b.hi, bp));
+        a.hi = s;
+        a.lo = __fadd_rn(a.lo, __fadd_rn(b.lo, err));
+    }
 };
 
 struct ArithF32 {
@@ -143,6 +173,7 @@ struct ArithF32 {
     static __device__ __forceinline__ UT stage(VT x) { return x; }
     static __device__ __forceinline__ void fma(Acc& a, KT k, UT u) { a.s = __fmaf_rn(k, u, a.s); }
     static __device__ __forceinline__ VT finish(const Acc& a) { return a.s; }
+    static __device__ __forceinline__ void combine(Acc& a, const Acc& b) { a.s += b.s; }
 };
 
 template <typename VT>
@@ -153,13 +184,14 @@ __device__ __forceinline__ VT load_u(const VT* u, uint32_t m, int bc_mode) {
     return x;
 }
 
-// Shared-memory layout of one CTA: S slots, then 2*S mbarriers, then the
-// per-warp u staging buffers (WPE only).
+// Shared-memory layout of one CTA: S slots, then 2*S mbarriers and a 16-byte
+// flag word, then extra_bytes of staging (per-warp u buffers of the WPE
+// kernel; u double buffers and partial sums of the warp-group kernel).
 struct RingLayout {
-    uint32_t slot_bytes, stages, warps, ubuf_bytes;
+    uint32_t slot_bytes, stages, warps, ubuf_bytes, extra_bytes;
     __host__ __device__ uint32_t bars_offset() const { return slot_bytes * stages; }
-    __host__ __device__ uint32_t ubuf_offset() const { return bars_offset() + 16 * stages; }
-    __host__ __device__ uint32_t total() const { return ubuf_offset() + ubuf_bytes * warps; }
+    __host__ __device__ uint32_t ubuf_offset() const { return bars_offset() + 16 * stages + 16; }
+    __host__ __device__ uint32_t total() const { return ubuf_offset() + extra_bytes; }
 };
 
 // ---- warp per element (n > 16) --------------------------------------------
@@ -306,6 +338,155 @@ __global__ void __launch_bounds__(9 * 32, 1) afm_wpe_kernel(SegArgs a, RingLayou
                 if (lane + 32 * t < n) us[lane + 32 * t] = A::stage(u_n[t]);
         }
     }
+}
+
+
+// ---- warp group per element (n > 16) ---------------------------------------
+// Same Ke layout as the WPE kernel (column-major per element). An element is
+// worked on by g = gr x gc warps: row group rg owns rows 32 rg + lane, column
+// group cg owns columns [cg n / gc, (cg+1) n / gc). The cg > 0 warps leave
+// their partial row sums in shared memory; after one named barrier per
+// element the cg == 0 warps add them in column-group order (deterministic) and
+// scatter. ng such groups run per CTA, group k of an element sequence taking
+// elements k, k+ng, ... of the CTA's range. u_e is staged per group in a
+// double buffer so that the next element's gather overlaps this one's product.
+struct GroupGeom {
+    uint32_t gr, gc, g, ng;
+};
+
+__host__ __device__ inline uint32_t wpg_ubuf_bytes(uint32_t n, uint32_t ut) { return (n * ut + 15) / 16 * 16; }
+
+template <int NT, typename A>
+__global__ void __launch_bounds__(17 * 32, 1) afm_wpg_kernel(SegArgs a, RingLayout L, GroupGeom G, uint32_t n_rt) {
+    using KT = typename A::KT;
+    using UT = typename A::UT;
+    using VT = typename A::VT;
+    using Acc = typename A::Acc;
+    const uint32_t n = NT ? NT : n_rt;
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + L.bars_offset());
+    uint64_t* empty = full + L.stages;
+    volatile int* abort = reinterpret_cast<volatile int*>(empty + L.stages);
+    const uint32_t ub = wpg_ubuf_bytes(n, sizeof(UT));
+    unsigned char* ubase = smem + L.ubuf_offset();                 // [ng][2] u buffers
+    Acc* pbase = reinterpret_cast<Acc*>(ubase + (size_t)G.ng * 2 * ub);  // [ng][2][gc-1][n] partials
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t S = L.stages;
+
+    const uint32_t per = a.units / gridDim.x, rem = a.units % gridDim.x;
+    const uint32_t begin = blockIdx.x * per + min(blockIdx.x, rem);
+    const uint32_t cnt = per + (blockIdx.x < rem ? 1u : 0u);
+
+    if (threadIdx.x == 0) {
+        for (uint32_t s = 0; s < S; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], G.g);
+        }
+        *abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+
+    if (warp == G.ng * G.g) {  // producer
+        if (lane == 0) {
+            const uint64_t pol = l2_evict_first_policy();
+            uint32_t issued = 0;
+            for (uint32_t i = 0; i < cnt; i++) {
+                const uint32_t s = i % S;
+                if (i >= S && !mbar_wait_abortable(&empty[s], ((i / S) - 1) & 1, abort)) break;
+                mbar_arrive_expect_tx(&full[s], (uint32_t)a.unit_bytes);
+                bulk_load(smem + (size_t)s * L.slot_bytes, a.ke + (size_t)(begin + i) * a.unit_bytes,
+                          (uint32_t)a.unit_bytes, &full[s], pol);
+                issued = i + 1;
+            }
+            if (*abort) {
+                // drain: every issued copy lands before the CTA's shared memory is released
+                atomicOr(a.err, kErrTimeout);
+                const uint32_t first = issued > S ? issued - S : 0;
+                const unsigned long long t0 = globaltimer_ns();
+                for (uint32_t i = first; i < issued; i++)
+                    while (!mbar_try_wait(&full[i % S], (i / S) & 1) && globaltimer_ns() - t0 < kWaitLimitNs) {
+                    }
+            }
+        }
+        return;
+    }
+
+    const uint32_t grp = warp / G.g, q = warp % G.g;
+    const uint32_t rg = q / G.gc, cg = q % G.gc;
+    const uint32_t r = 32 * rg + lane;
+    const bool rvalid = r < n;
+    const uint32_t cb = cg * n / G.gc, ce = (cg + 1) * n / G.gc;
+    const bool gatherer = (cg == 0);
+    const uint32_t bar_id = 1 + grp, bar_threads = G.g * 32;
+    const VT* __restrict__ u = static_cast<const VT*>(a.u);
+    VT* __restrict__ v = static_cast<VT*>(a.v);
+    unsigned char* ubuf0 = ubase + (size_t)(grp * 2) * ub;
+    const uint32_t pstride = (G.gc > 1 ? G.gc - 1 : 1) * n;
+    Acc* pbuf0 = pbase + (size_t)(grp * 2) * pstride;
+    auto ubuf = [&](uint32_t p) { return reinterpret_cast<UT*>(ubuf0 + (size_t)p * ub); };
+    auto pbuf = [&](uint32_t p) { return pbuf0 + (size_t)p * pstride; };
+
+    uint32_t dof_c = 0, dof_n = 0, dof_nn = 0;
+    VT vold_c = VT(0), vold_n = VT(0), u_n = VT(0);
+    auto map_at = [&](uint32_t i) { return rvalid ? __ldg(a.map + (size_t)(begin + i) * n + r) : 0u; };
+
+    uint32_t i = grp;
+    if (gatherer && i < cnt) {
+        dof_c = map_at(i);
+        if (rvalid) {
+            ubuf(0)[r] = A::stage(load_u(u, dof_c, a.bc_mode));
+            vold_c = v[dof_c & kDofMask];
+        }
+        if (i + G.ng < cnt) dof_n = map_at(i + G.ng);
+    }
+    named_barrier(bar_id, bar_threads);
+    for (uint32_t k = 0; i < cnt; i += G.ng, k++) {
+        const uint32_t par = k & 1;
+        if (gatherer && rvalid) {
+            if (i + G.ng < cnt) {
+                u_n = load_u(u, dof_n, a.bc_mode);
+                vold_n = v[dof_n & kDofMask];
+            }
+            if (i + 2 * G.ng < cnt) dof_nn = map_at(i + 2 * G.ng);
+        }
+        const uint32_t s = i % S;
+        Acc acc = A::zero();
+        if (mbar_wait_abortable(&full[s], (i / S) & 1, abort)) {
+            const KT* ks = reinterpret_cast<const KT*>(smem + (size_t)s * L.slot_bytes);
+            const UT* uu = ubuf(par);
+            if (rvalid) {
+                if constexpr (NT != 0) {
+                    constexpr uint32_t GR = (NT + 31) / 32;
+                    constexpr uint32_t GC = GR >= 3 ? 1 : 4 / GR;
+                    constexpr uint32_t TRIP = (NT + GC - 1) / GC;
+#pragma unroll
+                    for (uint32_t j = 0; j < TRIP; j++) {
+                        const uint32_t c = cb + j;
+                        if (c < ce) A::fma(acc, ks[(size_t)c * NT + r], uu[c]);
+                    }
+                } else {
+#pragma unroll 4
+                    for (uint32_t c = cb; c < ce; c++) A::fma(acc, ks[(size_t)c * n + r], uu[c]);
+                }
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&empty[s]);
+        }
+        if (!gatherer && rvalid) pbuf(par)[(cg - 1) * n + r] = acc;
+        if (gatherer && rvalid && i + G.ng < cnt) ubuf(par ^ 1)[r] = A::stage(u_n);
+        named_barrier(bar_id, bar_threads);
+        if (gatherer) {
+            for (uint32_t c2 = 1; c2 < G.gc; c2++) {
+                if (rvalid) A::combine(acc, pbuf(par)[(c2 - 1) * n + r]);
+            }
+            if (rvalid && !*abort) v[dof_c & kDofMask] = vold_c + A::finish(acc);
+            dof_c = dof_n;
+            vold_c = vold_n;
+            dof_n = dof_nn;
+        }
+    }
+    if (lane == 0 && *abort) atomicOr(a.err, kErrTimeout);
 }
 
 // ---- thread per element (n <= 16) ------------------------------------------

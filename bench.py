@@ -31,6 +31,8 @@ sys.path.insert(0, ROOT)
 WORKLOADS = {
     "hex20_elastic_64": dict(kind=2, n=64, ngt=3, jitter=0.1, seed=1,
                              desc="hex20 elasticity 64^3, 60x60 FP64 Ke, 3x3x3 Gauss, jitter 0.1h"),
+    "hex20_elastic_32": dict(kind=2, n=32, ngt=3, jitter=0.1, seed=1,
+                             desc="hex20 elasticity 32^3, 60x60 FP64 Ke, 3x3x3 Gauss, jitter 0.1h"),
     "hex8_poisson_32": dict(kind=0, n=32, ngt=2, jitter=0.0, seed=0,
                             desc="hex8 Poisson 32^3, 8x8 FP64 Ke, 2x2x2 Gauss"),
     "hex8_elastic_48": dict(kind=1, n=48, ngt=2, jitter=0.1, seed=3,
@@ -39,7 +41,8 @@ WORKLOADS = {
                              desc="tet10 Poisson 96^3 x 6 (5.3M tets), 10x10 Ke"),
 }
 PREC_NAMES = {"fp64": 0, "fp64_split": 1, "fp32": 2, "auto": 3}
-PREC_DTYPE = {0: "f64", 1: "f64 (double-float split, 2^-48 per entry)", 2: "f32"}
+PREC_DTYPE = {0: "f64", 1: "f64 (Ke as hi+lo f32 pair, double-float products; <=1e-12 rel. vs FP64)", 2: "f32"}
+PREC_KEYS = {0: "fp64", 1: "fp64_split", 2: "fp32"}
 CHUNK = 16384  # elements per generated block
 
 
@@ -191,97 +194,128 @@ def run_reference(args, w, rank):
     }
 
 
-def run_ours(args, w, rank, world, local_rank):
+def measure_device(A, n, steps, warmup, world, dev, rank, sample_clocks):
+    """Times `steps` matvecs on device-resident vectors (CUDA events on the operator's stream)."""
     import torch
-    dev = local_rank
-    torch.cuda.set_device(dev)
-    prec = PREC_NAMES[args.precision]
-    m, dmap, A = build_problem(w, prec, dev)
     info = A.info()
     stream_ptr = A.stream()
     stream = torch.cuda.ExternalStream(stream_ptr)
-    n = m.n_dofs
-    rng = np.random.default_rng(1234 + rank)
-    u_host = rng.uniform(-1, 1, n)
-    u = torch.tensor(u_host, dtype=torch.float64, device="cuda")
+    f32 = info["precision"] == 2
+    u_host = np.random.default_rng(1234 + rank).uniform(-1, 1, n)
+    u = torch.tensor(u_host, dtype=torch.float32 if f32 else torch.float64, device="cuda")
     v = torch.empty_like(u)
     torch.cuda.synchronize()
 
     def step():
-        A.matvec_device(v.data_ptr(), u.data_ptr(), stream_ptr)
+        if f32:
+            A.matvec_device_f32(v.data_ptr(), u.data_ptr(), stream_ptr)
+        else:
+            A.matvec_device(v.data_ptr(), u.data_ptr(), stream_ptr)
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         step()
     torch.cuda.synchronize()
-    # timed region: K matvecs bracketed by barrier + synchronize, CUDA events on the operator's stream
+    # timed region: K matvecs bracketed by barrier + synchronize
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(dev) as clk:
-        with torch.cuda.stream(stream):
-            ev0.record(stream)
-            for _ in range(args.steps):
-                step()
-            ev1.record(stream)
-        torch.cuda.synchronize()
+    clk = ClockSampler(dev) if sample_clocks else None
+    if clk:
+        clk.__enter__()
+    ev0.record(stream)
+    for _ in range(steps):
+        step()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    if clk:
+        clk.__exit__(None, None, None)
     ms = ev0.elapsed_time(ev1)
     A.synchronize()
     if world > 1:
         t = torch.tensor([ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
-    ms_step = ms / args.steps
-    alg = info["algorithmic_bytes"]
-    value = alg * world * args.steps / (ms * 1e-3) / 1e9
+    return info, ms, u_host, v, clk
 
-    # e2e: the reference-facing host call (copies u in, v out every step)
+
+def measure_e2e(A, u_host, v_dev, steps, world):
+    """The reference-facing host call afm_matvec: u H2D and v D2H inside every step."""
+    import ctypes as C
+    import torch
+    n = len(u_host)
     u_pin = torch.from_numpy(u_host).pin_memory()
     v_pin = torch.empty(n, dtype=torch.float64).pin_memory()
-    from amat_gb300.afm import _ptr  # noqa: F401
-    import ctypes as C
     lib = A._lib
     up, vp = C.c_void_p(u_pin.data_ptr()), C.c_void_p(v_pin.data_ptr())
     for _ in range(2):
-        lib.afm_matvec(A._h, vp, up, 1)
+        assert lib.afm_matvec(A._h, vp, up, 1) == 0
     if world > 1:
         torch.distributed.barrier()
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        st = lib.afm_matvec(A._h, vp, up, 1)
-        assert st == 0
+    for _ in range(steps):
+        assert lib.afm_matvec(A._h, vp, up, 1) == 0
     e2e_s = time.perf_counter() - t0
     if world > 1:
         t = torch.tensor([e2e_s], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         e2e_s = float(t.item())
-    e2e = alg * world * args.steps / e2e_s / 1e9
-    # the host call and the device call agree
-    assert np.array_equal(v_pin.numpy(), v.cpu().numpy())
+    # the host call and the device call agree bit for bit
+    assert np.array_equal(v_pin.numpy(), v_dev.cpu().numpy())
+    return e2e_s
 
+
+def run_ours(args, w, rank, world, local_rank):
+    import torch
+    dev = local_rank
+    torch.cuda.set_device(dev)
+    prec = PREC_NAMES[args.precision]
+    m, dmap, A = build_problem(w, prec, dev)
+    n = m.n_dofs
+    info, ms, u_host, v, clk = measure_device(A, n, args.steps, args.warmup, world, dev, rank, True)
+    ms_step = ms / args.steps
+    alg = info["algorithmic_bytes"]
+    value = alg * world * args.steps / (ms * 1e-3) / 1e9
+    f32 = info["precision"] == 2
+    e2e = None
+    if not f32:
+        e2e_s = measure_e2e(A, u_host, v, args.steps, world)
+        e2e = {"value": alg * world * args.steps / e2e_s / 1e9, "unit": "GB/s", "h2d_bytes_per_step": 8 * n,
+               "d2h_bytes_per_step": 8 * n}
+    native = None
+    if args.also_native and info["precision"] == 1:
+        # the same workload in native FP64 arithmetic, for comparison
+        A.close()
+        from amat_gb300 import Maps, aMatFree
+        m2, dmap2, A2 = build_problem(w, 0, dev)
+        info2, ms2, _, _, _ = measure_device(A2, n, args.steps, args.warmup, world, dev, rank, False)
+        a2 = info2["algorithmic_bytes"] / (ms2 / args.steps * 1e-3) / 1e9
+        native = {"value": a2 * world, "ms_per_step": ms2 / args.steps, "dtype": "f64 (native FMA)",
+                  "bound": "fp64 FMA (1.008 TFLOP/s measured)"}
+        A2.close()
     if rank != 0:
         return None
     peak, peak_kind = measured_peak()
     achieved = alg / (ms_step * 1e-3) / 1e9
-    key = "%s_%s" % (args.workload, args.precision)
-    traffic = ncu_traffic(key)
+    key = "%s_%s" % (args.workload, PREC_KEYS[info["precision"]])
     out = {
         "metric": "AFM matvec GB/s", "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
-        "scaling": "weak" if world > 1 else "weak", "vs_baseline": None,
-        "dtype": PREC_DTYPE[info["precision"]], "data": "synthetic",
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": PREC_DTYPE[info["precision"]], "data": "synthetic",
         "config": {"workload": w["desc"], "n_elements": m.n_elem, "n_dofs": n, "colors": info["n_colors"],
-                   "precision": args.precision, "parallelism": "replicas x%d" % world,
+                   "precision": PREC_KEYS[info["precision"]], "parallelism": "replicas x%d" % world,
                    "l2": "no flush: inputs %.2f GB > 129 MB L2" % (alg / 1e9)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                     "kernel": "afm matvec (one launch per colour + v zero fill), %d launches/step"
+                     "frac": achieved / peak, "traffic": ncu_traffic(key), "peak_kind": peak_kind,
+                     "kernel": "afm_wpg_kernel, one launch per colour + v zero fill (%d launches/step)"
                                % info["n_launches"],
                      "algorithmic_bytes_per_step": alg},
-        "e2e": {"value": e2e, "unit": "GB/s", "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n},
+        "e2e": e2e,
         "gpu_launches": (info["n_launches"] - 1) * args.steps,
     }
-    clk_sum = clk.summary()
+    if native:
+        out["fp64_native"] = native
+    clk_sum = clk.summary() if clk else None
     if clk_sum:
         out["clocks"] = clk_sum
     if args.cpu_sample_elems > 0:
@@ -301,7 +335,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="hex20_elastic_64", choices=sorted(WORKLOADS))
-    ap.add_argument("--precision", default="fp64", choices=sorted(PREC_NAMES))
+    ap.add_argument("--precision", default="auto", choices=sorted(PREC_NAMES))
+    ap.add_argument("--also-native", type=int, default=1, help="also time native FP64 when the split path runs")
     ap.add_argument("--cpu-sample-elems", type=int, default=32768)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
