@@ -46,6 +46,9 @@ class AfmMesh(C.Structure):
     ]
 
 
+# include/afm.h: largest operator of afm_solve_cg_device_noalloc
+NOALLOC_MAX_DOFS = 262144
+
 P = C.c_void_p
 U32 = C.c_uint32
 U64 = C.c_uint64
@@ -73,6 +76,7 @@ AFM_SIGNATURES = {
     "afm_get_trace": (I, [P, P]),
     "afm_solve_cg": (I, [P, P, P, D, D, I, I, P]),
     "afm_solve_cg_device": (I, [P, P, P, D, D, I, I, P]),
+    "afm_solve_cg_device_noalloc": (I, [P, P, P, D, D, I, I, P]),
     "afm_get_info": (I, [P, P]),
     "afm_get_colors": (I, [P, P]),
     "afm_get_stream": (I, [P, C.POINTER(P)]),

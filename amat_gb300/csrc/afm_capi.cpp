@@ -55,8 +55,20 @@ size_t segment_smem_bytes(const Segment& s, int prec) {
 using namespace afm;
 
 namespace {
-
 thread_local std::string g_last_error;
+}
+
+int afm::set_error(int status, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return status;
+}
+
+namespace {
 
 int fail(int status, const char* fmt, ...) {
     char buf[512];

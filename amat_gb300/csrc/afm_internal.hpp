@@ -62,6 +62,10 @@ size_t segment_smem_bytes(const Segment& s, int prec);
 // Sets the kernels' shared-memory attributes once per device.
 cudaError_t configure_kernels();
 
+// Records the calling thread's last error message (returned by
+// afm_last_error) and returns status.
+int set_error(int status, const char* fmt, ...);
+
 // Small vector kernels (afm_solver.cu).
 cudaError_t launch_set_constrained(double* v, const double* u, const uint32_t* idx, uint32_t n, cudaStream_t st);
 cudaError_t launch_scatter_values(double* v, const double* vals, const uint32_t* idx, uint32_t n, cudaStream_t st);

@@ -200,6 +200,27 @@ int afm_solve_cg(afm_operator* op, const double* b, double* x, double rtol, doub
 int afm_solve_cg_device(afm_operator* op, const double* d_b, double* d_x, double rtol, double atol, int maxit,
                         int norm_type, afm_solve_stats* stats);
 
+/* Largest operator (DoFs) afm_solve_cg_device_noalloc accepts. */
+#define AFM_NOALLOC_MAX_DOFS 262144u
+
+/* Jacobi-PCG like afm_solve_cg_device, for callers that cannot allocate
+ * device memory while they run. No counterpart in the reference.
+ * Who needs it: code embedded in an application that has already reserved the
+ * GPU's memory (a framework's caching allocator sized to the device, a fixed
+ * per-process budget under MPS), or a loop that must not stall, since
+ * cudaMalloc and cudaFree can synchronise the whole device. The call allocates
+ * nothing: its CG vectors and reduction partials live in one array compiled
+ * into the library (5 x AFM_NOALLOC_MAX_DOFS doubles plus 2.6k doubles of
+ * partials, about 10.5 MB), which every GPU that loads the library holds until
+ * the process exits. Operators with more DoFs fail with AFM_ERR_INVALID_ARG.
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * All calls on a device share the array and the call clears the solver state
+ * it needs at its start, so calls whose work overlaps on the GPU race: run
+ * them one at a time. Synchronous, like afm_solve_cg_device. */
+int afm_solve_cg_device_noalloc(afm_operator* op, const double* d_b, double* d_x, double rtol, double atol,
+                                int maxit, int norm_type, afm_solve_stats* stats);
+
 /* ---- introspection ------------------------------------------------------ */
 
 int afm_get_info(afm_operator* op, afm_info* info);
