@@ -77,6 +77,17 @@ AFM_SIGNATURES = {
     "afm_solve_cg": (I, [P, P, P, D, D, I, I, P]),
     "afm_solve_cg_device": (I, [P, P, P, D, D, I, I, P]),
     "afm_solve_cg_device_noalloc": (I, [P, P, P, D, D, I, I, P]),
+    "afm_solve_cg_mixed": (I, [P, P, P, D, D, I, D, I, P]),
+    "afm_solve_cg_mixed_device": (I, [P, P, P, D, D, I, D, I, P]),
+    "afm_matmult_bc_device_f32": (I, [P, P, P, P]),
+    "afm_matvec_batched_device": (I, [P, P, P, U32, U32, P]),
+    "afm_matvec_batched_device_f32": (I, [P, P, P, U32, U32, P]),
+    "afm_matmult_bc_batched_device": (I, [P, P, P, U32, U32, P]),
+    "afm_matmult_bc_batched_device_f32": (I, [P, P, P, U32, U32, P]),
+    "afm_get_batch_tuning": (I, [P, U32, U32, I, P, P, P]),
+    "afm_set_batch_tuning": (I, [P, U32, U32, I, I, I]),
+    "afm_solve_cg_batched_device": (I, [P, P, P, U32, D, D, I, P]),
+    "afm_solve_cg_batched_mixed_device": (I, [P, P, P, U32, D, D, I, D, I, P]),
     "afm_get_info": (I, [P, P]),
     "afm_get_colors": (I, [P, P]),
     "afm_get_stream": (I, [P, C.POINTER(P)]),

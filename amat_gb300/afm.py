@@ -200,6 +200,55 @@ class aMatFree:
             check(s, "afm_solve_cg")
         return x, st
 
+    def solve_mixed(self, rhs, x=None, rtol=1e-8, atol=0.0, max_outer=30, inner_rtol=1e-2, max_inner=10000,
+                    raise_on_fail=True):
+        """Mixed-precision iterative refinement: FP64 outer residual, FP32 inner Jacobi-PCG."""
+        b = np.ascontiguousarray(rhs, dtype=np.float64)
+        x = np.zeros(self.n_dofs) if x is None else np.ascontiguousarray(x, dtype=np.float64).copy()
+        st = AfmSolveStats()
+        s = self._lib.afm_solve_cg_mixed(self._h, _ptr(b), _ptr(x), float(rtol), float(atol), int(max_outer),
+                                         float(inner_rtol), int(max_inner), C.byref(st))
+        if raise_on_fail:
+            check(s, "afm_solve_cg_mixed")
+        return x, st
+
+    def matmult_bc_device_f32(self, v_ptr, u_ptr, stream=None):
+        check(self._lib.afm_matmult_bc_device_f32(self._h, C.c_void_p(v_ptr), C.c_void_p(u_ptr),
+                                                  C.c_void_p(stream) if stream else None), "afm_matmult_bc_device_f32")
+
+    # ---- batched (device blocks n_dofs x ld, row-major) ------------------
+    def matvec_batched_device(self, v_ptr, u_ptr, nrhs, ld=None, f32=False, bc=False, stream=None):
+        ld = nrhs if ld is None else ld
+        name = "afm_%s_batched_device%s" % ("matmult_bc" if bc else "matvec", "_f32" if f32 else "")
+        check(getattr(self._lib, name)(self._h, C.c_void_p(v_ptr), C.c_void_p(u_ptr), int(nrhs), int(ld),
+                                       C.c_void_p(stream) if stream else None), name)
+
+    def set_batch_tuning(self, nrhs, cols_per_thread, groups_per_cta, ld=None, f32=False):
+        ld = nrhs if ld is None else ld
+        check(self._lib.afm_set_batch_tuning(self._h, int(nrhs), int(ld), int(bool(f32)), int(cols_per_thread),
+                                             int(groups_per_cta)), "afm_set_batch_tuning")
+
+    def batch_tuning(self, nrhs, ld=None, f32=False):
+        ld = nrhs if ld is None else ld
+        tr, ng, ms = C.c_int(), C.c_int(), C.c_float()
+        check(self._lib.afm_get_batch_tuning(self._h, int(nrhs), int(ld), int(bool(f32)), C.byref(tr), C.byref(ng),
+                                             C.byref(ms)), "afm_get_batch_tuning")
+        return tr.value, ng.value, ms.value
+
+    def solve_batched_device(self, b_ptr, x_ptr, nrhs, rtol=1e-8, atol=0.0, maxit=100000, mixed=False,
+                             max_outer=30, inner_rtol=1e-2, max_inner=100000, raise_on_fail=True):
+        st = AfmSolveStats()
+        if mixed:
+            s = self._lib.afm_solve_cg_batched_mixed_device(self._h, C.c_void_p(b_ptr), C.c_void_p(x_ptr), int(nrhs),
+                                                            float(rtol), float(atol), int(max_outer),
+                                                            float(inner_rtol), int(max_inner), C.byref(st))
+        else:
+            s = self._lib.afm_solve_cg_batched_device(self._h, C.c_void_p(b_ptr), C.c_void_p(x_ptr), int(nrhs),
+                                                      float(rtol), float(atol), int(maxit), C.byref(st))
+        if raise_on_fail:
+            check(s, "batched solve")
+        return st
+
     def info(self):
         i = AfmInfo()
         check(self._lib.afm_get_info(self._h, C.byref(i)), "afm_get_info")

@@ -17,29 +17,43 @@
 #include <cmath>
 #include <numeric>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #ifdef _OPENMP
 #include <omp.h>
 #endif
 
+#include "afm_batched_solver.hpp"
 #include "afm_internal.hpp"
 #include "afm_solver.hpp"
 
 namespace afm {
-cudaError_t launch_segment_fp64(const Segment& s, const SegArgs& a, int sm_count, bool dup, cudaStream_t st);
-cudaError_t launch_segment_split(const Segment& s, const SegArgs& a, int sm_count, bool dup, cudaStream_t st);
-cudaError_t launch_segment_fp32(const Segment& s, const SegArgs& a, int sm_count, bool dup, cudaStream_t st);
+cudaError_t launch_segment_fp64(const Segment& s, const SegArgs& a, int sm_count, bool dup, bool pdl,
+                                 cudaStream_t st);
+cudaError_t launch_segment_split(const Segment& s, const SegArgs& a, int sm_count, bool dup, bool pdl,
+                                 cudaStream_t st);
+cudaError_t launch_segment_fp32(const Segment& s, const SegArgs& a, int sm_count, bool dup, bool pdl,
+                                 cudaStream_t st);
+cudaError_t launch_batched_fp64(const Segment& s, const BatchArgs& a, int sm_count, int tr, int ng, bool pdl,
+                                cudaStream_t st);
+cudaError_t launch_batched_split(const Segment& s, const BatchArgs& a, int sm_count, int tr, int ng, bool pdl,
+                                 cudaStream_t st);
+cudaError_t launch_batched_fp32(const Segment& s, const BatchArgs& a, int sm_count, int tr, int ng, bool pdl,
+                                cudaStream_t st);
+cudaError_t configure_kernels_fp64();
+cudaError_t configure_kernels_split();
+cudaError_t configure_kernels_fp32();
 size_t segment_smem_fp64(const Segment& s);
 size_t segment_smem_split(const Segment& s);
 size_t segment_smem_fp32(const Segment& s);
 
-cudaError_t launch_segment(const Segment& s, int prec, const SegArgs& a, int sm_count, bool dup,
+cudaError_t launch_segment(const Segment& s, int prec, const SegArgs& a, int sm_count, bool dup, bool pdl,
                            cudaStream_t stream) {
     switch (prec) {
-        case AFM_PREC_FP64: return launch_segment_fp64(s, a, sm_count, dup, stream);
-        case AFM_PREC_FP64_SPLIT: return launch_segment_split(s, a, sm_count, dup, stream);
-        default: return launch_segment_fp32(s, a, sm_count, dup, stream);
+        case AFM_PREC_FP64: return launch_segment_fp64(s, a, sm_count, dup, pdl, stream);
+        case AFM_PREC_FP64_SPLIT: return launch_segment_split(s, a, sm_count, dup, pdl, stream);
+        default: return launch_segment_fp32(s, a, sm_count, dup, pdl, stream);
     }
 }
 
@@ -115,7 +129,21 @@ size_t entry_bytes(int prec) { return prec == AFM_PREC_FP32 ? 4 : 8; }
 
 uint64_t round16(uint64_t b) { return (b + 15) / 16 * 16; }
 
+void drop_graph(afm_operator::CgGraph& g);
+
 void free_device(afm_operator* op) {
+    drop_graph(op->cg64);
+    drop_graph(op->cg32);
+    drop_graph(op->bcg64);
+    drop_graph(op->bcg32);
+    op->batch_tune.clear();
+    cudaFree(op->d_bwork);
+    cudaFree(op->d_bsc);
+    op->d_bwork = nullptr;
+    op->d_bsc = nullptr;
+    op->bwork_elems = 0;
+    op->bsc_elems = 0;
+    op->generation++;
     cudaFree(op->d_ke);
     cudaFree(op->d_map);
     cudaFree(op->d_diag);
@@ -180,12 +208,18 @@ template <>
 inline void put_entry<float>(unsigned char* base, size_t idx, double x) {
     reinterpret_cast<float*>(base)[idx] = (float)x;
 }
-struct SplitPair { float hi, lo; };
+// Split entries: hi = fl32(x) in the unit's hi plane, lo = fl32(x - hi) in
+// the lo plane that follows it, so the hi plane alone is the FP32 matrix.
+struct SplitPair {};
 template <>
 inline void put_entry<SplitPair>(unsigned char* base, size_t idx, double x) {
+    (void)base, (void)idx, (void)x;  // planar: written by put_split
+}
+inline void put_split(unsigned char* base, size_t idx, size_t plane, double x) {
     const float h = (float)x;
     const float l = (float)(x - (double)h);
-    reinterpret_cast<SplitPair*>(base)[idx] = {h, l};
+    reinterpret_cast<float*>(base)[idx] = h;
+    reinterpret_cast<float*>(base)[idx + plane] = l;
 }
 
 // Writes element e (at offset `rel` inside segment s) into the host image of
@@ -195,16 +229,27 @@ void layout_element(const afm_operator* op, const Segment& s, uint32_t e, uint64
                     unsigned char* chunk) {
     const uint32_t n = s.n;
     const double* k = op->ke.data() + op->kofs[e];
+    constexpr bool split = std::is_same<KT, SplitPair>::value;
     if (s.regime == REG_WPE) {
         unsigned char* dst = chunk + (rel - u0) * s.unit_bytes;
         for (uint32_t c = 0; c < n; c++)
-            for (uint32_t r = 0; r < n; r++) put_entry<KT>(dst, (size_t)c * n + r, k[(size_t)r * n + c]);
+            for (uint32_t r = 0; r < n; r++) {
+                if (split)
+                    put_split(dst, (size_t)c * n + r, s.plane, k[(size_t)r * n + c]);
+                else
+                    put_entry<KT>(dst, (size_t)c * n + r, k[(size_t)r * n + c]);
+            }
     } else {
         const uint64_t unit = rel / kTpeWidth, lane = rel % kTpeWidth;
         unsigned char* dst = chunk + (unit - u0) * s.unit_bytes;
         for (uint32_t r = 0; r < n; r++)
-            for (uint32_t c = 0; c < n; c++)
-                put_entry<KT>(dst, ((size_t)r * n + c) * kTpeWidth + lane, k[(size_t)r * n + c]);
+            for (uint32_t c = 0; c < n; c++) {
+                const size_t idx = ((size_t)r * n + c) * kTpeWidth + lane;
+                if (split)
+                    put_split(dst, idx, s.plane, k[(size_t)r * n + c]);
+                else
+                    put_entry<KT>(dst, idx, k[(size_t)r * n + c]);
+            }
     }
 }
 
@@ -268,6 +313,17 @@ int ensure_work(afm_operator* op, size_t vectors) {
     return AFM_SUCCESS;
 }
 
+int ensure_work32(afm_operator* op, size_t vectors) {
+    const size_t need = vectors * (size_t)std::max<uint32_t>(op->n_dofs, 1);
+    if (op->work32_elems >= need) return AFM_SUCCESS;
+    cudaFree(op->d_work32);
+    op->d_work32 = nullptr;
+    op->work32_elems = 0;
+    AFM_CUDA(cudaMalloc((void**)&op->d_work32, need * sizeof(float)));
+    op->work32_elems = need;
+    return AFM_SUCCESS;
+}
+
 int check_device_error(afm_operator* op) {
     int h = 0;
     AFM_CUDA(cudaMemcpyAsync(&h, op->d_err, sizeof(int), cudaMemcpyDeviceToHost, op->stream));
@@ -281,9 +337,13 @@ int check_device_error(afm_operator* op) {
 
 // v = K u (bc_mode 0) or the product of MatMult_mf without the final v_c = u_c
 // (bc_mode 1: constrained columns of u read as zero), device arrays.
-int enqueue_matvec(afm_operator* op, void* d_v, const void* d_u, int bc_mode, cudaStream_t st) {
-    const size_t vbytes = (size_t)op->n_dofs * (op->precision == AFM_PREC_FP32 ? 4 : 8);
+int enqueue_matvec(afm_operator* op, void* d_v, const void* d_u, int bc_mode, cudaStream_t st, bool f32 = false) {
+    // f32: FP32 product on float vectors, from an FP32 arena or from the hi
+    // plane of a split arena (half of each unit is copied)
+    const int kprec = f32 ? AFM_PREC_FP32 : op->precision;
+    const size_t vbytes = (size_t)op->n_dofs * (kprec == AFM_PREC_FP32 ? 4 : 8);
     AFM_CUDA(cudaMemsetAsync(d_v, 0, vbytes, st));
+    bool first = true;
     for (const Segment& s : op->segs) {
         if (s.units == 0) continue;
         SegArgs a;
@@ -294,15 +354,382 @@ int enqueue_matvec(afm_operator* op, void* d_v, const void* d_u, int bc_mode, cu
         a.units = s.units;
         a.count = s.count;
         a.unit_bytes = s.unit_bytes;
+        a.copy_bytes = (uint32_t)s.unit_bytes;
+        a.plane = s.plane;
+        if (f32 && op->precision == AFM_PREC_FP64_SPLIT) a.copy_bytes = s.plane * 4;
         a.bc_mode = bc_mode;
         a.err = op->d_err;
-        AFM_CUDA(launch_segment(s, op->precision, a, op->sm_count, op->dup_in_element, st));
+        // every launch after the first may overlap its prologue with the previous one's tail
+        AFM_CUDA(launch_segment(s, kprec, a, op->sm_count, op->dup_in_element, !first, st));
+        first = false;
     }
     return AFM_SUCCESS;
 }
 
 cudaStream_t pick_stream(afm_operator* op, void* stream) {
     return stream ? (cudaStream_t)stream : op->stream;
+}
+
+// ---- batched (multi right-hand side) products ------------------------------
+
+int enqueue_matvec_batched(afm_operator* op, void* d_V, const void* d_U, uint32_t nrhs, uint32_t ld, int bc_mode,
+                           cudaStream_t st, bool f32, int tr, int ng) {
+    const int kprec = f32 ? AFM_PREC_FP32 : op->precision;
+    const size_t vb = (kprec == AFM_PREC_FP32 ? 4 : 8);
+    AFM_CUDA(cudaMemsetAsync(d_V, 0, (size_t)op->n_dofs * ld * vb, st));
+    bool first = true;
+    for (const Segment& s : op->segs) {
+        if (s.units == 0) continue;
+        BatchArgs a;
+        a.ke = op->d_ke + s.ke_offset;
+        a.map = op->d_map + s.map_offset;
+        a.u = d_U;
+        a.v = d_V;
+        a.units = s.units;
+        a.count = s.count;
+        a.unit_bytes = s.unit_bytes;
+        a.copy_bytes = (uint32_t)s.unit_bytes;
+        a.plane = s.plane;
+        if (f32 && op->precision == AFM_PREC_FP64_SPLIT) a.copy_bytes = s.plane * 4;
+        a.nrhs = nrhs;
+        a.ld = ld;
+        a.bc_mode = bc_mode;
+        a.err = op->d_err;
+        cudaError_t e;
+        if (kprec == AFM_PREC_FP64)
+            e = launch_batched_fp64(s, a, op->sm_count, tr, ng, !first, st);
+        else if (kprec == AFM_PREC_FP64_SPLIT)
+            e = launch_batched_split(s, a, op->sm_count, tr, ng, !first, st);
+        else
+            e = launch_batched_fp32(s, a, op->sm_count, tr, ng, !first, st);
+        if (e != cudaSuccess) return fail(AFM_ERR_CUDA, "batched launch (n=%u, tr=%d, ng=%d): %s", s.n, tr, ng,
+                                          cudaGetErrorString(e));
+        first = false;
+    }
+    return AFM_SUCCESS;
+}
+
+int check_batched(afm_operator* op, uint32_t nrhs, uint32_t ld) {
+    if (!op->finalized) return fail(AFM_ERR_STATE, "batched product before finalize");
+    if (nrhs == 0 || nrhs > 256 || nrhs % 4 != 0 || ld < nrhs)
+        return fail(AFM_ERR_INVALID_ARG, "nrhs %u (multiple of 4, <= 256), ld %u", nrhs, ld);
+    for (const Segment& s : op->segs)
+        if (s.units && s.regime != REG_WPE)
+            return fail(AFM_NOT_IMPLEMENTED, "batched product needs elements with more than %u DoFs", kTpeMaxN);
+    if (op->dup_in_element) return fail(AFM_NOT_IMPLEMENTED, "batched product with a DoF listed twice in an element");
+    return AFM_SUCCESS;
+}
+
+// The project's autotuner: the first batched call for (nrhs, ld, arithmetic)
+// times every (columns per thread tile, element groups per CTA) candidate on
+// the caller's data, three runs each, and keeps the fastest for the operator.
+int batch_tuning(afm_operator* op, void* d_V, const void* d_U, uint32_t nrhs, uint32_t ld, bool f32, cudaStream_t st,
+                 int* tr, int* ng) {
+    const int kprec = f32 ? AFM_PREC_FP32 : op->precision;
+    const uint64_t key = ((uint64_t)nrhs << 40) | ((uint64_t)ld << 8) | (uint64_t)kprec;
+    for (const auto& t : op->batch_tune)
+        if (t.key == key) {
+            *tr = t.tr;
+            *ng = t.ng;
+            return AFM_SUCCESS;
+        }
+    std::vector<std::pair<int, int>> cand;
+    for (int g : {2, 3, 4}) cand.push_back({4, g});
+    if (kprec == AFM_PREC_FP32)
+        for (int g : {2, 4}) cand.push_back({8, g});
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 1e30f;
+    int btr = 4, bng = 2;
+    for (auto c : cand) {
+        if (nrhs % (uint32_t)c.first) continue;
+        int s = enqueue_matvec_batched(op, d_V, d_U, nrhs, ld, 0, st, f32, c.first, c.second);  // warm-up
+        if (s) {
+            g_last_error.clear();
+            continue;
+        }
+        cudaEventRecord(e0, st);
+        for (int r = 0; r < 3; r++) enqueue_matvec_batched(op, d_V, d_U, nrhs, ld, 0, st, f32, c.first, c.second);
+        cudaEventRecord(e1, st);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best) {
+            best = ms;
+            btr = c.first;
+            bng = c.second;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (best >= 1e30f) return fail(AFM_ERR_CUDA, "no batched kernel configuration runs");
+    op->batch_tune.push_back({key, btr, bng, best / 3.0f});
+    *tr = btr;
+    *ng = bng;
+    return AFM_SUCCESS;
+}
+
+template <typename T>
+int batched_product(afm_operator* op, T* d_V, const T* d_U, uint32_t nrhs, uint32_t ld, int bc_mode, void* stream) {
+    const bool f32 = std::is_same<T, float>::value;
+    int s = check_batched(op, nrhs, ld);
+    if (s) return s;
+    if (f32 && op->precision != AFM_PREC_FP32 && op->precision != AFM_PREC_FP64_SPLIT)
+        return fail(AFM_ERR_STATE, "FP32 product needs an FP32 or FP64_SPLIT operator");
+    if (!f32 && op->precision == AFM_PREC_FP32) return fail(AFM_ERR_STATE, "FP32 operator: use the _f32 entry");
+    if (!d_V || !d_U || (const void*)d_V == (const void*)d_U) return fail(AFM_ERR_INVALID_ARG, "bad blocks");
+    DeviceGuard g(op->device);
+    cudaStream_t st = pick_stream(op, stream);
+    int tr = 4, ng = 2;
+    s = batch_tuning(op, d_V, d_U, nrhs, ld, f32, st, &tr, &ng);
+    if (s) return s;
+    s = enqueue_matvec_batched(op, d_V, d_U, nrhs, ld, bc_mode, st, f32, tr, ng);
+    if (s) return s;
+    if (bc_mode) AFM_CUDA(launch_bset_constrained(d_V, d_U, op->d_bc_idx, op->n_bc, ld, nrhs, st));
+    return ok();
+}
+
+int ensure_bwork(afm_operator* op, size_t doubles) {
+    if (op->bwork_elems >= doubles) return AFM_SUCCESS;
+    cudaFree(op->d_bwork);
+    op->d_bwork = nullptr;
+    op->bwork_elems = 0;
+    AFM_CUDA(cudaMalloc((void**)&op->d_bwork, doubles * sizeof(double)));
+    op->bwork_elems = doubles;
+    return AFM_SUCCESS;
+}
+
+int ensure_bscalars(afm_operator* op, uint32_t nrhs) {
+    const size_t need = (size_t)nrhs * kBSlots + (size_t)kBBlocks * nrhs * 3;
+    if (op->bsc_elems < need) {
+        cudaFree(op->d_bsc);
+        op->d_bsc = nullptr;
+        op->bsc_elems = 0;
+        AFM_CUDA(cudaMalloc((void**)&op->d_bsc, need * sizeof(double)));
+        op->bsc_elems = need;
+    }
+    if (!op->d_bremain) AFM_CUDA(cudaMalloc((void**)&op->d_bremain, sizeof(unsigned int)));
+    if (!op->h_bremain) AFM_CUDA(cudaMallocHost((void**)&op->h_bremain, sizeof(unsigned int)));
+    return AFM_SUCCESS;
+}
+
+template <typename T>
+struct BVectors {
+    T *r, *z, *p, *q, *dinv, *x;
+};
+
+// Batched CG iterations after launch_bcg_init, as captured graphs of `batch`
+// steps; stops when the device counts no column still iterating.
+template <typename T>
+int run_bcg(afm_operator* op, const BVectors<T>& V, uint32_t R, double maxit, int tr, int ng, int* iters,
+            bool* breakdown = nullptr) {
+    cudaStream_t st = op->stream;
+    const size_t n = op->n_dofs;
+    double* sc = op->d_bsc;
+    double* part = op->d_bsc + (size_t)R * kBSlots;
+    unsigned int* remaining = op->d_bremain;
+    const bool f32 = std::is_same<T, float>::value;
+    const int batch = 4;
+    auto step = [&]() -> int {
+        int s = enqueue_matvec_batched(op, V.q, V.p, R, R, 1, st, f32, tr, ng);
+        if (s) return s;
+        AFM_CUDA(launch_bset_constrained(V.q, V.p, op->d_bc_idx, op->n_bc, R, R, st));
+        AFM_CUDA(launch_bcg_step_scalars(V.p, V.q, n, R, R, sc, part, st));
+        AFM_CUDA(launch_bcg_update(V.x, V.r, V.z, V.p, V.q, V.dinv, n, R, R, sc, part, maxit, remaining, st));
+        return AFM_SUCCESS;
+    };
+    afm_operator::CgGraph& gc = f32 ? op->bcg32 : op->bcg64;
+    const void* key[6] = {V.r, V.x, V.q, (const void*)(uintptr_t)R, (const void*)(uintptr_t)(tr * 16 + ng),
+                          (const void*)(uintptr_t)maxit};
+    bool same = gc.exec && gc.gen == op->generation;
+    for (int i = 0; i < 6 && same; i++) same = (gc.key[i] == key[i]);
+    if (!same) {
+        drop_graph(gc);
+        AFM_CUDA(cudaStreamSynchronize(st));
+        AFM_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        int s = AFM_SUCCESS;
+        for (int i = 0; i < batch && s == AFM_SUCCESS; i++) s = step();
+        if (s == AFM_SUCCESS && cudaMemcpyAsync(op->h_bremain, remaining, sizeof(unsigned int),
+                                                cudaMemcpyDeviceToHost, st) != cudaSuccess)
+            s = fail(AFM_ERR_CUDA, "capture: counter copy");
+        cudaGraph_t graph = nullptr;
+        const cudaError_t ec = cudaStreamEndCapture(st, &graph);
+        if (s != AFM_SUCCESS) {
+            if (graph) cudaGraphDestroy(graph);
+            return s;
+        }
+        if (ec != cudaSuccess) return fail(AFM_ERR_CUDA, "stream capture: %s", cudaGetErrorString(ec));
+        const cudaError_t ei = cudaGraphInstantiate(&gc.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ei != cudaSuccess) {
+            gc.exec = nullptr;
+            return fail(AFM_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ei));
+        }
+        gc.batch = batch;
+        gc.gen = op->generation;
+        for (int i = 0; i < 6; i++) gc.key[i] = key[i];
+    }
+    for (;;) {
+        AFM_CUDA(cudaGraphLaunch(gc.exec, st));
+        AFM_CUDA(cudaStreamSynchronize(st));
+        if (*op->h_bremain == 0) break;
+    }
+    std::vector<double> h((size_t)R * kBSlots);
+    AFM_CUDA(cudaMemcpy(h.data(), sc, h.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    int it = 0;
+    bool flag = false;
+    for (uint32_t j = 0; j < R; j++) {
+        it = std::max(it, (int)h[(size_t)j * kBSlots + B_ITER]);
+        flag = flag || h[(size_t)j * kBSlots + B_FLAG] != 0.0;
+    }
+    *iters = it;
+    if (breakdown) *breakdown = flag;
+    return AFM_SUCCESS;
+}
+
+// max over columns of ||b_j - A x_j|| / ||b_j|| in FP64 (split or FP64 arena)
+int batched_residual(afm_operator* op, const double* d_B, const double* d_X, uint32_t R, double* q, double* worst,
+                     int tr64, int ng64) {
+    cudaStream_t st = op->stream;
+    const size_t n = op->n_dofs;
+    int s = enqueue_matvec_batched(op, q, d_X, R, R, 1, st, false, tr64, ng64);
+    if (s) return s;
+    AFM_CUDA(launch_bset_constrained(q, d_X, op->d_bc_idx, op->n_bc, R, R, st));
+    AFM_CUDA(launch_axpby(q, d_B, 1.0, -1.0, n * R, st));  // q = b - A x
+    double* part = op->d_bsc + (size_t)R * kBSlots;
+    AFM_CUDA(launch_bnorm2(q, n, R, R, part, st));
+    std::vector<double> hp((size_t)kBBlocks * R), hb((size_t)kBBlocks * R);
+    AFM_CUDA(cudaMemcpyAsync(hp.data(), part, hp.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    AFM_CUDA(launch_bnorm2(d_B, n, R, R, part, st));
+    AFM_CUDA(cudaMemcpyAsync(hb.data(), part, hb.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    AFM_CUDA(cudaStreamSynchronize(st));
+    double w = 0.0;
+    for (uint32_t j = 0; j < R; j++) {
+        double rr = 0.0, bb = 0.0;
+        for (int b = 0; b < kBBlocks; b++) {
+            rr += hp[(size_t)b * R + j];
+            bb += hb[(size_t)b * R + j];
+        }
+        w = std::max(w, bb > 0 ? std::sqrt(rr / bb) : std::sqrt(rr));
+    }
+    *worst = w;
+    return AFM_SUCCESS;
+}
+
+
+// CG work vectors: residual r, preconditioned z, direction p, product q,
+// inverse diagonal, iterate x.
+template <typename T>
+struct CgVectors {
+    T *r, *z, *p, *q, *dinv, *x;
+};
+
+template <typename T>
+int cg_step(afm_operator* op, const CgVectors<T>& V, cudaStream_t st);
+template <>
+int cg_step<double>(afm_operator* op, const CgVectors<double>& V, cudaStream_t st) {
+    int s = enqueue_matvec(op, V.q, V.p, 1, st);
+    if (s) return s;
+    AFM_CUDA(launch_set_constrained(V.q, V.p, op->d_bc_idx, op->n_bc, st));
+    double* sc = op->d_scalars;
+    double* part = sc + kScalarSlots;
+    AFM_CUDA(launch_cg_alpha(V.p, V.q, op->n_dofs, sc, part, st));
+    AFM_CUDA(launch_cg_update(V.x, V.r, V.z, V.p, V.q, V.dinv, op->n_dofs, sc, part, st));
+    return AFM_SUCCESS;
+}
+template <>
+int cg_step<float>(afm_operator* op, const CgVectors<float>& V, cudaStream_t st) {
+    int s = enqueue_matvec(op, V.q, V.p, 1, st, true);
+    if (s) return s;
+    AFM_CUDA(launch_set_constrained(V.q, V.p, op->d_bc_idx, op->n_bc, st));
+    double* sc = op->d_scalars;
+    double* part = sc + kScalarSlots;
+    AFM_CUDA(launch_cg_alpha(V.p, V.q, op->n_dofs, sc, part, st));
+    AFM_CUDA(launch_cg_update(V.x, V.r, V.z, V.p, V.q, V.dinv, op->n_dofs, sc, part, st));
+    return AFM_SUCCESS;
+}
+
+void drop_graph(afm_operator::CgGraph& g) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    g = afm_operator::CgGraph();
+}
+
+// Runs CG iterations after launch_cg_init until the device marks the solve
+// done (monitored norm <= tol, maxit iterations, or breakdown). The iterations
+// run as a captured CUDA graph of `batch` steps followed by a copy of the
+// scalars to the pinned host mirror: one host round trip per batch instead of
+// one per iteration. Steps after convergence leave every vector unchanged, so
+// the result equals the iteration-by-iteration loop.
+template <typename T>
+int run_cg_iterations(afm_operator* op, afm_operator::CgGraph& gc, const CgVectors<T>& V, double tol, int maxit,
+                      int norm_type, int* iters, int* status) {
+    cudaStream_t st = op->stream;
+    double* h = op->h_scalars;
+    const double n0 = std::sqrt(norm_type ? h[S_ZZ] : h[S_RR]);
+    *iters = 0;
+    if (h[S_FLAG] != 0.0 || std::isnan(n0)) {
+        *status = AFM_ERR_BREAKDOWN;
+        return AFM_SUCCESS;
+    }
+    if (n0 <= tol) {
+        *status = AFM_SUCCESS;
+        return AFM_SUCCESS;
+    }
+    if (maxit <= 0) {
+        *status = AFM_ERR_MAXIT;
+        return AFM_SUCCESS;
+    }
+    // solver controls (device copies of tol, maxit, norm)
+    h[S_TOL] = tol;
+    h[S_MAXIT] = (double)maxit;
+    h[S_NORM] = (double)norm_type;
+    AFM_CUDA(cudaMemcpyAsync(op->d_scalars + S_DONE, h + S_DONE, sizeof(double) * (S_NORM - S_DONE + 1),
+                             cudaMemcpyHostToDevice, st));
+    const int batch = op->n_dofs > (1u << 20) ? 4 : 8;
+    const void* key[6] = {V.r, V.z, V.p, V.q, V.dinv, V.x};
+    bool same = gc.exec && gc.batch == batch && gc.gen == op->generation;
+    for (int i = 0; i < 6 && same; i++) same = (gc.key[i] == key[i]);
+    if (!same) {
+        drop_graph(gc);
+        AFM_CUDA(cudaStreamSynchronize(st));
+        AFM_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        int s = AFM_SUCCESS;
+        for (int i = 0; i < batch && s == AFM_SUCCESS; i++) s = cg_step<T>(op, V, st);
+        if (s == AFM_SUCCESS && cudaMemcpyAsync(h, op->d_scalars, sizeof(double) * kScalarSlots,
+                                                cudaMemcpyDeviceToHost, st) != cudaSuccess)
+            s = fail(AFM_ERR_CUDA, "capture: scalar copy");
+        cudaGraph_t graph = nullptr;
+        const cudaError_t ec = cudaStreamEndCapture(st, &graph);
+        if (s != AFM_SUCCESS) {
+            if (graph) cudaGraphDestroy(graph);
+            return s;
+        }
+        if (ec != cudaSuccess) return fail(AFM_ERR_CUDA, "stream capture: %s", cudaGetErrorString(ec));
+        const cudaError_t ei = cudaGraphInstantiate(&gc.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ei != cudaSuccess) {
+            gc.exec = nullptr;
+            return fail(AFM_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ei));
+        }
+        gc.batch = batch;
+        gc.gen = op->generation;
+        for (int i = 0; i < 6; i++) gc.key[i] = key[i];
+    }
+    for (;;) {
+        AFM_CUDA(cudaGraphLaunch(gc.exec, st));
+        AFM_CUDA(cudaStreamSynchronize(st));
+        if (h[S_DONE] != 0.0) break;
+    }
+    *iters = (int)h[S_ITER];
+    const double nrm = std::sqrt(norm_type ? h[S_ZZ] : h[S_RR]);
+    if (h[S_FLAG] != 0.0)
+        *status = AFM_ERR_BREAKDOWN;
+    else if (nrm <= tol)
+        *status = AFM_SUCCESS;
+    else
+        *status = AFM_ERR_MAXIT;
+    return AFM_SUCCESS;
 }
 
 }  // namespace
@@ -354,6 +781,10 @@ int afm_create(afm_operator** out, int bc_method, int device) {
         return fail(AFM_ERR_CUDA, "device %d is sm_%d%d; this library is built for sm_103a only", device,
                     prop.major, prop.minor);
     DeviceGuard g(device);
+    // kernels' shared-memory limits, before any launch or graph capture
+    if (configure_kernels_fp64() != cudaSuccess || configure_kernels_split() != cudaSuccess ||
+        configure_kernels_fp32() != cudaSuccess)
+        return fail(AFM_ERR_CUDA, "kernel configuration failed on device %d", device);
     auto* op = new afm_operator();
     op->device = device;
     op->bc_method = bc_method;
@@ -379,7 +810,9 @@ int afm_destroy(afm_operator* op) {
         free_device(op);
         cudaFree(op->d_err);
         cudaFree(op->d_scalars);
+        cudaFree(op->d_bremain);
         if (op->h_scalars) cudaFreeHost(op->h_scalars);
+        if (op->h_bremain) cudaFreeHost(op->h_bremain);
         if (op->stream) cudaStreamDestroy(op->stream);
     }
     delete op;
@@ -556,9 +989,17 @@ int afm_finalize(afm_operator* op) {
         if (s.regime == REG_TPE) {
             s.units = (s.count + kTpeWidth - 1) / kTpeWidth;
             s.unit_bytes = round16((uint64_t)s.n * s.n * eb * kTpeWidth);
+            if (prec == AFM_PREC_FP64_SPLIT) {
+                s.plane = s.n * s.n * kTpeWidth;
+                s.unit_bytes = 2ull * s.plane * 4;
+            }
         } else {
             s.units = s.count;
             s.unit_bytes = round16((uint64_t)s.n * s.n * eb);
+            if (prec == AFM_PREC_FP64_SPLIT) {
+                s.plane = (s.n * s.n + 3) / 4 * 4;  // 16-byte aligned planes
+                s.unit_bytes = 2ull * s.plane * 4;
+            }
         }
         s.ke_offset = ke_off;
         s.map_offset = map_off;
@@ -648,10 +1089,11 @@ int afm_matvec_device(afm_operator* op, double* d_v, const double* d_u, void* st
 int afm_matvec_device_f32(afm_operator* op, float* d_v, const float* d_u, void* stream) {
     AFM_CHECK_OP(op);
     if (!op->finalized) return fail(AFM_ERR_STATE, "matvec before finalize");
-    if (op->precision != AFM_PREC_FP32) return fail(AFM_ERR_STATE, "operator is not FP32");
+    if (op->precision != AFM_PREC_FP32 && op->precision != AFM_PREC_FP64_SPLIT)
+        return fail(AFM_ERR_STATE, "FP32 product needs an FP32 or FP64_SPLIT operator");
     if (!d_v || !d_u || (void*)d_v == (const void*)d_u) return fail(AFM_ERR_INVALID_ARG, "bad vectors");
     DeviceGuard g(op->device);
-    int s = enqueue_matvec(op, d_v, d_u, 0, pick_stream(op, stream));
+    int s = enqueue_matvec(op, d_v, d_u, 0, pick_stream(op, stream), true);
     return s == AFM_SUCCESS ? ok() : s;
 }
 
@@ -704,6 +1146,20 @@ int afm_matmult_bc(afm_operator* op, double* v, const double* u) {
     AFM_CUDA(cudaMemcpyAsync(v, dv, bytes, cudaMemcpyDeviceToHost, op->stream));
     s = check_device_error(op);
     return s == AFM_SUCCESS ? ok() : s;
+}
+
+int afm_matmult_bc_device_f32(afm_operator* op, float* d_v, const float* d_u, void* stream) {
+    AFM_CHECK_OP(op);
+    if (!op->finalized) return fail(AFM_ERR_STATE, "matmult before finalize");
+    if (op->precision != AFM_PREC_FP32 && op->precision != AFM_PREC_FP64_SPLIT)
+        return fail(AFM_ERR_STATE, "FP32 product needs an FP32 or FP64_SPLIT operator");
+    if (!d_v || !d_u || (void*)d_v == (const void*)d_u) return fail(AFM_ERR_INVALID_ARG, "bad vectors");
+    DeviceGuard g(op->device);
+    cudaStream_t st = pick_stream(op, stream);
+    int s = enqueue_matvec(op, d_v, d_u, 1, st, true);
+    if (s) return s;
+    AFM_CUDA(launch_set_constrained(d_v, d_u, op->d_bc_idx, op->n_bc, st));
+    return ok();
 }
 
 int afm_get_diagonal(afm_operator* op, double* diag) {
@@ -760,11 +1216,8 @@ int afm_solve_cg_device(afm_operator* op, const double* d_b, double* d_x, double
     int s = ensure_work(op, 8);
     if (s) return s;
     const size_t n = op->n_dofs;
-    double* r = op->d_work + 2 * n;
-    double* z = op->d_work + 3 * n;
-    double* p = op->d_work + 4 * n;
-    double* q = op->d_work + 5 * n;
-    double* dinv = op->d_work + 6 * n;
+    CgVectors<double> V{op->d_work + 2 * n, op->d_work + 3 * n, op->d_work + 4 * n, op->d_work + 5 * n,
+                        op->d_work + 6 * n, d_x};
     double* sc = op->d_scalars;
     double* part = op->d_scalars + kScalarSlots;
     cudaStream_t st = op->stream;
@@ -772,48 +1225,28 @@ int afm_solve_cg_device(afm_operator* op, const double* d_b, double* d_x, double
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     cudaEventRecord(e0, st);
-    AFM_CUDA(launch_invert(dinv, op->d_diag, n, st));
-    s = afm_matmult_bc_device(op, q, d_x, st);
+    AFM_CUDA(launch_invert(V.dinv, op->d_diag, n, st));
+    s = afm_matmult_bc_device(op, V.q, d_x, st);
     if (s) return s;
-    AFM_CUDA(launch_cg_init(d_b, q, dinv, r, z, p, n, sc, part, st));
+    AFM_CUDA(launch_cg_init(d_b, V.q, V.dinv, V.r, V.z, V.p, n, sc, part, st));
     AFM_CUDA(cudaMemcpyAsync(op->h_scalars, sc, sizeof(double) * kScalarSlots, cudaMemcpyDeviceToHost, st));
     AFM_CUDA(cudaStreamSynchronize(st));
     const double bn = std::sqrt(op->h_scalars[S_BB]);
     const double ref = (norm_type == AFM_CG_NORM_UNPRECONDITIONED) ? bn : std::sqrt(op->h_scalars[S_DB]);
     const double tol = std::max(rtol * ref, atol);
     int it = 0, status = AFM_ERR_MAXIT;
-    double rn = 0.0;
-    for (;;) {
-        const double* h = op->h_scalars;
-        rn = std::sqrt(norm_type == AFM_CG_NORM_UNPRECONDITIONED ? h[S_RR] : h[S_ZZ]);
-        if (h[S_FLAG] != 0.0 || std::isnan(rn)) {
-            status = AFM_ERR_BREAKDOWN;
-            break;
-        }
-        if (rn <= tol) {
-            status = AFM_SUCCESS;
-            break;
-        }
-        if (it >= maxit) break;
-        s = afm_matmult_bc_device(op, q, p, st);
-        if (s) return s;
-        AFM_CUDA(launch_cg_alpha(p, q, n, sc, part, st));
-        AFM_CUDA(launch_cg_update(d_x, r, z, p, q, dinv, n, sc, part, st));
-        AFM_CUDA(cudaMemcpyAsync(op->h_scalars, sc, sizeof(double) * kScalarSlots, cudaMemcpyDeviceToHost, st));
-        AFM_CUDA(cudaStreamSynchronize(st));
-        it++;
-    }
+    s = run_cg_iterations<double>(op, op->cg64, V, tol, maxit, norm_type, &it, &status);
+    if (s) return s;
     cudaEventRecord(e1, st);
     // true residual in FP64
-    s = afm_matmult_bc_device(op, q, d_x, st);
+    s = afm_matmult_bc_device(op, V.q, d_x, st);
     if (s) return s;
-    AFM_CUDA(launch_axpby(q, d_b, 1.0, -1.0, n, st));  // q = b - A x
-    AFM_CUDA(launch_dots(q, q, n, part, st));
-    std::vector<double> hp(kRedBlocks);
-    AFM_CUDA(cudaMemcpyAsync(hp.data(), part, sizeof(double) * kRedBlocks, cudaMemcpyDeviceToHost, st));
+    AFM_CUDA(launch_axpby(V.q, d_b, 1.0, -1.0, n, st));  // q = b - A x
+    AFM_CUDA(launch_norm2(V.q, n, sc, part, st));
+    AFM_CUDA(cudaMemcpyAsync(op->h_scalars, sc, sizeof(double) * kScalarSlots, cudaMemcpyDeviceToHost, st));
     AFM_CUDA(cudaStreamSynchronize(st));
-    double rr = 0.0;
-    for (double t : hp) rr += t;
+    const double rr = op->h_scalars[S_PQ];
+    const double rn = std::sqrt(norm_type == AFM_CG_NORM_UNPRECONDITIONED ? op->h_scalars[S_RR] : op->h_scalars[S_ZZ]);
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);
     cudaEventDestroy(e0);
@@ -851,6 +1284,327 @@ int afm_solve_cg(afm_operator* op, const double* b, double* x, double rtol, doub
     AFM_CUDA(cudaMemcpyAsync(x, dx, bytes, cudaMemcpyDeviceToHost, op->stream));
     AFM_CUDA(cudaStreamSynchronize(op->stream));
     if (st != AFM_SUCCESS) return fail(st, "%s", msg.c_str());
+    return ok();
+}
+
+// Iterative-refinement stopping rule. The FP64 residual of the refined x may
+// grow for a step before it falls (an FP32 correction that shrinks the error
+// can overshoot in the residual norm), so refinement stops only after
+// kIrMaxStall consecutive steps without a new smallest residual.
+constexpr int kIrMaxStall = 3;
+
+static bool ir_progress(double rn, double* best, int* stall) {
+    if (rn < *best) {
+        *best = rn;
+        *stall = 0;
+        return true;
+    }
+    return ++*stall < kIrMaxStall;
+}
+
+int afm_solve_cg_mixed_device(afm_operator* op, const double* d_b, double* d_x, double rtol, double atol,
+                              int max_outer, double inner_rtol, int max_inner, afm_solve_stats* stats) {
+    AFM_CHECK_OP(op);
+    if (!op->finalized) return fail(AFM_ERR_STATE, "solve before finalize");
+    if (op->precision != AFM_PREC_FP64_SPLIT)
+        return fail(AFM_ERR_STATE, "mixed-precision solve needs the FP64_SPLIT arena (hi plane = FP32 matrix)");
+    if (!d_b || !d_x) return fail(AFM_ERR_INVALID_ARG, "null vector");
+    DeviceGuard g(op->device);
+    int s = ensure_work(op, 8);
+    if (s) return s;
+    s = ensure_work32(op, 7);
+    if (s) return s;
+    const size_t n = op->n_dofs;
+    double* r64 = op->d_work + 2 * n;
+    double* q64 = op->d_work + 5 * n;
+    float* b32 = op->d_work32;
+    CgVectors<float> V{b32 + n, b32 + 2 * n, b32 + 3 * n, b32 + 4 * n, b32 + 6 * n, b32 + 5 * n};
+    double* sc = op->d_scalars;
+    double* part = op->d_scalars + kScalarSlots;
+    double* h = op->h_scalars;
+    cudaStream_t st = op->stream;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, st);
+    AFM_CUDA(launch_invert(V.dinv, op->d_diag, n, st));
+    AFM_CUDA(cudaMemsetAsync(V.x, 0, n * sizeof(float), st));
+    AFM_CUDA(launch_norm2(d_b, n, sc, part, st));
+    AFM_CUDA(cudaMemcpyAsync(h, sc, sizeof(double) * kScalarSlots, cudaMemcpyDeviceToHost, st));
+    AFM_CUDA(cudaStreamSynchronize(st));
+    const double bn = std::sqrt(h[S_PQ]);
+    const double tol = std::max(rtol * bn, atol);
+    int outer = 0, inner_total = 0, status = AFM_ERR_MAXIT, stall = 0;
+    double rn = 0.0, best = HUGE_VAL;
+    for (;;) {
+        // outer residual r = b - A x in FP64 (split arena, MatMult_mf semantics)
+        s = afm_matmult_bc_device(op, q64, d_x, st);
+        if (s) return s;
+        AFM_CUDA(cudaMemcpyAsync(r64, d_b, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+        AFM_CUDA(launch_axpby(r64, q64, -1.0, 1.0, n, st));
+        AFM_CUDA(launch_norm2(r64, n, sc, part, st));
+        AFM_CUDA(cudaMemcpyAsync(h, sc, sizeof(double) * kScalarSlots, cudaMemcpyDeviceToHost, st));
+        AFM_CUDA(cudaStreamSynchronize(st));
+        rn = std::sqrt(h[S_PQ]);
+        if (std::isnan(rn)) {
+            status = AFM_ERR_BREAKDOWN;
+            break;
+        }
+        if (rn <= tol) {
+            status = AFM_SUCCESS;
+            break;
+        }
+        if (!ir_progress(rn, &best, &stall) || outer >= max_outer) break;  // MAXIT
+        // inner FP32 Jacobi-PCG on A d = r from d = 0, FP64 dots and scalars
+        AFM_CUDA(launch_to_f32(b32, r64, n, st));
+        AFM_CUDA(cudaMemsetAsync(V.q, 0, n * sizeof(float), st));
+        AFM_CUDA(launch_cg_init(b32, V.q, V.dinv, V.r, V.z, V.p, n, sc, part, st));
+        AFM_CUDA(cudaMemcpyAsync(h, sc, sizeof(double) * kScalarSlots, cudaMemcpyDeviceToHost, st));
+        AFM_CUDA(cudaStreamSynchronize(st));
+        int it = 0, ist = 0;
+        s = run_cg_iterations<float>(op, op->cg32, V, inner_rtol * std::sqrt(h[S_BB]), max_inner, 0, &it, &ist);
+        if (s) return s;
+        inner_total += it;
+        AFM_CUDA(launch_add_f32(d_x, V.x, n, st));  // x += d, d = 0
+        outer++;
+    }
+    cudaEventRecord(e1, st);
+    AFM_CUDA(cudaStreamSynchronize(st));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    s = check_device_error(op);
+    if (s) return s;
+    if (stats) {
+        stats->iterations = inner_total;
+        stats->status = status;
+        stats->rel_residual = bn > 0 ? rn / bn : rn;
+        stats->residual_norm = rn;
+        stats->seconds = ms * 1e-3;
+        stats->refinements = outer;
+    }
+    if (status != AFM_SUCCESS)
+        return fail(status, status == AFM_ERR_MAXIT ? "refinement stopped after %d steps" : "breakdown after %d steps",
+                    outer);
+    return ok();
+}
+
+int afm_solve_cg_mixed(afm_operator* op, const double* b, double* x, double rtol, double atol, int max_outer,
+                       double inner_rtol, int max_inner, afm_solve_stats* stats) {
+    AFM_CHECK_OP(op);
+    if (!op->finalized) return fail(AFM_ERR_STATE, "solve before finalize");
+    if (!b || !x) return fail(AFM_ERR_INVALID_ARG, "null vector");
+    DeviceGuard g(op->device);
+    int s = ensure_work(op, 8);
+    if (s) return s;
+    double* db = op->d_work;
+    double* dx = op->d_work + op->n_dofs;
+    const size_t bytes = sizeof(double) * op->n_dofs;
+    AFM_CUDA(cudaMemcpyAsync(db, b, bytes, cudaMemcpyHostToDevice, op->stream));
+    AFM_CUDA(cudaMemcpyAsync(dx, x, bytes, cudaMemcpyHostToDevice, op->stream));
+    const int st = afm_solve_cg_mixed_device(op, db, dx, rtol, atol, max_outer, inner_rtol, max_inner, stats);
+    const std::string msg = g_last_error;
+    AFM_CUDA(cudaMemcpyAsync(x, dx, bytes, cudaMemcpyDeviceToHost, op->stream));
+    AFM_CUDA(cudaStreamSynchronize(op->stream));
+    if (st != AFM_SUCCESS) return fail(st, "%s", msg.c_str());
+    return ok();
+}
+
+int afm_matvec_batched_device(afm_operator* op, double* d_V, const double* d_U, uint32_t nrhs, uint32_t ld,
+                              void* stream) {
+    AFM_CHECK_OP(op);
+    return batched_product<double>(op, d_V, d_U, nrhs, ld, 0, stream);
+}
+
+int afm_matvec_batched_device_f32(afm_operator* op, float* d_V, const float* d_U, uint32_t nrhs, uint32_t ld,
+                                  void* stream) {
+    AFM_CHECK_OP(op);
+    return batched_product<float>(op, d_V, d_U, nrhs, ld, 0, stream);
+}
+
+int afm_matmult_bc_batched_device(afm_operator* op, double* d_V, const double* d_U, uint32_t nrhs, uint32_t ld,
+                                  void* stream) {
+    AFM_CHECK_OP(op);
+    return batched_product<double>(op, d_V, d_U, nrhs, ld, 1, stream);
+}
+
+int afm_matmult_bc_batched_device_f32(afm_operator* op, float* d_V, const float* d_U, uint32_t nrhs, uint32_t ld,
+                                      void* stream) {
+    AFM_CHECK_OP(op);
+    return batched_product<float>(op, d_V, d_U, nrhs, ld, 1, stream);
+}
+
+int afm_get_batch_tuning(afm_operator* op, uint32_t nrhs, uint32_t ld, int f32, int* cols_per_thread,
+                         int* groups_per_cta, float* ms) {
+    AFM_CHECK_OP(op);
+    const int kprec = f32 ? AFM_PREC_FP32 : op->precision;
+    const uint64_t key = ((uint64_t)nrhs << 40) | ((uint64_t)ld << 8) | (uint64_t)kprec;
+    for (const auto& t : op->batch_tune)
+        if (t.key == key) {
+            if (cols_per_thread) *cols_per_thread = t.tr;
+            if (groups_per_cta) *groups_per_cta = t.ng;
+            if (ms) *ms = t.ms;
+            return ok();
+        }
+    return fail(AFM_ERR_STATE, "no batched call with nrhs %u yet", nrhs);
+}
+
+int afm_set_batch_tuning(afm_operator* op, uint32_t nrhs, uint32_t ld, int f32, int cols_per_thread,
+                         int groups_per_cta) {
+    AFM_CHECK_OP(op);
+    if (!op->finalized) return fail(AFM_ERR_STATE, "before finalize");
+    if ((cols_per_thread != 4 && cols_per_thread != 8) || groups_per_cta < 1 || groups_per_cta > 4 ||
+        nrhs % (uint32_t)cols_per_thread)
+        return fail(AFM_ERR_INVALID_ARG, "tile %d x groups %d for nrhs %u", cols_per_thread, groups_per_cta, nrhs);
+    const int kprec = f32 ? AFM_PREC_FP32 : op->precision;
+    const uint64_t key = ((uint64_t)nrhs << 40) | ((uint64_t)ld << 8) | (uint64_t)kprec;
+    for (auto& t : op->batch_tune)
+        if (t.key == key) {
+            t.tr = cols_per_thread;
+            t.ng = groups_per_cta;
+            return ok();
+        }
+    op->batch_tune.push_back({key, cols_per_thread, groups_per_cta, 0.0f});
+    return ok();
+}
+
+int afm_solve_cg_batched_device(afm_operator* op, const double* d_B, double* d_X, uint32_t nrhs, double rtol,
+                                double atol, int maxit, afm_solve_stats* stats) {
+    AFM_CHECK_OP(op);
+    int s = check_batched(op, nrhs, nrhs);
+    if (s) return s;
+    if (op->precision == AFM_PREC_FP32) return fail(AFM_ERR_STATE, "FP32 operator");
+    if (!d_B || !d_X) return fail(AFM_ERR_INVALID_ARG, "null block");
+    DeviceGuard g(op->device);
+    const size_t n = op->n_dofs, N = n * nrhs;
+    s = ensure_bwork(op, 4 * N + n);
+    if (s) return s;
+    s = ensure_bscalars(op, nrhs);
+    if (s) return s;
+    BVectors<double> V{op->d_bwork, op->d_bwork + N, op->d_bwork + 2 * N, op->d_bwork + 3 * N, op->d_bwork + 4 * N,
+                       d_X};
+    cudaStream_t st = op->stream;
+    int tr = 4, ng = 2;
+    s = batch_tuning(op, V.q, d_X, nrhs, nrhs, false, st, &tr, &ng);
+    if (s) return s;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, st);
+    AFM_CUDA(launch_invert(V.dinv, op->d_diag, n, st));
+    s = enqueue_matvec_batched(op, V.q, d_X, nrhs, nrhs, 1, st, false, tr, ng);
+    if (s) return s;
+    AFM_CUDA(launch_bset_constrained(V.q, d_X, op->d_bc_idx, op->n_bc, nrhs, nrhs, st));
+    AFM_CUDA(launch_bcg_init(d_B, V.q, V.dinv, V.r, V.z, V.p, n, nrhs, nrhs, op->d_bsc,
+                             op->d_bsc + (size_t)nrhs * kBSlots, rtol, atol, st));
+    int it = 0;
+    bool breakdown = false;
+    s = run_bcg<double>(op, V, nrhs, (double)maxit, tr, ng, &it, &breakdown);
+    if (s) return s;
+    cudaEventRecord(e1, st);
+    double worst = 0.0;
+    s = batched_residual(op, d_B, d_X, nrhs, V.q, &worst, tr, ng);
+    if (s) return s;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    s = check_device_error(op);
+    if (s) return s;
+    const int status = breakdown ? AFM_ERR_BREAKDOWN : (it < maxit || worst <= rtol) ? AFM_SUCCESS : AFM_ERR_MAXIT;
+    if (stats) {
+        stats->iterations = it;
+        stats->status = status;
+        stats->rel_residual = worst;
+        stats->residual_norm = worst;
+        stats->seconds = ms * 1e-3;
+        stats->refinements = 0;
+    }
+    if (status != AFM_SUCCESS)
+        return fail(status, status == AFM_ERR_MAXIT ? "batched CG reached maxit=%d" : "batched CG breakdown (maxit %d)",
+                    maxit);
+    return ok();
+}
+
+int afm_solve_cg_batched_mixed_device(afm_operator* op, const double* d_B, double* d_X, uint32_t nrhs, double rtol,
+                                      double atol, int max_outer, double inner_rtol, int max_inner,
+                                      afm_solve_stats* stats) {
+    AFM_CHECK_OP(op);
+    int s = check_batched(op, nrhs, nrhs);
+    if (s) return s;
+    if (op->precision != AFM_PREC_FP64_SPLIT)
+        return fail(AFM_ERR_STATE, "mixed-precision solve needs the FP64_SPLIT arena (hi plane = FP32 matrix)");
+    if (!d_B || !d_X) return fail(AFM_ERR_INVALID_ARG, "null block");
+    DeviceGuard g(op->device);
+    const size_t n = op->n_dofs, N = n * nrhs;
+    // FP64: residual block and product block; FP32: rhs, r, z, p, q, d and 1/diag
+    s = ensure_bwork(op, 2 * N + (7 * N + n + 1) / 2 + 2);
+    if (s) return s;
+    s = ensure_bscalars(op, nrhs);
+    if (s) return s;
+    double* r64 = op->d_bwork;
+    double* q64 = op->d_bwork + N;
+    float* f = reinterpret_cast<float*>(op->d_bwork + 2 * N);
+    float* b32 = f;
+    BVectors<float> V{f + N, f + 2 * N, f + 3 * N, f + 4 * N, f + 6 * N, f + 5 * N};
+    cudaStream_t st = op->stream;
+    int tr64 = 4, ng64 = 2, tr32 = 4, ng32 = 2;
+    s = batch_tuning(op, q64, d_X, nrhs, nrhs, false, st, &tr64, &ng64);
+    if (s) return s;
+    AFM_CUDA(launch_to_f32(b32, d_B, N, st));
+    s = batch_tuning(op, V.q, b32, nrhs, nrhs, true, st, &tr32, &ng32);
+    if (s) return s;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, st);
+    AFM_CUDA(launch_invert(V.dinv, op->d_diag, n, st));
+    AFM_CUDA(cudaMemsetAsync(V.x, 0, N * sizeof(float), st));
+    int outer = 0, inner_total = 0, status = AFM_ERR_MAXIT, stall = 0;
+    double worst = 0.0, best = HUGE_VAL;
+    for (;;) {
+        // FP64 residual block R = B - A X and the worst column's relative norm
+        s = batched_residual(op, d_B, d_X, nrhs, q64, &worst, tr64, ng64);
+        if (s) return s;
+        if (std::isnan(worst)) {
+            status = AFM_ERR_BREAKDOWN;
+            break;
+        }
+        if (worst <= rtol) {
+            status = AFM_SUCCESS;
+            break;
+        }
+        if (!ir_progress(worst, &best, &stall) || outer >= max_outer) break;  // MAXIT
+        AFM_CUDA(cudaMemcpyAsync(r64, q64, N * sizeof(double), cudaMemcpyDeviceToDevice, st));
+        AFM_CUDA(launch_to_f32(b32, r64, N, st));
+        AFM_CUDA(cudaMemsetAsync(V.q, 0, N * sizeof(float), st));
+        AFM_CUDA(launch_bcg_init(b32, V.q, V.dinv, V.r, V.z, V.p, n, nrhs, nrhs, op->d_bsc,
+                                 op->d_bsc + (size_t)nrhs * kBSlots, inner_rtol, 0.0, st));
+        int it = 0;
+        s = run_bcg<float>(op, V, nrhs, (double)max_inner, tr32, ng32, &it);
+        if (s) return s;
+        inner_total += it;
+        AFM_CUDA(launch_add_f32(d_X, V.x, N, st));  // X += D, D = 0
+        outer++;
+    }
+    cudaEventRecord(e1, st);
+    AFM_CUDA(cudaStreamSynchronize(st));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    s = check_device_error(op);
+    if (s) return s;
+    if (stats) {
+        stats->iterations = inner_total;
+        stats->status = status;
+        stats->rel_residual = worst;
+        stats->residual_norm = worst;
+        stats->seconds = ms * 1e-3;
+        stats->refinements = outer;
+    }
+    if (status != AFM_SUCCESS) return fail(status, "batched refinement stopped after %d steps", outer);
     return ok();
 }
 

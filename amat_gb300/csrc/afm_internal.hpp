@@ -39,6 +39,7 @@ struct Segment {
     uint64_t ke_offset = 0;   // byte offset of the first unit in the Ke arena
     uint64_t unit_bytes = 0;  // arena bytes per unit (16-byte multiple)
     uint64_t map_offset = 0;  // uint32 offset of the first unit in the map
+    uint32_t plane = 0;       // FP64_SPLIT: entries per plane of a unit (the lo plane follows the hi plane)
 };
 
 // Arguments of one segment launch.
@@ -49,26 +50,39 @@ struct SegArgs {
     void* v;                  // double* or float*
     uint32_t units;
     uint32_t count;           // elements (TPE: last unit may be partial)
-    uint64_t unit_bytes;
+    uint64_t unit_bytes;      // stride between units in the arena
+    uint32_t copy_bytes;      // bytes copied per unit (the hi plane only for FP32 on a split arena)
+    uint32_t plane;           // entries per plane (split arena)
     int bc_mode;              // 1: constrained columns read as zero (MatMult_mf)
     int* err;
 };
 
+// Arguments of one batched (multi right-hand side) segment launch.
+struct BatchArgs {
+    const unsigned char* ke;
+    const uint32_t* map;
+    const void* u;  // n_dofs x ld, row-major
+    void* v;
+    uint32_t units, count;
+    uint64_t unit_bytes;
+    uint32_t copy_bytes, plane;
+    uint32_t nrhs, ld;
+    int bc_mode;
+    int* err;
+};
+
 // Launches one segment on stream. prec: afm_precision (FP64, FP64_SPLIT, FP32).
-cudaError_t launch_segment(const Segment& s, int prec, const SegArgs& a, int sm_count, bool dup_in_element,
+// pdl: allow the launch to begin while the previous kernel on the stream
+// drains (programmatic dependent launch; v is touched only after it ends).
+cudaError_t launch_segment(const Segment& s, int prec, const SegArgs& a, int sm_count, bool dup_in_element, bool pdl,
                            cudaStream_t stream);
 // Dynamic shared memory the launch of segment s uses (for reporting).
 size_t segment_smem_bytes(const Segment& s, int prec);
-// Sets the kernels' shared-memory attributes once per device.
-cudaError_t configure_kernels();
 
 // Records the calling thread's last error message (returned by
 // afm_last_error) and returns status.
 int set_error(int status, const char* fmt, ...);
 
-// Small vector kernels (afm_solver.cu).
-cudaError_t launch_set_constrained(double* v, const double* u, const uint32_t* idx, uint32_t n, cudaStream_t st);
-cudaError_t launch_scatter_values(double* v, const double* vals, const uint32_t* idx, uint32_t n, cudaStream_t st);
 
 }  // namespace afm
 
@@ -124,4 +138,28 @@ struct afm_operator {
     double* h_scalars = nullptr;     // pinned mirror
     float* d_work32 = nullptr;       // mixed-precision inner vectors
     size_t work32_elems = 0;
+
+    // captured CG iteration graphs (FP64 and FP32 inner), keyed by buffers
+    struct CgGraph {
+        cudaGraphExec_t exec = nullptr;
+        const void* key[6] = {};
+        int batch = 0;
+        uint64_t gen = 0;
+    };
+    CgGraph cg64, cg32, bcg64, bcg32;
+    uint64_t generation = 0;  // bumped whenever device buffers are released
+
+    // batched (multi right-hand side) state
+    double* d_bwork = nullptr;
+    size_t bwork_elems = 0;
+    double* d_bsc = nullptr;        // per-column scalars and column partials
+    size_t bsc_elems = 0;
+    unsigned int* d_bremain = nullptr;
+    unsigned int* h_bremain = nullptr;
+    struct BatchTune {
+        uint64_t key;
+        int tr, ng;
+        float ms;
+    };
+    std::vector<BatchTune> batch_tune;  // autotuner choices
 };

@@ -119,6 +119,9 @@ struct ArithF64 {
     using UT = double;
     using VT = double;
     struct Acc { double s; };
+    static __device__ __forceinline__ KT kload(const unsigned char* slot, size_t i, uint32_t) {
+        return reinterpret_cast<const double*>(slot)[i];
+    }
     static __device__ __forceinline__ Acc zero() { return {0.0}; }
     static __device__ __forceinline__ UT stage(VT x) { return x; }
     static __device__ __forceinline__ void fma(Acc& a, KT k, UT u) { a.s = __fma_rn(k, u, a.s); }
@@ -137,6 +140,11 @@ struct ArithSplit {
     using UT = float2;
     using VT = double;
     struct Acc { float hi, lo; };
+    // planar unit: hi plane, then the lo plane `plane` entries further on
+    static __device__ __forceinline__ KT kload(const unsigned char* slot, size_t i, uint32_t plane) {
+        const float* h = reinterpret_cast<const float*>(slot);
+        return make_float2(h[i], h[i + plane]);
+    }
     static __device__ __forceinline__ Acc zero() { return {0.0f, 0.0f}; }
     static __device__ __forceinline__ UT stage(VT x) {
         const float h = __double2float_rn(x);
@@ -169,6 +177,9 @@ struct ArithF32 {
     using UT = float;
     using VT = float;
     struct Acc { float s; };
+    static __device__ __forceinline__ KT kload(const unsigned char* slot, size_t i, uint32_t) {
+        return reinterpret_cast<const float*>(slot)[i];
+    }
     static __device__ __forceinline__ Acc zero() { return {0.0f}; }
     static __device__ __forceinline__ UT stage(VT x) { return x; }
     static __device__ __forceinline__ void fma(Acc& a, KT k, UT u) { a.s = __fmaf_rn(k, u, a.s); }
@@ -176,10 +187,65 @@ struct ArithF32 {
     static __device__ __forceinline__ void combine(Acc& a, const Acc& b) { a.s += b.s; }
 };
 
+__device__ __forceinline__ uint64_t l2_evict_last_policy() {
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+
+// Vector accesses with an L2 policy: u and v are gathered by every colour
+// pass and should stay in L2 while the element matrices stream past
+// (evict_last); the DoF map is read once per matvec (evict_first).
+__device__ __forceinline__ double ld_nc_hint(const double* p, uint64_t pol) {
+    double x;
+    asm volatile("ld.global.nc.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(x) : "l"(p), "l"(pol));
+    return x;
+}
+__device__ __forceinline__ float ld_nc_hint(const float* p, uint64_t pol) {
+    float x;
+    asm volatile("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(x) : "l"(p), "l"(pol));
+    return x;
+}
+__device__ __forceinline__ uint32_t ld_nc_hint(const uint32_t* p, uint64_t pol) {
+    uint32_t x;
+    asm volatile("ld.global.nc.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(x) : "l"(p), "l"(pol));
+    return x;
+}
+__device__ __forceinline__ double ld_hint(const double* p, uint64_t pol) {
+    double x;
+    asm volatile("ld.global.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(x) : "l"(p), "l"(pol) : "memory");
+    return x;
+}
+__device__ __forceinline__ float ld_hint(const float* p, uint64_t pol) {
+    float x;
+    asm volatile("ld.global.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(x) : "l"(p), "l"(pol) : "memory");
+    return x;
+}
+__device__ __forceinline__ void st_hint(double* p, double x, uint64_t pol) {
+    asm volatile("st.global.L2::cache_hint.f64 [%0], %1, %2;" ::"l"(p), "d"(x), "l"(pol) : "memory");
+}
+__device__ __forceinline__ void st_hint(float* p, float x, uint64_t pol) {
+    asm volatile("st.global.L2::cache_hint.f32 [%0], %1, %2;" ::"l"(p), "f"(x), "l"(pol) : "memory");
+}
+
+// Programmatic dependent launch: a colour launch may start (and prefetch its
+// element matrices) while the previous colour drains; every access to v waits
+// until the previous grid has completed and its writes are visible. Both are
+// no-ops for a launch without the programmatic-serialisation attribute.
+__device__ __forceinline__ void wait_prior_grid() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void allow_dependent_launch() { asm volatile("griddepcontrol.launch_dependents;"); }
+
 template <typename VT>
 __device__ __forceinline__ VT load_u(const VT* u, uint32_t m, int bc_mode) {
     const uint32_t d = m & kDofMask;
     VT x = __ldg(u + d);
+    if (bc_mode && (m & kBcFlag)) x = VT(0);
+    return x;
+}
+
+template <typename VT>
+__device__ __forceinline__ VT load_u_hint(const VT* u, uint32_t m, int bc_mode, uint64_t pol) {
+    VT x = ld_nc_hint(u + (m & kDofMask), pol);
     if (bc_mode && (m & kBcFlag)) x = VT(0);
     return x;
 }
@@ -232,13 +298,15 @@ __global__ void __launch_bounds__(9 * 32, 1) afm_wpe_kernel(SegArgs a, RingLayou
                     atomicOr(a.err, kErrTimeout);
                     break;
                 }
-                mbar_arrive_expect_tx(&full[s], (uint32_t)a.unit_bytes);
-                bulk_load(smem + (size_t)s * L.slot_bytes, a.ke + (size_t)(begin + i) * a.unit_bytes,
-                          (uint32_t)a.unit_bytes, &full[s], pol);
+                mbar_arrive_expect_tx(&full[s], a.copy_bytes);
+                bulk_load(smem + (size_t)s * L.slot_bytes, a.ke + (size_t)(begin + i) * a.unit_bytes, a.copy_bytes,
+                          &full[s], pol);
             }
+            allow_dependent_launch();
         }
         return;
     }
+    wait_prior_grid();
 
     const VT* __restrict__ u = static_cast<const VT*>(a.u);
     VT* __restrict__ v = static_cast<VT*>(a.v);
@@ -292,18 +360,17 @@ __global__ void __launch_bounds__(9 * 32, 1) afm_wpe_kernel(SegArgs a, RingLayou
             if (lane == 0) atomicOr(a.err, kErrTimeout);
             break;
         }
-        const KT* ks = reinterpret_cast<const KT*>(smem + (size_t)s * L.slot_bytes);
+        const unsigned char* ks = smem + (size_t)s * L.slot_bytes;
         typename A::Acc acc[RMAX];
 #pragma unroll
         for (int t = 0; t < RMAX; t++) acc[t] = A::zero();
 #pragma unroll(NT ? (NT < 64 ? NT : 16) : 4)
         for (uint32_t c = 0; c < n; c++) {
             const UT uc = us[c];
-            const KT* col = ks + (size_t)c * n;
 #pragma unroll
             for (int t = 0; t < RMAX; t++) {
                 const uint32_t r = lane + 32 * t;
-                if (r < n) A::fma(acc[t], col[r], uc);
+                if (r < n) A::fma(acc[t], A::kload(ks, (size_t)c * n + r, a.plane), uc);
             }
         }
         __syncwarp();
@@ -394,11 +461,12 @@ __global__ void __launch_bounds__(17 * 32, 1) afm_wpg_kernel(SegArgs a, RingLayo
             for (uint32_t i = 0; i < cnt; i++) {
                 const uint32_t s = i % S;
                 if (i >= S && !mbar_wait_abortable(&empty[s], ((i / S) - 1) & 1, abort)) break;
-                mbar_arrive_expect_tx(&full[s], (uint32_t)a.unit_bytes);
-                bulk_load(smem + (size_t)s * L.slot_bytes, a.ke + (size_t)(begin + i) * a.unit_bytes,
-                          (uint32_t)a.unit_bytes, &full[s], pol);
+                mbar_arrive_expect_tx(&full[s], a.copy_bytes);
+                bulk_load(smem + (size_t)s * L.slot_bytes, a.ke + (size_t)(begin + i) * a.unit_bytes, a.copy_bytes,
+                          &full[s], pol);
                 issued = i + 1;
             }
+            allow_dependent_launch();
             if (*abort) {
                 // drain: every issued copy lands before the CTA's shared memory is released
                 atomicOr(a.err, kErrTimeout);
@@ -429,31 +497,33 @@ __global__ void __launch_bounds__(17 * 32, 1) afm_wpg_kernel(SegArgs a, RingLayo
 
     uint32_t dof_c = 0, dof_n = 0, dof_nn = 0;
     VT vold_c = VT(0), vold_n = VT(0), u_n = VT(0);
-    auto map_at = [&](uint32_t i) { return rvalid ? __ldg(a.map + (size_t)(begin + i) * n + r) : 0u; };
+    const uint64_t keep = l2_evict_last_policy(), stream_pol = l2_evict_first_policy();
+    auto map_at = [&](uint32_t i) {
+        return rvalid ? ld_nc_hint(a.map + (size_t)(begin + i) * n + r, stream_pol) : 0u;
+    };
 
     uint32_t i = grp;
     if (gatherer && i < cnt) {
         dof_c = map_at(i);
-        if (rvalid) {
-            ubuf(0)[r] = A::stage(load_u(u, dof_c, a.bc_mode));
-            vold_c = v[dof_c & kDofMask];
-        }
+        if (rvalid) ubuf(0)[r] = A::stage(load_u_hint(u, dof_c, a.bc_mode, keep));
         if (i + G.ng < cnt) dof_n = map_at(i + G.ng);
     }
+    wait_prior_grid();
+    if (gatherer && i < cnt && rvalid) vold_c = ld_hint(v + (dof_c & kDofMask), keep);
     named_barrier(bar_id, bar_threads);
     for (uint32_t k = 0; i < cnt; i += G.ng, k++) {
         const uint32_t par = k & 1;
         if (gatherer && rvalid) {
             if (i + G.ng < cnt) {
-                u_n = load_u(u, dof_n, a.bc_mode);
-                vold_n = v[dof_n & kDofMask];
+                u_n = load_u_hint(u, dof_n, a.bc_mode, keep);
+                vold_n = ld_hint(v + (dof_n & kDofMask), keep);
             }
             if (i + 2 * G.ng < cnt) dof_nn = map_at(i + 2 * G.ng);
         }
         const uint32_t s = i % S;
         Acc acc = A::zero();
         if (mbar_wait_abortable(&full[s], (i / S) & 1, abort)) {
-            const KT* ks = reinterpret_cast<const KT*>(smem + (size_t)s * L.slot_bytes);
+            const unsigned char* ks = smem + (size_t)s * L.slot_bytes;
             const UT* uu = ubuf(par);
             if (rvalid) {
                 if constexpr (NT != 0) {
@@ -463,11 +533,11 @@ __global__ void __launch_bounds__(17 * 32, 1) afm_wpg_kernel(SegArgs a, RingLayo
 #pragma unroll
                     for (uint32_t j = 0; j < TRIP; j++) {
                         const uint32_t c = cb + j;
-                        if (c < ce) A::fma(acc, ks[(size_t)c * NT + r], uu[c]);
+                        if (c < ce) A::fma(acc, A::kload(ks, (size_t)c * NT + r, a.plane), uu[c]);
                     }
                 } else {
 #pragma unroll 4
-                    for (uint32_t c = cb; c < ce; c++) A::fma(acc, ks[(size_t)c * n + r], uu[c]);
+                    for (uint32_t c = cb; c < ce; c++) A::fma(acc, A::kload(ks, (size_t)c * n + r, a.plane), uu[c]);
                 }
             }
             __syncwarp();
@@ -480,7 +550,7 @@ __global__ void __launch_bounds__(17 * 32, 1) afm_wpg_kernel(SegArgs a, RingLayo
             for (uint32_t c2 = 1; c2 < G.gc; c2++) {
                 if (rvalid) A::combine(acc, pbuf(par)[(c2 - 1) * n + r]);
             }
-            if (rvalid && !*abort) v[dof_c & kDofMask] = vold_c + A::finish(acc);
+            if (rvalid && !*abort) st_hint(v + (dof_c & kDofMask), vold_c + A::finish(acc), keep);
             dof_c = dof_n;
             vold_c = vold_n;
             dof_n = dof_nn;
@@ -527,13 +597,15 @@ __global__ void __launch_bounds__(9 * 32, 1) afm_tpe_kernel(SegArgs a, RingLayou
                     atomicOr(a.err, kErrTimeout);
                     break;
                 }
-                mbar_arrive_expect_tx(&full[s], (uint32_t)a.unit_bytes);
-                bulk_load(smem + (size_t)s * L.slot_bytes, a.ke + (size_t)(begin + i) * a.unit_bytes,
-                          (uint32_t)a.unit_bytes, &full[s], pol);
+                mbar_arrive_expect_tx(&full[s], a.copy_bytes);
+                bulk_load(smem + (size_t)s * L.slot_bytes, a.ke + (size_t)(begin + i) * a.unit_bytes, a.copy_bytes,
+                          &full[s], pol);
             }
+            allow_dependent_launch();
         }
         return;
     }
+    wait_prior_grid();
 
     const VT* __restrict__ u = static_cast<const VT*>(a.u);
     VT* __restrict__ v = static_cast<VT*>(a.v);
@@ -579,7 +651,7 @@ __global__ void __launch_bounds__(9 * 32, 1) afm_tpe_kernel(SegArgs a, RingLayou
             if (lane == 0) atomicOr(a.err, kErrTimeout);
             break;
         }
-        const KT* ks = reinterpret_cast<const KT*>(smem + (size_t)s * L.slot_bytes) + lane;
+        const unsigned char* ks = smem + (size_t)s * L.slot_bytes;
         UT us[NM];
 #pragma unroll
         for (int c = 0; c < NM; c++) us[c] = A::stage(u_c[c]);
@@ -590,7 +662,7 @@ __global__ void __launch_bounds__(9 * 32, 1) afm_tpe_kernel(SegArgs a, RingLayou
             if (r < (int)n) {
 #pragma unroll
                 for (int c = 0; c < NM; c++)
-                    if (c < (int)n) A::fma(acc[r], ks[(size_t)(r * n + c) * kTpeWidth], us[c]);
+                    if (c < (int)n) A::fma(acc[r], A::kload(ks, (size_t)(r * n + c) * kTpeWidth + lane, a.plane), us[c]);
             }
         }
         __syncwarp();

@@ -2,4 +2,6 @@
 #define ARITH ArithF32
 #define LAUNCH_FN launch_segment_fp32
 #define SMEM_FN segment_smem_fp32
+#define CONFIG_FN configure_kernels_fp32
+#define BATCH_FN launch_batched_fp32
 #include "afm_mv_launch.inl"

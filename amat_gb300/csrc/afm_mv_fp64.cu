@@ -2,4 +2,6 @@
 #define ARITH ArithF64
 #define LAUNCH_FN launch_segment_fp64
 #define SMEM_FN segment_smem_fp64
+#define CONFIG_FN configure_kernels_fp64
+#define BATCH_FN launch_batched_fp64
 #include "afm_mv_launch.inl"

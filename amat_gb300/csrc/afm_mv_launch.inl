@@ -1,7 +1,9 @@
 // Instantiation and dispatch of the matvec kernels for one arithmetic policy
 // (included by afm_mv_fp64.cu, afm_mv_split.cu, afm_mv_fp32.cu, which define
 // ARITH and LAUNCH_FN so that the three compile in parallel).
-#include "afm_matvec.cuh"
+#include <algorithm>
+
+#include "afm_batched.cuh"
 
 namespace afm {
 
@@ -50,10 +52,10 @@ static uint32_t stages_for(uint32_t slot_bytes, uint32_t extra) {
 }
 
 // Ring layout and (for the warp-group kernel) group geometry of a segment.
-static RingLayout ring_layout(const Segment& s, bool dup, GroupGeom* geom) {
+static RingLayout ring_layout(const Segment& s, uint64_t copy_bytes, bool dup, GroupGeom* geom) {
     RingLayout L;
     const size_t ut = sizeof(typename ARITH::UT), acc = sizeof(typename ARITH::Acc);
-    L.slot_bytes = (uint32_t)((s.unit_bytes + kSlotAlign - 1) / kSlotAlign * kSlotAlign);
+    L.slot_bytes = (uint32_t)((copy_bytes + kSlotAlign - 1) / kSlotAlign * kSlotAlign);
     L.ubuf_bytes = 0;
     L.extra_bytes = 0;
     if (s.regime == REG_WPE && !dup) {
@@ -86,40 +88,119 @@ static RingLayout ring_layout(const Segment& s, bool dup, GroupGeom* geom) {
     return L;
 }
 
-cudaError_t LAUNCH_FN(const Segment& s, const SegArgs& a, int sm_count, bool dup, cudaStream_t stream) {
+cudaError_t LAUNCH_FN(const Segment& s, const SegArgs& a, int sm_count, bool dup, bool pdl, cudaStream_t stream) {
     if (s.units == 0) return cudaSuccess;
     GroupGeom G{1, 1, 1, 1};
-    const RingLayout L = ring_layout(s, dup, &G);
+    const RingLayout L = ring_layout(s, a.copy_bytes, dup, &G);
     if (L.stages < 2) return cudaErrorInvalidConfiguration;
     void* fn = pick_kernel(s.regime, s.n, dup);
     const uint32_t smem = L.total();
-    static thread_local int configured_dev = -1;
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (configured_dev != dev) {
-        for (int reg = 0; reg < 2; reg++)
-            for (uint32_t nn : {4u, 8u, 10u, 20u, 24u, 30u, 60u, 0u})
-                for (int d = 0; d < 2; d++) {
-                    void* f = pick_kernel(reg, nn == 0 ? 7u : nn, d != 0);
-                    cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                         (int)(kSmemBudget + 1024));
-                    if (e != cudaSuccess) return e;
-                }
-        configured_dev = dev;
-    }
     uint32_t grid = s.units < (uint32_t)sm_count ? s.units : (uint32_t)sm_count;
     dim3 block((L.warps + 1) * 32);
     uint32_t n_rt = s.n;
     SegArgs args = a;
     RingLayout Lc = L;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl ? 1 : 0;
     if (s.regime == REG_WPE && !dup) {
         void* params[] = {&args, &Lc, &G, &n_rt};
-        return cudaLaunchKernel(fn, dim3(grid), block, params, smem, stream);
+        return cudaLaunchKernelExC(&cfg, fn, params);
     }
     void* params[] = {&args, &Lc, &n_rt};
-    return cudaLaunchKernel(fn, dim3(grid), block, params, smem, stream);
+    return cudaLaunchKernelExC(&cfg, fn, params);
 }
 
-size_t SMEM_FN(const Segment& s) { return ring_layout(s, false, nullptr).total(); }
+// ---- batched (multi right-hand side) product, warp-group regime ----------
+
+namespace {
+template <int NT, int TR>
+void* batch_kernel_ptr() {
+    return (void*)afm_batched_kernel<NT, ARITH, TR>;
+}
+void* pick_batch_kernel(uint32_t n, int tr) {
+    if (tr == 8) {
+        switch (n) {
+            case 24: return batch_kernel_ptr<24, 8>();
+            case 60: return batch_kernel_ptr<60, 8>();
+            default: return batch_kernel_ptr<0, 8>();
+        }
+    }
+    switch (n) {
+        case 24: return batch_kernel_ptr<24, 4>();
+        case 60: return batch_kernel_ptr<60, 4>();
+        default: return batch_kernel_ptr<0, 4>();
+    }
+}
+}  // namespace
+
+// tr: columns per thread tile (4 or 8); ng: element groups per CTA (<= 4).
+cudaError_t BATCH_FN(const Segment& s, const BatchArgs& a, int sm_count, int tr, int ng, bool pdl,
+                     cudaStream_t stream) {
+    if (s.units == 0) return cudaSuccess;
+    if (s.regime != REG_WPE || (tr != 4 && tr != 8) || a.nrhs % tr != 0 || ng < 1 || ng > 4)
+        return cudaErrorInvalidValue;
+    BatchGeom G;
+    G.rtiles = (s.n + 3) / 4;
+    G.ctiles = a.nrhs / tr;
+    const uint32_t tiles = G.rtiles * G.ctiles;
+    G.gthreads = std::min<uint32_t>(128, (tiles + 31) / 32 * 32);
+    const uint32_t ub = batch_ubuf_bytes(s.n, a.nrhs, (uint32_t)sizeof(typename ARITH::UT));
+    RingLayout L;
+    L.slot_bytes = (a.copy_bytes + kSlotAlign - 1) / kSlotAlign * kSlotAlign;
+    L.ubuf_bytes = ub;
+    for (G.ng = (uint32_t)ng; G.ng >= 1; G.ng--) {
+        L.extra_bytes = G.ng * ub;
+        L.stages = stages_for(L.slot_bytes, L.extra_bytes);
+        if (L.stages >= 2) break;
+    }
+    if (G.ng == 0 || L.stages < 2) return cudaErrorInvalidConfiguration;
+    L.warps = G.ng * G.gthreads / 32;
+    void* fn = pick_batch_kernel(s.n, tr);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(s.units < (uint32_t)sm_count ? s.units : (uint32_t)sm_count);
+    cfg.blockDim = dim3(G.ng * G.gthreads + 32);
+    cfg.dynamicSmemBytes = L.total();
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    BatchArgs args = a;
+    uint32_t n_rt = s.n;
+    void* params[] = {&args, &L, &G, &n_rt};
+    return cudaLaunchKernelExC(&cfg, fn, params);
+}
+
+size_t SMEM_FN(const Segment& s) { return ring_layout(s, s.unit_bytes, false, nullptr).total(); }
+
+// Raises the dynamic shared-memory limit of every kernel instance on the
+// current device; called once per device before any launch or capture.
+cudaError_t CONFIG_FN() {
+    for (int reg = 0; reg < 2; reg++)
+        for (uint32_t nn : {4u, 8u, 10u, 20u, 24u, 30u, 60u, 0u})
+            for (int d = 0; d < 2; d++) {
+                void* f = pick_kernel(reg, nn == 0 ? 7u : nn, d != 0);
+                cudaError_t e =
+                    cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kSmemBudget + 1024));
+                if (e != cudaSuccess) return e;
+            }
+    for (int tr : {4, 8})
+        for (uint32_t nn : {24u, 60u, 7u}) {
+            cudaError_t e = cudaFuncSetAttribute(pick_batch_kernel(nn, tr), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)(kSmemBudget + 1024));
+            if (e != cudaSuccess) return e;
+        }
+    return cudaSuccess;
+}
+
 
 }  // namespace afm

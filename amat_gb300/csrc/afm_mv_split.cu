@@ -2,4 +2,6 @@
 #define ARITH ArithSplit
 #define LAUNCH_FN launch_segment_split
 #define SMEM_FN segment_smem_split
+#define CONFIG_FN configure_kernels_split
+#define BATCH_FN launch_batched_split
 #include "afm_mv_launch.inl"

@@ -135,7 +135,7 @@ extern "C" int afm_solve_cg_device_noalloc(afm_operator* op, const double* d_b, 
     s = afm_matmult_bc_device(op, q, d_x, st);
     if (s) return s;
     NA_CUDA(launch_axpby(q, d_b, 1.0, -1.0, n, st));
-    NA_CUDA(launch_cg_alpha(q, q, n, sc, part, st));
+    NA_CUDA(launch_norm2(q, n, sc, part, st));
     NA_CUDA(cudaMemcpyAsync(h, sc, sizeof(double) * kScalarSlots, cudaMemcpyDeviceToHost, st));
     NA_CUDA(cudaStreamSynchronize(st));
     const double rr = h[S_PQ];

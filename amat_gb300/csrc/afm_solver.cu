@@ -1,6 +1,8 @@
 // Vector kernels around the AFM matvec: boundary-condition wrapping of
 // MatMult_mf and the Jacobi-preconditioned CG of the example drivers' solve
-// (examples/include/solve.hpp:75-127), all in FP64 on the device.
+// (examples/include/solve.hpp:75-127). Vectors are T = double (the FP64 CG)
+// or T = float (the inner CG of the mixed-precision solve); every dot product
+// and step scalar is accumulated and held in FP64.
 //
 // Reductions are deterministic: a fixed grid of kRedBlocks x kRedThreads
 // threads sums fixed strided slices in index order, each block reduces in a
@@ -28,26 +30,27 @@ __device__ __forceinline__ double block_sum(double x, double* sh) {
     return r;
 }
 
-__global__ void __launch_bounds__(kRedThreads) k_set_constrained(double* v, const double* u, const uint32_t* idx,
-                                                                 uint32_t n) {
+__device__ __forceinline__ double final_sum(const double* part, double* sh) {
+    double s = 0.0;
+    for (int i = threadIdx.x; i < kRedBlocks; i += kRedThreads) s += part[i];
+    return block_sum(s, sh);
+}
+
+constexpr size_t kStride = (size_t)kRedBlocks * kRedThreads;
+
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads) k_set_constrained(T* v, const T* u, const uint32_t* idx, uint32_t n) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k < n) v[idx[k]] = u[idx[k]];
 }
 
-__global__ void __launch_bounds__(kRedThreads) k_scatter_values(double* v, const double* vals, const uint32_t* idx,
-                                                                uint32_t n) {
-    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < n) v[idx[k]] = vals[k];
-}
-
-// part[j*kRedBlocks + block] = partial sums of the requested products
-// (which: bit0 a.b, bit1 a.a, bit2 b.b).
-__global__ void __launch_bounds__(kRedThreads) k_dots(const double* __restrict__ a, const double* __restrict__ b,
-                                                      size_t n, double* part) {
+// part[j*kRedBlocks + block]: partial sums of a.b, a.a, b.b
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads) k_dots(const T* __restrict__ a, const T* __restrict__ b, size_t n,
+                                                      double* part) {
     __shared__ double sh[kRedThreads];
     double ab = 0.0, aa = 0.0, bb = 0.0;
-    const size_t stride = (size_t)kRedBlocks * kRedThreads;
-    for (size_t i = (size_t)blockIdx.x * kRedThreads + threadIdx.x; i < n; i += stride) {
+    for (size_t i = (size_t)blockIdx.x * kRedThreads + threadIdx.x; i < n; i += kStride) {
         const double x = a[i], y = b[i];
         ab = __fma_rn(x, y, ab);
         aa = __fma_rn(x, x, aa);
@@ -63,32 +66,25 @@ __global__ void __launch_bounds__(kRedThreads) k_dots(const double* __restrict__
     }
 }
 
-__device__ __forceinline__ double final_sum(const double* part, double* sh) {
-    double s = 0.0;
-    for (int i = threadIdx.x; i < kRedBlocks; i += kRedThreads) s += part[i];
-    return block_sum(s, sh);
-}
-
 // r = b - q, z = dinv r, p = z; partials of r.z, r.r, z.z, b.b, (dinv b).(dinv b)
-__global__ void __launch_bounds__(kRedThreads) k_cg_init(const double* __restrict__ b, const double* __restrict__ q,
-                                                         const double* __restrict__ dinv, double* __restrict__ r,
-                                                         double* __restrict__ z, double* __restrict__ p, size_t n,
-                                                         double* part) {
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads) k_cg_init(const T* __restrict__ b, const T* __restrict__ q,
+                                                         const T* __restrict__ dinv, T* __restrict__ r,
+                                                         T* __restrict__ z, T* __restrict__ p, size_t n, double* part) {
     __shared__ double sh[kRedThreads];
     double rz = 0, rr = 0, zz = 0, bb = 0, db = 0;
-    const size_t stride = (size_t)kRedBlocks * kRedThreads;
-    for (size_t i = (size_t)blockIdx.x * kRedThreads + threadIdx.x; i < n; i += stride) {
-        const double bi = b[i], di = dinv[i];
-        const double ri = bi - q[i];
-        const double zi = di * ri;
+    for (size_t i = (size_t)blockIdx.x * kRedThreads + threadIdx.x; i < n; i += kStride) {
+        const T bi = b[i], di = dinv[i];
+        const T ri = bi - q[i];
+        const T zi = di * ri;
         r[i] = ri;
         z[i] = zi;
         p[i] = zi;
-        rz = __fma_rn(ri, zi, rz);
-        rr = __fma_rn(ri, ri, rr);
-        zz = __fma_rn(zi, zi, zz);
-        bb = __fma_rn(bi, bi, bb);
-        const double t = di * bi;
+        rz = __fma_rn((double)ri, (double)zi, rz);
+        rr = __fma_rn((double)ri, (double)ri, rr);
+        zz = __fma_rn((double)zi, (double)zi, zz);
+        bb = __fma_rn((double)bi, (double)bi, bb);
+        const double t = (double)di * (double)bi;
         db = __fma_rn(t, t, db);
     }
     double v[5] = {rz, rr, zz, bb, db};
@@ -112,6 +108,8 @@ __global__ void __launch_bounds__(kRedThreads) k_cg_init_final(double* sc, const
         sc[S_BB] = bb;
         sc[S_DB] = db;
         sc[S_FLAG] = (rz < 0.0 || rz != rz) ? 1.0 : 0.0;
+        sc[S_DONE] = 0.0;
+        sc[S_ITER] = 0.0;
     }
 }
 
@@ -120,9 +118,14 @@ __global__ void __launch_bounds__(kRedThreads) k_cg_alpha(double* sc, const doub
     __shared__ double sh[kRedThreads];
     const double pq = final_sum(part, sh);
     if (threadIdx.x == 0) {
+        if (sc[S_DONE] != 0.0) {  // finished earlier: this iteration changes nothing
+            sc[S_ALPHA] = 0.0;
+            return;
+        }
         sc[S_PQ] = pq;
         if (!(pq > 0.0)) {
             sc[S_FLAG] = 1.0;
+            sc[S_DONE] = 1.0;
             sc[S_ALPHA] = 0.0;
         } else {
             sc[S_ALPHA] = sc[S_RZ] / pq;
@@ -130,25 +133,31 @@ __global__ void __launch_bounds__(kRedThreads) k_cg_alpha(double* sc, const doub
     }
 }
 
-// x += alpha p, r -= alpha q, z = dinv r; partials of r.z, r.r, z.z
-__global__ void __launch_bounds__(kRedThreads) k_cg_update(double* __restrict__ x, double* __restrict__ r,
-                                                           double* __restrict__ z, const double* __restrict__ p,
-                                                           const double* __restrict__ q,
-                                                           const double* __restrict__ dinv, size_t n,
-                                                           const double* sc, double* part) {
+// sc[S_PQ] = sum of the partials (a plain reduction, no CG bookkeeping)
+__global__ void __launch_bounds__(kRedThreads) k_sum(double* sc, const double* part) {
     __shared__ double sh[kRedThreads];
-    const double alpha = sc[S_ALPHA];
+    const double s = final_sum(part, sh);
+    if (threadIdx.x == 0) sc[S_PQ] = s;
+}
+
+// x += alpha p, r -= alpha q, z = dinv r; partials of r.z, r.r, z.z
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads) k_cg_update(T* __restrict__ x, T* __restrict__ r, T* __restrict__ z,
+                                                           const T* __restrict__ p, const T* __restrict__ q,
+                                                           const T* __restrict__ dinv, size_t n, const double* sc,
+                                                           double* part) {
+    __shared__ double sh[kRedThreads];
+    const T alpha = (T)sc[S_ALPHA];
     double rz = 0, rr = 0, zz = 0;
-    const size_t stride = (size_t)kRedBlocks * kRedThreads;
-    for (size_t i = (size_t)blockIdx.x * kRedThreads + threadIdx.x; i < n; i += stride) {
-        x[i] = __fma_rn(alpha, p[i], x[i]);
-        const double ri = __fma_rn(-alpha, q[i], r[i]);
-        const double zi = dinv[i] * ri;
+    for (size_t i = (size_t)blockIdx.x * kRedThreads + threadIdx.x; i < n; i += kStride) {
+        x[i] = alpha * p[i] + x[i];
+        const T ri = -alpha * q[i] + r[i];
+        const T zi = dinv[i] * ri;
         r[i] = ri;
         z[i] = zi;
-        rz = __fma_rn(ri, zi, rz);
-        rr = __fma_rn(ri, ri, rr);
-        zz = __fma_rn(zi, zi, zz);
+        rz = __fma_rn((double)ri, (double)zi, rz);
+        rr = __fma_rn((double)ri, (double)ri, rr);
+        zz = __fma_rn((double)zi, (double)zi, zz);
     }
     rz = block_sum(rz, sh);
     rr = block_sum(rr, sh);
@@ -167,27 +176,40 @@ __global__ void __launch_bounds__(kRedThreads) k_cg_beta(double* sc, const doubl
     const double rr = final_sum(part + kRedBlocks, sh);
     const double zz = final_sum(part + 2 * kRedBlocks, sh);
     if (threadIdx.x == 0) {
+        if (sc[S_DONE] != 0.0) {
+            sc[S_BETA] = 0.0;
+            return;
+        }
         const double old = sc[S_RZ];
         sc[S_BETA] = (old != 0.0) ? rz / old : 0.0;
         sc[S_RZ] = rz;
         sc[S_RR] = rr;
         sc[S_ZZ] = zz;
-        if (rz < 0.0 || rz != rz) sc[S_FLAG] = 1.0;
+        const double it = sc[S_ITER] + 1.0;
+        sc[S_ITER] = it;
+        const double nrm = sqrt(sc[S_NORM] != 0.0 ? zz : rr);
+        if (rz < 0.0 || rz != rz || nrm != nrm) {
+            sc[S_FLAG] = 1.0;
+            sc[S_DONE] = 1.0;
+        } else if (nrm <= sc[S_TOL] || (sc[S_MAXIT] > 0.0 && it >= sc[S_MAXIT])) {
+            sc[S_DONE] = 1.0;
+        }
     }
 }
 
-__global__ void __launch_bounds__(kRedThreads) k_cg_p(double* __restrict__ p, const double* __restrict__ z, size_t n,
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads) k_cg_p(T* __restrict__ p, const T* __restrict__ z, size_t n,
                                                       const double* sc) {
-    const double beta = sc[S_BETA];
+    const T beta = (T)sc[S_BETA];
     const size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
-        p[i] = __fma_rn(beta, p[i], z[i]);
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) p[i] = beta * p[i] + z[i];
 }
 
-__global__ void __launch_bounds__(kRedThreads) k_invert(double* __restrict__ dinv, const double* __restrict__ d,
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads) k_invert(T* __restrict__ dinv, const double* __restrict__ d,
                                                         size_t n) {
     const size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) dinv[i] = 1.0 / d[i];
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) dinv[i] = (T)(1.0 / d[i]);
 }
 
 __global__ void __launch_bounds__(kRedThreads) k_axpby(double* __restrict__ y, const double* __restrict__ x,
@@ -195,6 +217,22 @@ __global__ void __launch_bounds__(kRedThreads) k_axpby(double* __restrict__ y, c
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
         y[i] = __fma_rn(a, x[i], b * y[i]);
+}
+
+// out32 = fl32(in64)
+__global__ void __launch_bounds__(kRedThreads) k_to_f32(float* __restrict__ out, const double* __restrict__ in,
+                                                        size_t n) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) out[i] = (float)in[i];
+}
+
+// x64 += d32, d32 = 0
+__global__ void __launch_bounds__(kRedThreads) k_add_f32(double* __restrict__ x, float* __restrict__ d, size_t n) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        x[i] += (double)d[i];
+        d[i] = 0.0f;
+    }
 }
 
 inline unsigned grid_for(size_t n) {
@@ -206,46 +244,53 @@ inline unsigned grid_for(size_t n) {
 
 }  // namespace
 
-cudaError_t launch_set_constrained(double* v, const double* u, const uint32_t* idx, uint32_t n, cudaStream_t st) {
+template <typename T>
+cudaError_t launch_set_constrained(T* v, const T* u, const uint32_t* idx, uint32_t n, cudaStream_t st) {
     if (n == 0) return cudaSuccess;
-    k_set_constrained<<<(n + kRedThreads - 1) / kRedThreads, kRedThreads, 0, st>>>(v, u, idx, n);
+    k_set_constrained<T><<<(n + kRedThreads - 1) / kRedThreads, kRedThreads, 0, st>>>(v, u, idx, n);
     return cudaGetLastError();
 }
 
-cudaError_t launch_scatter_values(double* v, const double* vals, const uint32_t* idx, uint32_t n, cudaStream_t st) {
-    if (n == 0) return cudaSuccess;
-    k_scatter_values<<<(n + kRedThreads - 1) / kRedThreads, kRedThreads, 0, st>>>(v, vals, idx, n);
+template <typename T>
+cudaError_t launch_dots(const T* a, const T* b, size_t n, double* part, cudaStream_t st) {
+    k_dots<T><<<kRedBlocks, kRedThreads, 0, st>>>(a, b, n, part);
     return cudaGetLastError();
 }
 
-cudaError_t launch_dots(const double* a, const double* b, size_t n, double* part, cudaStream_t st) {
-    k_dots<<<kRedBlocks, kRedThreads, 0, st>>>(a, b, n, part);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_cg_init(const double* b, const double* q, const double* dinv, double* r, double* z, double* p,
-                           size_t n, double* sc, double* part, cudaStream_t st) {
-    k_cg_init<<<kRedBlocks, kRedThreads, 0, st>>>(b, q, dinv, r, z, p, n, part);
+template <typename T>
+cudaError_t launch_cg_init(const T* b, const T* q, const T* dinv, T* r, T* z, T* p, size_t n, double* sc,
+                           double* part, cudaStream_t st) {
+    k_cg_init<T><<<kRedBlocks, kRedThreads, 0, st>>>(b, q, dinv, r, z, p, n, part);
     k_cg_init_final<<<1, kRedThreads, 0, st>>>(sc, part);
     return cudaGetLastError();
 }
 
-cudaError_t launch_cg_alpha(const double* p, const double* q, size_t n, double* sc, double* part, cudaStream_t st) {
-    k_dots<<<kRedBlocks, kRedThreads, 0, st>>>(p, q, n, part);
+template <typename T>
+cudaError_t launch_cg_alpha(const T* p, const T* q, size_t n, double* sc, double* part, cudaStream_t st) {
+    k_dots<T><<<kRedBlocks, kRedThreads, 0, st>>>(p, q, n, part);
     k_cg_alpha<<<1, kRedThreads, 0, st>>>(sc, part);
     return cudaGetLastError();
 }
 
-cudaError_t launch_cg_update(double* x, double* r, double* z, double* p, const double* q, const double* dinv,
-                             size_t n, double* sc, double* part, cudaStream_t st) {
-    k_cg_update<<<kRedBlocks, kRedThreads, 0, st>>>(x, r, z, p, q, dinv, n, sc, part);
+template <typename T>
+cudaError_t launch_cg_update(T* x, T* r, T* z, T* p, const T* q, const T* dinv, size_t n, double* sc, double* part,
+                             cudaStream_t st) {
+    k_cg_update<T><<<kRedBlocks, kRedThreads, 0, st>>>(x, r, z, p, q, dinv, n, sc, part);
     k_cg_beta<<<1, kRedThreads, 0, st>>>(sc, part);
-    k_cg_p<<<grid_for(n), kRedThreads, 0, st>>>(p, z, n, sc);
+    k_cg_p<T><<<grid_for(n), kRedThreads, 0, st>>>(p, z, n, sc);
     return cudaGetLastError();
 }
 
-cudaError_t launch_invert(double* dinv, const double* d, size_t n, cudaStream_t st) {
-    k_invert<<<grid_for(n), kRedThreads, 0, st>>>(dinv, d, n);
+template <typename T>
+cudaError_t launch_invert(T* dinv, const double* d, size_t n, cudaStream_t st) {
+    k_invert<T><<<grid_for(n), kRedThreads, 0, st>>>(dinv, d, n);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_norm2(const T* a, size_t n, double* sc, double* part, cudaStream_t st) {
+    k_dots<T><<<kRedBlocks, kRedThreads, 0, st>>>(a, a, n, part);
+    k_sum<<<1, kRedThreads, 0, st>>>(sc, part);
     return cudaGetLastError();
 }
 
@@ -253,5 +298,29 @@ cudaError_t launch_axpby(double* y, const double* x, double a, double b, size_t 
     k_axpby<<<grid_for(n), kRedThreads, 0, st>>>(y, x, a, b, n);
     return cudaGetLastError();
 }
+
+cudaError_t launch_to_f32(float* out, const double* in, size_t n, cudaStream_t st) {
+    k_to_f32<<<grid_for(n), kRedThreads, 0, st>>>(out, in, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_add_f32(double* x, float* d, size_t n, cudaStream_t st) {
+    k_add_f32<<<grid_for(n), kRedThreads, 0, st>>>(x, d, n);
+    return cudaGetLastError();
+}
+
+#define AFM_SOLVER_INSTANCES(T)                                                                                       \
+    template cudaError_t launch_set_constrained<T>(T*, const T*, const uint32_t*, uint32_t, cudaStream_t);            \
+    template cudaError_t launch_dots<T>(const T*, const T*, size_t, double*, cudaStream_t);                           \
+    template cudaError_t launch_cg_init<T>(const T*, const T*, const T*, T*, T*, T*, size_t, double*, double*,        \
+                                           cudaStream_t);                                                             \
+    template cudaError_t launch_cg_alpha<T>(const T*, const T*, size_t, double*, double*, cudaStream_t);              \
+    template cudaError_t launch_cg_update<T>(T*, T*, T*, T*, const T*, const T*, size_t, double*, double*,            \
+                                             cudaStream_t);                                                           \
+    template cudaError_t launch_invert<T>(T*, const double*, size_t, cudaStream_t);                                   \
+    template cudaError_t launch_norm2<T>(const T*, size_t, double*, double*, cudaStream_t);
+
+AFM_SOLVER_INSTANCES(double)
+AFM_SOLVER_INSTANCES(float)
 
 }  // namespace afm

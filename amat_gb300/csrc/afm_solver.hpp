@@ -12,16 +12,39 @@ constexpr int kRedThreads = 256;
 
 // Scalar slots of the solver state (device array of kScalarSlots doubles,
 // followed by kPartialSlots reduction partials).
-enum : int { S_RZ = 0, S_PQ, S_ALPHA, S_BETA, S_RR, S_ZZ, S_BB, S_DB, S_FLAG, kScalarSlots = 16 };
+// S_TOL, S_MAXIT, S_NORM are set by the host before the iterations; the
+// kernels keep S_ITER and raise S_DONE on convergence (monitored norm <=
+// S_TOL), on S_MAXIT iterations (when > 0) or on breakdown (S_FLAG), after
+// which further iterations leave every vector unchanged. That lets a captured
+// graph run several iterations without reading anything back.
+enum : int {
+    S_RZ = 0, S_PQ, S_ALPHA, S_BETA, S_RR, S_ZZ, S_BB, S_DB, S_FLAG,
+    S_DONE, S_TOL, S_ITER, S_MAXIT, S_NORM,
+    kScalarSlots = 16
+};
 constexpr int kPartialSlots = 5 * kRedBlocks;
 
-cudaError_t launch_dots(const double* a, const double* b, size_t n, double* part, cudaStream_t st);
-cudaError_t launch_cg_init(const double* b, const double* q, const double* dinv, double* r, double* z, double* p,
-                           size_t n, double* sc, double* part, cudaStream_t st);
-cudaError_t launch_cg_alpha(const double* p, const double* q, size_t n, double* sc, double* part, cudaStream_t st);
-cudaError_t launch_cg_update(double* x, double* r, double* z, double* p, const double* q, const double* dinv,
-                             size_t n, double* sc, double* part, cudaStream_t st);
-cudaError_t launch_invert(double* dinv, const double* d, size_t n, cudaStream_t st);
+// T = double (FP64 CG) or float (inner CG of the mixed-precision solve);
+// dot products and scalars are FP64 in both.
+template <typename T>
+cudaError_t launch_set_constrained(T* v, const T* u, const uint32_t* idx, uint32_t n, cudaStream_t st);
+template <typename T>
+cudaError_t launch_dots(const T* a, const T* b, size_t n, double* part, cudaStream_t st);
+template <typename T>
+cudaError_t launch_cg_init(const T* b, const T* q, const T* dinv, T* r, T* z, T* p, size_t n, double* sc,
+                           double* part, cudaStream_t st);
+template <typename T>
+cudaError_t launch_cg_alpha(const T* p, const T* q, size_t n, double* sc, double* part, cudaStream_t st);
+template <typename T>
+cudaError_t launch_cg_update(T* x, T* r, T* z, T* p, const T* q, const T* dinv, size_t n, double* sc, double* part,
+                             cudaStream_t st);
+template <typename T>
+cudaError_t launch_invert(T* dinv, const double* d, size_t n, cudaStream_t st);
+// sc[S_PQ] = ||a||^2 (no CG bookkeeping)
+template <typename T>
+cudaError_t launch_norm2(const T* a, size_t n, double* sc, double* part, cudaStream_t st);
 cudaError_t launch_axpby(double* y, const double* x, double a, double b, size_t n, cudaStream_t st);
+cudaError_t launch_to_f32(float* out, const double* in, size_t n, cudaStream_t st);
+cudaError_t launch_add_f32(double* x, float* d, size_t n, cudaStream_t st);
 
 }  // namespace afm

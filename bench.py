@@ -328,6 +328,136 @@ def run_ours(args, w, rank, world, local_rank):
     return out
 
 
+def build_bc_problem(w, dev):
+    """Operator with the workload's boundary conditions (FP64_SPLIT arena: FP64 residual + FP32 view)."""
+    from amat_gb300 import Maps, aMatFree
+    from amat_gb300 import problems as P
+    t0 = time.time()
+    m = P.Mesh(w["kind"], w["n"], jitter=w["jitter"], seed=w["seed"])
+    dofs, vals = m.boundary_conditions()
+    maps = Maps()
+    maps.set_map(m.n_elem, m.dof_map(), m.ndpe, m.n_dofs)
+    maps.set_bdr_map(dofs, vals)
+    A = aMatFree(maps, 0, dev)
+    A.set_precision(PREC_NAMES["fp64_split"])
+    buf = np.empty((CHUNK, m.ndpe, m.ndpe))
+    for e0 in range(0, m.n_elem, CHUNK):
+        c = min(CHUNK, m.n_elem - e0)
+        m.element_matrices(e0, c, ngt=w["ngt"], out=buf[:c])
+        A.set_element_matrices(e0, buf[:c])
+    A.finalize()
+    log("solve setup %.1fs, %d DoF, %d constrained" % (time.time() - t0, m.n_dofs, len(dofs)))
+    return m, dofs, vals, A
+
+
+def run_solve(args, w, rank, world, local_rank):
+    """CG solves/s: FP64 Jacobi-PCG and mixed-precision refinement on the same system."""
+    import torch
+    from amat_gb300 import problems as P
+    dev = local_rank
+    torch.cuda.set_device(dev)
+    m, dofs, vals, A = build_bc_problem(w, dev)
+    rhs = A.apply_bc(m.load(ngt=w["ngt"]))
+    rtol = args.rtol
+    x64, st = A.solve(rhs, rtol=rtol, atol=0.0, maxit=100000)  # warm-up (captures the graphs)
+    log("fp64 CG: %d iterations, rel residual %.3e, %.3f s" % (st.iterations, st.rel_residual, st.seconds))
+    xm, stm = A.solve_mixed(rhs, rtol=rtol, atol=0.0, inner_rtol=args.inner_rtol, raise_on_fail=False)
+    log("mixed: status %d, %d refinements, %d inner iterations, rel residual %.3e, %.3f s" % (
+        stm.status, stm.refinements, stm.iterations, stm.rel_residual, stm.seconds))
+    if stm.status != 0:
+        raise SystemExit("mixed-precision solve did not converge")
+    t64, tmx = [], []
+    for _ in range(args.steps):
+        x64, st = A.solve(rhs, rtol=rtol, atol=0.0, maxit=100000)
+        t64.append(st.seconds)
+        xm, stm = A.solve_mixed(rhs, rtol=rtol, atol=0.0, inner_rtol=args.inner_rtol)
+        tmx.append(stm.seconds)
+    s64 = args.steps / sum(t64)
+    smx = args.steps / sum(tmx)
+    out = {"metric": "CG solves/s at %g rel. residual" % rtol, "value": smx, "unit": "solves/s", "n_gpus": world,
+           "steps": args.steps, "warmup": 1, "ms_per_step": 1e3 / smx, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32 inner / f64 residual", "data": "synthetic",
+           "config": {"workload": w["desc"], "n_dofs": m.n_dofs, "n_elements": m.n_elem, "rtol": rtol,
+                      "inner_rtol": args.inner_rtol},
+           "mixed": {"solves_per_s": smx, "inner_iterations": stm.iterations, "refinements": stm.refinements,
+                     "rel_residual": stm.rel_residual,
+                     "rel_error_vs_fp64_solution": float(np.linalg.norm(xm - x64) / np.linalg.norm(x64))},
+           "fp64": {"solves_per_s": s64, "iterations": st.iterations, "rel_residual": st.rel_residual,
+                    "dtype": "f64 (split arena)"},
+           "speedup_vs_fp64": smx / s64}
+    if P.KIND_DPN[w["kind"]] == 1:
+        c = m.coords
+        exact = np.sin(2 * np.pi * c[:, 0]) * np.sin(2 * np.pi * c[:, 1]) * np.sin(2 * np.pi * c[:, 2]) / (12 * np.pi ** 2)
+        out["analytic_rel_error_max"] = float(np.abs(xm - exact).max() / np.abs(exact).max())
+    return out if rank == 0 else None
+
+
+def run_batched(args, w, rank, world, local_rank):
+    """Block CG solves/s on nrhs load cases at once (FP32 inner batched CG under FP64 refinement),
+    against single-vector FP64 Jacobi-PCG on the same operator."""
+    import torch
+    dev = local_rank
+    torch.cuda.set_device(dev)
+    m, dofs, vals, A = build_bc_problem(w, dev)
+    n, R, rtol = m.n_dofs, args.nrhs, args.rtol
+    # R load cases N(0,1) per DoF; the constrained DoFs carry the (zero) prescribed values
+    B = np.random.default_rng(w["seed"]).standard_normal((n, R))
+    assert not np.any(vals)
+    B[dofs.astype(np.int64), :] = 0.0
+    dB = torch.tensor(B, device="cuda")
+    dX = torch.zeros_like(dB)
+    torch.cuda.synchronize()
+
+    def batched(mixed):
+        dX.zero_()
+        torch.cuda.synchronize()
+        return A.solve_batched_device(dB.data_ptr(), dX.data_ptr(), R, rtol=rtol, atol=0.0, mixed=mixed,
+                                      inner_rtol=args.inner_rtol, maxit=200000)
+
+    # warm-up: autotuner, graph capture
+    for _ in range(max(1, args.warmup - 2)):
+        stm = batched(True)
+    log("batched mixed: %d refinements, %d inner iterations, worst rel residual %.3e, %.3f s" % (
+        stm.refinements, stm.iterations, stm.rel_residual, stm.seconds))
+    tuning = {"fp32": A.batch_tuning(R, f32=True), "fp64": A.batch_tuning(R)}
+    clk = ClockSampler(dev)
+    with clk:
+        tm = [batched(True).seconds for _ in range(args.steps)]
+    smx = R * args.steps / sum(tm)
+    Xm = dX.cpu().numpy()
+    # single-vector FP64 CG on a few columns (the plain GPU path)
+    cols = list(range(min(R, args.single_cols)))
+    t64, x64 = [], {}
+    A.solve(B[:, 0], rtol=rtol, atol=0.0, maxit=200000)  # graph capture
+    for j in cols:
+        x, st = A.solve(B[:, j], rtol=rtol, atol=0.0, maxit=200000)
+        t64.append(st.seconds)
+        x64[j] = x
+    s64 = len(cols) / sum(t64)
+    err = max(float(np.linalg.norm(Xm[:, j] - x64[j]) / np.linalg.norm(x64[j])) for j in cols)
+    out = {"metric": "CG solves/s at %g rel. residual (%d load cases per solve)" % (rtol, R), "value": smx,
+           "unit": "solves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": 1e3 * sum(tm) / args.steps, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32 inner (batched) / f64 residual", "data": "synthetic",
+           "config": {"workload": w["desc"], "n_dofs": n, "n_elements": m.n_elem, "nrhs": R, "rtol": rtol,
+                      "inner_rtol": args.inner_rtol, "loads": "N(0,1) per DoF, seed %d" % w["seed"],
+                      "tuning (cols_per_thread, groups, ms)": tuning},
+           "batched_mixed": {"solves_per_s": smx, "inner_iterations": stm.iterations,
+                             "refinements": stm.refinements, "worst_rel_residual": stm.rel_residual,
+                             "max_rel_diff_vs_fp64_single": err},
+           "fp64_single": {"solves_per_s": s64, "iterations": st.iterations, "rel_residual": st.rel_residual,
+                           "columns_timed": len(cols)},
+           "speedup_vs_fp64_single": smx / s64}
+    if args.batched_fp64:
+        st64 = batched(False)
+        out["batched_fp64"] = {"solves_per_s": R / st64.seconds, "iterations": st64.iterations,
+                               "worst_rel_residual": st64.rel_residual}
+    clk_sum = clk.summary()
+    if clk_sum:
+        out["clocks"] = clk_sum
+    return out if rank == 0 else None
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -338,6 +468,12 @@ def main():
     ap.add_argument("--precision", default="auto", choices=sorted(PREC_NAMES))
     ap.add_argument("--also-native", type=int, default=1, help="also time native FP64 when the split path runs")
     ap.add_argument("--cpu-sample-elems", type=int, default=32768)
+    ap.add_argument("--mode", default="matvec", choices=["matvec", "solve", "batched"])
+    ap.add_argument("--nrhs", type=int, default=64)
+    ap.add_argument("--single-cols", type=int, default=2, help="columns solved one by one for the FP64 comparison")
+    ap.add_argument("--batched-fp64", type=int, default=0, help="also time the FP64 batched block CG")
+    ap.add_argument("--rtol", type=float, default=1e-8)
+    ap.add_argument("--inner-rtol", type=float, default=1e-2)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     w = WORKLOADS[args.workload]
@@ -351,7 +487,8 @@ def main():
             import torch
             torch.cuda.set_device(local_rank)
             torch.distributed.init_process_group("nccl")
-        out = run_ours(args, w, rank, world, local_rank)
+        run = {"matvec": run_ours, "solve": run_solve, "batched": run_batched}[args.mode]
+        out = run(args, w, rank, world, local_rank)
         if world > 1:
             import torch
             torch.distributed.destroy_process_group()

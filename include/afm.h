@@ -167,7 +167,8 @@ int afm_matvec(afm_operator* op, double* v, const double* u, int is_ghosted);
 /* v = K u on device arrays, enqueued on stream (NULL: the operator's stream)
  * and returned without waiting. */
 int afm_matvec_device(afm_operator* op, double* d_v, const double* d_u, void* stream);
-/* FP32 operator on float device vectors (needs AFM_PREC_FP32 Ke). */
+/* FP32 product on float device vectors: from an AFM_PREC_FP32 arena, or from
+ * the hi plane (the FP32-rounded Ke) of an AFM_PREC_FP64_SPLIT arena. */
 int afm_matvec_device_f32(afm_operator* op, float* d_v, const float* d_u, void* stream);
 
 /* aMatFree::MatMult_mf (include/aMatFree.hpp:3894-3941): u_c taken as zero
@@ -199,6 +200,63 @@ int afm_solve_cg(afm_operator* op, const double* b, double* x, double rtol, doub
 /* Same on device arrays (synchronous; returns when x is written). */
 int afm_solve_cg_device(afm_operator* op, const double* d_b, double* d_x, double rtol, double atol, int maxit,
                         int norm_type, afm_solve_stats* stats);
+
+/* Mixed-precision solve of the same system (no counterpart in the
+ * reference): iterative refinement whose
+ * outer residual r = b - A x is computed in FP64 with the FP64_SPLIT element
+ * matrices (MatMult_mf semantics), and whose correction A d = r is solved by
+ * Jacobi-PCG on the FP32 matrix (the hi plane of the same arena, half the
+ * bytes) with FP32 vectors and FP64 dot products and step scalars. Each inner
+ * solve stops at inner_rtol relative to its right-hand side or after
+ * max_inner iterations; the outer loop stops at ||b - A x|| <= max(rtol ||b||,
+ * atol), after max_outer steps, or after three steps in a row that do not
+ * bring a new smallest residual (one step may raise it before it falls).
+ * Needs an FP64_SPLIT operator (AFM_PREC_AUTO with in-range Ke). stats:
+ * iterations = inner iterations, refinements = outer steps. */
+int afm_solve_cg_mixed(afm_operator* op, const double* b, double* x, double rtol, double atol, int max_outer,
+                       double inner_rtol, int max_inner, afm_solve_stats* stats);
+int afm_solve_cg_mixed_device(afm_operator* op, const double* d_b, double* d_x, double rtol, double atol,
+                              int max_outer, double inner_rtol, int max_inner, afm_solve_stats* stats);
+/* MatMult_mf in FP32 on float device vectors (FP32 or FP64_SPLIT operator). */
+int afm_matmult_bc_device_f32(afm_operator* op, float* d_v, const float* d_u, void* stream);
+
+/* ---- batched: many right-hand sides at once -------------------------------
+ * Blocks are n_dofs x ld row-major device arrays (the nrhs values of one DoF
+ * are contiguous); nrhs is a multiple of 4, at most 256; every element must
+ * have more than 16 DoFs. Each element matrix is streamed once per call and
+ * applied to all columns (for example hex8 elasticity with 64 right-hand
+ * sides). The first call for a given (nrhs, ld,
+ * arithmetic) runs the autotuner, which times the kernel's tile shapes on the
+ * caller's data and keeps the fastest for the operator. No counterpart in the
+ * reference, whose matvec takes one vector. */
+int afm_matvec_batched_device(afm_operator* op, double* d_V, const double* d_U, uint32_t nrhs, uint32_t ld,
+                              void* stream);
+int afm_matvec_batched_device_f32(afm_operator* op, float* d_V, const float* d_U, uint32_t nrhs, uint32_t ld,
+                                  void* stream);
+/* MatMult_mf semantics column by column. */
+int afm_matmult_bc_batched_device(afm_operator* op, double* d_V, const double* d_U, uint32_t nrhs, uint32_t ld,
+                                  void* stream);
+int afm_matmult_bc_batched_device_f32(afm_operator* op, float* d_V, const float* d_U, uint32_t nrhs, uint32_t ld,
+                                      void* stream);
+/* The autotuner's choice for (nrhs, ld, f32): columns per thread tile,
+ * element groups per CTA, and the time of one product in ms. */
+int afm_get_batch_tuning(afm_operator* op, uint32_t nrhs, uint32_t ld, int f32, int* cols_per_thread,
+                         int* groups_per_cta, float* ms);
+/* Pins the batched kernel configuration for (nrhs, ld, f32) instead of the
+ * autotuner's choice: cols_per_thread 4 or 8, groups_per_cta 1..4. */
+int afm_set_batch_tuning(afm_operator* op, uint32_t nrhs, uint32_t ld, int f32, int cols_per_thread,
+                         int groups_per_cta);
+/* Batched Jacobi-PCG: one CG per column (own scalars and stopping test
+ * ||b_j - A x_j|| <= max(rtol ||b_j||, atol)), all advanced together, the
+ * iterations captured in CUDA graphs. FP64 arithmetic of the operator. ld =
+ * nrhs. stats->rel_residual: worst column. */
+int afm_solve_cg_batched_device(afm_operator* op, const double* d_B, double* d_X, uint32_t nrhs, double rtol,
+                                double atol, int maxit, afm_solve_stats* stats);
+/* Batched mixed-precision refinement: FP64 residual block on the split arena,
+ * inner batched Jacobi-PCG in FP32 (FP64 scalars) to inner_rtol per column. */
+int afm_solve_cg_batched_mixed_device(afm_operator* op, const double* d_B, double* d_X, uint32_t nrhs, double rtol,
+                                      double atol, int max_outer, double inner_rtol, int max_inner,
+                                      afm_solve_stats* stats);
 
 /* Largest operator (DoFs) afm_solve_cg_device_noalloc accepts. */
 #define AFM_NOALLOC_MAX_DOFS 262144u

@@ -76,7 +76,14 @@ def ref():
 
 
 def _p(a):
+    # Raw pointer only: the caller must keep `a` alive across the C call, so
+    # never pass a temporary (np.ascontiguousarray of a strided view is a
+    # fresh copy that Python may free before the call runs).
     return C.c_void_p(a.ctypes.data) if a is not None else None
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
 
 
 class Problem:
@@ -100,15 +107,16 @@ class Problem:
 
     # ---- oracle (restatement) ----
     def matvec(self, u):
+        u = _f64(u)
         v = np.empty(self.n_dofs)
-        lib().oracle_matvec(self.n_elem, self.n_dofs, _p(self.offsets), _p(self.map), _p(self.ke),
-                            _p(np.ascontiguousarray(u, dtype=np.float64)), _p(v))
+        lib().oracle_matvec(self.n_elem, self.n_dofs, _p(self.offsets), _p(self.map), _p(self.ke), _p(u), _p(v))
         return v
 
     def matvec_omp(self, u, v=None):
+        u = _f64(u)
         v = np.empty(self.n_dofs) if v is None else v
         t = lib().oracle_matvec_omp(self.n_elem, self.n_dofs, _p(self.offsets), _p(self.map), _p(self.ke), None,
-                                    _p(np.ascontiguousarray(u, dtype=np.float64)), _p(v))
+                                    _p(u), _p(v))
         return v, t
 
     def coloring(self):
@@ -126,10 +134,10 @@ class Problem:
         return d
 
     def matmult_bc(self, u):
+        u = _f64(u)
         v = np.empty(self.n_dofs)
         lib().oracle_matmult_bc(self.n_elem, self.n_dofs, _p(self.offsets), _p(self.map), _p(self.ke),
-                                _p(self.constrained), len(self.constrained),
-                                _p(np.ascontiguousarray(u, dtype=np.float64)), _p(v))
+                                _p(self.constrained), len(self.constrained), _p(u), _p(v))
         return v
 
     def apply_bc_rhs(self, rhs, bc_method=0):
@@ -139,11 +147,12 @@ class Problem:
         return r
 
     def pcg(self, b, x0=None, rtol=1e-10, atol=0.0, maxit=10000, norm_type=0, bc_method=0):
+        b = _f64(b)
         x = np.zeros(self.n_dofs) if x0 is None else np.array(x0, dtype=np.float64, copy=True)
         res = C.c_double()
         it = lib().oracle_pcg(self.n_elem, self.n_dofs, _p(self.offsets), _p(self.map), _p(self.ke),
-                              _p(self.constrained), len(self.constrained), bc_method,
-                              _p(np.ascontiguousarray(b, dtype=np.float64)), _p(x), rtol, atol, maxit, norm_type,
+                              _p(self.constrained), len(self.constrained), bc_method, _p(b), _p(x), rtol, atol,
+                              maxit, norm_type,
                               C.byref(res))
         return x, it, res.value
 

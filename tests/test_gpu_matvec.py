@@ -68,6 +68,47 @@ def test_fp32_operator(gpu, name):
     assert rel(v.cpu().double().numpy(), g["matvec"]) < FP32_RTOL
 
 
+@pytest.mark.parametrize("name", ["hex8_poisson_4", "mixed_random", "hex20_elastic_2", "tet10_elastic_2"])
+def test_fp32_product_from_split_arena(gpu, name):
+    """The hi plane of the split arena is the FP32 element matrix: FP32 product, half the bytes."""
+    import torch
+    g = load(name)
+    A = make_operator(g, 0, PRECISION.FP64_SPLIT)
+    u = torch.tensor(g["u"], dtype=torch.float32, device="cuda")
+    v = torch.empty_like(u)
+    torch.cuda.synchronize()
+    A.matvec_device_f32(v.data_ptr(), u.data_ptr())
+    A.synchronize()
+    assert rel(v.cpu().double().numpy(), g["matvec"]) < FP32_RTOL
+    w = torch.empty_like(u)
+    A.matmult_bc_device_f32(w.data_ptr(), u.data_ptr())
+    A.synchronize()
+    assert rel(w.cpu().double().numpy(), g["matmult_bc"]) < FP32_RTOL
+
+
+@pytest.mark.parametrize("kind,n", [(P.TET10_POISSON, 24), (P.HEX8_POISSON, 40), (P.HEX20_ELASTIC, 16)])
+def test_fp32_view_at_scale(gpu, kind, n):
+    """FP32 product of the split arena's hi plane against the FP64 product, many units per CTA."""
+    import torch
+    m = P.Mesh(kind, n, jitter=0.12, seed=4)
+    ke = m.element_matrices(ngt=3 if kind == P.HEX20_ELASTIC else 2)
+    maps = Maps()
+    maps.set_map(m.n_elem, m.dof_map(), m.ndpe, m.n_dofs)
+    A = aMatFree(maps)
+    A.set_precision(PRECISION.FP64_SPLIT)
+    A.set_element_matrices(0, ke)
+    A.finalize()
+    u = np.random.default_rng(5).uniform(-1, 1, m.n_dofs)
+    v64 = np.empty(m.n_dofs)
+    A.matvec(v64, u, True)
+    du = torch.tensor(u, dtype=torch.float32, device="cuda")
+    dv = torch.empty_like(du)
+    torch.cuda.synchronize()
+    A.matvec_device_f32(dv.data_ptr(), du.data_ptr())
+    A.synchronize()
+    assert rel(dv.cpu().double().numpy(), v64) < 1e-5
+
+
 def test_device_entry_on_torch_stream(gpu):
     import torch
     g = load("hex20_elastic_2")

@@ -87,3 +87,43 @@ def test_cg_breakdown_and_maxit_are_reported(gpu):
     # the operator stays usable after both
     x, st = A.solve(rhs, rtol=1e-10, atol=0.0)
     assert st.status == 0
+
+
+def test_mixed_precision_refinement(gpu):
+    """FP32 inner Jacobi-PCG with FP64 outer residual reaches the FP64 tolerance."""
+    m, ke, dofs, vals, A = poisson(12, jitter=0.15, seed=7, prec=PRECISION.FP64_SPLIT)
+    rhs = A.apply_bc(m.load())
+    x64, st64 = A.solve(rhs, rtol=1e-10, atol=0.0)
+    x, st = A.solve_mixed(rhs, rtol=1e-8, atol=0.0, inner_rtol=1e-4)
+    assert st.status == 0 and st.rel_residual <= 1e-8
+    assert st.refinements >= 2 and st.iterations > 0
+    assert rel(x, x64) < 1e-6
+    pr = oracle.Problem(m.n_dofs, m.dof_map(), ke, dofs, vals)
+    r = rhs - pr.matmult_bc(x)
+    assert np.linalg.norm(r) <= 1.01e-8 * np.linalg.norm(rhs)
+
+
+def test_mixed_precision_needs_split_arena(gpu):
+    m, ke, dofs, vals, A = poisson(4, prec=PRECISION.FP64)
+    with pytest.raises(AfmError) as e:
+        A.solve_mixed(A.apply_bc(m.load()))
+    assert e.value.name == "ERR_STATE"
+
+
+def test_mixed_precision_tet10(gpu):
+    """Mixed refinement on a jittered tet10 Poisson mesh (thread-per-element regime, many colours)."""
+    m = P.Mesh(P.TET10_POISSON, 10, jitter=0.15, seed=2)
+    ke = m.element_matrices()
+    dofs, vals = m.boundary_conditions()
+    maps = Maps()
+    maps.set_map(m.n_elem, m.dof_map(), m.ndpe, m.n_dofs)
+    maps.set_bdr_map(dofs, vals)
+    A = aMatFree(maps)
+    A.set_precision(PRECISION.FP64_SPLIT)
+    A.set_element_matrices(0, ke)
+    A.finalize()
+    rhs = A.apply_bc(m.load())
+    x64, st64 = A.solve(rhs, rtol=1e-10, atol=0.0)
+    x, st = A.solve_mixed(rhs, rtol=1e-8, atol=0.0, inner_rtol=1e-4, raise_on_fail=False)
+    assert st.status == 0, (st.refinements, st.iterations, st.rel_residual)
+    assert rel(x, x64) < 1e-6

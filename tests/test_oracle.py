@@ -106,3 +106,16 @@ def test_oracle_pcg_reports_breakdown():
     b[3] = np.nan
     _, it, _ = p.pcg(b, rtol=1e-12)
     assert it == -1
+
+
+def test_oracle_accepts_strided_columns():
+    """A column of a row-major block (a strided view) gives the same product
+    as its contiguous copy: the wrapper keeps the converted array alive."""
+    g = load("mixed_random")
+    p = problem(g)
+    U = np.random.default_rng(5).uniform(-1, 1, (p.n_dofs, 16))
+    for j in (0, 7, 15):
+        col = U[:, j]
+        assert not col.flags.c_contiguous
+        assert np.array_equal(p.matvec(col), p.matvec(col.copy()))
+        assert np.array_equal(p.matmult_bc(col), p.matmult_bc(col.copy()))
