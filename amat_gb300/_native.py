@@ -16,7 +16,7 @@ STATUS = {
     4: "NULL_L2G_MAP", 5: "GHOST_NODE_NOT_FOUND", 6: "UNKNOWN_MAT_TYPE", 7: "WRONG_COMMUNICATION",
     8: "UNKNOWN_DOF_TYPE", 9: "UNKNOWN_CONSTRAINT", 10: "UNKNOWN_BC_METH", 11: "NOT_IMPLEMENTED",
     12: "GLOBAL_DOF_ID_NOT_FOUND", 100: "ERR_CUDA", 101: "ERR_OOM", 102: "ERR_TIMEOUT", 103: "ERR_BREAKDOWN",
-    104: "ERR_STATE", 105: "ERR_INVALID_ARG", 106: "ERR_MAXIT",
+    104: "ERR_STATE", 105: "ERR_INVALID_ARG", 106: "ERR_MAXIT", 107: "ERR_INTERNAL",
 }
 
 
@@ -25,7 +25,8 @@ class AfmInfo(C.Structure):
         ("n_elements", C.c_uint32), ("n_dofs", C.c_uint32), ("n_colors", C.c_uint32),
         ("max_dofs_per_element", C.c_uint32), ("precision", C.c_int), ("ke_bytes", C.c_uint64),
         ("map_bytes", C.c_uint64), ("algorithmic_bytes", C.c_uint64), ("algorithmic_flops", C.c_double),
-        ("n_launches", C.c_uint32), ("device", C.c_int),
+        ("n_launches", C.c_uint32), ("device", C.c_int), ("n_patches", C.c_uint32),
+        ("n_patch_colors", C.c_uint32), ("patch_index_bytes", C.c_uint64),
     ]
 
 
@@ -61,6 +62,8 @@ AFM_SIGNATURES = {
     "afm_destroy": (I, [P]),
     "afm_set_matfree_type": (I, [P, I]),
     "afm_set_precision": (I, [P, I]),
+    "afm_set_patch_mode": (I, [P, I]),
+    "afm_patch_plan_host_matvec": (I, [U32, U32, P, P, P, P, P, P, P]),
     "afm_set_map": (I, [P, U32, P, U32, P, U32, P, U64, U64, U64]),
     "afm_set_bdr_map": (I, [P, P, P, U32]),
     "afm_set_element_matrix": (I, [P, U32, P, U32, U32, U32]),

@@ -179,6 +179,7 @@ __global__ void k_bbeta(double* sc, const double* part, uint32_t R, double maxit
     }
     const double rz = bsum(part, 0, R, j), rr = bsum(part, 1, R, j);
     c[B_BETA] = (c[B_RZ] != 0.0) ? rz / c[B_RZ] : 0.0;
+    c[B_RZOLD] = c[B_RZ];
     c[B_RZ] = rz;
     c[B_RR] = rr;
     const double it = c[B_ITER] + 1.0;
@@ -200,8 +201,85 @@ __global__ void __launch_bounds__(kBThreads) k_bp(T* __restrict__ p, const T* __
     for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < total; k += stride) {
         const size_t i = k / R;
         const uint32_t j = (uint32_t)(k % R);
+        // a finished column keeps its last direction
+        if (sc[(size_t)j * kBSlots + B_DONE] != 0.0) continue;
         const T beta = (T)sc[(size_t)j * kBSlots + B_BETA];
         p[i * ld + j] = beta * p[i * ld + j] + z[i * ld + j];
+    }
+}
+
+__global__ void k_bstore_norm(double* sc, const double* part, uint32_t R) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= R) return;
+    sc[(size_t)j * kBSlots + B_BN] = sqrt(bsum(part, 0, R, j));
+}
+
+__global__ void k_bcheck(double* sc, const double* part, uint32_t R, double rtol, double atol) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= R) return;
+    double* c = sc + (size_t)j * kBSlots;
+    const double rr = bsum(part, 0, R, j);
+    c[B_TRR] = rr;
+    c[B_CONV] = (sqrt(rr) <= fmax(rtol * c[B_BN], atol)) ? 1.0 : 0.0;
+}
+
+__global__ void __launch_bounds__(kBThreads) k_breliable(const double* __restrict__ r64, float* __restrict__ r,
+                                                         float* __restrict__ z, const float* __restrict__ p,
+                                                         const float* __restrict__ dinv, size_t n, uint32_t R,
+                                                         double* part) {
+    __shared__ double sh[kBThreads];
+    uint32_t ry, j, rstep;
+    row_col<float>(R, ry, j, rstep);
+    double rz = 0, rr = 0, rp = 0;
+    if (ry < rstep && j < R) {
+        const size_t chunk = (n + kBBlocks - 1) / kBBlocks;
+        const size_t r0 = (size_t)blockIdx.x * chunk, r1 = min(n, r0 + chunk);
+        for (size_t i = r0 + ry; i < r1; i += rstep) {
+            const size_t k = i * R + j;
+            const float ri = (float)r64[k];
+            const float zi = dinv[i] * ri;
+            r[k] = ri;
+            z[k] = zi;
+            rz = __fma_rn((double)ri, (double)zi, rz);
+            rr = __fma_rn((double)ri, (double)ri, rr);
+            rp = __fma_rn((double)ri, (double)p[k], rp);
+        }
+    }
+    double v[3] = {rz, rr, rp};
+    for (int qq = 0; qq < 3; qq++) {
+        col_reduce(ry < rstep ? v[qq] : 0.0, R, ry, j, rstep, sh);
+        if (ry == 0 && j < R) part[((size_t)qq * kBBlocks + blockIdx.x) * R + j] = sh[j];
+        __syncthreads();
+    }
+}
+
+__global__ void k_breliable_final(double* sc, const double* part, uint32_t R, double inner_rtol) {
+    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= R) return;
+    double* c = sc + (size_t)j * kBSlots;
+    const double rz = bsum(part, 0, R, j), rr = bsum(part, 1, R, j), rp = bsum(part, 2, R, j);
+    const bool restart = c[B_FLAG] != 0.0;  // the recursion broke down: fresh direction
+    const bool bad = (rz < 0.0 || rz != rz);
+    c[B_BETA] = (!restart && !bad && c[B_RZOLD] > 0.0) ? rz / c[B_RZOLD] : 0.0;
+    c[B_GAMMA] = (!restart && !bad && rz > 0.0) ? rp / rz : 0.0;
+    c[B_RZ] = rz;
+    c[B_RR] = rr;
+    c[B_ITER] = 0.0;
+    c[B_FLAG] = bad ? 1.0 : 0.0;
+    c[B_TOL] = inner_rtol * sqrt(rr);
+    c[B_DONE] = (c[B_CONV] != 0.0 || c[B_FLAG] != 0.0 || rr == 0.0) ? 1.0 : 0.0;
+}
+
+// p = z + beta (p - gamma z) per column
+__global__ void __launch_bounds__(kBThreads) k_breliable_p(float* __restrict__ p, const float* __restrict__ z, size_t n,
+                                                           uint32_t R, const double* sc) {
+    const size_t total = n * (size_t)R;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < total; k += stride) {
+        const uint32_t j = (uint32_t)(k % R);
+        const double* c = sc + (size_t)j * kBSlots;
+        const float beta = (float)c[B_BETA];
+        p[k] = __fmaf_rn(beta, p[k], (float)(1.0 - c[B_BETA] * c[B_GAMMA]) * z[k]);
     }
 }
 
@@ -254,6 +332,27 @@ cudaError_t launch_bcg_update(T* x, T* r, T* z, T* p, const T* q, const T* dinv,
     cudaMemsetAsync(remaining, 0, sizeof(unsigned int), st);
     k_bbeta<<<(R + 63) / 64, 64, 0, st>>>(sc, part, R, maxit, remaining);
     k_bp<T><<<grid_for(n * R), kBThreads, 0, st>>>(p, z, n, ld, R, sc);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bstore_norm(const double* a, size_t n, uint32_t R, double* sc, double* part, cudaStream_t st) {
+    k_bdots<double, 1><<<kBBlocks, kBThreads, 0, st>>>(a, a, nullptr, n, R, R, part);
+    k_bstore_norm<<<(R + 63) / 64, 64, 0, st>>>(sc, part, R);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bcheck(const double* a, size_t n, uint32_t R, double* sc, double* part, double rtol, double atol,
+                          cudaStream_t st) {
+    k_bdots<double, 1><<<kBBlocks, kBThreads, 0, st>>>(a, a, nullptr, n, R, R, part);
+    k_bcheck<<<(R + 63) / 64, 64, 0, st>>>(sc, part, R, rtol, atol);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_breliable(const double* r64, float* r, float* z, float* p, const float* dinv, size_t n, uint32_t R,
+                             double* sc, double* part, double inner_rtol, cudaStream_t st) {
+    k_breliable<<<kBBlocks, kBThreads, 0, st>>>(r64, r, z, p, dinv, n, R, part);
+    k_breliable_final<<<(R + 63) / 64, 64, 0, st>>>(sc, part, R, inner_rtol);
+    k_breliable_p<<<grid_for(n * R), kBThreads, 0, st>>>(p, z, n, R, sc);
     return cudaGetLastError();
 }
 

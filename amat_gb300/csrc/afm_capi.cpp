@@ -26,6 +26,7 @@
 
 #include "afm_batched_solver.hpp"
 #include "afm_internal.hpp"
+#include "afm_mixed.hpp"
 #include "afm_solver.hpp"
 
 namespace afm {
@@ -44,6 +45,30 @@ cudaError_t launch_batched_fp32(const Segment& s, const BatchArgs& a, int sm_cou
 cudaError_t configure_kernels_fp64();
 cudaError_t configure_kernels_split();
 cudaError_t configure_kernels_fp32();
+cudaError_t launch_patches_fp64(const PatchPlanGeom& pg, const PatchArgs& a, int sm_count, bool pdl, cudaStream_t st);
+cudaError_t launch_patches_split(const PatchPlanGeom& pg, const PatchArgs& a, int sm_count, bool pdl, cudaStream_t st);
+cudaError_t launch_patches_fp32(const PatchPlanGeom& pg, const PatchArgs& a, int sm_count, bool pdl, cudaStream_t st);
+size_t patch_smem_fp64(const PatchPlanGeom& pg, uint32_t copy_bytes);
+size_t patch_smem_split(const PatchPlanGeom& pg, uint32_t copy_bytes);
+size_t patch_smem_fp32(const PatchPlanGeom& pg, uint32_t copy_bytes);
+
+cudaError_t launch_patches(int prec, const PatchPlanGeom& pg, const PatchArgs& a, int sm_count, bool pdl,
+                           cudaStream_t stream) {
+    switch (prec) {
+        case AFM_PREC_FP64: return launch_patches_fp64(pg, a, sm_count, pdl, stream);
+        case AFM_PREC_FP64_SPLIT: return launch_patches_split(pg, a, sm_count, pdl, stream);
+        default: return launch_patches_fp32(pg, a, sm_count, pdl, stream);
+    }
+}
+
+size_t patch_smem_bytes(int prec, const PatchPlanGeom& pg, uint32_t copy_bytes) {
+    switch (prec) {
+        case AFM_PREC_FP64: return patch_smem_fp64(pg, copy_bytes);
+        case AFM_PREC_FP64_SPLIT: return patch_smem_split(pg, copy_bytes);
+        default: return patch_smem_fp32(pg, copy_bytes);
+    }
+}
+
 size_t segment_smem_fp64(const Segment& s);
 size_t segment_smem_split(const Segment& s);
 size_t segment_smem_fp32(const Segment& s);
@@ -151,6 +176,10 @@ void free_device(afm_operator* op) {
     cudaFree(op->d_bc_val);
     cudaFree(op->d_work);
     cudaFree(op->d_work32);
+    cudaFree(op->d_patch_desc);
+    cudaFree(op->d_patch_idx);
+    op->d_patch_desc = nullptr;
+    op->d_patch_idx = nullptr;
     op->d_ke = nullptr;
     op->d_map = nullptr;
     op->d_diag = nullptr;
@@ -253,6 +282,243 @@ void layout_element(const afm_operator* op, const Segment& s, uint32_t e, uint64
     }
 }
 
+// Patch plan of the small-element path (afm_patch.cuh). Patches grow
+// breadth first over shared DoFs from the lowest unassigned element, up to
+// P elements and kPatchMaxDofs distinct DoFs; patches get first-fit colours
+// in creation order (no two patches of a colour share a DoF). Fills the
+// element slots (op->perm, kNoElement for empty slots), one TPE-layout
+// segment covering every slot, the patch descriptors and index blocks.
+// Returns false (and leaves the operator to the colour-segment path) when the
+// patches need more than 64 colours or do not fit the shared memory.
+bool build_patch_plan(afm_operator* op, uint32_t n, int prec, std::vector<PatchDesc>& desc,
+                      std::vector<unsigned char>& idx) {
+    const uint32_t P = (n <= 10) ? 256 : 128;
+    const uint32_t NE = op->n_elem, ND = op->n_dofs;
+    const uint32_t* off = op->offsets.data();
+    const uint32_t* map = op->map.data();
+    // DoF -> elements
+    std::vector<uint64_t> doff((size_t)ND + 1, 0);
+    for (uint32_t x : op->map) doff[(size_t)x + 1]++;
+    for (size_t d = 0; d < ND; d++) doff[d + 1] += doff[d];
+    std::vector<uint32_t> del(op->map.size());
+    {
+        std::vector<uint64_t> pos(doff.begin(), doff.end() - 1);
+        for (uint32_t e = 0; e < NE; e++)
+            for (uint32_t i = off[e]; i < off[e + 1]; i++) del[pos[map[i]]++] = e;
+    }
+    // breadth-first patches
+    std::vector<int32_t> owner(NE, -1);
+    std::vector<uint32_t> dstamp(ND, UINT32_MAX), qstamp(NE, UINT32_MAX), queue;
+    std::vector<uint32_t> pel, poff(1, 0);
+    pel.reserve(NE);
+    uint32_t np = 0;
+    for (uint32_t seed = 0; seed < NE; seed++) {
+        if (owner[seed] >= 0) continue;
+        queue.clear();
+        queue.push_back(seed);
+        qstamp[seed] = np;
+        uint32_t cnt = 0, nd = 0;
+        for (size_t h = 0; h < queue.size() && cnt < P; h++) {
+            const uint32_t e = queue[h];
+            const uint32_t* m = map + off[e];
+            uint32_t add = 0;
+            for (uint32_t i = 0; i < n; i++) add += (dstamp[m[i]] != np);
+            if (nd + add > kPatchMaxDofs) continue;
+            owner[e] = (int32_t)np;
+            cnt++;
+            nd += add;
+            pel.push_back(e);
+            for (uint32_t i = 0; i < n; i++) dstamp[m[i]] = np;
+            for (uint32_t i = 0; i < n; i++)
+                for (uint64_t k = doff[m[i]]; k < doff[(size_t)m[i] + 1]; k++) {
+                    const uint32_t f = del[k];
+                    if (owner[f] < 0 && qstamp[f] != np) {
+                        qstamp[f] = np;
+                        queue.push_back(f);
+                    }
+                }
+        }
+        poff.push_back((uint32_t)pel.size());
+        np++;
+    }
+    // first-fit patch colours
+    std::vector<uint64_t> dmask(ND, 0);
+    std::vector<uint32_t> pcol(np);
+    uint32_t ncol = 0;
+    for (uint32_t q = 0; q < np; q++) {
+        uint64_t forb = 0;
+        for (uint32_t k = poff[q]; k < poff[q + 1]; k++)
+            for (uint32_t i = off[pel[k]]; i < off[pel[k] + 1]; i++) forb |= dmask[map[i]];
+        if (forb == ~0ull) return false;
+        const uint32_t c = (uint32_t)__builtin_ctzll(~forb);
+        pcol[q] = c;
+        ncol = std::max(ncol, c + 1);
+        for (uint32_t k = poff[q]; k < poff[q + 1]; k++)
+            for (uint32_t i = off[pel[k]]; i < off[pel[k] + 1]; i++) dmask[map[i]] |= 1ull << c;
+    }
+    std::vector<uint32_t> order(np);
+    std::iota(order.begin(), order.end(), 0u);
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return pcol[a] < pcol[b]; });
+    op->patch_color_first.assign(ncol + 1, 0);
+    for (uint32_t q = 0; q < np; q++) op->patch_color_first[pcol[q] + 1]++;
+    for (uint32_t c = 0; c < ncol; c++) op->patch_color_first[c + 1] += op->patch_color_first[c];
+
+    // sizes: local DoFs, units and index bytes per patch (colour order)
+    auto local_dofs = [&](uint32_t q, std::vector<uint32_t>& ld) {
+        ld.clear();
+        for (uint32_t k = poff[q]; k < poff[q + 1]; k++)
+            for (uint32_t i = off[pel[k]]; i < off[pel[k] + 1]; i++) ld.push_back(map[i]);
+        std::sort(ld.begin(), ld.end());
+        ld.erase(std::unique(ld.begin(), ld.end()), ld.end());
+    };
+    desc.assign(np, PatchDesc{});
+#pragma omp parallel
+    {
+        std::vector<uint32_t> ld;
+#pragma omp for schedule(dynamic, 64)
+        for (int64_t x = 0; x < (int64_t)np; x++) {
+            const uint32_t q = order[x];
+            local_dofs(q, ld);
+            PatchDesc& d = desc[x];
+            d.elems = poff[q + 1] - poff[q];
+            d.units = (d.elems + 31) / 32;
+            d.ndof = (uint32_t)ld.size();
+            d.idx_bytes = patch_slot_off(d.ndof, d.units, n) + patch_r16(d.elems * n * 2);
+        }
+    }
+    const size_t eb = entry_bytes(prec);
+    Segment s;
+    s.color = 0;
+    s.n = n;
+    s.regime = REG_TPE;
+    s.first_pos = 0;
+    s.unit_bytes = round16((uint64_t)n * n * eb * kTpeWidth);
+    if (prec == AFM_PREC_FP64_SPLIT) {
+        s.plane = n * n * kTpeWidth;
+        s.unit_bytes = 2ull * s.plane * 4;
+    }
+    PatchPlanGeom& G = op->patch_geom;
+    G = PatchPlanGeom{};
+    G.n = n;
+    uint64_t units = 0, ib = 0;
+    for (PatchDesc& d : desc) {
+        d.ke_off = units * s.unit_bytes;
+        d.idx_off = ib;
+        units += d.units;
+        ib += d.idx_bytes;
+        G.max_slots = std::max(G.max_slots, d.units * 32);
+        G.max_ndof = std::max(G.max_ndof, d.ndof);
+        G.max_idx = std::max(G.max_idx, d.idx_bytes);
+    }
+    if (patch_smem_bytes(prec, G, (uint32_t)s.unit_bytes) == 0) return false;
+    s.units = (uint32_t)units;
+    s.count = (uint32_t)(units * kTpeWidth);
+    s.ke_offset = 0;
+    s.map_offset = 0;
+
+    // element slots and index blocks
+    std::vector<uint8_t> is_bc(ND, 0);
+    for (uint32_t d : op->bc_unique) is_bc[d] = 1;
+    op->perm.assign((size_t)units * kTpeWidth, kNoElement);
+    idx.assign(ib, 0);
+#pragma omp parallel
+    {
+        std::vector<uint32_t> ld, cntd;
+#pragma omp for schedule(dynamic, 64)
+        for (int64_t x = 0; x < (int64_t)np; x++) {
+            const uint32_t q = order[x];
+            const PatchDesc& d = desc[x];
+            local_dofs(q, ld);
+            const uint64_t slot0 = d.ke_off / s.unit_bytes * kTpeWidth;
+            for (uint32_t el = 0; el < d.elems; el++) op->perm[slot0 + el] = pel[poff[q] + el];
+            unsigned char* blk = idx.data() + d.idx_off;
+            uint32_t* glob = reinterpret_cast<uint32_t*>(blk);
+            uint16_t* lmap = reinterpret_cast<uint16_t*>(blk + patch_lmap_off(d.ndof));
+            uint16_t* coff = reinterpret_cast<uint16_t*>(blk + patch_csr_off(d.ndof, d.units, n));
+            uint16_t* slot = reinterpret_cast<uint16_t*>(blk + patch_slot_off(d.ndof, d.units, n));
+            for (uint32_t k = 0; k < d.ndof; k++) glob[k] = ld[k] | (is_bc[ld[k]] ? kBcFlag : 0u);
+            auto loc = [&](uint32_t g) {
+                return (uint32_t)(std::lower_bound(ld.begin(), ld.end(), g) - ld.begin());
+            };
+            cntd.assign(d.ndof + 1, 0);
+            for (uint32_t el = 0; el < d.elems; el++) {
+                const uint32_t* m = map + off[pel[poff[q] + el]];
+                const uint32_t un = el / 32, lane = el % 32;
+                for (uint32_t c = 0; c < n; c++) {
+                    const uint32_t l = loc(m[c]);
+                    lmap[((size_t)un * n + c) * 32 + lane] = (uint16_t)l;
+                    cntd[l + 1]++;
+                }
+            }
+            for (uint32_t k = 0; k < d.ndof; k++) cntd[k + 1] += cntd[k];
+            for (uint32_t k = 0; k <= d.ndof; k++) coff[k] = (uint16_t)cntd[k];
+            const uint32_t cap = d.units * 32;
+            for (uint32_t el = 0; el < d.elems; el++) {
+                const uint32_t* m = map + off[pel[poff[q] + el]];
+                for (uint32_t r = 0; r < n; r++) slot[cntd[loc(m[r])]++] = (uint16_t)(r * cap + el);
+            }
+        }
+    }
+    op->segs.assign(1, s);
+    op->n_patches = np;
+    return true;
+}
+
+// Colour-sorted element order (colour, then element size) and one segment
+// per (colour, size) with its arena and map offsets.
+void build_segments(afm_operator* op, int prec) {
+    op->perm.resize(op->n_elem);
+    std::iota(op->perm.begin(), op->perm.end(), 0u);
+    std::stable_sort(op->perm.begin(), op->perm.end(), [&](uint32_t a, uint32_t b) {
+        if (op->colors[a] != op->colors[b]) return op->colors[a] < op->colors[b];
+        const uint32_t na = op->offsets[a + 1] - op->offsets[a], nb = op->offsets[b + 1] - op->offsets[b];
+        return na < nb;
+    });
+
+    op->segs.clear();
+    const size_t eb = entry_bytes(prec);
+    uint64_t ke_off = 0, map_off = 0;
+    for (uint32_t p = 0; p < op->n_elem;) {
+        const uint32_t e = op->perm[p];
+        Segment s;
+        s.color = op->colors[e];
+        s.n = op->offsets[e + 1] - op->offsets[e];
+        s.regime = (s.n <= kTpeMaxN) ? REG_TPE : REG_WPE;
+        s.first_pos = p;
+        uint32_t q = p;
+        while (q < op->n_elem) {
+            const uint32_t f = op->perm[q];
+            if (op->colors[f] != s.color || op->offsets[f + 1] - op->offsets[f] != s.n) break;
+            q++;
+        }
+        s.count = q - p;
+        if (s.regime == REG_TPE) {
+            s.units = (s.count + kTpeWidth - 1) / kTpeWidth;
+            s.unit_bytes = round16((uint64_t)s.n * s.n * eb * kTpeWidth);
+            if (prec == AFM_PREC_FP64_SPLIT) {
+                s.plane = s.n * s.n * kTpeWidth;
+                s.unit_bytes = 2ull * s.plane * 4;
+            }
+        } else {
+            s.units = s.count;
+            s.unit_bytes = round16((uint64_t)s.n * s.n * eb);
+            if (prec == AFM_PREC_FP64_SPLIT) {
+                s.plane = (s.n * s.n + 3) / 4 * 4;  // 16-byte aligned planes
+                s.unit_bytes = 2ull * s.plane * 4;
+            }
+        }
+        s.ke_offset = ke_off;
+        s.map_offset = map_off;
+        ke_off += s.unit_bytes * s.units;
+        map_off += (uint64_t)s.units * (s.regime == REG_TPE ? kTpeWidth : 1) * s.n;
+        map_off = (map_off + 3) / 4 * 4;  // keep 16-byte alignment of each segment's map
+        op->segs.push_back(s);
+        p = q;
+    }
+    op->ke_bytes = ke_off;
+    op->map_bytes = map_off * sizeof(uint32_t);
+}
+
 int upload_arena(afm_operator* op) {
     // staging in pinned memory, chunks of ~256 MB of whole units
     const size_t kChunk = 256ull << 20;
@@ -281,6 +547,7 @@ int upload_arena(afm_operator* op) {
 #pragma omp parallel for schedule(static)
             for (int64_t rel = (int64_t)el0; rel < (int64_t)el1; rel++) {
                 const uint32_t e = op->perm[s.first_pos + rel];
+                if (e == kNoElement) continue;  // empty slot of a patch
                 if (op->precision == AFM_PREC_FP64)
                     layout_element<double>(op, s, e, rel, u0, stage);
                 else if (op->precision == AFM_PREC_FP64_SPLIT)
@@ -344,6 +611,27 @@ int enqueue_matvec(afm_operator* op, void* d_v, const void* d_u, int bc_mode, cu
     const size_t vbytes = (size_t)op->n_dofs * (kprec == AFM_PREC_FP32 ? 4 : 8);
     AFM_CUDA(cudaMemsetAsync(d_v, 0, vbytes, st));
     bool first = true;
+    if (op->use_patches) {
+        const Segment& s = op->segs[0];
+        for (size_t c = 0; c + 1 < op->patch_color_first.size(); c++) {
+            PatchArgs a;
+            a.desc = op->d_patch_desc + op->patch_color_first[c];
+            a.count = op->patch_color_first[c + 1] - op->patch_color_first[c];
+            a.ke = op->d_ke;
+            a.idx = op->d_patch_idx;
+            a.u = d_u;
+            a.v = d_v;
+            a.unit_bytes = s.unit_bytes;
+            a.copy_bytes = (uint32_t)s.unit_bytes;
+            a.plane = s.plane;
+            if (f32 && op->precision == AFM_PREC_FP64_SPLIT) a.copy_bytes = s.plane * 4;
+            a.bc_mode = bc_mode;
+            a.err = op->d_err;
+            AFM_CUDA(launch_patches(kprec, op->patch_geom, a, op->sm_count, !first, st));
+            first = false;
+        }
+        return AFM_SUCCESS;
+    }
     for (const Segment& s : op->segs) {
         if (s.units == 0) continue;
         SegArgs a;
@@ -661,6 +949,46 @@ void drop_graph(afm_operator::CgGraph& g) {
 // scalars to the pinned host mirror: one host round trip per batch instead of
 // one per iteration. Steps after convergence leave every vector unchanged, so
 // the result equals the iteration-by-iteration loop.
+// The captured CG iteration batch of gc for the vectors V (re-captured when
+// the vectors, the batch size or the operator's device buffers changed). The
+// graph ends with a copy of the scalars to the pinned host mirror. The stream
+// must be idle.
+template <typename T>
+int ensure_cg_graph(afm_operator* op, afm_operator::CgGraph& gc, const CgVectors<T>& V) {
+    cudaStream_t st = op->stream;
+    double* h = op->h_scalars;
+    const int batch = op->n_dofs > (1u << 20) ? 4 : 8;
+    const void* key[6] = {V.r, V.z, V.p, V.q, V.dinv, V.x};
+    bool same = gc.exec && gc.batch == batch && gc.gen == op->generation;
+    for (int i = 0; i < 6 && same; i++) same = (gc.key[i] == key[i]);
+    if (same) return AFM_SUCCESS;
+    drop_graph(gc);
+    AFM_CUDA(cudaStreamSynchronize(st));
+    AFM_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    int s = AFM_SUCCESS;
+    for (int i = 0; i < batch && s == AFM_SUCCESS; i++) s = cg_step<T>(op, V, st);
+    if (s == AFM_SUCCESS &&
+        cudaMemcpyAsync(h, op->d_scalars, sizeof(double) * kScalarSlots, cudaMemcpyDeviceToHost, st) != cudaSuccess)
+        s = fail(AFM_ERR_CUDA, "capture: scalar copy");
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(st, &graph);
+    if (s != AFM_SUCCESS) {
+        if (graph) cudaGraphDestroy(graph);
+        return s;
+    }
+    if (ec != cudaSuccess) return fail(AFM_ERR_CUDA, "stream capture: %s", cudaGetErrorString(ec));
+    const cudaError_t ei = cudaGraphInstantiate(&gc.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ei != cudaSuccess) {
+        gc.exec = nullptr;
+        return fail(AFM_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ei));
+    }
+    gc.batch = batch;
+    gc.gen = op->generation;
+    for (int i = 0; i < 6; i++) gc.key[i] = key[i];
+    return AFM_SUCCESS;
+}
+
 template <typename T>
 int run_cg_iterations(afm_operator* op, afm_operator::CgGraph& gc, const CgVectors<T>& V, double tol, int maxit,
                       int norm_type, int* iters, int* status) {
@@ -686,36 +1014,8 @@ int run_cg_iterations(afm_operator* op, afm_operator::CgGraph& gc, const CgVecto
     h[S_NORM] = (double)norm_type;
     AFM_CUDA(cudaMemcpyAsync(op->d_scalars + S_DONE, h + S_DONE, sizeof(double) * (S_NORM - S_DONE + 1),
                              cudaMemcpyHostToDevice, st));
-    const int batch = op->n_dofs > (1u << 20) ? 4 : 8;
-    const void* key[6] = {V.r, V.z, V.p, V.q, V.dinv, V.x};
-    bool same = gc.exec && gc.batch == batch && gc.gen == op->generation;
-    for (int i = 0; i < 6 && same; i++) same = (gc.key[i] == key[i]);
-    if (!same) {
-        drop_graph(gc);
-        AFM_CUDA(cudaStreamSynchronize(st));
-        AFM_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-        int s = AFM_SUCCESS;
-        for (int i = 0; i < batch && s == AFM_SUCCESS; i++) s = cg_step<T>(op, V, st);
-        if (s == AFM_SUCCESS && cudaMemcpyAsync(h, op->d_scalars, sizeof(double) * kScalarSlots,
-                                                cudaMemcpyDeviceToHost, st) != cudaSuccess)
-            s = fail(AFM_ERR_CUDA, "capture: scalar copy");
-        cudaGraph_t graph = nullptr;
-        const cudaError_t ec = cudaStreamEndCapture(st, &graph);
-        if (s != AFM_SUCCESS) {
-            if (graph) cudaGraphDestroy(graph);
-            return s;
-        }
-        if (ec != cudaSuccess) return fail(AFM_ERR_CUDA, "stream capture: %s", cudaGetErrorString(ec));
-        const cudaError_t ei = cudaGraphInstantiate(&gc.exec, graph, 0);
-        cudaGraphDestroy(graph);
-        if (ei != cudaSuccess) {
-            gc.exec = nullptr;
-            return fail(AFM_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ei));
-        }
-        gc.batch = batch;
-        gc.gen = op->generation;
-        for (int i = 0; i < 6; i++) gc.key[i] = key[i];
-    }
+    int s = ensure_cg_graph<T>(op, gc, V);
+    if (s) return s;
     for (;;) {
         AFM_CUDA(cudaGraphLaunch(gc.exec, st));
         AFM_CUDA(cudaStreamSynchronize(st));
@@ -732,7 +1032,206 @@ int run_cg_iterations(afm_operator* op, afm_operator::CgGraph& gc, const CgVecto
     return AFM_SUCCESS;
 }
 
+// Iterative-refinement stopping rule. The FP64 residual of the refined x may
+// grow for a step before it falls (an FP32 correction that shrinks the error
+// can overshoot in the residual norm), so refinement stops only after
+// kIrMaxStall consecutive steps without a new smallest residual.
+constexpr int kIrMaxStall = 3;
+
+bool ir_progress(double rn, double* best, int* stall) {
+    if (rn < *best) {
+        *best = rn;
+        *stall = 0;
+        return true;
+    }
+    return ++*stall < kIrMaxStall;
+}
+
 }  // namespace
+
+// ---- resumable mixed-precision solve (afm_mixed.hpp) ------------------------
+
+namespace afm {
+
+namespace {
+
+struct MixedVectors {
+    double *r64, *q64;
+    float* b32;
+    CgVectors<float> V;
+};
+
+MixedVectors mixed_vectors(afm_operator* op) {
+    const size_t n = op->n_dofs;
+    float* b32 = op->d_work32;
+    return MixedVectors{op->d_work + 2 * n, op->d_work + 5 * n, b32,
+                        CgVectors<float>{b32 + n, b32 + 2 * n, b32 + 3 * n, b32 + 4 * n, b32 + 6 * n, b32 + 5 * n}};
+}
+
+int mixed_record(MixedSolve& m) {
+    AFM_CUDA(cudaMemcpyAsync(m.op->h_scalars, m.op->d_scalars, sizeof(double) * kScalarSlots,
+                             cudaMemcpyDeviceToHost, m.op->stream));
+    AFM_CUDA(cudaEventRecord(m.ev, m.op->stream));
+    return AFM_SUCCESS;
+}
+
+// FP64 true residual r = b - A x (split arena, MatMult_mf semantics), ||r||^2 into S_PQ
+int mixed_residual(MixedSolve& m) {
+    afm_operator* op = m.op;
+    const MixedVectors W = mixed_vectors(op);
+    const size_t n = op->n_dofs;
+    cudaStream_t st = op->stream;
+    int s = afm_matmult_bc_device(op, W.q64, m.d_x, st);
+    if (s) return s;
+    AFM_CUDA(cudaMemcpyAsync(W.r64, m.d_b, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    AFM_CUDA(launch_axpby(W.r64, W.q64, -1.0, 1.0, n, st));
+    AFM_CUDA(launch_norm2(W.r64, n, op->d_scalars, op->d_scalars + kScalarSlots, st));
+    m.phase = MS_RESID;
+    return mixed_record(m);
+}
+
+int mixed_finish(MixedSolve& m, int status) {
+    m.status = status;
+    m.phase = MS_DONE;
+    AFM_CUDA(cudaEventRecord(m.e1, m.op->stream));
+    return AFM_SUCCESS;
+}
+
+// the FP32 segment ended: x += x_s, then the FP64 residual
+int mixed_segment_end(MixedSolve& m, int iters, int seg_status) {
+    m.inner_total += iters;
+    m.fresh = (seg_status == AFM_ERR_BREAKDOWN);
+    AFM_CUDA(launch_add_f32(m.d_x, mixed_vectors(m.op).V.x, m.op->n_dofs, m.op->stream));
+    m.outer++;
+    return mixed_residual(m);
+}
+
+}  // namespace
+
+int mixed_begin(MixedSolve& m) {
+    afm_operator* op = m.op;
+    AFM_CHECK_OP(op);
+    if (!op->finalized) return fail(AFM_ERR_STATE, "solve before finalize");
+    if (op->precision != AFM_PREC_FP64_SPLIT)
+        return fail(AFM_ERR_STATE, "mixed-precision solve needs the FP64_SPLIT arena (hi plane = FP32 matrix)");
+    if (!m.d_b || !m.d_x) return fail(AFM_ERR_INVALID_ARG, "null vector");
+    DeviceGuard g(op->device);
+    int s = ensure_work(op, 8);
+    if (s) return s;
+    s = ensure_work32(op, 7);
+    if (s) return s;
+    AFM_CUDA(cudaEventCreateWithFlags(&m.ev, cudaEventDisableTiming));
+    AFM_CUDA(cudaEventCreate(&m.e0));
+    AFM_CUDA(cudaEventCreate(&m.e1));
+    const MixedVectors W = mixed_vectors(op);
+    const size_t n = op->n_dofs;
+    cudaStream_t st = op->stream;
+    AFM_CUDA(cudaEventRecord(m.e0, st));
+    AFM_CUDA(launch_invert(W.V.dinv, op->d_diag, n, st));
+    AFM_CUDA(cudaMemsetAsync(W.V.x, 0, n * sizeof(float), st));
+    AFM_CUDA(launch_norm2(m.d_b, n, op->d_scalars, op->d_scalars + kScalarSlots, st));
+    m.phase = MS_NORMB;
+    return mixed_record(m);
+}
+
+bool mixed_ready(const MixedSolve& m) { return m.ev && cudaEventQuery(m.ev) == cudaSuccess; }
+
+int mixed_advance(MixedSolve& m) {
+    afm_operator* op = m.op;
+    DeviceGuard g(op->device);
+    double* h = op->h_scalars;
+    const size_t n = op->n_dofs;
+    cudaStream_t st = op->stream;
+    const MixedVectors W = mixed_vectors(op);
+    double* sc = op->d_scalars;
+    double* part = sc + kScalarSlots;
+    switch (m.phase) {
+        case MS_NORMB:
+            m.bn = std::sqrt(h[S_PQ]);
+            m.tol = std::max(m.rtol * m.bn, m.atol);
+            return mixed_residual(m);
+        case MS_RESID: {
+            m.rn = std::sqrt(h[S_PQ]);
+            if (std::isnan(m.rn)) return mixed_finish(m, AFM_ERR_BREAKDOWN);
+            if (m.rn <= m.tol) return mixed_finish(m, AFM_SUCCESS);
+            if (!ir_progress(m.rn, &m.best, &m.stall) || m.outer >= m.max_outer)
+                return mixed_finish(m, AFM_ERR_MAXIT);
+            if (m.fresh) {
+                // FP32 Jacobi-PCG on A d = r from d = 0
+                AFM_CUDA(launch_to_f32(W.b32, W.r64, n, st));
+                AFM_CUDA(cudaMemsetAsync(W.V.q, 0, n * sizeof(float), st));
+                AFM_CUDA(launch_cg_init(W.b32, W.V.q, W.V.dinv, W.V.r, W.V.z, W.V.p, n, sc, part, st));
+            } else {
+                // reliable update: the recursion continues from the true residual
+                AFM_CUDA(launch_cg_reliable(W.r64, W.V.r, W.V.z, W.V.p, W.V.dinv, n, sc, part, st));
+            }
+            // the segment ends once the FP32 residual has dropped by inner_rtol
+            m.inner_tol = std::max(m.inner_rtol * m.rn, m.tol);
+            m.phase = MS_SEGSTART;
+            return mixed_record(m);
+        }
+        case MS_SEGSTART: {
+            const double n0 = std::sqrt(h[S_RR]);
+            if (h[S_FLAG] != 0.0 || std::isnan(n0)) return mixed_segment_end(m, 0, AFM_ERR_BREAKDOWN);
+            if (n0 <= m.inner_tol) return mixed_segment_end(m, 0, AFM_SUCCESS);
+            if (m.max_inner <= 0) return mixed_segment_end(m, 0, AFM_ERR_MAXIT);
+            h[S_TOL] = m.inner_tol;
+            h[S_MAXIT] = (double)m.max_inner;
+            h[S_NORM] = 0.0;
+            AFM_CUDA(cudaMemcpyAsync(sc + S_DONE, h + S_DONE, sizeof(double) * (S_NORM - S_DONE + 1),
+                                     cudaMemcpyHostToDevice, st));
+            int s = ensure_cg_graph<float>(op, op->cg32, W.V);
+            if (s) return s;
+            AFM_CUDA(cudaGraphLaunch(op->cg32.exec, st));
+            AFM_CUDA(cudaEventRecord(m.ev, st));
+            m.phase = MS_ITER;
+            return AFM_SUCCESS;
+        }
+        case MS_ITER: {
+            if (h[S_DONE] == 0.0) {
+                AFM_CUDA(cudaGraphLaunch(op->cg32.exec, st));
+                AFM_CUDA(cudaEventRecord(m.ev, st));
+                return AFM_SUCCESS;
+            }
+            const double nrm = std::sqrt(h[S_RR]);
+            const int seg = h[S_FLAG] != 0.0 ? AFM_ERR_BREAKDOWN : (nrm <= m.inner_tol ? AFM_SUCCESS : AFM_ERR_MAXIT);
+            return mixed_segment_end(m, (int)h[S_ITER], seg);
+        }
+        default:
+            return fail(AFM_ERR_STATE, "mixed solve step in phase %d", m.phase);
+    }
+}
+
+int mixed_end(MixedSolve& m, afm_solve_stats* stats) {
+    int s = AFM_SUCCESS;
+    float ms = 0.f;
+    if (m.phase == MS_DONE && m.op) {
+        DeviceGuard g(m.op->device);
+        if (cudaEventSynchronize(m.e1) == cudaSuccess) cudaEventElapsedTime(&ms, m.e0, m.e1);
+        s = check_device_error(m.op);
+    }
+    if (m.ev) cudaEventDestroy(m.ev);
+    if (m.e0) cudaEventDestroy(m.e0);
+    if (m.e1) cudaEventDestroy(m.e1);
+    m.ev = m.e0 = m.e1 = nullptr;
+    if (s) return s;
+    if (m.phase != MS_DONE) return fail(AFM_ERR_STATE, "mixed solve not finished");
+    if (stats) {
+        stats->iterations = m.inner_total;
+        stats->status = m.status;
+        stats->rel_residual = m.bn > 0 ? m.rn / m.bn : m.rn;
+        stats->residual_norm = m.rn;
+        stats->seconds = ms * 1e-3;
+        stats->refinements = m.outer;
+    }
+    if (m.status != AFM_SUCCESS)
+        return fail(m.status, m.status == AFM_ERR_MAXIT ? "refinement stopped after %d steps"
+                                                        : "breakdown after %d steps",
+                    m.outer);
+    return ok();
+}
+
+}  // namespace afm
 
 extern "C" {
 
@@ -760,6 +1259,7 @@ const char* afm_status_string(int s) {
         case AFM_ERR_STATE: return "ERR_STATE";
         case AFM_ERR_INVALID_ARG: return "ERR_INVALID_ARG";
         case AFM_ERR_MAXIT: return "ERR_MAXIT";
+        case AFM_ERR_INTERNAL: return "ERR_INTERNAL";
         default: return "UNKNOWN_STATUS";
     }
 }
@@ -830,6 +1330,13 @@ int afm_set_precision(afm_operator* op, int p) {
     AFM_CHECK_OP(op);
     if (p < AFM_PREC_FP64 || p > AFM_PREC_AUTO) return fail(AFM_ERR_INVALID_ARG, "precision %d", p);
     op->precision_req = p;
+    op->finalized = false;
+    return ok();
+}
+
+int afm_set_patch_mode(afm_operator* op, int enable) {
+    AFM_CHECK_OP(op);
+    op->patch_mode = enable ? 1 : 0;
     op->finalized = false;
     return ok();
 }
@@ -958,65 +1465,40 @@ int afm_finalize(afm_operator* op) {
     }
     op->precision = prec;
 
-    // colouring and colour-sorted order
+    // colouring (the reference's greedy colouring, also the segment order)
     op->n_colors = color_elements(op->n_dofs, op->n_elem, op->offsets, op->map, op->colors);
-    op->perm.resize(op->n_elem);
-    std::iota(op->perm.begin(), op->perm.end(), 0u);
-    std::stable_sort(op->perm.begin(), op->perm.end(), [&](uint32_t a, uint32_t b) {
-        if (op->colors[a] != op->colors[b]) return op->colors[a] < op->colors[b];
-        const uint32_t na = op->offsets[a + 1] - op->offsets[a], nb = op->offsets[b + 1] - op->offsets[b];
-        return na < nb;
-    });
 
-    // segments and their arena / map offsets
+    // small elements of one size: patch plan
+    std::vector<PatchDesc> pdesc;
+    std::vector<unsigned char> pidx;
+    op->use_patches = false;
+    op->n_patches = 0;
+    op->patch_color_first.clear();
     op->segs.clear();
-    const size_t eb = entry_bytes(prec);
-    uint64_t ke_off = 0, map_off = 0;
-    for (uint32_t p = 0; p < op->n_elem;) {
-        const uint32_t e = op->perm[p];
-        Segment s;
-        s.color = op->colors[e];
-        s.n = op->offsets[e + 1] - op->offsets[e];
-        s.regime = (s.n <= kTpeMaxN) ? REG_TPE : REG_WPE;
-        s.first_pos = p;
-        uint32_t q = p;
-        while (q < op->n_elem) {
-            const uint32_t f = op->perm[q];
-            if (op->colors[f] != s.color || op->offsets[f + 1] - op->offsets[f] != s.n) break;
-            q++;
-        }
-        s.count = q - p;
-        if (s.regime == REG_TPE) {
-            s.units = (s.count + kTpeWidth - 1) / kTpeWidth;
-            s.unit_bytes = round16((uint64_t)s.n * s.n * eb * kTpeWidth);
-            if (prec == AFM_PREC_FP64_SPLIT) {
-                s.plane = s.n * s.n * kTpeWidth;
-                s.unit_bytes = 2ull * s.plane * 4;
-            }
-        } else {
-            s.units = s.count;
-            s.unit_bytes = round16((uint64_t)s.n * s.n * eb);
-            if (prec == AFM_PREC_FP64_SPLIT) {
-                s.plane = (s.n * s.n + 3) / 4 * 4;  // 16-byte aligned planes
-                s.unit_bytes = 2ull * s.plane * 4;
-            }
-        }
-        s.ke_offset = ke_off;
-        s.map_offset = map_off;
-        ke_off += s.unit_bytes * s.units;
-        map_off += (uint64_t)s.units * (s.regime == REG_TPE ? kTpeWidth : 1) * s.n;
-        map_off = (map_off + 3) / 4 * 4;  // keep 16-byte alignment of each segment's map
-        op->segs.push_back(s);
-        p = q;
+    {
+        bool uniform = op->n_elem > 0;
+        const uint32_t n0 = op->n_elem ? op->offsets[1] - op->offsets[0] : 0;
+        for (uint32_t e = 0; e < op->n_elem && uniform; e++) uniform = (op->offsets[e + 1] - op->offsets[e] == n0);
+        if (op->patch_mode && uniform && !op->dup_in_element && n0 >= 1 && n0 <= kPatchMaxN)
+            op->use_patches = build_patch_plan(op, n0, prec, pdesc, pidx);
+        if (!op->use_patches) op->segs.clear();
     }
-    op->ke_bytes = ke_off;
-    op->map_bytes = map_off * sizeof(uint32_t);
+
+    // colour-sorted order and segments (elements not run as patches)
+    if (!op->use_patches) {
+        build_segments(op, prec);
+    } else {
+        op->ke_bytes = (uint64_t)op->segs[0].units * op->segs[0].unit_bytes;
+        op->map_bytes = 0;  // the patch index blocks replace the map
+    }
+    const uint64_t map_off = op->map_bytes / sizeof(uint32_t);
 
     // device map with constrained columns flagged
     std::vector<uint8_t> is_bc(op->n_dofs, 0);
     for (uint32_t d : op->bc_unique) is_bc[d] = 1;
     std::vector<uint32_t> hmap(map_off, 0);
     for (const Segment& s : op->segs) {
+        if (op->use_patches) break;
         for (uint32_t rel = 0; rel < s.count; rel++) {
             const uint32_t e = op->perm[s.first_pos + rel];
             for (uint32_t i = 0; i < s.n; i++) {
@@ -1066,6 +1548,14 @@ int afm_finalize(afm_operator* op) {
                                  op->stream));
         AFM_CUDA(cudaMemcpyAsync(op->d_bc_val, op->values.data(), sizeof(double) * op->n_bc,
                                  cudaMemcpyHostToDevice, op->stream));
+    }
+    if (op->use_patches) {
+        op->patch_idx_bytes = pidx.size();
+        AFM_CUDA(cudaMalloc((void**)&op->d_patch_desc, sizeof(PatchDesc) * std::max<size_t>(pdesc.size(), 1)));
+        AFM_CUDA(cudaMalloc((void**)&op->d_patch_idx, std::max<size_t>(pidx.size(), 16)));
+        AFM_CUDA(cudaMemcpyAsync(op->d_patch_desc, pdesc.data(), sizeof(PatchDesc) * pdesc.size(),
+                                 cudaMemcpyHostToDevice, op->stream));
+        AFM_CUDA(cudaMemcpyAsync(op->d_patch_idx, pidx.data(), pidx.size(), cudaMemcpyHostToDevice, op->stream));
     }
     AFM_CUDA(cudaStreamSynchronize(op->stream));
     int st = upload_arena(op);
@@ -1287,107 +1777,28 @@ int afm_solve_cg(afm_operator* op, const double* b, double* x, double rtol, doub
     return ok();
 }
 
-// Iterative-refinement stopping rule. The FP64 residual of the refined x may
-// grow for a step before it falls (an FP32 correction that shrinks the error
-// can overshoot in the residual norm), so refinement stops only after
-// kIrMaxStall consecutive steps without a new smallest residual.
-constexpr int kIrMaxStall = 3;
-
-static bool ir_progress(double rn, double* best, int* stall) {
-    if (rn < *best) {
-        *best = rn;
-        *stall = 0;
-        return true;
-    }
-    return ++*stall < kIrMaxStall;
-}
 
 int afm_solve_cg_mixed_device(afm_operator* op, const double* d_b, double* d_x, double rtol, double atol,
                               int max_outer, double inner_rtol, int max_inner, afm_solve_stats* stats) {
-    AFM_CHECK_OP(op);
-    if (!op->finalized) return fail(AFM_ERR_STATE, "solve before finalize");
-    if (op->precision != AFM_PREC_FP64_SPLIT)
-        return fail(AFM_ERR_STATE, "mixed-precision solve needs the FP64_SPLIT arena (hi plane = FP32 matrix)");
-    if (!d_b || !d_x) return fail(AFM_ERR_INVALID_ARG, "null vector");
-    DeviceGuard g(op->device);
-    int s = ensure_work(op, 8);
-    if (s) return s;
-    s = ensure_work32(op, 7);
-    if (s) return s;
-    const size_t n = op->n_dofs;
-    double* r64 = op->d_work + 2 * n;
-    double* q64 = op->d_work + 5 * n;
-    float* b32 = op->d_work32;
-    CgVectors<float> V{b32 + n, b32 + 2 * n, b32 + 3 * n, b32 + 4 * n, b32 + 6 * n, b32 + 5 * n};
-    double* sc = op->d_scalars;
-    double* part = op->d_scalars + kScalarSlots;
-    double* h = op->h_scalars;
-    cudaStream_t st = op->stream;
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
-    cudaEventRecord(e0, st);
-    AFM_CUDA(launch_invert(V.dinv, op->d_diag, n, st));
-    AFM_CUDA(cudaMemsetAsync(V.x, 0, n * sizeof(float), st));
-    AFM_CUDA(launch_norm2(d_b, n, sc, part, st));
-    AFM_CUDA(cudaMemcpyAsync(h, sc, sizeof(double) * kScalarSlots, cudaMemcpyDeviceToHost, st));
-    AFM_CUDA(cudaStreamSynchronize(st));
-    const double bn = std::sqrt(h[S_PQ]);
-    const double tol = std::max(rtol * bn, atol);
-    int outer = 0, inner_total = 0, status = AFM_ERR_MAXIT, stall = 0;
-    double rn = 0.0, best = HUGE_VAL;
-    for (;;) {
-        // outer residual r = b - A x in FP64 (split arena, MatMult_mf semantics)
-        s = afm_matmult_bc_device(op, q64, d_x, st);
-        if (s) return s;
-        AFM_CUDA(cudaMemcpyAsync(r64, d_b, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
-        AFM_CUDA(launch_axpby(r64, q64, -1.0, 1.0, n, st));
-        AFM_CUDA(launch_norm2(r64, n, sc, part, st));
-        AFM_CUDA(cudaMemcpyAsync(h, sc, sizeof(double) * kScalarSlots, cudaMemcpyDeviceToHost, st));
-        AFM_CUDA(cudaStreamSynchronize(st));
-        rn = std::sqrt(h[S_PQ]);
-        if (std::isnan(rn)) {
-            status = AFM_ERR_BREAKDOWN;
+    MixedSolve m;
+    m.op = op;
+    m.d_b = d_b;
+    m.d_x = d_x;
+    m.rtol = rtol;
+    m.atol = atol;
+    m.max_outer = max_outer;
+    m.inner_rtol = inner_rtol;
+    m.max_inner = max_inner;
+    int s = mixed_begin(m);
+    while (s == AFM_SUCCESS && m.phase != MS_DONE) {
+        if (cudaEventSynchronize(m.ev) != cudaSuccess) {
+            s = fail(AFM_ERR_CUDA, "mixed solve: %s", cudaGetErrorString(cudaGetLastError()));
             break;
         }
-        if (rn <= tol) {
-            status = AFM_SUCCESS;
-            break;
-        }
-        if (!ir_progress(rn, &best, &stall) || outer >= max_outer) break;  // MAXIT
-        // inner FP32 Jacobi-PCG on A d = r from d = 0, FP64 dots and scalars
-        AFM_CUDA(launch_to_f32(b32, r64, n, st));
-        AFM_CUDA(cudaMemsetAsync(V.q, 0, n * sizeof(float), st));
-        AFM_CUDA(launch_cg_init(b32, V.q, V.dinv, V.r, V.z, V.p, n, sc, part, st));
-        AFM_CUDA(cudaMemcpyAsync(h, sc, sizeof(double) * kScalarSlots, cudaMemcpyDeviceToHost, st));
-        AFM_CUDA(cudaStreamSynchronize(st));
-        int it = 0, ist = 0;
-        s = run_cg_iterations<float>(op, op->cg32, V, inner_rtol * std::sqrt(h[S_BB]), max_inner, 0, &it, &ist);
-        if (s) return s;
-        inner_total += it;
-        AFM_CUDA(launch_add_f32(d_x, V.x, n, st));  // x += d, d = 0
-        outer++;
+        s = mixed_advance(m);
     }
-    cudaEventRecord(e1, st);
-    AFM_CUDA(cudaStreamSynchronize(st));
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, e0, e1);
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    s = check_device_error(op);
-    if (s) return s;
-    if (stats) {
-        stats->iterations = inner_total;
-        stats->status = status;
-        stats->rel_residual = bn > 0 ? rn / bn : rn;
-        stats->residual_norm = rn;
-        stats->seconds = ms * 1e-3;
-        stats->refinements = outer;
-    }
-    if (status != AFM_SUCCESS)
-        return fail(status, status == AFM_ERR_MAXIT ? "refinement stopped after %d steps" : "breakdown after %d steps",
-                    outer);
-    return ok();
+    const int st = mixed_end(m, stats);
+    return s != AFM_SUCCESS ? s : st;
 }
 
 int afm_solve_cg_mixed(afm_operator* op, const double* b, double* x, double rtol, double atol, int max_outer,
@@ -1538,12 +1949,11 @@ int afm_solve_cg_batched_mixed_device(afm_operator* op, const double* d_B, doubl
     if (!d_B || !d_X) return fail(AFM_ERR_INVALID_ARG, "null block");
     DeviceGuard g(op->device);
     const size_t n = op->n_dofs, N = n * nrhs;
-    // FP64: residual block and product block; FP32: rhs, r, z, p, q, d and 1/diag
+    // FP64: residual block (and a spare); FP32: rhs, r, z, p, q, d and 1/diag
     s = ensure_bwork(op, 2 * N + (7 * N + n + 1) / 2 + 2);
     if (s) return s;
     s = ensure_bscalars(op, nrhs);
     if (s) return s;
-    double* r64 = op->d_bwork;
     double* q64 = op->d_bwork + N;
     float* f = reinterpret_cast<float*>(op->d_bwork + 2 * N);
     float* b32 = f;
@@ -1561,31 +1971,53 @@ int afm_solve_cg_batched_mixed_device(afm_operator* op, const double* d_B, doubl
     cudaEventRecord(e0, st);
     AFM_CUDA(launch_invert(V.dinv, op->d_diag, n, st));
     AFM_CUDA(cudaMemsetAsync(V.x, 0, N * sizeof(float), st));
+    double* sc = op->d_bsc;
+    double* part = op->d_bsc + (size_t)nrhs * kBSlots;
+    AFM_CUDA(launch_bstore_norm(d_B, n, nrhs, sc, part, st));
+    std::vector<double> hs((size_t)nrhs * kBSlots);
     int outer = 0, inner_total = 0, status = AFM_ERR_MAXIT, stall = 0;
     double worst = 0.0, best = HUGE_VAL;
     for (;;) {
-        // FP64 residual block R = B - A X and the worst column's relative norm
-        s = batched_residual(op, d_B, d_X, nrhs, q64, &worst, tr64, ng64);
+        // FP64 residual block R = B - A X and per-column convergence
+        s = enqueue_matvec_batched(op, q64, d_X, nrhs, nrhs, 1, st, false, tr64, ng64);
         if (s) return s;
-        if (std::isnan(worst)) {
+        AFM_CUDA(launch_bset_constrained(q64, d_X, op->d_bc_idx, op->n_bc, nrhs, nrhs, st));
+        AFM_CUDA(launch_axpby(q64, d_B, 1.0, -1.0, N, st));  // q = b - A x
+        AFM_CUDA(launch_bcheck(q64, n, nrhs, sc, part, rtol, atol, st));
+        AFM_CUDA(cudaMemcpyAsync(hs.data(), sc, hs.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+        AFM_CUDA(cudaStreamSynchronize(st));
+        bool all = true, nan = false;
+        worst = 0.0;
+        for (uint32_t j = 0; j < nrhs; j++) {
+            const double* c = &hs[(size_t)j * kBSlots];
+            const double rn = std::sqrt(c[B_TRR]);
+            nan = nan || std::isnan(rn);
+            all = all && c[B_CONV] != 0.0;
+            worst = std::max(worst, c[B_BN] > 0 ? rn / c[B_BN] : rn);
+        }
+        if (nan) {
             status = AFM_ERR_BREAKDOWN;
             break;
         }
-        if (worst <= rtol) {
+        if (all) {
             status = AFM_SUCCESS;
             break;
         }
         if (!ir_progress(worst, &best, &stall) || outer >= max_outer) break;  // MAXIT
-        AFM_CUDA(cudaMemcpyAsync(r64, q64, N * sizeof(double), cudaMemcpyDeviceToDevice, st));
-        AFM_CUDA(launch_to_f32(b32, r64, N, st));
-        AFM_CUDA(cudaMemsetAsync(V.q, 0, N * sizeof(float), st));
-        AFM_CUDA(launch_bcg_init(b32, V.q, V.dinv, V.r, V.z, V.p, n, nrhs, nrhs, op->d_bsc,
-                                 op->d_bsc + (size_t)nrhs * kBSlots, inner_rtol, 0.0, st));
+        if (outer == 0) {
+            // FP32 block Jacobi-PCG on A D = R from D = 0
+            AFM_CUDA(launch_to_f32(b32, q64, N, st));
+            AFM_CUDA(cudaMemsetAsync(V.q, 0, N * sizeof(float), st));
+            AFM_CUDA(launch_bcg_init(b32, V.q, V.dinv, V.r, V.z, V.p, n, nrhs, nrhs, sc, part, inner_rtol, 0.0, st));
+        } else {
+            // reliable update: each column's recursion continues from its true residual
+            AFM_CUDA(launch_breliable(q64, V.r, V.z, V.p, V.dinv, n, nrhs, sc, part, inner_rtol, st));
+        }
         int it = 0;
         s = run_bcg<float>(op, V, nrhs, (double)max_inner, tr32, ng32, &it);
         if (s) return s;
         inner_total += it;
-        AFM_CUDA(launch_add_f32(d_X, V.x, N, st));  // X += D, D = 0
+        AFM_CUDA(launch_add_f32(d_X, V.x, N, st));  // X += X_s, X_s = 0
         outer++;
     }
     cudaEventRecord(e1, st);
@@ -1605,6 +2037,100 @@ int afm_solve_cg_batched_mixed_device(afm_operator* op, const double* d_B, doubl
         stats->refinements = outer;
     }
     if (status != AFM_SUCCESS) return fail(status, "batched refinement stopped after %d steps", outer);
+    return ok();
+}
+
+int afm_patch_plan_host_matvec(uint32_t n_elem, uint32_t n_dofs, const uint32_t* offsets, const uint32_t* map,
+                               const double* ke, const double* u, double* v, uint32_t* n_patches,
+                               uint32_t* n_patch_colors) {
+    if (!offsets || !map || !ke || !u || !v || n_elem == 0) return fail(AFM_ERR_INVALID_ARG, "bad arguments");
+    afm_operator op;
+    op.n_elem = n_elem;
+    op.n_dofs = n_dofs;
+    op.offsets.assign(offsets, offsets + n_elem + 1);
+    op.map.assign(map, map + offsets[n_elem]);
+    const uint32_t n = offsets[1] - offsets[0];
+    for (uint32_t e = 0; e < n_elem; e++) {
+        if (offsets[e + 1] - offsets[e] != n) return fail(AFM_NOT_IMPLEMENTED, "elements of different sizes");
+        for (uint32_t i = offsets[e]; i < offsets[e + 1]; i++) {
+            if (map[i] >= n_dofs) return fail(AFM_INDEX_OUT_OF_BOUNDS, "DoF %u", map[i]);
+            for (uint32_t k = offsets[e]; k < i; k++)
+                if (map[k] == map[i]) return fail(AFM_NOT_IMPLEMENTED, "element %u lists DoF %u twice", e, map[i]);
+        }
+    }
+    if (n == 0 || n > kPatchMaxN) return fail(AFM_NOT_IMPLEMENTED, "n = %u", n);
+    std::vector<PatchDesc> desc;
+    std::vector<unsigned char> idx;
+    if (!build_patch_plan(&op, n, AFM_PREC_FP64, desc, idx)) return fail(AFM_NOT_IMPLEMENTED, "no patch plan");
+    const Segment& s = op.segs[0];
+    // every element in exactly one slot; slots agree with the descriptors
+    std::vector<uint32_t> seen(n_elem, 0);
+    for (uint32_t e : op.perm)
+        if (e != kNoElement) seen[e]++;
+    for (uint32_t e = 0; e < n_elem; e++)
+        if (seen[e] != 1) return fail(AFM_ERR_INTERNAL, "element %u in %u slots", e, seen[e]);
+    std::fill(v, v + n_dofs, 0.0);
+    std::vector<uint32_t> stamp(n_dofs, UINT32_MAX);
+    std::vector<double> us, ve;
+    const size_t ncol = op.patch_color_first.size() - 1;
+    for (size_t c = 0; c < ncol; c++) {
+        for (uint32_t x = op.patch_color_first[c]; x < op.patch_color_first[c + 1]; x++) {
+            const PatchDesc& d = desc[x];
+            if (d.idx_off % 16 || d.idx_bytes % 16 || d.ke_off % s.unit_bytes || d.idx_off + d.idx_bytes > idx.size() ||
+                d.ndof > op.patch_geom.max_ndof || d.units * 32 > op.patch_geom.max_slots ||
+                d.idx_bytes > op.patch_geom.max_idx || d.elems > d.units * 32 || d.ndof == 0)
+                return fail(AFM_ERR_INTERNAL, "patch %u descriptor", x);
+            const unsigned char* blk = idx.data() + d.idx_off;
+            const uint32_t* glob = reinterpret_cast<const uint32_t*>(blk);
+            const uint16_t* lmap = reinterpret_cast<const uint16_t*>(blk + patch_lmap_off(d.ndof));
+            const uint16_t* coff = reinterpret_cast<const uint16_t*>(blk + patch_csr_off(d.ndof, d.units, n));
+            const uint16_t* slot = reinterpret_cast<const uint16_t*>(blk + patch_slot_off(d.ndof, d.units, n));
+            const uint32_t cap = d.units * 32;
+            // patches of one colour share no DoF
+            for (uint32_t k = 0; k < d.ndof; k++) {
+                const uint32_t g = glob[k] & kDofMask;
+                if (g >= n_dofs || (k && g <= (glob[k - 1] & kDofMask)))
+                    return fail(AFM_ERR_INTERNAL, "patch %u DoF list", x);
+                if (stamp[g] == c) return fail(AFM_ERR_INTERNAL, "colour %zu: DoF %u in two patches", c, g);
+                stamp[g] = (uint32_t)c;
+            }
+            if (coff[0] != 0 || coff[d.ndof] != d.elems * n) return fail(AFM_ERR_INTERNAL, "patch %u offsets", x);
+            us.assign(d.ndof, 0.0);
+            for (uint32_t k = 0; k < d.ndof; k++) us[k] = u[glob[k] & kDofMask];
+            ve.assign((size_t)n * cap, -1.0);
+            const uint64_t slot0 = d.ke_off / s.unit_bytes * kTpeWidth;
+            for (uint32_t un = 0; un < d.units; un++)
+                for (uint32_t lane = 0; lane < 32; lane++) {
+                    const uint32_t el = un * 32 + lane;
+                    const uint32_t e = op.perm[slot0 + el];
+                    if ((el < d.elems) != (e != kNoElement)) return fail(AFM_ERR_INTERNAL, "patch %u slot %u", x, el);
+                    for (uint32_t r = 0; r < n; r++) {
+                        double acc = 0.0;
+                        for (uint32_t cc = 0; cc < n; cc++) {
+                            const uint32_t l = lmap[((size_t)un * n + cc) * 32 + lane];
+                            if (l >= d.ndof) return fail(AFM_ERR_INTERNAL, "patch %u local index", x);
+                            if (e != kNoElement) {
+                                if ((glob[l] & kDofMask) != map[offsets[e] + cc])
+                                    return fail(AFM_ERR_INTERNAL, "patch %u element %u column %u", x, e, cc);
+                                acc += ke[(size_t)e * n * n + (size_t)r * n + cc] * us[l];
+                            }
+                        }
+                        ve[(size_t)r * cap + el] = acc;
+                    }
+                }
+            for (uint32_t k = 0; k < d.ndof; k++) {
+                double sum = 0.0;
+                for (uint32_t q = coff[k]; q < coff[k + 1]; q++) {
+                    if (slot[q] >= n * cap || (slot[q] % cap) >= d.elems)
+                        return fail(AFM_ERR_INTERNAL, "patch %u contribution slot", x);
+                    sum += ve[slot[q]];
+                }
+                v[glob[k] & kDofMask] += sum;
+            }
+        }
+    }
+    if (n_patches) *n_patches = op.n_patches;
+    if (n_patch_colors) *n_patch_colors = (uint32_t)ncol;
     return ok();
 }
 
@@ -1631,9 +2157,15 @@ int afm_get_info(afm_operator* op, afm_info* info) {
     info->algorithmic_bytes = alg + 2 * vb * (uint64_t)op->n_dofs;
     info->algorithmic_flops = fl;
     uint32_t launches = 1;  // the zero fill of v
-    for (const Segment& s : op->segs)
-        if (s.units) launches++;
+    if (op->use_patches)
+        launches += (uint32_t)op->patch_color_first.size() - 1;
+    else
+        for (const Segment& s : op->segs)
+            if (s.units) launches++;
     info->n_launches = launches;
+    info->n_patches = op->n_patches;
+    info->n_patch_colors = op->use_patches ? (uint32_t)op->patch_color_first.size() - 1 : 0;
+    info->patch_index_bytes = op->use_patches ? op->patch_idx_bytes : 0;
     info->device = op->device;
     return ok();
 }

@@ -71,6 +71,70 @@ struct BatchArgs {
     int* err;
 };
 
+// ---- patch path (small elements) -----------------------------------------
+// Elements with at most kPatchMaxN DoFs (all of one size, no DoF listed twice
+// in an element) run as patches: compact groups of up to kPatchElems elements,
+// coloured so that patches of one colour share no DoF (see afm_patch.cuh).
+constexpr uint32_t kPatchMaxN = 12;
+constexpr uint32_t kPatchMaxDofs = 1024;  // local DoFs per patch (uint16 indices)
+
+constexpr uint32_t kNoElement = 0xffffffffu;  // empty element slot
+
+#ifdef __CUDACC__
+#define AFM_HD __host__ __device__
+#else
+#define AFM_HD
+#endif
+// Byte offsets inside one patch index block (all 16-byte aligned): glob
+// (uint32 x ndof), lmap (uint16 x units x n x 32), csr_off (uint16 x ndof+1),
+// slot (uint16 x contributions).
+AFM_HD inline uint32_t patch_r16(uint32_t x) { return (x + 15u) & ~15u; }
+AFM_HD inline uint32_t patch_lmap_off(uint32_t ndof) { return patch_r16(ndof * 4u); }
+AFM_HD inline uint32_t patch_csr_off(uint32_t ndof, uint32_t units, uint32_t n) {
+    return patch_lmap_off(ndof) + units * n * 64u;
+}
+AFM_HD inline uint32_t patch_slot_off(uint32_t ndof, uint32_t units, uint32_t n) {
+    return patch_csr_off(ndof, units, n) + patch_r16((ndof + 1u) * 2u);
+}
+
+// One patch: its Ke units and its index block (both 16-byte aligned).
+struct PatchDesc {
+    uint64_t ke_off;     // bytes into the Ke arena
+    uint64_t idx_off;    // bytes into the index arena
+    uint32_t units;      // units of 32 element slots
+    uint32_t ndof;       // local DoFs
+    uint32_t idx_bytes;  // size of the index block (16-byte multiple)
+    uint32_t elems;      // elements (the rest of the slots are empty)
+};
+
+// Arguments of one patch-colour launch.
+struct PatchArgs {
+    const PatchDesc* desc;    // the colour's first patch
+    uint32_t count;           // patches of the colour
+    const unsigned char* ke;  // Ke arena
+    const unsigned char* idx; // index arena
+    const void* u;
+    void* v;
+    uint64_t unit_bytes;      // stride between units
+    uint32_t copy_bytes;      // bytes copied per unit (hi plane only for FP32 on a split arena)
+    uint32_t plane;           // entries per plane (split arena)
+    int bc_mode;
+    int* err;
+};
+
+// Patch launch geometry shared by all colours of an operator.
+struct PatchPlanGeom {
+    uint32_t n = 0;           // DoFs per element
+    uint32_t max_slots = 0;   // largest patch, in element slots (32 x units)
+    uint32_t max_ndof = 0;    // largest local DoF count
+    uint32_t max_idx = 0;     // largest index block, bytes
+};
+
+cudaError_t launch_patches(int prec, const PatchPlanGeom& pg, const PatchArgs& a, int sm_count, bool pdl,
+                           cudaStream_t stream);
+// Shared memory of a patch launch (0 if it does not fit).
+size_t patch_smem_bytes(int prec, const PatchPlanGeom& pg, uint32_t copy_bytes);
+
 // Launches one segment on stream. prec: afm_precision (FP64, FP64_SPLIT, FP32).
 // pdl: allow the launch to begin while the previous kernel on the stream
 // drains (programmatic dependent launch; v is touched only after it ends).
@@ -102,6 +166,7 @@ struct afm_operator {
     std::vector<uint32_t> offsets;  // n_elem + 1
     std::vector<uint32_t> map;      // global DoF ids
     bool dup_in_element = false;    // some element lists a DoF twice
+    int patch_mode = 1;             // 1: small elements run as patches when eligible; 0: colour segments
 
     // boundary conditions
     std::vector<uint64_t> constrained;
@@ -148,6 +213,15 @@ struct afm_operator {
     };
     CgGraph cg64, cg32, bcg64, bcg32;
     uint64_t generation = 0;  // bumped whenever device buffers are released
+
+    // patch path (small elements): patches in colour order
+    bool use_patches = false;
+    afm::PatchPlanGeom patch_geom;
+    std::vector<uint32_t> patch_color_first;  // n_patch_colors + 1 offsets into the patch list
+    uint32_t n_patches = 0;
+    afm::PatchDesc* d_patch_desc = nullptr;
+    unsigned char* d_patch_idx = nullptr;
+    size_t patch_idx_bytes = 0;
 
     // batched (multi right-hand side) state
     double* d_bwork = nullptr;

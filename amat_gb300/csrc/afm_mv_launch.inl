@@ -4,6 +4,7 @@
 #include <algorithm>
 
 #include "afm_batched.cuh"
+#include "afm_patch.cuh"
 
 namespace afm {
 
@@ -180,6 +181,59 @@ cudaError_t BATCH_FN(const Segment& s, const BatchArgs& a, int sm_count, int tr,
     return cudaLaunchKernelExC(&cfg, fn, params);
 }
 
+// ---- patch path (small elements) -----------------------------------------
+
+namespace {
+void* pick_patch_kernel(uint32_t n) {
+    switch (n) {
+        case 4: return (void*)afm_patch_kernel<4, ARITH>;
+        case 8: return (void*)afm_patch_kernel<8, ARITH>;
+        case 10: return (void*)afm_patch_kernel<10, ARITH>;
+        default: return (void*)afm_patch_kernel<0, ARITH>;
+    }
+}
+
+PatchLayout patch_layout(const PatchPlanGeom& pg, uint32_t copy_bytes) {
+    PatchLayout L;
+    L.slot_bytes = (copy_bytes + kSlotAlign - 1) / kSlotAlign * kSlotAlign;
+    L.idx_bytes = patch_r16(pg.max_idx);
+    L.us_bytes = patch_r16(pg.max_ndof * (uint32_t)sizeof(typename ARITH::UT));
+    L.ve_bytes = patch_r16(pg.n * pg.max_slots * (uint32_t)sizeof(typename ARITH::VT));
+    const uint32_t fixed = 64 + 2 * L.group_bytes();
+    L.stages = 0;
+    if (fixed < kSmemBudget) {
+        const uint32_t st = (kSmemBudget - fixed) / (L.slot_bytes + 16);
+        L.stages = st > 16 ? 16 : st;
+    }
+    return L;
+}
+}  // namespace
+
+cudaError_t PATCH_FN(const PatchPlanGeom& pg, const PatchArgs& a, int sm_count, bool pdl, cudaStream_t stream) {
+    if (a.count == 0) return cudaSuccess;
+    PatchLayout L = patch_layout(pg, a.copy_bytes);
+    if (L.stages < 2 || pg.n == 0 || pg.n > kPatchMaxN) return cudaErrorInvalidConfiguration;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(a.count < (uint32_t)sm_count ? a.count : (uint32_t)sm_count);
+    cfg.blockDim = dim3(kPatchThreads);
+    cfg.dynamicSmemBytes = L.total();
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    PatchArgs args = a;
+    uint32_t n_rt = pg.n;
+    void* params[] = {&args, &L, &n_rt};
+    return cudaLaunchKernelExC(&cfg, pick_patch_kernel(pg.n), params);
+}
+
+size_t PATCH_SMEM_FN(const PatchPlanGeom& pg, uint32_t copy_bytes) {
+    const PatchLayout L = patch_layout(pg, copy_bytes);
+    return L.stages >= 2 ? L.total() : 0;
+}
+
 size_t SMEM_FN(const Segment& s) { return ring_layout(s, s.unit_bytes, false, nullptr).total(); }
 
 // Raises the dynamic shared-memory limit of every kernel instance on the
@@ -193,6 +247,11 @@ cudaError_t CONFIG_FN() {
                     cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kSmemBudget + 1024));
                 if (e != cudaSuccess) return e;
             }
+    for (uint32_t nn : {4u, 8u, 10u, 0u}) {
+        cudaError_t e = cudaFuncSetAttribute(pick_patch_kernel(nn), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)(kSmemBudget + 1024));
+        if (e != cudaSuccess) return e;
+    }
     for (int tr : {4, 8})
         for (uint32_t nn : {24u, 60u, 7u}) {
             cudaError_t e = cudaFuncSetAttribute(pick_batch_kernel(nn, tr), cudaFuncAttributeMaxDynamicSharedMemorySize,

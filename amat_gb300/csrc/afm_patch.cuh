@@ -1,0 +1,207 @@
+// Patch kernel for small elements (n <= kPatchMaxN): v += sum over the patches
+// of one patch colour of P_p^T (sum over the patch's elements of P_e^T Ke P_e) P_p u.
+//
+// A patch is a compact group of up to 256 elements (128 when n > 10), grown
+// breadth first over shared DoFs when the operator is finalised. Patches of one
+// colour share no DoF. Per patch an index block is stored:
+//   glob[ndof]           sorted global DoF ids (kBcFlag on constrained DoFs)
+//   lmap[units][n][32]   uint16 local DoF index of column c of element slot
+//   csr_off[ndof + 1]    uint16: contributions of local DoF d are
+//   slot[...]            slot[csr_off[d] .. csr_off[d+1]), each r * cap + e
+//                        (row r of element slot e; cap = 32 units)
+// and the patch's Ke as units of 32 element slots in the thread-per-element
+// layout (entry (r, c) of slot l at (r n + c) 32 + l; empty slots are zero).
+//
+// CTA = 2 consumer groups of 4 warps + 1 producer warp; group g takes the
+// CTA's patches g, g + 2, ... The producer's elected lane copies each
+// patch's index block into the group's buffer (one bulk copy) and streams
+// its Ke units through the shared ring. A group: gathers u of the patch's
+// DoFs into shared memory once; each lane multiplies one element slot and
+// writes its n products to a shared buffer; then each DoF sums its
+// contributions in the stored order and does one v = v_old + sum. No atomics;
+// the order of every sum is fixed by the index block, so v is
+// bit-reproducible. u and v cross HBM about once per patch instead of once
+// per element colour.
+#pragma once
+
+#include "afm_matvec.cuh"
+
+namespace afm {
+
+// Shared-memory layout: ring slots, mbarriers (full[S], empty[S], idx_full[2],
+// idx_empty[2]) and the abort flag, then per group: index block, staged u,
+// element products.
+struct PatchLayout {
+    uint32_t slot_bytes, stages;
+    uint32_t idx_bytes, us_bytes, ve_bytes;  // per group, 16-byte multiples
+    __host__ __device__ uint32_t bars_offset() const { return slot_bytes * stages; }
+    __host__ __device__ uint32_t group_offset() const { return bars_offset() + 16u * stages + 64u; }
+    __host__ __device__ uint32_t group_bytes() const { return idx_bytes + us_bytes + ve_bytes; }
+    __host__ __device__ uint32_t total() const { return group_offset() + 2u * group_bytes(); }
+};
+
+constexpr uint32_t kPatchGroupWarps = 4;
+constexpr uint32_t kPatchGroupThreads = kPatchGroupWarps * 32;
+constexpr uint32_t kPatchThreads = 2 * kPatchGroupThreads + 32;
+
+template <int NT, typename A>
+__global__ void __launch_bounds__(kPatchThreads, 1) afm_patch_kernel(PatchArgs a, PatchLayout L, uint32_t n_rt) {
+    using KT = typename A::KT;
+    using UT = typename A::UT;
+    using VT = typename A::VT;
+    constexpr int NM = NT ? NT : 12;
+    const uint32_t n = NT ? NT : n_rt;
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + L.bars_offset());
+    uint64_t* empty = full + L.stages;
+    uint64_t* idx_full = empty + L.stages;
+    uint64_t* idx_empty = idx_full + 2;
+    volatile int* abort = reinterpret_cast<volatile int*>(idx_empty + 2);
+    const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t S = L.stages;
+
+    const uint32_t per = a.count / gridDim.x, rem = a.count % gridDim.x;
+    const uint32_t begin = blockIdx.x * per + min(blockIdx.x, rem);
+    const uint32_t cnt = per + (blockIdx.x < rem ? 1u : 0u);
+    const PatchDesc* __restrict__ desc = a.desc + begin;
+
+    if (tid == 0) {
+        for (uint32_t s = 0; s < S; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        for (int g = 0; g < 2; g++) {
+            mbar_init(&idx_full[g], 1);
+            mbar_init(&idx_empty[g], 1);
+        }
+        *abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+
+    if (warp == 2 * kPatchGroupWarps) {  // producer
+        if (lane == 0) {
+            const uint64_t pol = l2_evict_first_policy();
+            uint32_t issued = 0;          // Ke units
+            uint32_t idx_issued[2] = {0, 0};
+            bool stop = false;
+            for (uint32_t k = 0; k < cnt && !stop; k++) {
+                const uint32_t g = k & 1, j = k >> 1;
+                const PatchDesc d = desc[k];
+                if (j >= 1 && !mbar_wait_abortable(&idx_empty[g], (j - 1) & 1, abort)) break;
+                mbar_arrive_expect_tx(&idx_full[g], d.idx_bytes);
+                bulk_load(smem + L.group_offset() + g * L.group_bytes(), a.idx + d.idx_off, d.idx_bytes,
+                          &idx_full[g], pol);
+                idx_issued[g] = j + 1;
+                for (uint32_t u = 0; u < d.units; u++) {
+                    const uint32_t s = issued % S;
+                    if (issued >= S && !mbar_wait_abortable(&empty[s], ((issued / S) - 1) & 1, abort)) {
+                        stop = true;
+                        break;
+                    }
+                    mbar_arrive_expect_tx(&full[s], a.copy_bytes);
+                    bulk_load(smem + (size_t)s * L.slot_bytes, a.ke + d.ke_off + (uint64_t)u * a.unit_bytes,
+                              a.copy_bytes, &full[s], pol);
+                    issued++;
+                }
+            }
+            allow_dependent_launch();
+            if (*abort) {
+                // wait (bounded) for the copies still in flight before the CTA exits
+                atomicOr(a.err, kErrTimeout);
+                const unsigned long long t0 = globaltimer_ns();
+                const uint32_t first = issued > S ? issued - S : 0;
+                for (uint32_t i = first; i < issued; i++)
+                    while (!mbar_try_wait(&full[i % S], (i / S) & 1) && globaltimer_ns() - t0 < kWaitLimitNs) {
+                    }
+                for (int g = 0; g < 2; g++)
+                    if (idx_issued[g])
+                        while (!mbar_try_wait(&idx_full[g], (idx_issued[g] - 1) & 1) &&
+                               globaltimer_ns() - t0 < kWaitLimitNs) {
+                        }
+            }
+        }
+        return;
+    }
+
+    const uint32_t g = warp / kPatchGroupWarps, wg = warp % kPatchGroupWarps, t = tid % kPatchGroupThreads;
+    const uint32_t bar_id = 1 + g;
+    unsigned char* gbase = smem + L.group_offset() + g * L.group_bytes();
+    UT* us = reinterpret_cast<UT*>(gbase + L.idx_bytes);
+    VT* ve = reinterpret_cast<VT*>(gbase + L.idx_bytes + L.us_bytes);
+    const VT* __restrict__ u = static_cast<const VT*>(a.u);
+    VT* __restrict__ v = static_cast<VT*>(a.v);
+    const uint64_t keep = l2_evict_last_policy();
+
+    // ring index of this group's first unit: units of the patches before it
+    uint32_t base = (g == 1 && cnt > 0) ? desc[0].units : 0u;
+    bool waited_prior = false;
+    for (uint32_t k = g; k < cnt; k += 2) {
+        const PatchDesc d = desc[k];
+        const uint32_t j = k >> 1;
+        const bool iok = mbar_wait_abortable(&idx_full[g], j & 1, abort);
+        const uint32_t* glob = reinterpret_cast<const uint32_t*>(gbase);
+        const uint16_t* lmap = reinterpret_cast<const uint16_t*>(gbase + patch_lmap_off(d.ndof));
+        const uint16_t* coff = reinterpret_cast<const uint16_t*>(gbase + patch_csr_off(d.ndof, d.units, n));
+        const uint16_t* slot = reinterpret_cast<const uint16_t*>(gbase + patch_slot_off(d.ndof, d.units, n));
+        const uint32_t cap = d.units * 32u;
+
+        // u of the patch's DoFs, once
+        if (iok)
+            for (uint32_t i = t; i < d.ndof; i += kPatchGroupThreads) {
+                const uint32_t m = glob[i];
+                VT x = ld_nc_hint(u + (m & kDofMask), keep);
+                if (a.bc_mode && (m & kBcFlag)) x = VT(0);
+                us[i] = A::stage(x);
+            }
+        named_barrier(bar_id, kPatchGroupThreads);
+
+        // element products: lane l of warp w takes slot (unit w + 4 i, lane l)
+        for (uint32_t un = wg; un < d.units; un += kPatchGroupWarps) {
+            const uint32_t ii = base + un, s = ii % S;
+            const bool ok = iok && mbar_wait_abortable(&full[s], (ii / S) & 1, abort);
+            if (ok) {
+                const unsigned char* ks = smem + (size_t)s * L.slot_bytes;
+                UT ul[NM];
+#pragma unroll
+                for (int c = 0; c < NM; c++)
+                    if (c < (int)n) ul[c] = us[lmap[(un * n + c) * 32u + lane]];
+                const uint32_t e = un * 32u + lane;
+#pragma unroll
+                for (int r = 0; r < NM; r++) {
+                    if (r < (int)n) {
+                        typename A::Acc acc = A::zero();
+#pragma unroll
+                        for (int c = 0; c < NM; c++)
+                            if (c < (int)n) A::fma(acc, A::kload(ks, (size_t)(r * n + c) * 32u + lane, a.plane), ul[c]);
+                        ve[r * cap + e] = A::finish(acc);
+                    }
+                }
+            }
+            __syncwarp();
+            if (ok && lane == 0) mbar_arrive(&empty[s]);
+        }
+        named_barrier(bar_id, kPatchGroupThreads);
+
+        // each DoF sums its contributions in stored order; one v update
+        if (!waited_prior) {
+            wait_prior_grid();
+            waited_prior = true;
+        }
+        if (iok && !*abort)
+            for (uint32_t i = t; i < d.ndof; i += kPatchGroupThreads) {
+                VT sum = VT(0);
+                const uint32_t q1 = coff[i + 1];
+                for (uint32_t q = coff[i]; q < q1; q++) sum += ve[slot[q]];
+                VT* p = v + (glob[i] & kDofMask);
+                st_hint(p, ld_hint(p, keep) + sum, keep);
+            }
+        named_barrier(bar_id, kPatchGroupThreads);
+        if (t == 0) mbar_arrive(&idx_empty[g]);
+        base += d.units + (k + 1 < cnt ? desc[k + 1].units : 0u);
+    }
+    if (!waited_prior) wait_prior_grid();
+    if (t == 0 && *abort) atomicOr(a.err, kErrTimeout);
+}
+
+}  // namespace afm

@@ -1,0 +1,286 @@
+// Serving loop for many CG solves on different operators (afm_server_* in
+// include/afm.h; no counterpart in the reference).
+//
+// A request carries its own operator (maps and element matrices set on the
+// host) and load. Requests wait in a FIFO queue and are admitted while the
+// server's HBM budget, the device's free memory and the slot limit allow.
+// Admission finalises the operator on a worker thread (colouring, patch plan,
+// upload of Ke and maps), so the polling thread never blocks on host work.
+// An admitted request keeps all of its state on the device: Ke, maps, b, x
+// and the Krylov vectors of its mixed-precision solve (afm_mixed.hpp). Every
+// poll takes the next step of each request whose previous step has finished
+// on the GPU; each request runs on its own stream, so the kernels of all
+// running requests overlap on the device, and requests that arrive while
+// others run are admitted as soon as slots and memory free up (continuous
+// batching). A finished request copies x back asynchronously, releases its
+// device memory at once, and waits for afm_server_take.
+//
+// Each request's arithmetic is independent of the others (own operator, own
+// vectors, deterministic kernels), so its result is the same alone and in
+// any mix, bit for bit.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <chrono>
+#include <deque>
+#include <future>
+#include <unordered_map>
+#include <vector>
+
+#include "afm_internal.hpp"
+#include "afm_mixed.hpp"
+
+namespace {
+
+enum ReqState : int { RQ_QUEUED = 0, RQ_ADMITTING, RQ_RUNNING, RQ_COPYING, RQ_DONE };
+
+struct Request {
+    uint64_t id = 0;
+    afm_operator* op = nullptr;
+    std::vector<double> b;
+    double rtol = 1e-8, inner_rtol = 0.1;
+    uint64_t est_bytes = 0;
+    int state = RQ_QUEUED;
+    std::future<int> fin;
+    double* d_bx = nullptr;  // b then x on the device
+    double* h_x = nullptr;   // pinned copy of x
+    cudaEvent_t copied = nullptr;
+    afm::MixedSolve ms;
+    afm_solve_stats stats{};
+    int status = AFM_SUCCESS;
+    std::string message;
+    double t_submit = 0, t_admit = 0, t_start = 0, t_done = 0;
+};
+
+double now_s() {
+    using namespace std::chrono;
+    return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+// Device bytes a request holds once admitted: element matrices (8 bytes per
+// entry in every arena but FP32), maps or patch index blocks, diagonal, the
+// solver's FP64 and FP32 work vectors, b and x; 10% and 1 MB of slack.
+uint64_t estimate_bytes(const afm_operator* op) {
+    uint64_t ke = 0;
+    for (uint32_t e = 0; e < op->n_elem; e++) {
+        const uint64_t n = op->offsets[e + 1] - op->offsets[e];
+        ke += n * n * 8 + 8 * n;
+    }
+    const uint64_t vec = (uint64_t)op->n_dofs * (8 * 8 + 7 * 4 + 3 * 8);
+    return (ke + vec) * 11 / 10 + (1u << 20);
+}
+
+}  // namespace
+
+struct afm_server {
+    int device = 0;
+    uint64_t budget = 0, in_use = 0, reserve = 0;
+    uint32_t max_active = 0;
+    uint64_t next_id = 1;
+    std::deque<Request*> queue;
+    std::vector<Request*> active;  // admitting, running or copying
+    std::unordered_map<uint64_t, Request*> all;
+};
+
+namespace {
+
+void release_device(Request* r) {
+    if (r->d_bx) cudaFree(r->d_bx);
+    r->d_bx = nullptr;
+    if (r->copied) cudaEventDestroy(r->copied);
+    r->copied = nullptr;
+    if (r->op) afm_destroy(r->op);
+    r->op = nullptr;
+}
+
+void finish(afm_server* s, Request* r, int status, const char* msg) {
+    r->status = status;
+    if (msg) r->message = msg;
+    r->state = RQ_DONE;
+    r->t_done = now_s();
+    release_device(r);
+    s->in_use -= r->est_bytes;
+}
+
+// admission: FIFO while the budget, free device memory and slots allow
+void admit(afm_server* s) {
+    while (!s->queue.empty() && s->active.size() < s->max_active) {
+        Request* r = s->queue.front();
+        size_t free_b = 0, total_b = 0;
+        if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) break;
+        const bool fits = s->in_use + r->est_bytes <= s->budget && r->est_bytes + s->reserve <= free_b;
+        if (!fits && !s->active.empty()) break;  // wait for memory to free up
+        s->queue.pop_front();
+        s->in_use += r->est_bytes;
+        r->state = RQ_ADMITTING;
+        r->t_admit = now_s();
+        afm_operator* op = r->op;
+        const int dev = s->device;
+        r->fin = std::async(std::launch::async, [op, dev]() {
+            cudaSetDevice(dev);
+            return afm_finalize(op);
+        });
+        s->active.push_back(r);
+    }
+}
+
+int start(afm_server* s, Request* r) {
+    (void)s;
+    afm_operator* op = r->op;
+    const size_t n = op->n_dofs;
+    if (cudaMalloc((void**)&r->d_bx, 2 * n * sizeof(double)) != cudaSuccess) return AFM_ERR_OOM;
+    if (cudaMallocHost((void**)&r->h_x, std::max<size_t>(n, 1) * sizeof(double)) != cudaSuccess) return AFM_ERR_OOM;
+    if (cudaEventCreateWithFlags(&r->copied, cudaEventDisableTiming) != cudaSuccess) return AFM_ERR_CUDA;
+    if (cudaMemcpyAsync(r->d_bx, r->b.data(), n * sizeof(double), cudaMemcpyHostToDevice, op->stream) != cudaSuccess ||
+        cudaMemsetAsync(r->d_bx + n, 0, n * sizeof(double), op->stream) != cudaSuccess)
+        return AFM_ERR_CUDA;
+    r->ms = afm::MixedSolve{};
+    r->ms.op = op;
+    r->ms.d_b = r->d_bx;
+    r->ms.d_x = r->d_bx + n;
+    r->ms.rtol = r->rtol;
+    r->ms.atol = 0.0;
+    r->ms.inner_rtol = r->inner_rtol;
+    r->ms.max_outer = 200;
+    r->ms.max_inner = 1000000;
+    r->t_start = now_s();
+    return afm::mixed_begin(r->ms);
+}
+
+}  // namespace
+
+extern "C" {
+
+int afm_server_create(afm_server** out, int device, uint64_t hbm_budget_bytes, uint32_t max_active) {
+    if (!out) return afm::set_error(AFM_ERR_INVALID_ARG, "out is null");
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return afm::set_error(AFM_ERR_CUDA, "no CUDA device");
+    if (device < 0) cudaGetDevice(&device);
+    if (device >= ndev) return afm::set_error(AFM_ERR_INVALID_ARG, "device %d of %d", device, ndev);
+    if (cudaSetDevice(device) != cudaSuccess) return afm::set_error(AFM_ERR_CUDA, "cudaSetDevice(%d)", device);
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return afm::set_error(AFM_ERR_CUDA, "cudaMemGetInfo");
+    auto* s = new afm_server();
+    s->device = device;
+    s->budget = hbm_budget_bytes ? hbm_budget_bytes : (uint64_t)(free_b * 0.85);
+    s->reserve = std::min<uint64_t>(total_b / 50, 2ull << 30);
+    s->max_active = max_active ? max_active : 32;
+    *out = s;
+    return afm::set_error(AFM_SUCCESS, "");
+}
+
+int afm_server_submit(afm_server* s, afm_operator* op, const double* b, double rtol, double inner_rtol, uint64_t* id) {
+    if (!s || !op || !b || !id) return afm::set_error(AFM_ERR_INVALID_ARG, "null argument");
+    if (!op->have_map) return afm::set_error(AFM_ERR_STATE, "operator without a map");
+    if (op->device != s->device) return afm::set_error(AFM_ERR_INVALID_ARG, "operator on device %d", op->device);
+    if (!(rtol > 0.0) || !(inner_rtol > 0.0) || inner_rtol >= 1.0)
+        return afm::set_error(AFM_ERR_INVALID_ARG, "rtol %g, inner_rtol %g", rtol, inner_rtol);
+    auto* r = new Request();
+    r->id = s->next_id++;
+    r->op = op;
+    r->b.assign(b, b + op->n_dofs);
+    r->rtol = rtol;
+    r->inner_rtol = inner_rtol;
+    r->est_bytes = estimate_bytes(op);
+    r->t_submit = now_s();
+    s->queue.push_back(r);
+    s->all[r->id] = r;
+    *id = r->id;
+    return afm::set_error(AFM_SUCCESS, "");
+}
+
+int afm_server_poll(afm_server* s, uint32_t* n_queued, uint32_t* n_active) {
+    if (!s) return afm::set_error(AFM_ERR_INVALID_ARG, "null server");
+    cudaSetDevice(s->device);
+    admit(s);
+    std::vector<Request*> still;
+    still.reserve(s->active.size());
+    for (Request* r : s->active) {
+        if (r->state == RQ_ADMITTING &&
+            r->fin.wait_for(std::chrono::seconds(0)) == std::future_status::ready) {
+            const int st = r->fin.get();
+            if (st != AFM_SUCCESS) {
+                finish(s, r, st, "finalize failed");
+                continue;
+            }
+            r->op->precision_req = r->op->precision;
+            const int s2 = start(s, r);
+            if (s2 != AFM_SUCCESS) {
+                finish(s, r, s2, afm_last_error());
+                continue;
+            }
+            r->state = RQ_RUNNING;
+        }
+        if (r->state == RQ_RUNNING) {
+            int st = AFM_SUCCESS;
+            while (st == AFM_SUCCESS && r->ms.phase != afm::MS_DONE && afm::mixed_ready(r->ms))
+                st = afm::mixed_advance(r->ms);
+            if (st != AFM_SUCCESS) {
+                afm::mixed_end(r->ms, nullptr);
+                finish(s, r, st, afm_last_error());
+                continue;
+            }
+            if (r->ms.phase == afm::MS_DONE) {
+                const size_t n = r->op->n_dofs;
+                cudaMemcpyAsync(r->h_x, r->d_bx + n, n * sizeof(double), cudaMemcpyDeviceToHost, r->op->stream);
+                cudaEventRecord(r->copied, r->op->stream);
+                r->state = RQ_COPYING;
+            }
+        }
+        if (r->state == RQ_COPYING && cudaEventQuery(r->copied) == cudaSuccess) {
+            const int st = afm::mixed_end(r->ms, &r->stats);
+            finish(s, r, st, st ? afm_last_error() : nullptr);
+            continue;
+        }
+        still.push_back(r);
+    }
+    s->active.swap(still);
+    admit(s);
+    if (n_queued) *n_queued = (uint32_t)s->queue.size();
+    if (n_active) *n_active = (uint32_t)s->active.size();
+    return afm::set_error(AFM_SUCCESS, "");
+}
+
+int afm_server_take(afm_server* s, uint64_t id, double* x, afm_solve_stats* stats, double* times) {
+    if (!s) return afm::set_error(AFM_ERR_INVALID_ARG, "null server");
+    auto it = s->all.find(id);
+    if (it == s->all.end()) return afm::set_error(AFM_ERR_INVALID_ARG, "unknown request %llu", (unsigned long long)id);
+    Request* r = it->second;
+    if (r->state != RQ_DONE) return afm::set_error(AFM_ERR_STATE, "request %llu not finished", (unsigned long long)id);
+    const int status = r->status;
+    const std::string msg = r->message;
+    if (x && r->h_x) memcpy(x, r->h_x, r->b.size() * sizeof(double));
+    if (stats) *stats = r->stats;
+    if (times) {
+        times[0] = r->t_submit;
+        times[1] = r->t_admit;
+        times[2] = r->t_start;
+        times[3] = r->t_done;
+    }
+    if (r->h_x) cudaFreeHost(r->h_x);
+    s->all.erase(it);
+    delete r;
+    if (status != AFM_SUCCESS) return afm::set_error(status, "request failed: %s", msg.c_str());
+    return afm::set_error(AFM_SUCCESS, "");
+}
+
+int afm_server_destroy(afm_server* s) {
+    if (!s) return AFM_SUCCESS;
+    cudaSetDevice(s->device);
+    for (Request* r : s->active)
+        if (r->state == RQ_ADMITTING) r->fin.wait();
+    cudaDeviceSynchronize();
+    for (auto& kv : s->all) {
+        Request* r = kv.second;
+        if (r->ms.ev) afm::mixed_end(r->ms, nullptr);
+        release_device(r);
+        if (r->h_x) cudaFreeHost(r->h_x);
+        delete r;
+    }
+    delete s;
+    return AFM_SUCCESS;
+}
+
+}  // extern "C"

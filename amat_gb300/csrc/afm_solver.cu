@@ -113,6 +113,62 @@ __global__ void __launch_bounds__(kRedThreads) k_cg_init_final(double* sc, const
     }
 }
 
+// Reliable update of the FP32 recursion of the mixed-precision solve, pass 1:
+// r = fl32(r64) (the FP64 true residual), z = dinv r; partials of r.z, r.r,
+// z.z and r.p (p = the last direction p_k)
+__global__ void __launch_bounds__(kRedThreads) k_cg_reliable(const double* __restrict__ r64, float* __restrict__ r,
+                                                             float* __restrict__ z, const float* __restrict__ p,
+                                                             const float* __restrict__ dinv, size_t n, double* part) {
+    __shared__ double sh[kRedThreads];
+    double rz = 0, rr = 0, zz = 0, rp = 0;
+    for (size_t i = (size_t)blockIdx.x * kRedThreads + threadIdx.x; i < n; i += kStride) {
+        const float ri = (float)r64[i];
+        const float zi = dinv[i] * ri;
+        r[i] = ri;
+        z[i] = zi;
+        rz = __fma_rn((double)ri, (double)zi, rz);
+        rr = __fma_rn((double)ri, (double)ri, rr);
+        zz = __fma_rn((double)zi, (double)zi, zz);
+        rp = __fma_rn((double)ri, (double)p[i], rp);
+    }
+    double v[4] = {rz, rr, zz, rp};
+    for (int j = 0; j < 4; j++) {
+        const double s = block_sum(v[j], sh);
+        if (threadIdx.x == 0) part[j * kRedBlocks + blockIdx.x] = s;
+    }
+}
+
+// pass 2 (one block): beta = r.z / r_k.z_k, gamma = r.p / r.z; S_DONE, S_ITER cleared
+__global__ void __launch_bounds__(kRedThreads) k_cg_reliable_final(double* sc, const double* part) {
+    __shared__ double sh[kRedThreads];
+    const double rz = final_sum(part, sh);
+    const double rr = final_sum(part + kRedBlocks, sh);
+    const double zz = final_sum(part + 2 * kRedBlocks, sh);
+    const double rp = final_sum(part + 3 * kRedBlocks, sh);
+    if (threadIdx.x == 0) {
+        const double old = sc[S_RZOLD];
+        const bool bad = (rz < 0.0 || rz != rz);
+        sc[S_BETA] = (!bad && old > 0.0) ? rz / old : 0.0;
+        sc[S_GAMMA] = (!bad && rz > 0.0) ? rp / rz : 0.0;
+        sc[S_RZ] = rz;
+        sc[S_RR] = rr;
+        sc[S_ZZ] = zz;
+        sc[S_FLAG] = bad ? 1.0 : 0.0;
+        sc[S_DONE] = 0.0;
+        sc[S_ITER] = 0.0;
+    }
+}
+
+// pass 3: p = z + beta (p - gamma z)
+__global__ void __launch_bounds__(kRedThreads) k_cg_reliable_p(float* __restrict__ p, const float* __restrict__ z,
+                                                               size_t n, const double* sc) {
+    const float beta = (float)sc[S_BETA];
+    const float c = (float)(1.0 - sc[S_BETA] * sc[S_GAMMA]);
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+        p[i] = __fmaf_rn(beta, p[i], c * z[i]);
+}
+
 // alpha = rz / (p.q); flag on p.q <= 0 or NaN
 __global__ void __launch_bounds__(kRedThreads) k_cg_alpha(double* sc, const double* part) {
     __shared__ double sh[kRedThreads];
@@ -182,6 +238,7 @@ __global__ void __launch_bounds__(kRedThreads) k_cg_beta(double* sc, const doubl
         }
         const double old = sc[S_RZ];
         sc[S_BETA] = (old != 0.0) ? rz / old : 0.0;
+        sc[S_RZOLD] = old;
         sc[S_RZ] = rz;
         sc[S_RR] = rr;
         sc[S_ZZ] = zz;
@@ -200,6 +257,9 @@ __global__ void __launch_bounds__(kRedThreads) k_cg_beta(double* sc, const doubl
 template <typename T>
 __global__ void __launch_bounds__(kRedThreads) k_cg_p(T* __restrict__ p, const T* __restrict__ z, size_t n,
                                                       const double* sc) {
+    // a finished solve keeps its last direction (the mixed-precision solve
+    // continues from it after a reliable update)
+    if (sc[S_DONE] != 0.0) return;
     const T beta = (T)sc[S_BETA];
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) p[i] = beta * p[i] + z[i];
@@ -291,6 +351,14 @@ template <typename T>
 cudaError_t launch_norm2(const T* a, size_t n, double* sc, double* part, cudaStream_t st) {
     k_dots<T><<<kRedBlocks, kRedThreads, 0, st>>>(a, a, n, part);
     k_sum<<<1, kRedThreads, 0, st>>>(sc, part);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cg_reliable(const double* r64, float* r, float* z, float* p, const float* dinv, size_t n,
+                               double* sc, double* part, cudaStream_t st) {
+    k_cg_reliable<<<kRedBlocks, kRedThreads, 0, st>>>(r64, r, z, p, dinv, n, part);
+    k_cg_reliable_final<<<1, kRedThreads, 0, st>>>(sc, part);
+    k_cg_reliable_p<<<grid_for(n), kRedThreads, 0, st>>>(p, z, n, sc);
     return cudaGetLastError();
 }
 

@@ -17,9 +17,12 @@ constexpr int kRedThreads = 256;
 // S_TOL), on S_MAXIT iterations (when > 0) or on breakdown (S_FLAG), after
 // which further iterations leave every vector unchanged. That lets a captured
 // graph run several iterations without reading anything back.
+// S_RZOLD keeps r.z of the step before the last update (the reliable update
+// of the mixed-precision solve needs it); S_GAMMA is that update's
+// orthogonalisation coefficient.
 enum : int {
     S_RZ = 0, S_PQ, S_ALPHA, S_BETA, S_RR, S_ZZ, S_BB, S_DB, S_FLAG,
-    S_DONE, S_TOL, S_ITER, S_MAXIT, S_NORM,
+    S_DONE, S_TOL, S_ITER, S_MAXIT, S_NORM, S_RZOLD, S_GAMMA,
     kScalarSlots = 16
 };
 constexpr int kPartialSlots = 5 * kRedBlocks;
@@ -43,6 +46,13 @@ cudaError_t launch_invert(T* dinv, const double* d, size_t n, cudaStream_t st);
 // sc[S_PQ] = ||a||^2 (no CG bookkeeping)
 template <typename T>
 cudaError_t launch_norm2(const T* a, size_t n, double* sc, double* part, cudaStream_t st);
+// Reliable update of the FP32 recursion (after a segment stopped on S_DONE,
+// p is still the last direction p_k): r = fl32(r64), z = dinv r,
+// p = z + beta (p - gamma z) with beta = r.z / r_k.z_k and gamma = r.p / r.z,
+// so that the new residual is orthogonal to the kept direction again;
+// sc[S_RZ], sc[S_RR], sc[S_ZZ] of the new residual; S_DONE and S_ITER cleared.
+cudaError_t launch_cg_reliable(const double* r64, float* r, float* z, float* p, const float* dinv, size_t n,
+                               double* sc, double* part, cudaStream_t st);
 cudaError_t launch_axpby(double* y, const double* x, double a, double b, size_t n, cudaStream_t st);
 cudaError_t launch_to_f32(float* out, const double* in, size_t n, cudaStream_t st);
 cudaError_t launch_add_f32(double* x, float* d, size_t n, cudaStream_t st);

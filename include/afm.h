@@ -52,7 +52,8 @@ typedef enum afm_status {
     AFM_ERR_BREAKDOWN = 103,         /* CG breakdown: p.Ap <= 0, r.z < 0 or NaN */
     AFM_ERR_STATE = 104,             /* call out of order (e.g. matvec before finalize) */
     AFM_ERR_INVALID_ARG = 105,       /* null pointer, bad size, unsupported option */
-    AFM_ERR_MAXIT = 106              /* CG stopped at maxit without converging */
+    AFM_ERR_MAXIT = 106,             /* CG stopped at maxit without converging */
+    AFM_ERR_INTERNAL = 107           /* an internal consistency check failed */
 } afm_status;
 
 /* par::BC_METH (include/enums.hpp:20-21) */
@@ -97,6 +98,9 @@ typedef struct afm_info {
     double algorithmic_flops;   /* per matvec: sum_e 2 n_e^2 */
     uint32_t n_launches;        /* kernel launches per matvec */
     int device;
+    uint32_t n_patches;         /* small-element patches (0: colour segments) */
+    uint32_t n_patch_colors;    /* colours of the patch conflict graph */
+    uint64_t patch_index_bytes; /* device bytes of the patch index blocks */
 } afm_info;
 
 typedef struct afm_solve_stats {
@@ -121,6 +125,14 @@ int afm_destroy(afm_operator* op);
 int afm_set_matfree_type(afm_operator* op, int matfree_type);
 /* Arithmetic of the stored Ke; call before afm_finalize. Default AUTO. */
 int afm_set_precision(afm_operator* op, int precision);
+/* Execution of small elements (no counterpart in the reference). enable = 1
+ * (default): when every element has the same size n <= 12 and lists no DoF
+ * twice, the matvec runs over patches, compact groups of up to 256 elements
+ * whose vector entries are staged in shared memory; patches of one colour
+ * share no DoF. enable = 0: one launch per element colour, as for larger
+ * elements. Both are deterministic and agree within rounding. Takes effect at
+ * the next afm_finalize. */
+int afm_set_patch_mode(afm_operator* op, int enable);
 
 /* ---- maps (par::Maps) --------------------------------------------------- */
 
@@ -202,17 +214,17 @@ int afm_solve_cg_device(afm_operator* op, const double* d_b, double* d_x, double
                         int norm_type, afm_solve_stats* stats);
 
 /* Mixed-precision solve of the same system (no counterpart in the
- * reference): iterative refinement whose
- * outer residual r = b - A x is computed in FP64 with the FP64_SPLIT element
- * matrices (MatMult_mf semantics), and whose correction A d = r is solved by
- * Jacobi-PCG on the FP32 matrix (the hi plane of the same arena, half the
- * bytes) with FP32 vectors and FP64 dot products and step scalars. Each inner
- * solve stops at inner_rtol relative to its right-hand side or after
- * max_inner iterations; the outer loop stops at ||b - A x|| <= max(rtol ||b||,
- * atol), after max_outer steps, or after three steps in a row that do not
- * bring a new smallest residual (one step may raise it before it falls).
+ * reference): Jacobi-PCG whose recursion runs in FP32 (the FP32 matrix, the
+ * hi plane of the FP64_SPLIT arena at half the bytes; FP32 vectors; FP64 dot
+ * products and step scalars) with reliable updates in FP64: once the FP32
+ * residual has dropped by inner_rtol (or after max_inner iterations), the FP32
+ * increment is added to x in FP64, the true residual r = b - A x is computed
+ * in FP64 with the split element matrices (MatMult_mf semantics) and replaces
+ * the FP32 residual, and the recursion continues with its search direction.
+ * The solve stops at ||b - A x|| <= max(rtol ||b||, atol), after max_outer
+ * updates, or after three updates in a row without a new smallest residual.
  * Needs an FP64_SPLIT operator (AFM_PREC_AUTO with in-range Ke). stats:
- * iterations = inner iterations, refinements = outer steps. */
+ * iterations = FP32 iterations, refinements = FP64 residual updates. */
 int afm_solve_cg_mixed(afm_operator* op, const double* b, double* x, double rtol, double atol, int max_outer,
                        double inner_rtol, int max_inner, afm_solve_stats* stats);
 int afm_solve_cg_mixed_device(afm_operator* op, const double* d_b, double* d_x, double rtol, double atol,
@@ -257,6 +269,17 @@ int afm_solve_cg_batched_device(afm_operator* op, const double* d_B, double* d_X
 int afm_solve_cg_batched_mixed_device(afm_operator* op, const double* d_B, double* d_X, uint32_t nrhs, double rtol,
                                       double atol, int max_outer, double inner_rtol, int max_inner,
                                       afm_solve_stats* stats);
+
+/* Host-side check of the small-element patch plan (no device work, no
+ * counterpart in the reference): builds the patch plan afm_finalize would
+ * build for this map (same-size elements, n <= 12, no DoF twice in an
+ * element) and evaluates v = K u on the CPU by walking the plan's index
+ * blocks the way the patch kernel does (FP64, ke row-major n x n per
+ * element). Checks every structural invariant on the way and returns
+ * AFM_ERR_INTERNAL with a message when one fails. */
+int afm_patch_plan_host_matvec(uint32_t n_elem, uint32_t n_dofs, const uint32_t* offsets, const uint32_t* map,
+                               const double* ke, const double* u, double* v, uint32_t* n_patches,
+                               uint32_t* n_patch_colors);
 
 /* Largest operator (DoFs) afm_solve_cg_device_noalloc accepts. */
 #define AFM_NOALLOC_MAX_DOFS 262144u

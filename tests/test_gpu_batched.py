@@ -150,3 +150,30 @@ def test_batched_cg_matches_single_solves(gpu, mixed):
         assert rel(X[:, j], x) < 1e-7
         r = B[:, j] - pr.matmult_bc(X[:, j])
         assert np.linalg.norm(r) <= 1.01e-9 * np.linalg.norm(B[:, j])
+
+
+def test_batched_mixed_reliable_updates(gpu):
+    """The FP32 block recursion continues across FP64 residual updates (its
+    iteration count stays near the FP64 block CG's), and columns that meet
+    their tolerance early (here a zero load case) stay frozen."""
+    import torch
+    m, ke, dofs, A = elastic(6, PRECISION.FP64_SPLIT, bc=True)
+    nrhs = 8
+    B = np.random.default_rng(11).normal(size=(m.n_dofs, nrhs))
+    B[:, 5] = 0.0
+    B[dofs.astype(np.int64), :] = 0.0
+    dB = torch.tensor(B, device="cuda")
+    dX = torch.zeros_like(dB)
+    st64 = A.solve_batched_device(dB.data_ptr(), dX.data_ptr(), nrhs, rtol=1e-8)
+    dX.zero_()
+    torch.cuda.synchronize()
+    st = A.solve_batched_device(dB.data_ptr(), dX.data_ptr(), nrhs, rtol=1e-8, mixed=True, inner_rtol=0.1)
+    X = dX.cpu().numpy()
+    assert st.status == 0 and st.rel_residual <= 1e-8
+    assert st.refinements >= 3
+    assert st.iterations <= 1.5 * st64.iterations + 10, (st.iterations, st64.iterations)
+    assert not np.any(X[:, 5])
+    pr = oracle.Problem(m.n_dofs, m.dof_map(), ke, dofs, np.zeros(len(dofs)))
+    for j in (0, 7):
+        r = B[:, j] - pr.matmult_bc(X[:, j])
+        assert np.linalg.norm(r) <= 1.01e-8 * np.linalg.norm(B[:, j])

@@ -261,3 +261,58 @@ def test_misuse_is_reported(gpu):
     with pytest.raises(AfmError) as e:
         aMatFree(ghost)
     assert e.value.name == "WRONG_COMMUNICATION"
+
+
+def _mesh_operator(kind, shape, jitter, prec, patch, bc=True):
+    m = P.Mesh(kind, *shape, jitter=jitter, seed=2)
+    ke = m.element_matrices()
+    maps = Maps()
+    maps.set_map(m.n_elem, m.dof_map(), m.ndpe, m.n_dofs)
+    dofs, vals = m.boundary_conditions() if bc else (np.zeros(0, np.uint64), np.zeros(0))
+    maps.set_bdr_map(dofs, vals)
+    A = aMatFree(maps)
+    A.set_precision(prec)
+    A.set_patch_mode(patch)
+    A.set_element_matrices(0, ke)
+    A.finalize()
+    return m, ke, dofs, vals, A
+
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("kind,shape,jitter", [
+    (P.HEX8_POISSON, (12, 12, 12), 0.1),
+    (P.HEX8_POISSON, (40, 1, 1), 0.0),
+    (P.TET10_POISSON, (10, 10, 10), 0.15),
+    (P.TET10_POISSON, (24, 24, 24), 0.15),
+])
+def test_patch_path_against_oracle(gpu, kind, shape, jitter, prec):
+    """Small elements as shared-memory patches: v = K u and MatMult_mf against
+    the oracle, the same products through one launch per colour, and two
+    calls in a row bit for bit."""
+    import torch
+    m, ke, dofs, vals, A = _mesh_operator(kind, shape, jitter, prec, 1)
+    info = A.info()
+    assert info["n_patches"] > 0 and info["n_launches"] == info["n_patch_colors"] + 1
+    _, _, _, _, B = _mesh_operator(kind, shape, jitter, prec, 0)
+    assert B.info()["n_patches"] == 0
+    pr = oracle.Problem(m.n_dofs, m.dof_map(), ke, dofs, vals)
+    u = np.random.default_rng(3).uniform(-1, 1, m.n_dofs)
+    v, w = np.empty(m.n_dofs), np.empty(m.n_dofs)
+    A.matvec(v, u, True)
+    B.matvec(w, u, True)
+    vo = pr.matvec(u)
+    assert rel(v, vo) < FP64_RTOL and rel(w, vo) < FP64_RTOL
+    A.matmult_bc(v, u)
+    assert rel(v, pr.matmult_bc(u)) < FP64_RTOL
+    du = torch.tensor(u, device="cuda")
+    dv1, dv2 = torch.empty_like(du), torch.empty_like(du)
+    A.matvec_device(dv1.data_ptr(), du.data_ptr())
+    A.matvec_device(dv2.data_ptr(), du.data_ptr())
+    A.synchronize()
+    assert torch.equal(dv1, dv2)
+    if prec == PRECISION.FP64_SPLIT:
+        du32 = du.float()
+        dv32 = torch.empty_like(du32)
+        A.matvec_device_f32(dv32.data_ptr(), du32.data_ptr())
+        A.synchronize()
+        assert rel(dv32.double().cpu().numpy(), vo) < FP32_RTOL

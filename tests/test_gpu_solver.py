@@ -127,3 +127,16 @@ def test_mixed_precision_tet10(gpu):
     x, st = A.solve_mixed(rhs, rtol=1e-8, atol=0.0, inner_rtol=1e-4, raise_on_fail=False)
     assert st.status == 0, (st.refinements, st.iterations, st.rel_residual)
     assert rel(x, x64) < 1e-6
+
+
+def test_mixed_precision_keeps_the_krylov_space(gpu):
+    """Reliable updates continue one FP32 recursion, so the FP32 iteration
+    count stays near the FP64 one instead of restarting per refinement."""
+    m, ke, dofs, vals, A = poisson(16, jitter=0.15, seed=5, prec=PRECISION.FP64_SPLIT)
+    rhs = A.apply_bc(m.load())
+    x64, st64 = A.solve(rhs, rtol=1e-8, atol=0.0)
+    x, st = A.solve_mixed(rhs, rtol=1e-8, atol=0.0, inner_rtol=0.1)
+    assert st.status == 0 and st.rel_residual <= 1e-8
+    assert st.refinements >= 3
+    assert st.iterations <= 1.5 * st64.iterations + 10, (st.iterations, st64.iterations)
+    assert rel(x, x64) < 1e-6
