@@ -63,6 +63,11 @@ AFM_SIGNATURES = {
     "afm_set_matfree_type": (I, [P, I]),
     "afm_set_precision": (I, [P, I]),
     "afm_set_patch_mode": (I, [P, I]),
+    "afm_server_create": (I, [P, I, U64, U32]),
+    "afm_server_submit": (I, [P, P, P, D, D, P]),
+    "afm_server_poll": (I, [P, P, P]),
+    "afm_server_take": (I, [P, U64, P, P, P, P]),
+    "afm_server_destroy": (I, [P]),
     "afm_patch_plan_host_matvec": (I, [U32, U32, P, P, P, P, P, P, P]),
     "afm_set_map": (I, [P, U32, P, U32, P, U32, P, U64, U64, U64]),
     "afm_set_bdr_map": (I, [P, P, P, U32]),

@@ -227,10 +227,11 @@ class aMatFree:
         check(getattr(self._lib, name)(self._h, C.c_void_p(v_ptr), C.c_void_p(u_ptr), int(nrhs), int(ld),
                                        C.c_void_p(stream) if stream else None), name)
 
-    def set_batch_tuning(self, nrhs, cols_per_thread, groups_per_cta, ld=None, f32=False):
+    def set_batch_tuning(self, nrhs, cols_per_thread, rows_per_thread, ld=None, f32=False):
+        """Pins the batched lane tile (columns, rows): (8, 2), (8, 4), (8, 6) or (4, 4)."""
         ld = nrhs if ld is None else ld
         check(self._lib.afm_set_batch_tuning(self._h, int(nrhs), int(ld), int(bool(f32)), int(cols_per_thread),
-                                             int(groups_per_cta)), "afm_set_batch_tuning")
+                                             int(rows_per_thread)), "afm_set_batch_tuning")
 
     def batch_tuning(self, nrhs, ld=None, f32=False):
         ld = nrhs if ld is None else ld
@@ -240,7 +241,10 @@ class aMatFree:
         return tr.value, ng.value, ms.value
 
     def solve_batched_device(self, b_ptr, x_ptr, nrhs, rtol=1e-8, atol=0.0, maxit=100000, mixed=False,
-                             max_outer=30, inner_rtol=1e-2, max_inner=100000, raise_on_fail=True):
+                             max_outer=200, inner_rtol=1e-2, max_inner=64, raise_on_fail=True):
+        """Block Jacobi-PCG on nrhs columns (device blocks n_dofs x nrhs). mixed: FP32 block recursion with
+        FP64 reliable updates; each FP32 segment ends after max_inner iterations (or once a column's residual
+        fell by inner_rtol; the block waits for its slowest column, so short segments keep every column busy)."""
         st = AfmSolveStats()
         if mixed:
             s = self._lib.afm_solve_cg_batched_mixed_device(self._h, C.c_void_p(b_ptr), C.c_void_p(x_ptr), int(nrhs),

@@ -2,8 +2,9 @@
 // over n_dofs x ld blocks (column j of every block belongs to solve j).
 // Every column has its own FP64 scalars (rz, alpha, beta, norms, done flag);
 // a finished column is frozen (alpha = beta = 0) while the others continue.
-// Column reductions are deterministic: a fixed grid of kBRows-row chunks per
-// block, a fixed in-block order, then a fixed-order sum over the blocks.
+// Column reductions are deterministic: a fixed grid of kBBlocks row chunks, a
+// fixed in-block order, then a fixed tree over the block partials per column.
+// Every thread moves 16 bytes of one row per access.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -14,59 +15,106 @@ namespace afm {
 namespace {
 
 constexpr int kBThreads = 256;
+constexpr int kFinThreads = 128;
 
-// Block (rows r of columns j): thread (ry, j) with ry in [0, kBThreads / R).
+// Thread geometry of the row-chunk kernels: block b owns a contiguous chunk
+// of rows; a thread owns VEC = 16 / sizeof(T) consecutive columns (one 16-byte
+// access), tpr = R / VEC threads cover a row and rstep = kBThreads / tpr rows
+// are in flight per pass.
 template <typename T>
-__device__ __forceinline__ void row_col(uint32_t R, uint32_t& ry, uint32_t& j, uint32_t& rstep) {
-    rstep = kBThreads / R;
-    ry = threadIdx.x / R;
-    j = threadIdx.x % R;
-}
-
-// Sums v over the rstep row lanes of the block for every column; result in
-// sh[j] (fixed order).
-__device__ __forceinline__ void col_reduce(double v, uint32_t R, uint32_t ry, uint32_t j, uint32_t rstep, double* sh) {
-    sh[ry * R + j] = v;
-    __syncthreads();
-    if (ry == 0) {
-        double s = 0.0;
-        for (uint32_t y = 0; y < rstep; y++) s += sh[y * R + j];
-        sh[j] = s;
+struct Geo {
+    static constexpr uint32_t VEC = 16 / sizeof(T);
+    uint32_t tpr, rstep, ry, col;
+    bool active;
+    size_t r0, r1;
+    __device__ Geo(size_t n, uint32_t R) {
+        tpr = R / VEC;
+        rstep = kBThreads / tpr;
+        ry = threadIdx.x / tpr;
+        col = (threadIdx.x % tpr) * VEC;
+        active = ry < rstep;
+        const size_t chunk = (n + gridDim.x - 1) / gridDim.x;
+        r0 = (size_t)blockIdx.x * chunk;
+        r1 = r0 + chunk < n ? r0 + chunk : n;
     }
-    __syncthreads();
+};
+
+template <typename T>
+__device__ __forceinline__ void ldv(const T* p, T* x) {
+    if constexpr (sizeof(T) == 4) {
+        const float4 t = *reinterpret_cast<const float4*>(p);
+        x[0] = t.x, x[1] = t.y, x[2] = t.z, x[3] = t.w;
+    } else {
+        const double2 t = *reinterpret_cast<const double2*>(p);
+        x[0] = t.x, x[1] = t.y;
+    }
+}
+template <typename T>
+__device__ __forceinline__ void stv(T* p, const T* x) {
+    if constexpr (sizeof(T) == 4)
+        *reinterpret_cast<float4*>(p) = make_float4(x[0], x[1], x[2], x[3]);
+    else
+        *reinterpret_cast<double2*>(p) = make_double2(x[0], x[1]);
 }
 
-// partials of up to 3 column dot products: part[(q * kBBlocks + block) * R + j]
+// Column sums of the block for Q quantities (acc[q][v] of this thread's VEC
+// columns), in a fixed order over the block's rows; block partials at
+// part[(q * gridDim.x + block) * R + column].
 template <typename T, int Q>
-__global__ void __launch_bounds__(kBThreads) k_bdots(const T* __restrict__ a, const T* __restrict__ b,
-                                                     const T* __restrict__ c, size_t n, uint32_t ld, uint32_t R,
-                                                     double* part) {
-    __shared__ double sh[kBThreads];
-    uint32_t ry, j, rstep;
-    row_col<T>(R, ry, j, rstep);
-    double s0 = 0, s1 = 0, s2 = 0;
-    if (ry < rstep && j < R) {
-        const size_t chunk = (n + kBBlocks - 1) / kBBlocks;
-        const size_t r0 = (size_t)blockIdx.x * chunk, r1 = min(n, r0 + chunk);
-        for (size_t i = r0 + ry; i < r1; i += rstep) {
-            const double x = a[i * ld + j];
-            s0 = __fma_rn(x, (double)b[i * ld + j], s0);
-            if (Q > 1) s1 = __fma_rn(x, x, s1);
-            if (Q > 2) s2 = __fma_rn((double)c[i * ld + j], (double)c[i * ld + j], s2);
-        }
-    }
-    double v[3] = {s0, s1, s2};
+__device__ __forceinline__ void block_cols(const double (&acc)[Q][16 / sizeof(T)], const Geo<T>& g, uint32_t R,
+                                           double* part, double* sh) {
+    constexpr uint32_t VEC = Geo<T>::VEC;
+#pragma unroll
     for (int q = 0; q < Q; q++) {
-        col_reduce(ry < rstep ? v[q] : 0.0, R, ry, j, rstep, sh);
-        if (ry == 0 && j < R) part[((size_t)q * kBBlocks + blockIdx.x) * R + j] = sh[j];
+        if (g.active)
+#pragma unroll
+            for (uint32_t v = 0; v < VEC; v++) sh[g.ry * R + g.col + v] = acc[q][v];
+        __syncthreads();
+        if (g.active && g.ry == 0)
+#pragma unroll
+            for (uint32_t v = 0; v < VEC; v++) {
+                double s = 0.0;
+                for (uint32_t y = 0; y < g.rstep; y++) s += sh[y * R + g.col + v];
+                part[((size_t)q * gridDim.x + blockIdx.x) * R + g.col + v] = s;
+            }
         __syncthreads();
     }
 }
 
-__device__ __forceinline__ double bsum(const double* part, uint32_t q, uint32_t R, uint32_t j) {
+// Sum over the nb block partials of quantity q, column j (one block per
+// column, fixed tree); valid in thread 0.
+__device__ __forceinline__ double col_total(const double* part, uint32_t q, uint32_t j, uint32_t R, uint32_t nb,
+                                            double* sh) {
     double s = 0.0;
-    for (int b = 0; b < kBBlocks; b++) s += part[((size_t)q * kBBlocks + b) * R + j];
-    return s;
+    for (uint32_t b = threadIdx.x; b < nb; b += kFinThreads) s += part[((size_t)q * nb + b) * R + j];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = kFinThreads / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    const double r = sh[0];
+    __syncthreads();
+    return r;
+}
+
+// per column a.b (a == b: squared norms)
+template <typename T>
+__global__ void __launch_bounds__(kBThreads) k_bdots(const T* __restrict__ a, const T* __restrict__ b, size_t n,
+                                                     uint32_t ld, uint32_t R, double* part) {
+    __shared__ double sh[kBThreads * 4];
+    const Geo<T> g(n, R);
+    constexpr uint32_t VEC = Geo<T>::VEC;
+    double acc[1][VEC] = {};
+    if (g.active)
+        for (size_t i = g.r0 + g.ry; i < g.r1; i += g.rstep) {
+            T x[VEC], y[VEC];
+            ldv(a + i * ld + g.col, x);
+            ldv(b + i * ld + g.col, y);
+#pragma unroll
+            for (uint32_t v = 0; v < VEC; v++) acc[0][v] = __fma_rn((double)x[v], (double)y[v], acc[0][v]);
+        }
+    block_cols<T, 1>(acc, g, R, part, sh);
 }
 
 // init: r = b - q, z = dinv r, p = z; per column rz, rr, bb
@@ -75,40 +123,42 @@ __global__ void __launch_bounds__(kBThreads) k_binit(const T* __restrict__ b, co
                                                      const T* __restrict__ dinv, T* __restrict__ r, T* __restrict__ z,
                                                      T* __restrict__ p, size_t n, uint32_t ld, uint32_t R,
                                                      double* part) {
-    __shared__ double sh[kBThreads];
-    uint32_t ry, j, rstep;
-    row_col<T>(R, ry, j, rstep);
-    double rz = 0, rr = 0, bb = 0;
-    if (ry < rstep && j < R) {
-        const size_t chunk = (n + kBBlocks - 1) / kBBlocks;
-        const size_t r0 = (size_t)blockIdx.x * chunk, r1 = min(n, r0 + chunk);
-        for (size_t i = r0 + ry; i < r1; i += rstep) {
-            const size_t k = i * ld + j;
-            const T bi = b[k];
-            const T ri = bi - q[k];
-            const T zi = dinv[i] * ri;
-            r[k] = ri;
-            z[k] = zi;
-            p[k] = zi;
-            rz = __fma_rn((double)ri, (double)zi, rz);
-            rr = __fma_rn((double)ri, (double)ri, rr);
-            bb = __fma_rn((double)bi, (double)bi, bb);
+    __shared__ double sh[kBThreads * 4];
+    const Geo<T> g(n, R);
+    constexpr uint32_t VEC = Geo<T>::VEC;
+    double acc[3][VEC] = {};
+    if (g.active)
+        for (size_t i = g.r0 + g.ry; i < g.r1; i += g.rstep) {
+            const size_t k = i * ld + g.col;
+            T bi[VEC], qi[VEC], ri[VEC], zi[VEC];
+            ldv(b + k, bi);
+            ldv(q + k, qi);
+            const T di = dinv[i];
+#pragma unroll
+            for (uint32_t v = 0; v < VEC; v++) {
+                ri[v] = bi[v] - qi[v];
+                zi[v] = di * ri[v];
+                acc[0][v] = __fma_rn((double)ri[v], (double)zi[v], acc[0][v]);
+                acc[1][v] = __fma_rn((double)ri[v], (double)ri[v], acc[1][v]);
+                acc[2][v] = __fma_rn((double)bi[v], (double)bi[v], acc[2][v]);
+            }
+            stv(r + k, ri);
+            stv(z + k, zi);
+            stv(p + k, zi);
         }
-    }
-    double v[3] = {rz, rr, bb};
-    for (int qq = 0; qq < 3; qq++) {
-        col_reduce(ry < rstep ? v[qq] : 0.0, R, ry, j, rstep, sh);
-        if (ry == 0 && j < R) part[((size_t)qq * kBBlocks + blockIdx.x) * R + j] = sh[j];
-        __syncthreads();
-    }
+    block_cols<T, 3>(acc, g, R, part, sh);
 }
 
-// scalars: sc[j * kBSlots + slot]
-__global__ void k_binit_final(double* sc, const double* part, uint32_t R, double rtol, double atol) {
-    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= R) return;
+// scalars: sc[j * kBSlots + slot]; one block per column
+__global__ void __launch_bounds__(kFinThreads) k_binit_final(double* sc, const double* part, uint32_t R, uint32_t nb,
+                                                             double rtol, double atol) {
+    __shared__ double sh[kFinThreads];
+    const uint32_t j = blockIdx.x;
+    const double rz = col_total(part, 0, j, R, nb, sh);
+    const double rr = col_total(part, 1, j, R, nb, sh);
+    const double bb = col_total(part, 2, j, R, nb, sh);
+    if (threadIdx.x) return;
     double* c = sc + (size_t)j * kBSlots;
-    const double rz = bsum(part, 0, R, j), rr = bsum(part, 1, R, j), bb = bsum(part, 2, R, j);
     c[B_RZ] = rz;
     c[B_RR] = rr;
     c[B_BB] = bb;
@@ -118,11 +168,12 @@ __global__ void k_binit_final(double* sc, const double* part, uint32_t R, double
     c[B_DONE] = (c[B_FLAG] != 0.0 || sqrt(rr) <= c[B_TOL]) ? 1.0 : 0.0;
 }
 
-__global__ void k_balpha(double* sc, const double* part, uint32_t R) {
-    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= R) return;
+__global__ void __launch_bounds__(kFinThreads) k_balpha(double* sc, const double* part, uint32_t R, uint32_t nb) {
+    __shared__ double sh[kFinThreads];
+    const uint32_t j = blockIdx.x;
+    const double pq = col_total(part, 0, j, R, nb, sh);
+    if (threadIdx.x) return;
     double* c = sc + (size_t)j * kBSlots;
-    const double pq = bsum(part, 0, R, j);
     if (c[B_DONE] != 0.0) {
         c[B_ALPHA] = 0.0;
         return;
@@ -142,42 +193,50 @@ __global__ void __launch_bounds__(kBThreads) k_bupdate(T* __restrict__ x, T* __r
                                                        const T* __restrict__ p, const T* __restrict__ q,
                                                        const T* __restrict__ dinv, size_t n, uint32_t ld, uint32_t R,
                                                        const double* sc, double* part) {
-    __shared__ double sh[kBThreads];
-    uint32_t ry, j, rstep;
-    row_col<T>(R, ry, j, rstep);
-    double rz = 0, rr = 0;
-    if (ry < rstep && j < R) {
-        const T alpha = (T)sc[(size_t)j * kBSlots + B_ALPHA];
-        const size_t chunk = (n + kBBlocks - 1) / kBBlocks;
-        const size_t r0 = (size_t)blockIdx.x * chunk, r1 = min(n, r0 + chunk);
-        for (size_t i = r0 + ry; i < r1; i += rstep) {
-            const size_t k = i * ld + j;
-            x[k] = alpha * p[k] + x[k];
-            const T ri = -alpha * q[k] + r[k];
-            const T zi = dinv[i] * ri;
-            r[k] = ri;
-            z[k] = zi;
-            rz = __fma_rn((double)ri, (double)zi, rz);
-            rr = __fma_rn((double)ri, (double)ri, rr);
+    __shared__ double sh[kBThreads * 4];
+    const Geo<T> g(n, R);
+    constexpr uint32_t VEC = Geo<T>::VEC;
+    double acc[2][VEC] = {};
+    if (g.active) {
+        T alpha[VEC];
+#pragma unroll
+        for (uint32_t v = 0; v < VEC; v++) alpha[v] = (T)sc[(size_t)(g.col + v) * kBSlots + B_ALPHA];
+        for (size_t i = g.r0 + g.ry; i < g.r1; i += g.rstep) {
+            const size_t k = i * ld + g.col;
+            T xi[VEC], ri[VEC], pi[VEC], qi[VEC], zi[VEC];
+            ldv(x + k, xi);
+            ldv(r + k, ri);
+            ldv(p + k, pi);
+            ldv(q + k, qi);
+            const T di = dinv[i];
+#pragma unroll
+            for (uint32_t v = 0; v < VEC; v++) {
+                xi[v] = alpha[v] * pi[v] + xi[v];
+                ri[v] = -alpha[v] * qi[v] + ri[v];
+                zi[v] = di * ri[v];
+                acc[0][v] = __fma_rn((double)ri[v], (double)zi[v], acc[0][v]);
+                acc[1][v] = __fma_rn((double)ri[v], (double)ri[v], acc[1][v]);
+            }
+            stv(x + k, xi);
+            stv(r + k, ri);
+            stv(z + k, zi);
         }
     }
-    double v[2] = {rz, rr};
-    for (int qq = 0; qq < 2; qq++) {
-        col_reduce(ry < rstep ? v[qq] : 0.0, R, ry, j, rstep, sh);
-        if (ry == 0 && j < R) part[((size_t)qq * kBBlocks + blockIdx.x) * R + j] = sh[j];
-        __syncthreads();
-    }
+    block_cols<T, 2>(acc, g, R, part, sh);
 }
 
-__global__ void k_bbeta(double* sc, const double* part, uint32_t R, double maxit, unsigned int* remaining) {
-    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= R) return;
+__global__ void __launch_bounds__(kFinThreads) k_bbeta(double* sc, const double* part, uint32_t R, uint32_t nb,
+                                                       double maxit, unsigned int* remaining) {
+    __shared__ double sh[kFinThreads];
+    const uint32_t j = blockIdx.x;
+    const double rz = col_total(part, 0, j, R, nb, sh);
+    const double rr = col_total(part, 1, j, R, nb, sh);
+    if (threadIdx.x) return;
     double* c = sc + (size_t)j * kBSlots;
     if (c[B_DONE] != 0.0) {
         c[B_BETA] = 0.0;
         return;
     }
-    const double rz = bsum(part, 0, R, j), rr = bsum(part, 1, R, j);
     c[B_BETA] = (c[B_RZ] != 0.0) ? rz / c[B_RZ] : 0.0;
     c[B_RZOLD] = c[B_RZ];
     c[B_RZ] = rz;
@@ -193,32 +252,50 @@ __global__ void k_bbeta(double* sc, const double* part, uint32_t R, double maxit
     if (c[B_DONE] == 0.0) atomicAdd(remaining, 1u);
 }
 
+// p = beta p + z per column; a finished column keeps its last direction
 template <typename T>
 __global__ void __launch_bounds__(kBThreads) k_bp(T* __restrict__ p, const T* __restrict__ z, size_t n, uint32_t ld,
                                                   uint32_t R, const double* sc) {
-    const size_t total = n * (size_t)R;
-    const size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < total; k += stride) {
-        const size_t i = k / R;
-        const uint32_t j = (uint32_t)(k % R);
-        // a finished column keeps its last direction
-        if (sc[(size_t)j * kBSlots + B_DONE] != 0.0) continue;
-        const T beta = (T)sc[(size_t)j * kBSlots + B_BETA];
-        p[i * ld + j] = beta * p[i * ld + j] + z[i * ld + j];
+    const Geo<T> g(n, R);
+    constexpr uint32_t VEC = Geo<T>::VEC;
+    if (!g.active) return;
+    T beta[VEC];
+    bool run[VEC], any = false;
+#pragma unroll
+    for (uint32_t v = 0; v < VEC; v++) {
+        const double* c = sc + (size_t)(g.col + v) * kBSlots;
+        run[v] = c[B_DONE] == 0.0;
+        beta[v] = (T)c[B_BETA];
+        any = any || run[v];
+    }
+    if (!any) return;
+    for (size_t i = g.r0 + g.ry; i < g.r1; i += g.rstep) {
+        const size_t k = i * ld + g.col;
+        T pi[VEC], zi[VEC];
+        ldv(p + k, pi);
+        ldv(z + k, zi);
+#pragma unroll
+        for (uint32_t v = 0; v < VEC; v++)
+            if (run[v]) pi[v] = beta[v] * pi[v] + zi[v];
+        stv(p + k, pi);
     }
 }
 
-__global__ void k_bstore_norm(double* sc, const double* part, uint32_t R) {
-    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= R) return;
-    sc[(size_t)j * kBSlots + B_BN] = sqrt(bsum(part, 0, R, j));
+__global__ void __launch_bounds__(kFinThreads) k_bstore_norm(double* sc, const double* part, uint32_t R,
+                                                             uint32_t nb) {
+    __shared__ double sh[kFinThreads];
+    const uint32_t j = blockIdx.x;
+    const double s = col_total(part, 0, j, R, nb, sh);
+    if (threadIdx.x == 0) sc[(size_t)j * kBSlots + B_BN] = sqrt(s);
 }
 
-__global__ void k_bcheck(double* sc, const double* part, uint32_t R, double rtol, double atol) {
-    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= R) return;
+__global__ void __launch_bounds__(kFinThreads) k_bcheck(double* sc, const double* part, uint32_t R, uint32_t nb,
+                                                        double rtol, double atol) {
+    __shared__ double sh[kFinThreads];
+    const uint32_t j = blockIdx.x;
+    const double rr = col_total(part, 0, j, R, nb, sh);
+    if (threadIdx.x) return;
     double* c = sc + (size_t)j * kBSlots;
-    const double rr = bsum(part, 0, R, j);
     c[B_TRR] = rr;
     c[B_CONV] = (sqrt(rr) <= fmax(rtol * c[B_BN], atol)) ? 1.0 : 0.0;
 }
@@ -227,37 +304,42 @@ __global__ void __launch_bounds__(kBThreads) k_breliable(const double* __restric
                                                          float* __restrict__ z, const float* __restrict__ p,
                                                          const float* __restrict__ dinv, size_t n, uint32_t R,
                                                          double* part) {
-    __shared__ double sh[kBThreads];
-    uint32_t ry, j, rstep;
-    row_col<float>(R, ry, j, rstep);
-    double rz = 0, rr = 0, rp = 0;
-    if (ry < rstep && j < R) {
-        const size_t chunk = (n + kBBlocks - 1) / kBBlocks;
-        const size_t r0 = (size_t)blockIdx.x * chunk, r1 = min(n, r0 + chunk);
-        for (size_t i = r0 + ry; i < r1; i += rstep) {
-            const size_t k = i * R + j;
-            const float ri = (float)r64[k];
-            const float zi = dinv[i] * ri;
-            r[k] = ri;
-            z[k] = zi;
-            rz = __fma_rn((double)ri, (double)zi, rz);
-            rr = __fma_rn((double)ri, (double)ri, rr);
-            rp = __fma_rn((double)ri, (double)p[k], rp);
+    __shared__ double sh[kBThreads * 4];
+    const Geo<float> g(n, R);
+    constexpr uint32_t VEC = Geo<float>::VEC;
+    double acc[3][VEC] = {};
+    if (g.active)
+        for (size_t i = g.r0 + g.ry; i < g.r1; i += g.rstep) {
+            const size_t k = i * R + g.col;
+            double t0[2], t1[2];
+            ldv(r64 + k, t0);
+            ldv(r64 + k + 2, t1);
+            const float ri[4] = {(float)t0[0], (float)t0[1], (float)t1[0], (float)t1[1]};
+            float zi[4], pi[4];
+            ldv(p + k, pi);
+            const float di = dinv[i];
+#pragma unroll
+            for (uint32_t v = 0; v < VEC; v++) {
+                zi[v] = di * ri[v];
+                acc[0][v] = __fma_rn((double)ri[v], (double)zi[v], acc[0][v]);
+                acc[1][v] = __fma_rn((double)ri[v], (double)ri[v], acc[1][v]);
+                acc[2][v] = __fma_rn((double)ri[v], (double)pi[v], acc[2][v]);
+            }
+            stv(r + k, ri);
+            stv(z + k, zi);
         }
-    }
-    double v[3] = {rz, rr, rp};
-    for (int qq = 0; qq < 3; qq++) {
-        col_reduce(ry < rstep ? v[qq] : 0.0, R, ry, j, rstep, sh);
-        if (ry == 0 && j < R) part[((size_t)qq * kBBlocks + blockIdx.x) * R + j] = sh[j];
-        __syncthreads();
-    }
+    block_cols<float, 3>(acc, g, R, part, sh);
 }
 
-__global__ void k_breliable_final(double* sc, const double* part, uint32_t R, double inner_rtol) {
-    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= R) return;
+__global__ void __launch_bounds__(kFinThreads) k_breliable_final(double* sc, const double* part, uint32_t R,
+                                                                 uint32_t nb, double inner_rtol) {
+    __shared__ double sh[kFinThreads];
+    const uint32_t j = blockIdx.x;
+    const double rz = col_total(part, 0, j, R, nb, sh);
+    const double rr = col_total(part, 1, j, R, nb, sh);
+    const double rp = col_total(part, 2, j, R, nb, sh);
+    if (threadIdx.x) return;
     double* c = sc + (size_t)j * kBSlots;
-    const double rz = bsum(part, 0, R, j), rr = bsum(part, 1, R, j), rp = bsum(part, 2, R, j);
     const bool restart = c[B_FLAG] != 0.0;  // the recursion broke down: fresh direction
     const bool bad = (rz < 0.0 || rz != rz);
     c[B_BETA] = (!restart && !bad && c[B_RZOLD] > 0.0) ? rz / c[B_RZOLD] : 0.0;
@@ -273,13 +355,24 @@ __global__ void k_breliable_final(double* sc, const double* part, uint32_t R, do
 // p = z + beta (p - gamma z) per column
 __global__ void __launch_bounds__(kBThreads) k_breliable_p(float* __restrict__ p, const float* __restrict__ z, size_t n,
                                                            uint32_t R, const double* sc) {
-    const size_t total = n * (size_t)R;
-    const size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < total; k += stride) {
-        const uint32_t j = (uint32_t)(k % R);
-        const double* c = sc + (size_t)j * kBSlots;
-        const float beta = (float)c[B_BETA];
-        p[k] = __fmaf_rn(beta, p[k], (float)(1.0 - c[B_BETA] * c[B_GAMMA]) * z[k]);
+    const Geo<float> g(n, R);
+    constexpr uint32_t VEC = Geo<float>::VEC;
+    if (!g.active) return;
+    float beta[VEC], cz[VEC];
+#pragma unroll
+    for (uint32_t v = 0; v < VEC; v++) {
+        const double* c = sc + (size_t)(g.col + v) * kBSlots;
+        beta[v] = (float)c[B_BETA];
+        cz[v] = (float)(1.0 - c[B_BETA] * c[B_GAMMA]);
+    }
+    for (size_t i = g.r0 + g.ry; i < g.r1; i += g.rstep) {
+        const size_t k = i * R + g.col;
+        float pi[VEC], zi[VEC];
+        ldv(p + k, pi);
+        ldv(z + k, zi);
+#pragma unroll
+        for (uint32_t v = 0; v < VEC; v++) pi[v] = __fmaf_rn(beta[v], pi[v], cz[v] * zi[v]);
+        stv(p + k, pi);
     }
 }
 
@@ -291,11 +384,6 @@ __global__ void k_bset_constrained(T* v, const T* u, const uint32_t* idx, uint32
     const uint32_t c = idx[k / R];
     const uint32_t j = (uint32_t)(k % R);
     v[(size_t)c * ld + j] = u[(size_t)c * ld + j];
-}
-
-unsigned grid_for(size_t n) {
-    size_t g = (n + kBThreads - 1) / kBThreads;
-    return (unsigned)(g > 4096 ? 4096 : (g == 0 ? 1 : g));
 }
 
 }  // namespace
@@ -313,15 +401,15 @@ template <typename T>
 cudaError_t launch_bcg_init(const T* b, const T* q, const T* dinv, T* r, T* z, T* p, size_t n, uint32_t ld,
                             uint32_t R, double* sc, double* part, double rtol, double atol, cudaStream_t st) {
     k_binit<T><<<kBBlocks, kBThreads, 0, st>>>(b, q, dinv, r, z, p, n, ld, R, part);
-    k_binit_final<<<(R + 63) / 64, 64, 0, st>>>(sc, part, R, rtol, atol);
+    k_binit_final<<<R, kFinThreads, 0, st>>>(sc, part, R, kBBlocks, rtol, atol);
     return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t launch_bcg_step_scalars(const T* p, const T* q, size_t n, uint32_t ld, uint32_t R, double* sc,
                                     double* part, cudaStream_t st) {
-    k_bdots<T, 1><<<kBBlocks, kBThreads, 0, st>>>(p, q, nullptr, n, ld, R, part);
-    k_balpha<<<(R + 63) / 64, 64, 0, st>>>(sc, part, R);
+    k_bdots<T><<<kBBlocks, kBThreads, 0, st>>>(p, q, n, ld, R, part);
+    k_balpha<<<R, kFinThreads, 0, st>>>(sc, part, R, kBBlocks);
     return cudaGetLastError();
 }
 
@@ -330,35 +418,35 @@ cudaError_t launch_bcg_update(T* x, T* r, T* z, T* p, const T* q, const T* dinv,
                               double* sc, double* part, double maxit, unsigned int* remaining, cudaStream_t st) {
     k_bupdate<T><<<kBBlocks, kBThreads, 0, st>>>(x, r, z, p, q, dinv, n, ld, R, sc, part);
     cudaMemsetAsync(remaining, 0, sizeof(unsigned int), st);
-    k_bbeta<<<(R + 63) / 64, 64, 0, st>>>(sc, part, R, maxit, remaining);
-    k_bp<T><<<grid_for(n * R), kBThreads, 0, st>>>(p, z, n, ld, R, sc);
+    k_bbeta<<<R, kFinThreads, 0, st>>>(sc, part, R, kBBlocks, maxit, remaining);
+    k_bp<T><<<kBBlocks, kBThreads, 0, st>>>(p, z, n, ld, R, sc);
     return cudaGetLastError();
 }
 
 cudaError_t launch_bstore_norm(const double* a, size_t n, uint32_t R, double* sc, double* part, cudaStream_t st) {
-    k_bdots<double, 1><<<kBBlocks, kBThreads, 0, st>>>(a, a, nullptr, n, R, R, part);
-    k_bstore_norm<<<(R + 63) / 64, 64, 0, st>>>(sc, part, R);
+    k_bdots<double><<<kBBlocks, kBThreads, 0, st>>>(a, a, n, R, R, part);
+    k_bstore_norm<<<R, kFinThreads, 0, st>>>(sc, part, R, kBBlocks);
     return cudaGetLastError();
 }
 
 cudaError_t launch_bcheck(const double* a, size_t n, uint32_t R, double* sc, double* part, double rtol, double atol,
                           cudaStream_t st) {
-    k_bdots<double, 1><<<kBBlocks, kBThreads, 0, st>>>(a, a, nullptr, n, R, R, part);
-    k_bcheck<<<(R + 63) / 64, 64, 0, st>>>(sc, part, R, rtol, atol);
+    k_bdots<double><<<kBBlocks, kBThreads, 0, st>>>(a, a, n, R, R, part);
+    k_bcheck<<<R, kFinThreads, 0, st>>>(sc, part, R, kBBlocks, rtol, atol);
     return cudaGetLastError();
 }
 
 cudaError_t launch_breliable(const double* r64, float* r, float* z, float* p, const float* dinv, size_t n, uint32_t R,
                              double* sc, double* part, double inner_rtol, cudaStream_t st) {
     k_breliable<<<kBBlocks, kBThreads, 0, st>>>(r64, r, z, p, dinv, n, R, part);
-    k_breliable_final<<<(R + 63) / 64, 64, 0, st>>>(sc, part, R, inner_rtol);
-    k_breliable_p<<<grid_for(n * R), kBThreads, 0, st>>>(p, z, n, R, sc);
+    k_breliable_final<<<R, kFinThreads, 0, st>>>(sc, part, R, kBBlocks, inner_rtol);
+    k_breliable_p<<<kBBlocks, kBThreads, 0, st>>>(p, z, n, R, sc);
     return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t launch_bnorm2(const T* a, size_t n, uint32_t ld, uint32_t R, double* out_part, cudaStream_t st) {
-    k_bdots<T, 1><<<kBBlocks, kBThreads, 0, st>>>(a, a, nullptr, n, ld, R, out_part);
+    k_bdots<T><<<kBBlocks, kBThreads, 0, st>>>(a, a, n, ld, R, out_part);
     return cudaGetLastError();
 }
 

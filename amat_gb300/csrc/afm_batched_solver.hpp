@@ -7,7 +7,7 @@
 
 namespace afm {
 
-constexpr int kBBlocks = 256;  // row chunks of the column reductions
+constexpr int kBBlocks = 1024;  // row chunks of the column reductions
 
 // Per-column scalar slots: sc[j * kBSlots + slot].
 // B_BN: ||b_j||; B_TRR: ||b_j - A x_j||^2 in FP64 at the last residual check;

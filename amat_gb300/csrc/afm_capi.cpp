@@ -154,6 +154,20 @@ size_t entry_bytes(int prec) { return prec == AFM_PREC_FP32 ? 4 : 8; }
 
 uint64_t round16(uint64_t b) { return (b + 15) / 16 * 16; }
 
+// The operator's device buffers are stream-ordered allocations on its own
+// stream: releasing them (finalize again, destroy) never synchronises the
+// device, so other operators' work keeps running. Work a caller enqueued on
+// its own streams with this operator must be ordered before such a release.
+template <typename T>
+cudaError_t dalloc(afm_operator* op, T** p, size_t bytes) {
+    return cudaMallocAsync((void**)p, bytes, op->stream);
+}
+template <typename T>
+void dfree(afm_operator* op, T*& p) {
+    if (p) cudaFreeAsync(p, op->stream);
+    p = nullptr;
+}
+
 void drop_graph(afm_operator::CgGraph& g);
 
 void free_device(afm_operator* op) {
@@ -162,31 +176,20 @@ void free_device(afm_operator* op) {
     drop_graph(op->bcg64);
     drop_graph(op->bcg32);
     op->batch_tune.clear();
-    cudaFree(op->d_bwork);
-    cudaFree(op->d_bsc);
-    op->d_bwork = nullptr;
-    op->d_bsc = nullptr;
+    dfree(op, op->d_bwork);
+    dfree(op, op->d_bsc);
     op->bwork_elems = 0;
     op->bsc_elems = 0;
     op->generation++;
-    cudaFree(op->d_ke);
-    cudaFree(op->d_map);
-    cudaFree(op->d_diag);
-    cudaFree(op->d_bc_idx);
-    cudaFree(op->d_bc_val);
-    cudaFree(op->d_work);
-    cudaFree(op->d_work32);
-    cudaFree(op->d_patch_desc);
-    cudaFree(op->d_patch_idx);
-    op->d_patch_desc = nullptr;
-    op->d_patch_idx = nullptr;
-    op->d_ke = nullptr;
-    op->d_map = nullptr;
-    op->d_diag = nullptr;
-    op->d_bc_idx = nullptr;
-    op->d_bc_val = nullptr;
-    op->d_work = nullptr;
-    op->d_work32 = nullptr;
+    dfree(op, op->d_ke);
+    dfree(op, op->d_map);
+    dfree(op, op->d_diag);
+    dfree(op, op->d_bc_idx);
+    dfree(op, op->d_bc_val);
+    dfree(op, op->d_work);
+    dfree(op, op->d_work32);
+    dfree(op, op->d_patch_desc);
+    dfree(op, op->d_patch_idx);
     op->work_elems = 0;
     op->work32_elems = 0;
 }
@@ -284,7 +287,7 @@ void layout_element(const afm_operator* op, const Segment& s, uint32_t e, uint64
 
 // Patch plan of the small-element path (afm_patch.cuh). Patches grow
 // breadth first over shared DoFs from the lowest unassigned element, up to
-// P elements and kPatchMaxDofs distinct DoFs; patches get first-fit colours
+// 128 elements and kPatchMaxDofs distinct DoFs; patches get first-fit colours
 // in creation order (no two patches of a colour share a DoF). Fills the
 // element slots (op->perm, kNoElement for empty slots), one TPE-layout
 // segment covering every slot, the patch descriptors and index blocks.
@@ -292,7 +295,7 @@ void layout_element(const afm_operator* op, const Segment& s, uint32_t e, uint64
 // patches need more than 64 colours or do not fit the shared memory.
 bool build_patch_plan(afm_operator* op, uint32_t n, int prec, std::vector<PatchDesc>& desc,
                       std::vector<unsigned char>& idx) {
-    const uint32_t P = (n <= 10) ? 256 : 128;
+    const uint32_t P = 128;
     const uint32_t NE = op->n_elem, ND = op->n_dofs;
     const uint32_t* off = op->offsets.data();
     const uint32_t* map = op->map.data();
@@ -520,9 +523,13 @@ void build_segments(afm_operator* op, int prec) {
 }
 
 int upload_arena(afm_operator* op) {
-    // staging in pinned memory, chunks of ~256 MB of whole units
-    const size_t kChunk = 256ull << 20;
+    // staging in pinned memory, chunks of up to 256 MB of whole units (no more
+    // than the arena: pinning is slow and small operators need little)
+    uint64_t largest = 0;
+    for (const Segment& s : op->segs) largest = std::max<uint64_t>(largest, s.unit_bytes);
+    const size_t kChunk = (size_t)std::max<uint64_t>(std::min<uint64_t>(256ull << 20, op->ke_bytes), largest);
     unsigned char* stage = nullptr;
+    if (kChunk == 0) return AFM_SUCCESS;
     AFM_CUDA(cudaMallocHost((void**)&stage, kChunk));
     int status = AFM_SUCCESS;
     for (const Segment& s : op->segs) {
@@ -572,10 +579,9 @@ int upload_arena(afm_operator* op) {
 int ensure_work(afm_operator* op, size_t vectors) {
     const size_t need = vectors * (size_t)std::max<uint32_t>(op->n_dofs, 1);
     if (op->work_elems >= need) return AFM_SUCCESS;
-    cudaFree(op->d_work);
-    op->d_work = nullptr;
+    dfree(op, op->d_work);
     op->work_elems = 0;
-    AFM_CUDA(cudaMalloc((void**)&op->d_work, need * sizeof(double)));
+    AFM_CUDA(dalloc(op, &op->d_work, need * sizeof(double)));
     op->work_elems = need;
     return AFM_SUCCESS;
 }
@@ -583,22 +589,22 @@ int ensure_work(afm_operator* op, size_t vectors) {
 int ensure_work32(afm_operator* op, size_t vectors) {
     const size_t need = vectors * (size_t)std::max<uint32_t>(op->n_dofs, 1);
     if (op->work32_elems >= need) return AFM_SUCCESS;
-    cudaFree(op->d_work32);
-    op->d_work32 = nullptr;
+    dfree(op, op->d_work32);
     op->work32_elems = 0;
-    AFM_CUDA(cudaMalloc((void**)&op->d_work32, need * sizeof(float)));
+    AFM_CUDA(dalloc(op, &op->d_work32, need * sizeof(float)));
     op->work32_elems = need;
     return AFM_SUCCESS;
 }
 
 int check_device_error(afm_operator* op) {
-    int h = 0;
-    AFM_CUDA(cudaMemcpyAsync(&h, op->d_err, sizeof(int), cudaMemcpyDeviceToHost, op->stream));
+    int h[kErrWords] = {0};
+    AFM_CUDA(cudaMemcpyAsync(h, op->d_err, sizeof(h), cudaMemcpyDeviceToHost, op->stream));
     AFM_CUDA(cudaStreamSynchronize(op->stream));
-    if (h & kErrTimeout) {
-        cudaMemsetAsync(op->d_err, 0, sizeof(int), op->stream);
-        return fail(AFM_ERR_TIMEOUT, "a device wait exceeded its time limit");
-    }
+    if (h[0]) cudaMemsetAsync(op->d_err, 0, sizeof(h), op->stream);
+    if (h[0] & kErrBounds)
+        return fail(AFM_ERR_INTERNAL, "device bounds check %d failed (block %d, thread %d: %d %d %d)", h[1], h[2],
+                    h[3], h[4], h[5], h[6]);
+    if (h[0] & kErrTimeout) return fail(AFM_ERR_TIMEOUT, "a device wait exceeded its time limit");
     return AFM_SUCCESS;
 }
 
@@ -683,6 +689,7 @@ int enqueue_matvec_batched(afm_operator* op, void* d_V, const void* d_U, uint32_
         a.ld = ld;
         a.bc_mode = bc_mode;
         a.err = op->d_err;
+        a.n_dofs = op->n_dofs;
         cudaError_t e;
         if (kprec == AFM_PREC_FP64)
             e = launch_batched_fp64(s, a, op->sm_count, tr, ng, !first, st);
@@ -699,8 +706,8 @@ int enqueue_matvec_batched(afm_operator* op, void* d_V, const void* d_U, uint32_
 
 int check_batched(afm_operator* op, uint32_t nrhs, uint32_t ld) {
     if (!op->finalized) return fail(AFM_ERR_STATE, "batched product before finalize");
-    if (nrhs == 0 || nrhs > 256 || nrhs % 4 != 0 || ld < nrhs)
-        return fail(AFM_ERR_INVALID_ARG, "nrhs %u (multiple of 4, <= 256), ld %u", nrhs, ld);
+    if (nrhs == 0 || nrhs > 256 || nrhs % 4 != 0 || ld < nrhs || ld % 4 != 0)
+        return fail(AFM_ERR_INVALID_ARG, "nrhs %u (multiple of 4, <= 256), ld %u (>= nrhs, multiple of 4)", nrhs, ld);
     for (const Segment& s : op->segs)
         if (s.units && s.regime != REG_WPE)
             return fail(AFM_NOT_IMPLEMENTED, "batched product needs elements with more than %u DoFs", kTpeMaxN);
@@ -721,10 +728,8 @@ int batch_tuning(afm_operator* op, void* d_V, const void* d_U, uint32_t nrhs, ui
             *ng = t.ng;
             return AFM_SUCCESS;
         }
-    std::vector<std::pair<int, int>> cand;
-    for (int g : {2, 3, 4}) cand.push_back({4, g});
-    if (kprec == AFM_PREC_FP32)
-        for (int g : {2, 4}) cand.push_back({8, g});
+    // (columns, rows) of the lane tile
+    const std::vector<std::pair<int, int>> cand = {{8, 6}, {8, 4}, {8, 2}, {4, 4}};
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -767,6 +772,7 @@ int batched_product(afm_operator* op, T* d_V, const T* d_U, uint32_t nrhs, uint3
         return fail(AFM_ERR_STATE, "FP32 product needs an FP32 or FP64_SPLIT operator");
     if (!f32 && op->precision == AFM_PREC_FP32) return fail(AFM_ERR_STATE, "FP32 operator: use the _f32 entry");
     if (!d_V || !d_U || (const void*)d_V == (const void*)d_U) return fail(AFM_ERR_INVALID_ARG, "bad blocks");
+    if (((uintptr_t)d_V | (uintptr_t)d_U) % 16) return fail(AFM_ERR_INVALID_ARG, "blocks must be 16-byte aligned");
     DeviceGuard g(op->device);
     cudaStream_t st = pick_stream(op, stream);
     int tr = 4, ng = 2;
@@ -780,10 +786,9 @@ int batched_product(afm_operator* op, T* d_V, const T* d_U, uint32_t nrhs, uint3
 
 int ensure_bwork(afm_operator* op, size_t doubles) {
     if (op->bwork_elems >= doubles) return AFM_SUCCESS;
-    cudaFree(op->d_bwork);
-    op->d_bwork = nullptr;
+    dfree(op, op->d_bwork);
     op->bwork_elems = 0;
-    AFM_CUDA(cudaMalloc((void**)&op->d_bwork, doubles * sizeof(double)));
+    AFM_CUDA(dalloc(op, &op->d_bwork, doubles * sizeof(double)));
     op->bwork_elems = doubles;
     return AFM_SUCCESS;
 }
@@ -791,13 +796,12 @@ int ensure_bwork(afm_operator* op, size_t doubles) {
 int ensure_bscalars(afm_operator* op, uint32_t nrhs) {
     const size_t need = (size_t)nrhs * kBSlots + (size_t)kBBlocks * nrhs * 3;
     if (op->bsc_elems < need) {
-        cudaFree(op->d_bsc);
-        op->d_bsc = nullptr;
+        dfree(op, op->d_bsc);
         op->bsc_elems = 0;
-        AFM_CUDA(cudaMalloc((void**)&op->d_bsc, need * sizeof(double)));
+        AFM_CUDA(dalloc(op, &op->d_bsc, need * sizeof(double)));
         op->bsc_elems = need;
     }
-    if (!op->d_bremain) AFM_CUDA(cudaMalloc((void**)&op->d_bremain, sizeof(unsigned int)));
+    if (!op->d_bremain) AFM_CUDA(dalloc(op, &op->d_bremain, sizeof(unsigned int)));
     if (!op->h_bremain) AFM_CUDA(cudaMallocHost((void**)&op->h_bremain, sizeof(unsigned int)));
     return AFM_SUCCESS;
 }
@@ -1032,11 +1036,12 @@ int run_cg_iterations(afm_operator* op, afm_operator::CgGraph& gc, const CgVecto
     return AFM_SUCCESS;
 }
 
-// Iterative-refinement stopping rule. The FP64 residual of the refined x may
-// grow for a step before it falls (an FP32 correction that shrinks the error
-// can overshoot in the residual norm), so refinement stops only after
-// kIrMaxStall consecutive steps without a new smallest residual.
-constexpr int kIrMaxStall = 3;
+// Stopping rule of the FP64 updates of the mixed-precision solves. The
+// residual norm of CG is not monotone (it can rise or plateau for a few
+// hundred iterations), so a solve stops early only after kIrMaxStall
+// consecutive updates without a new smallest FP64 residual; max_outer bounds
+// the rest.
+constexpr int kIrMaxStall = 10;
 
 bool ir_progress(double rn, double* best, int* stall) {
     if (rn < *best) {
@@ -1290,13 +1295,13 @@ int afm_create(afm_operator** out, int bc_method, int device) {
     op->bc_method = bc_method;
     op->sm_count = prop.multiProcessorCount;
     if (cudaStreamCreateWithFlags(&op->stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaMalloc((void**)&op->d_err, sizeof(int)) != cudaSuccess ||
-        cudaMalloc((void**)&op->d_scalars, sizeof(double) * (kScalarSlots + kPartialSlots)) != cudaSuccess ||
+        dalloc(op, &op->d_err, sizeof(int) * kErrWords) != cudaSuccess ||
+        dalloc(op, &op->d_scalars, sizeof(double) * (kScalarSlots + kPartialSlots)) != cudaSuccess ||
         cudaMallocHost((void**)&op->h_scalars, sizeof(double) * kScalarSlots) != cudaSuccess) {
         afm_destroy(op);
         return fail(AFM_ERR_CUDA, "afm_create: stream or buffer allocation failed");
     }
-    cudaMemsetAsync(op->d_err, 0, sizeof(int), op->stream);
+    cudaMemsetAsync(op->d_err, 0, sizeof(int) * kErrWords, op->stream);
     cudaStreamSynchronize(op->stream);
     *out = op;
     return ok();
@@ -1308,9 +1313,12 @@ int afm_destroy(afm_operator* op) {
         DeviceGuard g(op->device);
         if (op->stream) cudaStreamSynchronize(op->stream);
         free_device(op);
-        cudaFree(op->d_err);
-        cudaFree(op->d_scalars);
-        cudaFree(op->d_bremain);
+        if (op->stream) {
+            dfree(op, op->d_err);
+            dfree(op, op->d_scalars);
+            dfree(op, op->d_bremain);
+            cudaStreamSynchronize(op->stream);
+        }
         if (op->h_scalars) cudaFreeHost(op->h_scalars);
         if (op->h_bremain) cudaFreeHost(op->h_bremain);
         if (op->stream) cudaStreamDestroy(op->stream);
@@ -1533,12 +1541,12 @@ int afm_finalize(afm_operator* op) {
         if (is_bc[d]) op->diag_host[d] = bc_diag;
 
     // uploads
-    AFM_CUDA(cudaMalloc((void**)&op->d_ke, std::max<size_t>(op->ke_bytes, 16)));
-    AFM_CUDA(cudaMalloc((void**)&op->d_map, std::max<size_t>(op->map_bytes, 16)));
-    AFM_CUDA(cudaMalloc((void**)&op->d_diag, sizeof(double) * std::max<uint32_t>(op->n_dofs, 1)));
+    AFM_CUDA(dalloc(op, &op->d_ke, std::max<size_t>(op->ke_bytes, 16)));
+    AFM_CUDA(dalloc(op, &op->d_map, std::max<size_t>(op->map_bytes, 16)));
+    AFM_CUDA(dalloc(op, &op->d_diag, sizeof(double) * std::max<uint32_t>(op->n_dofs, 1)));
     op->n_bc = (uint32_t)op->constrained.size();
-    AFM_CUDA(cudaMalloc((void**)&op->d_bc_idx, sizeof(uint32_t) * std::max<uint32_t>(op->n_bc, 1)));
-    AFM_CUDA(cudaMalloc((void**)&op->d_bc_val, sizeof(double) * std::max<uint32_t>(op->n_bc, 1)));
+    AFM_CUDA(dalloc(op, &op->d_bc_idx, sizeof(uint32_t) * std::max<uint32_t>(op->n_bc, 1)));
+    AFM_CUDA(dalloc(op, &op->d_bc_val, sizeof(double) * std::max<uint32_t>(op->n_bc, 1)));
     std::vector<uint32_t> bci(op->constrained.begin(), op->constrained.end());
     AFM_CUDA(cudaMemcpyAsync(op->d_map, hmap.data(), op->map_bytes, cudaMemcpyHostToDevice, op->stream));
     AFM_CUDA(cudaMemcpyAsync(op->d_diag, op->diag_host.data(), sizeof(double) * op->n_dofs, cudaMemcpyHostToDevice,
@@ -1551,8 +1559,8 @@ int afm_finalize(afm_operator* op) {
     }
     if (op->use_patches) {
         op->patch_idx_bytes = pidx.size();
-        AFM_CUDA(cudaMalloc((void**)&op->d_patch_desc, sizeof(PatchDesc) * std::max<size_t>(pdesc.size(), 1)));
-        AFM_CUDA(cudaMalloc((void**)&op->d_patch_idx, std::max<size_t>(pidx.size(), 16)));
+        AFM_CUDA(dalloc(op, &op->d_patch_desc, sizeof(PatchDesc) * std::max<size_t>(pdesc.size(), 1)));
+        AFM_CUDA(dalloc(op, &op->d_patch_idx, std::max<size_t>(pidx.size(), 16)));
         AFM_CUDA(cudaMemcpyAsync(op->d_patch_desc, pdesc.data(), sizeof(PatchDesc) * pdesc.size(),
                                  cudaMemcpyHostToDevice, op->stream));
         AFM_CUDA(cudaMemcpyAsync(op->d_patch_idx, pidx.data(), pidx.size(), cudaMemcpyHostToDevice, op->stream));
@@ -1847,14 +1855,14 @@ int afm_matmult_bc_batched_device_f32(afm_operator* op, float* d_V, const float*
 }
 
 int afm_get_batch_tuning(afm_operator* op, uint32_t nrhs, uint32_t ld, int f32, int* cols_per_thread,
-                         int* groups_per_cta, float* ms) {
+                         int* rows_per_thread, float* ms) {
     AFM_CHECK_OP(op);
     const int kprec = f32 ? AFM_PREC_FP32 : op->precision;
     const uint64_t key = ((uint64_t)nrhs << 40) | ((uint64_t)ld << 8) | (uint64_t)kprec;
     for (const auto& t : op->batch_tune)
         if (t.key == key) {
             if (cols_per_thread) *cols_per_thread = t.tr;
-            if (groups_per_cta) *groups_per_cta = t.ng;
+            if (rows_per_thread) *rows_per_thread = t.ng;
             if (ms) *ms = t.ms;
             return ok();
         }
@@ -1862,12 +1870,14 @@ int afm_get_batch_tuning(afm_operator* op, uint32_t nrhs, uint32_t ld, int f32, 
 }
 
 int afm_set_batch_tuning(afm_operator* op, uint32_t nrhs, uint32_t ld, int f32, int cols_per_thread,
-                         int groups_per_cta) {
+                         int rows_per_thread) {
     AFM_CHECK_OP(op);
     if (!op->finalized) return fail(AFM_ERR_STATE, "before finalize");
-    if ((cols_per_thread != 4 && cols_per_thread != 8) || groups_per_cta < 1 || groups_per_cta > 4 ||
-        nrhs % (uint32_t)cols_per_thread)
-        return fail(AFM_ERR_INVALID_ARG, "tile %d x groups %d for nrhs %u", cols_per_thread, groups_per_cta, nrhs);
+    const bool tile_ok = (cols_per_thread == 4 && rows_per_thread == 4) ||
+                         (cols_per_thread == 8 && (rows_per_thread == 2 || rows_per_thread == 4 || rows_per_thread == 6));
+    if (!tile_ok || nrhs % (uint32_t)cols_per_thread)
+        return fail(AFM_ERR_INVALID_ARG, "tile %d rows x %d columns for nrhs %u", rows_per_thread, cols_per_thread, nrhs);
+    const int groups_per_cta = rows_per_thread;
     const int kprec = f32 ? AFM_PREC_FP32 : op->precision;
     const uint64_t key = ((uint64_t)nrhs << 40) | ((uint64_t)ld << 8) | (uint64_t)kprec;
     for (auto& t : op->batch_tune)
@@ -1887,6 +1897,7 @@ int afm_solve_cg_batched_device(afm_operator* op, const double* d_B, double* d_X
     if (s) return s;
     if (op->precision == AFM_PREC_FP32) return fail(AFM_ERR_STATE, "FP32 operator");
     if (!d_B || !d_X) return fail(AFM_ERR_INVALID_ARG, "null block");
+    if (((uintptr_t)d_B | (uintptr_t)d_X) % 16) return fail(AFM_ERR_INVALID_ARG, "blocks must be 16-byte aligned");
     DeviceGuard g(op->device);
     const size_t n = op->n_dofs, N = n * nrhs;
     s = ensure_bwork(op, 4 * N + n);
@@ -1947,6 +1958,7 @@ int afm_solve_cg_batched_mixed_device(afm_operator* op, const double* d_B, doubl
     if (op->precision != AFM_PREC_FP64_SPLIT)
         return fail(AFM_ERR_STATE, "mixed-precision solve needs the FP64_SPLIT arena (hi plane = FP32 matrix)");
     if (!d_B || !d_X) return fail(AFM_ERR_INVALID_ARG, "null block");
+    if (((uintptr_t)d_B | (uintptr_t)d_X) % 16) return fail(AFM_ERR_INVALID_ARG, "blocks must be 16-byte aligned");
     DeviceGuard g(op->device);
     const size_t n = op->n_dofs, N = n * nrhs;
     // FP64: residual block (and a spare); FP32: rhs, r, z, p, q, d and 1/diag

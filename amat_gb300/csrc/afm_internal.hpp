@@ -25,8 +25,11 @@ constexpr uint32_t kMaxN = 96;           // largest element supported (3 rows pe
 constexpr uint32_t kBcFlag = 0x80000000u;  // map bit: DoF is constrained
 constexpr uint32_t kDofMask = 0x7fffffffu;
 
-// Device error flags (bit set in *err).
+// Device error flags (bit set in err[0]); err[1..6] record the first failed
+// bounds check (kind, block, thread and three values); kErrWords ints in all.
 constexpr int kErrTimeout = 1;
+constexpr int kErrBounds = 2;
+constexpr int kErrWords = 8;
 
 // One launch of the matvec: the elements of one colour that share n.
 struct Segment {
@@ -69,6 +72,8 @@ struct BatchArgs {
     uint32_t nrhs, ld;
     int bc_mode;
     int* err;
+    uint32_t n_dofs;      // rows of U and V (bounds checks)
+    uint32_t smem_total;  // dynamic shared memory of the launch (bounds checks)
 };
 
 // ---- patch path (small elements) -----------------------------------------
@@ -232,7 +237,7 @@ struct afm_operator {
     unsigned int* h_bremain = nullptr;
     struct BatchTune {
         uint64_t key;
-        int tr, ng;
+        int tr, ng;  // lane tile: columns, rows
         float ms;
     };
     std::vector<BatchTune> batch_tune;  // autotuner choices

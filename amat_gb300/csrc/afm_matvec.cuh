@@ -111,6 +111,20 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t b
         : "memory");
 }
 
+// Records a failed bounds check (the access is skipped by the caller): the
+// first failure's kind, block, thread and three values in err[1..6], and
+// kErrBounds in err[0]; the host reports AFM_ERR_INTERNAL.
+__device__ __forceinline__ void report_bad(int* err, int kind, uint32_t a0, uint32_t a1, uint32_t a2) {
+    if (atomicCAS(err + 1, 0, kind) == 0) {
+        err[2] = (int)blockIdx.x;
+        err[3] = (int)threadIdx.x;
+        err[4] = (int)a0;
+        err[5] = (int)a1;
+        err[6] = (int)a2;
+    }
+    atomicOr(err, kErrBounds);
+}
+
 // ---- arithmetic policies ----------------------------------------------------
 // KT: stored Ke entry, UT: staged u entry, VT: vector entry, Acc: accumulator.
 
@@ -253,12 +267,37 @@ __device__ __forceinline__ VT load_u_hint(const VT* u, uint32_t m, int bc_mode, 
 // Shared-memory layout of one CTA: S slots, then 2*S mbarriers and a 16-byte
 // flag word, then extra_bytes of staging (per-warp u buffers of the WPE
 // kernel; u double buffers and partial sums of the warp-group kernel).
+// After the flag word come S uint32 slot tags (the ring index each slot was
+// last loaded with; see ring_wait).
 struct RingLayout {
     uint32_t slot_bytes, stages, warps, ubuf_bytes, extra_bytes;
     __host__ __device__ uint32_t bars_offset() const { return slot_bytes * stages; }
-    __host__ __device__ uint32_t ubuf_offset() const { return bars_offset() + 16 * stages + 16; }
+    __host__ __device__ uint32_t tags_offset() const { return bars_offset() + 16 * stages + 16; }
+    __host__ __device__ uint32_t ubuf_offset() const { return tags_offset() + ((4 * stages + 15) & ~15u); }
     __host__ __device__ uint32_t total() const { return ubuf_offset() + extra_bytes; }
 };
+
+// Waits until ring slot s holds ring index ii. A parity test alone cannot tell
+// round r of a slot from round r - 2 (a consumer that reaches a slot while its
+// previous round is still loading would pass at once), so the producer
+// writes the slot's tag = ring index before the arrive that completes the
+// phase, and the consumer accepts the phase only with the matching tag.
+// Bounded like mbar_wait_abortable.
+__device__ __forceinline__ bool ring_wait(uint64_t* full, const volatile uint32_t* tag, uint32_t s, uint32_t ii,
+                                          uint32_t S, volatile int* abort) {
+    const uint32_t par = (ii / S) & 1;
+    if (mbar_try_wait(&full[s], par) && tag[s] == ii) return true;
+    const unsigned long long t0 = globaltimer_ns();
+    for (;;) {
+        for (int k = 0; k < 64; k++)
+            if (mbar_try_wait(&full[s], par) && tag[s] == ii) return true;
+        if (*abort) return false;
+        if (globaltimer_ns() - t0 > kWaitLimitNs) {
+            *abort = 1;
+            return false;
+        }
+    }
+}
 
 // ---- warp per element (n > 16) --------------------------------------------
 // Ke of one element: column-major, entry (r, c) at c*n + r. Lane l owns rows
@@ -434,6 +473,7 @@ __global__ void __launch_bounds__(17 * 32, 1) afm_wpg_kernel(SegArgs a, RingLayo
     uint64_t* full = reinterpret_cast<uint64_t*>(smem + L.bars_offset());
     uint64_t* empty = full + L.stages;
     volatile int* abort = reinterpret_cast<volatile int*>(empty + L.stages);
+    volatile uint32_t* tag = reinterpret_cast<volatile uint32_t*>(smem + L.tags_offset());
     const uint32_t ub = wpg_ubuf_bytes(n, sizeof(UT));
     unsigned char* ubase = smem + L.ubuf_offset();                 // [ng][2] u buffers
     Acc* pbase = reinterpret_cast<Acc*>(ubase + (size_t)G.ng * 2 * ub);  // [ng][2][gc-1][n] partials
@@ -448,6 +488,7 @@ __global__ void __launch_bounds__(17 * 32, 1) afm_wpg_kernel(SegArgs a, RingLayo
         for (uint32_t s = 0; s < S; s++) {
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], G.g);
+            tag[s] = 0xffffffffu;
         }
         *abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -461,6 +502,7 @@ __global__ void __launch_bounds__(17 * 32, 1) afm_wpg_kernel(SegArgs a, RingLayo
             for (uint32_t i = 0; i < cnt; i++) {
                 const uint32_t s = i % S;
                 if (i >= S && !mbar_wait_abortable(&empty[s], ((i / S) - 1) & 1, abort)) break;
+                tag[s] = i;
                 mbar_arrive_expect_tx(&full[s], a.copy_bytes);
                 bulk_load(smem + (size_t)s * L.slot_bytes, a.ke + (size_t)(begin + i) * a.unit_bytes, a.copy_bytes,
                           &full[s], pol);
@@ -522,7 +564,7 @@ __global__ void __launch_bounds__(17 * 32, 1) afm_wpg_kernel(SegArgs a, RingLayo
         }
         const uint32_t s = i % S;
         Acc acc = A::zero();
-        if (mbar_wait_abortable(&full[s], (i / S) & 1, abort)) {
+        if (ring_wait(full, tag, s, i, S, abort)) {
             const unsigned char* ks = smem + (size_t)s * L.slot_bytes;
             const UT* uu = ubuf(par);
             if (rvalid) {

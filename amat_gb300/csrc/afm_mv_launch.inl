@@ -46,9 +46,11 @@ void* pick_kernel(int regime, uint32_t n, bool dup) {
 
 }  // namespace
 
+// Ring stages that fit beside `extra` bytes: per stage the slot, two
+// mbarriers and a tag; 32 bytes for the flag word and the tags' padding.
 static uint32_t stages_for(uint32_t slot_bytes, uint32_t extra) {
-    if (extra + 16 >= kSmemBudget) return 0;
-    uint32_t st = (kSmemBudget - extra - 16) / (slot_bytes + 16);
+    if (extra + 32 >= kSmemBudget) return 0;
+    uint32_t st = (kSmemBudget - extra - 32) / (slot_bytes + 20);
     return st > 16 ? 16 : st;
 }
 
@@ -96,7 +98,11 @@ cudaError_t LAUNCH_FN(const Segment& s, const SegArgs& a, int sm_count, bool dup
     if (L.stages < 2) return cudaErrorInvalidConfiguration;
     void* fn = pick_kernel(s.regime, s.n, dup);
     const uint32_t smem = L.total();
-    uint32_t grid = s.units < (uint32_t)sm_count ? s.units : (uint32_t)sm_count;
+    // at least 4 elements (2 thread-per-element units) per CTA: a small segment occupies few SMs
+    // and leaves the rest to concurrent work (other operators' streams)
+    const uint32_t per_cta = s.regime == REG_TPE ? 2u : 4u;
+    const uint32_t want = (s.units + per_cta - 1) / per_cta;
+    uint32_t grid = want < (uint32_t)sm_count ? want : (uint32_t)sm_count;
     dim3 block((L.warps + 1) * 32);
     uint32_t n_rt = s.n;
     SegArgs args = a;
@@ -119,55 +125,53 @@ cudaError_t LAUNCH_FN(const Segment& s, const SegArgs& a, int sm_count, bool dup
     return cudaLaunchKernelExC(&cfg, fn, params);
 }
 
-// ---- batched (multi right-hand side) product, warp-group regime ----------
+// ---- batched (multi right-hand side) product, warp per element -------------
 
 namespace {
-template <int NT, int TR>
+template <int NT, int RT, int CT>
 void* batch_kernel_ptr() {
-    return (void*)afm_batched_kernel<NT, ARITH, TR>;
+    return (void*)afm_batched_kernel<NT, ARITH, RT, CT>;
 }
-void* pick_batch_kernel(uint32_t n, int tr) {
-    if (tr == 8) {
-        switch (n) {
-            case 24: return batch_kernel_ptr<24, 8>();
-            case 60: return batch_kernel_ptr<60, 8>();
-            default: return batch_kernel_ptr<0, 8>();
-        }
-    }
-    switch (n) {
-        case 24: return batch_kernel_ptr<24, 4>();
-        case 60: return batch_kernel_ptr<60, 4>();
-        default: return batch_kernel_ptr<0, 4>();
+template <int RT, int CT>
+void* batch_kernel_n(uint32_t n) {
+    return n == 24 ? batch_kernel_ptr<24, RT, CT>() : batch_kernel_ptr<0, RT, CT>();
+}
+// lane tile rows x columns: (2, 8), (4, 4), (4, 8), (6, 8)
+void* pick_batch_kernel(uint32_t n, int rt, int ct) {
+    if (ct == 4) return rt == 4 ? batch_kernel_n<4, 4>(n) : nullptr;
+    if (ct != 8) return nullptr;
+    switch (rt) {
+        case 2: return batch_kernel_n<2, 8>(n);
+        case 4: return batch_kernel_n<4, 8>(n);
+        case 6: return batch_kernel_n<6, 8>(n);
+        default: return nullptr;
     }
 }
 }  // namespace
 
-// tr: columns per thread tile (4 or 8); ng: element groups per CTA (<= 4).
-cudaError_t BATCH_FN(const Segment& s, const BatchArgs& a, int sm_count, int tr, int ng, bool pdl,
+// ct: columns per lane tile (4 or 8); rt: rows per lane tile (2, 4 or 6).
+cudaError_t BATCH_FN(const Segment& s, const BatchArgs& a, int sm_count, int ct, int rt, bool pdl,
                      cudaStream_t stream) {
     if (s.units == 0) return cudaSuccess;
-    if (s.regime != REG_WPE || (tr != 4 && tr != 8) || a.nrhs % tr != 0 || ng < 1 || ng > 4)
-        return cudaErrorInvalidValue;
-    BatchGeom G;
-    G.rtiles = (s.n + 3) / 4;
-    G.ctiles = a.nrhs / tr;
-    const uint32_t tiles = G.rtiles * G.ctiles;
-    G.gthreads = std::min<uint32_t>(128, (tiles + 31) / 32 * 32);
-    const uint32_t ub = batch_ubuf_bytes(s.n, a.nrhs, (uint32_t)sizeof(typename ARITH::UT));
+    void* fn = pick_batch_kernel(s.n, rt, ct);
+    if (s.regime != REG_WPE || !fn || a.nrhs % ct != 0) return cudaErrorInvalidValue;
     RingLayout L;
     L.slot_bytes = (a.copy_bytes + kSlotAlign - 1) / kSlotAlign * kSlotAlign;
-    L.ubuf_bytes = ub;
-    for (G.ng = (uint32_t)ng; G.ng >= 1; G.ng--) {
-        L.extra_bytes = G.ng * ub;
+    L.ubuf_bytes = batch_buf_bytes(s.n, a.nrhs, (uint32_t)sizeof(typename ARITH::VT));
+    // Consumers take elements round robin and wait on full[i % S] by parity,
+    // which tells only two consecutive phases apart: a warp must never reach a
+    // slot whose previous round is still loading, so the ring keeps at least
+    // two stages more than there are consumer warps (as ring_layout does).
+    for (L.warps = 8; L.warps >= 1; L.warps--) {
+        L.extra_bytes = L.warps * 2 * L.ubuf_bytes;
         L.stages = stages_for(L.slot_bytes, L.extra_bytes);
-        if (L.stages >= 2) break;
+        if (L.stages >= L.warps + 2) break;
     }
-    if (G.ng == 0 || L.stages < 2) return cudaErrorInvalidConfiguration;
-    L.warps = G.ng * G.gthreads / 32;
-    void* fn = pick_batch_kernel(s.n, tr);
+    if (L.warps == 0 || L.stages < L.warps + 2) return cudaErrorInvalidConfiguration;
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(s.units < (uint32_t)sm_count ? s.units : (uint32_t)sm_count);
-    cfg.blockDim = dim3(G.ng * G.gthreads + 32);
+    const uint32_t want = (s.units + 3) / 4;  // at least 4 elements per CTA
+    cfg.gridDim = dim3(want < (uint32_t)sm_count ? want : (uint32_t)sm_count);
+    cfg.blockDim = dim3((L.warps + 1) * 32);
     cfg.dynamicSmemBytes = L.total();
     cfg.stream = stream;
     cudaLaunchAttribute attr[1];
@@ -176,8 +180,9 @@ cudaError_t BATCH_FN(const Segment& s, const BatchArgs& a, int sm_count, int tr,
     cfg.attrs = attr;
     cfg.numAttrs = pdl ? 1 : 0;
     BatchArgs args = a;
+    args.smem_total = L.total();
     uint32_t n_rt = s.n;
-    void* params[] = {&args, &L, &G, &n_rt};
+    void* params[] = {&args, &L, &n_rt};
     return cudaLaunchKernelExC(&cfg, fn, params);
 }
 
@@ -199,10 +204,10 @@ PatchLayout patch_layout(const PatchPlanGeom& pg, uint32_t copy_bytes) {
     L.idx_bytes = patch_r16(pg.max_idx);
     L.us_bytes = patch_r16(pg.max_ndof * (uint32_t)sizeof(typename ARITH::UT));
     L.ve_bytes = patch_r16(pg.n * pg.max_slots * (uint32_t)sizeof(typename ARITH::VT));
-    const uint32_t fixed = 64 + 2 * L.group_bytes();
+    const uint32_t fixed = 16 * kPatchGroups + 16 + 16 + kPatchGroups * L.group_bytes();
     L.stages = 0;
     if (fixed < kSmemBudget) {
-        const uint32_t st = (kSmemBudget - fixed) / (L.slot_bytes + 16);
+        const uint32_t st = (kSmemBudget - fixed) / (L.slot_bytes + 20);
         L.stages = st > 16 ? 16 : st;
     }
     return L;
@@ -252,10 +257,11 @@ cudaError_t CONFIG_FN() {
                                              (int)(kSmemBudget + 1024));
         if (e != cudaSuccess) return e;
     }
-    for (int tr : {4, 8})
-        for (uint32_t nn : {24u, 60u, 7u}) {
-            cudaError_t e = cudaFuncSetAttribute(pick_batch_kernel(nn, tr), cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 (int)(kSmemBudget + 1024));
+    const int tiles[4][2] = {{2, 8}, {4, 4}, {4, 8}, {6, 8}};
+    for (const auto& t : tiles)
+        for (uint32_t nn : {24u, 7u}) {
+            cudaError_t e = cudaFuncSetAttribute(pick_batch_kernel(nn, t[0], t[1]),
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kSmemBudget + 1024));
             if (e != cudaSuccess) return e;
         }
     return cudaSuccess;

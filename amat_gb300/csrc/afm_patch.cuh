@@ -1,8 +1,8 @@
 // Patch kernel for small elements (n <= kPatchMaxN): v += sum over the patches
 // of one patch colour of P_p^T (sum over the patch's elements of P_e^T Ke P_e) P_p u.
 //
-// A patch is a compact group of up to 256 elements (128 when n > 10), grown
-// breadth first over shared DoFs when the operator is finalised. Patches of one
+// A patch is a compact group of up to 128 elements, grown breadth first over
+// shared DoFs when the operator is finalised. Patches of one
 // colour share no DoF. Per patch an index block is stored:
 //   glob[ndof]           sorted global DoF ids (kBcFlag on constrained DoFs)
 //   lmap[units][n][32]   uint16 local DoF index of column c of element slot
@@ -12,8 +12,10 @@
 // and the patch's Ke as units of 32 element slots in the thread-per-element
 // layout (entry (r, c) of slot l at (r n + c) 32 + l; empty slots are zero).
 //
-// CTA = 2 consumer groups of 4 warps + 1 producer warp; group g takes the
-// CTA's patches g, g + 2, ... The producer's elected lane copies each
+// CTA = kPatchGroups consumer groups of kPatchGroupWarps warps + 1 producer
+// warp; group g takes the CTA's patches g, g + G, ... (G patches in flight
+// per SM, so one patch's gather and reduce latency hides behind the others'
+// products). The producer's elected lane copies each
 // patch's index block into the group's buffer (one bulk copy) and streams
 // its Ke units through the shared ring. A group: gathers u of the patch's
 // DoFs into shared memory once; each lane multiplies one element slot and
@@ -28,21 +30,24 @@
 
 namespace afm {
 
-// Shared-memory layout: ring slots, mbarriers (full[S], empty[S], idx_full[2],
-// idx_empty[2]) and the abort flag, then per group: index block, staged u,
-// element products.
+constexpr uint32_t kPatchGroups = 4;
+constexpr uint32_t kPatchGroupWarps = 2;
+constexpr uint32_t kPatchGroupThreads = kPatchGroupWarps * 32;
+constexpr uint32_t kPatchThreads = kPatchGroups * kPatchGroupThreads + 32;
+constexpr int kBatch = 8;  // global loads a thread keeps in flight in the gather and the update
+
+// Shared-memory layout: ring slots, mbarriers (full[S], empty[S], idx_full[G],
+// idx_empty[G]) and the abort flag, the slot tags (ring_wait), then per group:
+// index block, staged u, element products.
 struct PatchLayout {
     uint32_t slot_bytes, stages;
     uint32_t idx_bytes, us_bytes, ve_bytes;  // per group, 16-byte multiples
     __host__ __device__ uint32_t bars_offset() const { return slot_bytes * stages; }
-    __host__ __device__ uint32_t group_offset() const { return bars_offset() + 16u * stages + 64u; }
+    __host__ __device__ uint32_t tags_offset() const { return bars_offset() + 16u * stages + 16u * kPatchGroups + 16u; }
+    __host__ __device__ uint32_t group_offset() const { return tags_offset() + ((4u * stages + 15u) & ~15u); }
     __host__ __device__ uint32_t group_bytes() const { return idx_bytes + us_bytes + ve_bytes; }
-    __host__ __device__ uint32_t total() const { return group_offset() + 2u * group_bytes(); }
+    __host__ __device__ uint32_t total() const { return group_offset() + kPatchGroups * group_bytes(); }
 };
-
-constexpr uint32_t kPatchGroupWarps = 4;
-constexpr uint32_t kPatchGroupThreads = kPatchGroupWarps * 32;
-constexpr uint32_t kPatchThreads = 2 * kPatchGroupThreads + 32;
 
 template <int NT, typename A>
 __global__ void __launch_bounds__(kPatchThreads, 1) afm_patch_kernel(PatchArgs a, PatchLayout L, uint32_t n_rt) {
@@ -55,8 +60,9 @@ __global__ void __launch_bounds__(kPatchThreads, 1) afm_patch_kernel(PatchArgs a
     uint64_t* full = reinterpret_cast<uint64_t*>(smem + L.bars_offset());
     uint64_t* empty = full + L.stages;
     uint64_t* idx_full = empty + L.stages;
-    uint64_t* idx_empty = idx_full + 2;
-    volatile int* abort = reinterpret_cast<volatile int*>(idx_empty + 2);
+    uint64_t* idx_empty = idx_full + kPatchGroups;
+    volatile int* abort = reinterpret_cast<volatile int*>(idx_empty + kPatchGroups);
+    volatile uint32_t* tag = reinterpret_cast<volatile uint32_t*>(smem + L.tags_offset());
     const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const uint32_t S = L.stages;
 
@@ -69,8 +75,9 @@ __global__ void __launch_bounds__(kPatchThreads, 1) afm_patch_kernel(PatchArgs a
         for (uint32_t s = 0; s < S; s++) {
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
+            tag[s] = 0xffffffffu;
         }
-        for (int g = 0; g < 2; g++) {
+        for (uint32_t g = 0; g < kPatchGroups; g++) {
             mbar_init(&idx_full[g], 1);
             mbar_init(&idx_empty[g], 1);
         }
@@ -79,14 +86,14 @@ __global__ void __launch_bounds__(kPatchThreads, 1) afm_patch_kernel(PatchArgs a
     }
     __syncthreads();
 
-    if (warp == 2 * kPatchGroupWarps) {  // producer
+    if (warp == kPatchGroups * kPatchGroupWarps) {  // producer
         if (lane == 0) {
             const uint64_t pol = l2_evict_first_policy();
-            uint32_t issued = 0;          // Ke units
-            uint32_t idx_issued[2] = {0, 0};
+            uint32_t issued = 0;  // Ke units
+            uint32_t idx_issued[kPatchGroups] = {};
             bool stop = false;
             for (uint32_t k = 0; k < cnt && !stop; k++) {
-                const uint32_t g = k & 1, j = k >> 1;
+                const uint32_t g = k % kPatchGroups, j = k / kPatchGroups;
                 const PatchDesc d = desc[k];
                 if (j >= 1 && !mbar_wait_abortable(&idx_empty[g], (j - 1) & 1, abort)) break;
                 mbar_arrive_expect_tx(&idx_full[g], d.idx_bytes);
@@ -99,6 +106,7 @@ __global__ void __launch_bounds__(kPatchThreads, 1) afm_patch_kernel(PatchArgs a
                         stop = true;
                         break;
                     }
+                    tag[s] = issued;
                     mbar_arrive_expect_tx(&full[s], a.copy_bytes);
                     bulk_load(smem + (size_t)s * L.slot_bytes, a.ke + d.ke_off + (uint64_t)u * a.unit_bytes,
                               a.copy_bytes, &full[s], pol);
@@ -114,7 +122,7 @@ __global__ void __launch_bounds__(kPatchThreads, 1) afm_patch_kernel(PatchArgs a
                 for (uint32_t i = first; i < issued; i++)
                     while (!mbar_try_wait(&full[i % S], (i / S) & 1) && globaltimer_ns() - t0 < kWaitLimitNs) {
                     }
-                for (int g = 0; g < 2; g++)
+                for (uint32_t g = 0; g < kPatchGroups; g++)
                     if (idx_issued[g])
                         while (!mbar_try_wait(&idx_full[g], (idx_issued[g] - 1) & 1) &&
                                globaltimer_ns() - t0 < kWaitLimitNs) {
@@ -134,11 +142,12 @@ __global__ void __launch_bounds__(kPatchThreads, 1) afm_patch_kernel(PatchArgs a
     const uint64_t keep = l2_evict_last_policy();
 
     // ring index of this group's first unit: units of the patches before it
-    uint32_t base = (g == 1 && cnt > 0) ? desc[0].units : 0u;
+    uint32_t base = 0;
+    for (uint32_t k = 0; k < g && k < cnt; k++) base += desc[k].units;
     bool waited_prior = false;
-    for (uint32_t k = g; k < cnt; k += 2) {
+    for (uint32_t k = g; k < cnt; k += kPatchGroups) {
         const PatchDesc d = desc[k];
-        const uint32_t j = k >> 1;
+        const uint32_t j = k / kPatchGroups;
         const bool iok = mbar_wait_abortable(&idx_full[g], j & 1, abort);
         const uint32_t* glob = reinterpret_cast<const uint32_t*>(gbase);
         const uint16_t* lmap = reinterpret_cast<const uint16_t*>(gbase + patch_lmap_off(d.ndof));
@@ -146,20 +155,31 @@ __global__ void __launch_bounds__(kPatchThreads, 1) afm_patch_kernel(PatchArgs a
         const uint16_t* slot = reinterpret_cast<const uint16_t*>(gbase + patch_slot_off(d.ndof, d.units, n));
         const uint32_t cap = d.units * 32u;
 
-        // u of the patch's DoFs, once
+        // u of the patch's DoFs, once; kBatch independent loads in flight per
+        // thread before any of them is used (in-order issue would otherwise
+        // pay one memory latency per DoF)
         if (iok)
-            for (uint32_t i = t; i < d.ndof; i += kPatchGroupThreads) {
-                const uint32_t m = glob[i];
-                VT x = ld_nc_hint(u + (m & kDofMask), keep);
-                if (a.bc_mode && (m & kBcFlag)) x = VT(0);
-                us[i] = A::stage(x);
+            for (uint32_t i0 = t; i0 < d.ndof; i0 += kPatchGroupThreads * kBatch) {
+                uint32_t m[kBatch];
+                VT x[kBatch];
+#pragma unroll
+                for (int q = 0; q < kBatch; q++) {
+                    const uint32_t i = i0 + q * kPatchGroupThreads;
+                    m[q] = i < d.ndof ? glob[i] : 0u;
+                    x[q] = i < d.ndof ? ld_nc_hint(u + (m[q] & kDofMask), keep) : VT(0);
+                }
+#pragma unroll
+                for (int q = 0; q < kBatch; q++) {
+                    const uint32_t i = i0 + q * kPatchGroupThreads;
+                    if (i < d.ndof) us[i] = A::stage((a.bc_mode && (m[q] & kBcFlag)) ? VT(0) : x[q]);
+                }
             }
         named_barrier(bar_id, kPatchGroupThreads);
 
-        // element products: lane l of warp w takes slot (unit w + 4 i, lane l)
+        // element products: lane l of warp w takes slot (unit w + W i, lane l)
         for (uint32_t un = wg; un < d.units; un += kPatchGroupWarps) {
             const uint32_t ii = base + un, s = ii % S;
-            const bool ok = iok && mbar_wait_abortable(&full[s], (ii / S) & 1, abort);
+            const bool ok = iok && ring_wait(full, tag, s, ii, S, abort);
             if (ok) {
                 const unsigned char* ks = smem + (size_t)s * L.slot_bytes;
                 UT ul[NM];
@@ -189,16 +209,30 @@ __global__ void __launch_bounds__(kPatchThreads, 1) afm_patch_kernel(PatchArgs a
             waited_prior = true;
         }
         if (iok && !*abort)
-            for (uint32_t i = t; i < d.ndof; i += kPatchGroupThreads) {
-                VT sum = VT(0);
-                const uint32_t q1 = coff[i + 1];
-                for (uint32_t q = coff[i]; q < q1; q++) sum += ve[slot[q]];
-                VT* p = v + (glob[i] & kDofMask);
-                st_hint(p, ld_hint(p, keep) + sum, keep);
+            for (uint32_t i0 = t; i0 < d.ndof; i0 += kPatchGroupThreads * kBatch) {
+                uint32_t gi[kBatch];
+                VT old[kBatch];
+#pragma unroll
+                for (int q = 0; q < kBatch; q++) {
+                    const uint32_t i = i0 + q * kPatchGroupThreads;
+                    gi[q] = i < d.ndof ? (glob[i] & kDofMask) : 0u;
+                    old[q] = i < d.ndof ? ld_hint(v + gi[q], keep) : VT(0);
+                }
+#pragma unroll
+                for (int q = 0; q < kBatch; q++) {
+                    const uint32_t i = i0 + q * kPatchGroupThreads;
+                    if (i < d.ndof) {
+                        VT sum = VT(0);
+                        const uint32_t q1 = coff[i + 1];
+                        for (uint32_t c = coff[i]; c < q1; c++) sum += ve[slot[c]];
+                        st_hint(v + gi[q], old[q] + sum, keep);
+                    }
+                }
             }
         named_barrier(bar_id, kPatchGroupThreads);
         if (t == 0) mbar_arrive(&idx_empty[g]);
-        base += d.units + (k + 1 < cnt ? desc[k + 1].units : 0u);
+        // skip the other groups' patches up to this group's next one
+        for (uint32_t k2 = k; k2 < k + kPatchGroups && k2 < cnt; k2++) base += desc[k2].units;
     }
     if (!waited_prior) wait_prior_grid();
     if (t == 0 && *abort) atomicOr(a.err, kErrTimeout);

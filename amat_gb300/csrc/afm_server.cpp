@@ -23,8 +23,11 @@
 #include <string.h>
 
 #include <chrono>
+#include <condition_variable>
 #include <deque>
 #include <future>
+#include <mutex>
+#include <thread>
 #include <unordered_map>
 #include <vector>
 
@@ -44,7 +47,7 @@ struct Request {
     int state = RQ_QUEUED;
     std::future<int> fin;
     double* d_bx = nullptr;  // b then x on the device
-    double* h_x = nullptr;   // pinned copy of x
+    std::vector<double> x;   // result on the host
     cudaEvent_t copied = nullptr;
     afm::MixedSolve ms;
     afm_solve_stats stats{};
@@ -81,17 +84,43 @@ struct afm_server {
     std::deque<Request*> queue;
     std::vector<Request*> active;  // admitting, running or copying
     std::unordered_map<uint64_t, Request*> all;
+    // finished operators are destroyed on a background thread: releasing
+    // pinned host memory can wait for the whole device, which must not stall
+    // the polling thread
+    std::thread reaper;
+    std::mutex mu;
+    std::condition_variable cv;
+    std::deque<afm_operator*> graveyard;
+    bool stop = false;
 };
 
 namespace {
 
-void release_device(Request* r) {
-    if (r->d_bx) cudaFree(r->d_bx);
+void release_device(afm_server* s, Request* r) {
+    if (r->d_bx && r->op) cudaFreeAsync(r->d_bx, r->op->stream);
     r->d_bx = nullptr;
     if (r->copied) cudaEventDestroy(r->copied);
     r->copied = nullptr;
-    if (r->op) afm_destroy(r->op);
+    if (r->op) {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->graveyard.push_back(r->op);
+        s->cv.notify_one();
+    }
     r->op = nullptr;
+}
+
+void reap(afm_server* s) {
+    cudaSetDevice(s->device);
+    std::unique_lock<std::mutex> lk(s->mu);
+    for (;;) {
+        s->cv.wait(lk, [s] { return s->stop || !s->graveyard.empty(); });
+        if (s->graveyard.empty() && s->stop) return;
+        afm_operator* op = s->graveyard.front();
+        s->graveyard.pop_front();
+        lk.unlock();
+        afm_destroy(op);
+        lk.lock();
+    }
 }
 
 void finish(afm_server* s, Request* r, int status, const char* msg) {
@@ -99,13 +128,19 @@ void finish(afm_server* s, Request* r, int status, const char* msg) {
     if (msg) r->message = msg;
     r->state = RQ_DONE;
     r->t_done = now_s();
-    release_device(r);
+    release_device(s, r);
     s->in_use -= r->est_bytes;
 }
 
+// At most this many operators are finalised at once: each finalize runs
+// OpenMP loops over all host cores, and more in parallel only contend.
+constexpr int kMaxFinalizing = 2;
+
 // admission: FIFO while the budget, free device memory and slots allow
 void admit(afm_server* s) {
-    while (!s->queue.empty() && s->active.size() < s->max_active) {
+    int finalizing = 0;
+    for (const Request* r : s->active) finalizing += (r->state == RQ_ADMITTING);
+    while (!s->queue.empty() && s->active.size() < s->max_active && finalizing < kMaxFinalizing) {
         Request* r = s->queue.front();
         size_t free_b = 0, total_b = 0;
         if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) break;
@@ -122,6 +157,7 @@ void admit(afm_server* s) {
             return afm_finalize(op);
         });
         s->active.push_back(r);
+        finalizing++;
     }
 }
 
@@ -129,8 +165,7 @@ int start(afm_server* s, Request* r) {
     (void)s;
     afm_operator* op = r->op;
     const size_t n = op->n_dofs;
-    if (cudaMalloc((void**)&r->d_bx, 2 * n * sizeof(double)) != cudaSuccess) return AFM_ERR_OOM;
-    if (cudaMallocHost((void**)&r->h_x, std::max<size_t>(n, 1) * sizeof(double)) != cudaSuccess) return AFM_ERR_OOM;
+    if (cudaMallocAsync((void**)&r->d_bx, 2 * n * sizeof(double), op->stream) != cudaSuccess) return AFM_ERR_OOM;
     if (cudaEventCreateWithFlags(&r->copied, cudaEventDisableTiming) != cudaSuccess) return AFM_ERR_CUDA;
     if (cudaMemcpyAsync(r->d_bx, r->b.data(), n * sizeof(double), cudaMemcpyHostToDevice, op->stream) != cudaSuccess ||
         cudaMemsetAsync(r->d_bx + n, 0, n * sizeof(double), op->stream) != cudaSuccess)
@@ -167,6 +202,7 @@ int afm_server_create(afm_server** out, int device, uint64_t hbm_budget_bytes, u
     s->budget = hbm_budget_bytes ? hbm_budget_bytes : (uint64_t)(free_b * 0.85);
     s->reserve = std::min<uint64_t>(total_b / 50, 2ull << 30);
     s->max_active = max_active ? max_active : 32;
+    s->reaper = std::thread(reap, s);
     *out = s;
     return afm::set_error(AFM_SUCCESS, "");
 }
@@ -205,7 +241,6 @@ int afm_server_poll(afm_server* s, uint32_t* n_queued, uint32_t* n_active) {
                 finish(s, r, st, "finalize failed");
                 continue;
             }
-            r->op->precision_req = r->op->precision;
             const int s2 = start(s, r);
             if (s2 != AFM_SUCCESS) {
                 finish(s, r, s2, afm_last_error());
@@ -223,8 +258,10 @@ int afm_server_poll(afm_server* s, uint32_t* n_queued, uint32_t* n_active) {
                 continue;
             }
             if (r->ms.phase == afm::MS_DONE) {
+                // the solve's work has finished: a pageable copy returns quickly
                 const size_t n = r->op->n_dofs;
-                cudaMemcpyAsync(r->h_x, r->d_bx + n, n * sizeof(double), cudaMemcpyDeviceToHost, r->op->stream);
+                r->x.resize(n);
+                cudaMemcpyAsync(r->x.data(), r->d_bx + n, n * sizeof(double), cudaMemcpyDeviceToHost, r->op->stream);
                 cudaEventRecord(r->copied, r->op->stream);
                 r->state = RQ_COPYING;
             }
@@ -243,15 +280,17 @@ int afm_server_poll(afm_server* s, uint32_t* n_queued, uint32_t* n_active) {
     return afm::set_error(AFM_SUCCESS, "");
 }
 
-int afm_server_take(afm_server* s, uint64_t id, double* x, afm_solve_stats* stats, double* times) {
-    if (!s) return afm::set_error(AFM_ERR_INVALID_ARG, "null server");
+int afm_server_take(afm_server* s, uint64_t id, int* finished, double* x, afm_solve_stats* stats, double* times) {
+    if (!s || !finished) return afm::set_error(AFM_ERR_INVALID_ARG, "null argument");
+    *finished = 0;
     auto it = s->all.find(id);
     if (it == s->all.end()) return afm::set_error(AFM_ERR_INVALID_ARG, "unknown request %llu", (unsigned long long)id);
     Request* r = it->second;
-    if (r->state != RQ_DONE) return afm::set_error(AFM_ERR_STATE, "request %llu not finished", (unsigned long long)id);
+    if (r->state != RQ_DONE) return afm::set_error(AFM_SUCCESS, "");
+    *finished = 1;
     const int status = r->status;
     const std::string msg = r->message;
-    if (x && r->h_x) memcpy(x, r->h_x, r->b.size() * sizeof(double));
+    if (x && r->x.size() == r->b.size()) memcpy(x, r->x.data(), r->x.size() * sizeof(double));
     if (stats) *stats = r->stats;
     if (times) {
         times[0] = r->t_submit;
@@ -259,7 +298,6 @@ int afm_server_take(afm_server* s, uint64_t id, double* x, afm_solve_stats* stat
         times[2] = r->t_start;
         times[3] = r->t_done;
     }
-    if (r->h_x) cudaFreeHost(r->h_x);
     s->all.erase(it);
     delete r;
     if (status != AFM_SUCCESS) return afm::set_error(status, "request failed: %s", msg.c_str());
@@ -275,10 +313,15 @@ int afm_server_destroy(afm_server* s) {
     for (auto& kv : s->all) {
         Request* r = kv.second;
         if (r->ms.ev) afm::mixed_end(r->ms, nullptr);
-        release_device(r);
-        if (r->h_x) cudaFreeHost(r->h_x);
+        release_device(s, r);
         delete r;
     }
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stop = true;
+        s->cv.notify_one();
+    }
+    s->reaper.join();
     delete s;
     return AFM_SUCCESS;
 }

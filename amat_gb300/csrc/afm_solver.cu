@@ -4,10 +4,11 @@
 // or T = float (the inner CG of the mixed-precision solve); every dot product
 // and step scalar is accumulated and held in FP64.
 //
-// Reductions are deterministic: a fixed grid of kRedBlocks x kRedThreads
+// Reductions are deterministic: a grid of nb = red_blocks(n) x kRedThreads
 // threads sums fixed strided slices in index order, each block reduces in a
-// fixed tree, and one block reduces the kRedBlocks partials in a fixed tree.
-// The result depends only on n, never on the device or on timing.
+// fixed tree, and one block reduces the nb partials in a fixed tree. The
+// result depends only on n, never on the device or on timing. (nb grows with
+// n up to kRedBlocks, so a small solve occupies few SMs.)
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -30,13 +31,13 @@ __device__ __forceinline__ double block_sum(double x, double* sh) {
     return r;
 }
 
-__device__ __forceinline__ double final_sum(const double* part, double* sh) {
+__device__ __forceinline__ double final_sum(const double* part, double* sh, uint32_t nb) {
     double s = 0.0;
-    for (int i = threadIdx.x; i < kRedBlocks; i += kRedThreads) s += part[i];
+    for (uint32_t i = threadIdx.x; i < nb; i += kRedThreads) s += part[i];
     return block_sum(s, sh);
 }
 
-constexpr size_t kStride = (size_t)kRedBlocks * kRedThreads;
+#define kStride ((size_t)gridDim.x * kRedThreads)
 
 template <typename T>
 __global__ void __launch_bounds__(kRedThreads) k_set_constrained(T* v, const T* u, const uint32_t* idx, uint32_t n) {
@@ -94,13 +95,13 @@ __global__ void __launch_bounds__(kRedThreads) k_cg_init(const T* __restrict__ b
     }
 }
 
-__global__ void __launch_bounds__(kRedThreads) k_cg_init_final(double* sc, const double* part) {
+__global__ void __launch_bounds__(kRedThreads) k_cg_init_final(double* sc, const double* part, uint32_t nb) {
     __shared__ double sh[kRedThreads];
-    const double rz = final_sum(part, sh);
-    const double rr = final_sum(part + kRedBlocks, sh);
-    const double zz = final_sum(part + 2 * kRedBlocks, sh);
-    const double bb = final_sum(part + 3 * kRedBlocks, sh);
-    const double db = final_sum(part + 4 * kRedBlocks, sh);
+    const double rz = final_sum(part, sh, nb);
+    const double rr = final_sum(part + kRedBlocks, sh, nb);
+    const double zz = final_sum(part + 2 * kRedBlocks, sh, nb);
+    const double bb = final_sum(part + 3 * kRedBlocks, sh, nb);
+    const double db = final_sum(part + 4 * kRedBlocks, sh, nb);
     if (threadIdx.x == 0) {
         sc[S_RZ] = rz;
         sc[S_RR] = rr;
@@ -139,12 +140,12 @@ __global__ void __launch_bounds__(kRedThreads) k_cg_reliable(const double* __res
 }
 
 // pass 2 (one block): beta = r.z / r_k.z_k, gamma = r.p / r.z; S_DONE, S_ITER cleared
-__global__ void __launch_bounds__(kRedThreads) k_cg_reliable_final(double* sc, const double* part) {
+__global__ void __launch_bounds__(kRedThreads) k_cg_reliable_final(double* sc, const double* part, uint32_t nb) {
     __shared__ double sh[kRedThreads];
-    const double rz = final_sum(part, sh);
-    const double rr = final_sum(part + kRedBlocks, sh);
-    const double zz = final_sum(part + 2 * kRedBlocks, sh);
-    const double rp = final_sum(part + 3 * kRedBlocks, sh);
+    const double rz = final_sum(part, sh, nb);
+    const double rr = final_sum(part + kRedBlocks, sh, nb);
+    const double zz = final_sum(part + 2 * kRedBlocks, sh, nb);
+    const double rp = final_sum(part + 3 * kRedBlocks, sh, nb);
     if (threadIdx.x == 0) {
         const double old = sc[S_RZOLD];
         const bool bad = (rz < 0.0 || rz != rz);
@@ -170,9 +171,9 @@ __global__ void __launch_bounds__(kRedThreads) k_cg_reliable_p(float* __restrict
 }
 
 // alpha = rz / (p.q); flag on p.q <= 0 or NaN
-__global__ void __launch_bounds__(kRedThreads) k_cg_alpha(double* sc, const double* part) {
+__global__ void __launch_bounds__(kRedThreads) k_cg_alpha(double* sc, const double* part, uint32_t nb) {
     __shared__ double sh[kRedThreads];
-    const double pq = final_sum(part, sh);
+    const double pq = final_sum(part, sh, nb);
     if (threadIdx.x == 0) {
         if (sc[S_DONE] != 0.0) {  // finished earlier: this iteration changes nothing
             sc[S_ALPHA] = 0.0;
@@ -190,9 +191,9 @@ __global__ void __launch_bounds__(kRedThreads) k_cg_alpha(double* sc, const doub
 }
 
 // sc[S_PQ] = sum of the partials (a plain reduction, no CG bookkeeping)
-__global__ void __launch_bounds__(kRedThreads) k_sum(double* sc, const double* part) {
+__global__ void __launch_bounds__(kRedThreads) k_sum(double* sc, const double* part, uint32_t nb) {
     __shared__ double sh[kRedThreads];
-    const double s = final_sum(part, sh);
+    const double s = final_sum(part, sh, nb);
     if (threadIdx.x == 0) sc[S_PQ] = s;
 }
 
@@ -226,11 +227,11 @@ __global__ void __launch_bounds__(kRedThreads) k_cg_update(T* __restrict__ x, T*
 }
 
 // beta = rz_new / rz
-__global__ void __launch_bounds__(kRedThreads) k_cg_beta(double* sc, const double* part) {
+__global__ void __launch_bounds__(kRedThreads) k_cg_beta(double* sc, const double* part, uint32_t nb) {
     __shared__ double sh[kRedThreads];
-    const double rz = final_sum(part, sh);
-    const double rr = final_sum(part + kRedBlocks, sh);
-    const double zz = final_sum(part + 2 * kRedBlocks, sh);
+    const double rz = final_sum(part, sh, nb);
+    const double rr = final_sum(part + kRedBlocks, sh, nb);
+    const double zz = final_sum(part + 2 * kRedBlocks, sh, nb);
     if (threadIdx.x == 0) {
         if (sc[S_DONE] != 0.0) {
             sc[S_BETA] = 0.0;
@@ -313,30 +314,33 @@ cudaError_t launch_set_constrained(T* v, const T* u, const uint32_t* idx, uint32
 
 template <typename T>
 cudaError_t launch_dots(const T* a, const T* b, size_t n, double* part, cudaStream_t st) {
-    k_dots<T><<<kRedBlocks, kRedThreads, 0, st>>>(a, b, n, part);
+    k_dots<T><<<red_blocks(n), kRedThreads, 0, st>>>(a, b, n, part);
     return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t launch_cg_init(const T* b, const T* q, const T* dinv, T* r, T* z, T* p, size_t n, double* sc,
                            double* part, cudaStream_t st) {
-    k_cg_init<T><<<kRedBlocks, kRedThreads, 0, st>>>(b, q, dinv, r, z, p, n, part);
-    k_cg_init_final<<<1, kRedThreads, 0, st>>>(sc, part);
+    const uint32_t nb = red_blocks(n);
+    k_cg_init<T><<<nb, kRedThreads, 0, st>>>(b, q, dinv, r, z, p, n, part);
+    k_cg_init_final<<<1, kRedThreads, 0, st>>>(sc, part, nb);
     return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t launch_cg_alpha(const T* p, const T* q, size_t n, double* sc, double* part, cudaStream_t st) {
-    k_dots<T><<<kRedBlocks, kRedThreads, 0, st>>>(p, q, n, part);
-    k_cg_alpha<<<1, kRedThreads, 0, st>>>(sc, part);
+    const uint32_t nb = red_blocks(n);
+    k_dots<T><<<nb, kRedThreads, 0, st>>>(p, q, n, part);
+    k_cg_alpha<<<1, kRedThreads, 0, st>>>(sc, part, nb);
     return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t launch_cg_update(T* x, T* r, T* z, T* p, const T* q, const T* dinv, size_t n, double* sc, double* part,
                              cudaStream_t st) {
-    k_cg_update<T><<<kRedBlocks, kRedThreads, 0, st>>>(x, r, z, p, q, dinv, n, sc, part);
-    k_cg_beta<<<1, kRedThreads, 0, st>>>(sc, part);
+    const uint32_t nb = red_blocks(n);
+    k_cg_update<T><<<nb, kRedThreads, 0, st>>>(x, r, z, p, q, dinv, n, sc, part);
+    k_cg_beta<<<1, kRedThreads, 0, st>>>(sc, part, nb);
     k_cg_p<T><<<grid_for(n), kRedThreads, 0, st>>>(p, z, n, sc);
     return cudaGetLastError();
 }
@@ -349,15 +353,17 @@ cudaError_t launch_invert(T* dinv, const double* d, size_t n, cudaStream_t st) {
 
 template <typename T>
 cudaError_t launch_norm2(const T* a, size_t n, double* sc, double* part, cudaStream_t st) {
-    k_dots<T><<<kRedBlocks, kRedThreads, 0, st>>>(a, a, n, part);
-    k_sum<<<1, kRedThreads, 0, st>>>(sc, part);
+    const uint32_t nb = red_blocks(n);
+    k_dots<T><<<nb, kRedThreads, 0, st>>>(a, a, n, part);
+    k_sum<<<1, kRedThreads, 0, st>>>(sc, part, nb);
     return cudaGetLastError();
 }
 
 cudaError_t launch_cg_reliable(const double* r64, float* r, float* z, float* p, const float* dinv, size_t n,
                                double* sc, double* part, cudaStream_t st) {
-    k_cg_reliable<<<kRedBlocks, kRedThreads, 0, st>>>(r64, r, z, p, dinv, n, part);
-    k_cg_reliable_final<<<1, kRedThreads, 0, st>>>(sc, part);
+    const uint32_t nb = red_blocks(n);
+    k_cg_reliable<<<nb, kRedThreads, 0, st>>>(r64, r, z, p, dinv, n, part);
+    k_cg_reliable_final<<<1, kRedThreads, 0, st>>>(sc, part, nb);
     k_cg_reliable_p<<<grid_for(n), kRedThreads, 0, st>>>(p, z, n, sc);
     return cudaGetLastError();
 }

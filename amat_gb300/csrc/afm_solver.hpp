@@ -10,6 +10,13 @@ namespace afm {
 constexpr int kRedBlocks = 512;
 constexpr int kRedThreads = 256;
 
+// Blocks of a reduction over n entries: about 2048 entries per block, at
+// least 1 and at most kRedBlocks (a function of n only: deterministic sums).
+inline uint32_t red_blocks(size_t n) {
+    const size_t b = (n + 2047) / 2048;
+    return (uint32_t)(b < 1 ? 1 : (b > (size_t)kRedBlocks ? (size_t)kRedBlocks : b));
+}
+
 // Scalar slots of the solver state (device array of kScalarSlots doubles,
 // followed by kPartialSlots reduction partials).
 // S_TOL, S_MAXIT, S_NORM are set by the host before the iterations; the

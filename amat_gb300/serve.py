@@ -1,0 +1,64 @@
+"""Serving loop for many CG solves on different operators (afm_server_* in
+include/afm.h): FIFO admission by HBM budget, device-resident state, every
+admitted request advanced by non-blocking polls on its own stream."""
+import ctypes as C
+
+import numpy as np
+
+from ._native import AfmSolveStats, check, libafm
+
+
+class Server:
+    def __init__(self, device=0, hbm_budget=0, max_active=0):
+        self._lib = libafm()
+        h = C.c_void_p()
+        check(self._lib.afm_server_create(C.byref(h), int(device), int(hbm_budget), int(max_active)),
+              "afm_server_create")
+        self._h = h
+        self._n = {}
+
+    def submit(self, A, b, rtol=1e-8, inner_rtol=0.1):
+        """Queues a solve of A x = b (A: aMatFree with maps and element matrices set; the server takes it
+        over and A can no longer be used). Returns the request id."""
+        bb = np.ascontiguousarray(b, dtype=np.float64)
+        if len(bb) != A.n_dofs:
+            raise ValueError("b has %d entries, the operator %d DoFs" % (len(bb), A.n_dofs))
+        rid = C.c_uint64()
+        check(self._lib.afm_server_submit(self._h, A._h, C.c_void_p(bb.ctypes.data), float(rtol), float(inner_rtol),
+                                          C.byref(rid)), "afm_server_submit")
+        A._h = None  # owned by the server now
+        self._n[rid.value] = len(bb)
+        return rid.value
+
+    def poll(self):
+        """Admits and advances without blocking; returns (queued, admitted)."""
+        q, a = C.c_uint32(), C.c_uint32()
+        check(self._lib.afm_server_poll(self._h, C.byref(q), C.byref(a)), "afm_server_poll")
+        return q.value, a.value
+
+    def take(self, rid):
+        """(x, stats, times) of a finished request (times: submit, admit, start, done on the steady clock),
+        or None while it runs. Raises AfmError if the solve failed."""
+        x = np.empty(self._n[rid])
+        st = AfmSolveStats()
+        t = (C.c_double * 4)()
+        fin = C.c_int()
+        s = self._lib.afm_server_take(self._h, C.c_uint64(rid), C.byref(fin), C.c_void_p(x.ctypes.data),
+                                      C.byref(st), t)
+        if s == 0 and not fin.value:
+            return None
+        if fin.value:
+            del self._n[rid]
+        check(s, "afm_server_take")
+        return x, st, tuple(t)
+
+    def close(self):
+        if getattr(self, "_h", None) is not None:
+            self._lib.afm_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -39,6 +39,12 @@ WORKLOADS = {
                             desc="hex8 elasticity 48^3, 24x24 FP64 Ke"),
     "tet10_poisson_96": dict(kind=3, n=96, ngt=2, jitter=0.15, seed=2,
                              desc="tet10 Poisson 96^3 x 6 (5.3M tets), 10x10 Ke"),
+    "tet10_poisson_48": dict(kind=3, n=48, ngt=2, jitter=0.15, seed=2,
+                             desc="tet10 Poisson 48^3 x 6 (663k tets), 10x10 Ke"),
+    "tet10_poisson_64": dict(kind=3, n=64, ngt=2, jitter=0.15, seed=2,
+                             desc="tet10 Poisson 64^3 x 6 (1.57M tets), 10x10 Ke"),
+    "hex8_poisson_96": dict(kind=0, n=96, ngt=2, jitter=0.1, seed=0,
+                            desc="hex8 Poisson 96^3, 8x8 FP64 Ke, 2x2x2 Gauss, jitter 0.1h"),
 }
 PREC_NAMES = {"fp64": 0, "fp64_split": 1, "fp32": 2, "auto": 3}
 PREC_DTYPE = {0: "f64", 1: "f64 (Ke as hi+lo f32 pair, double-float products; <=1e-12 rel. vs FP64)", 2: "f32"}
@@ -412,7 +418,7 @@ def run_batched(args, w, rank, world, local_rank):
         dX.zero_()
         torch.cuda.synchronize()
         return A.solve_batched_device(dB.data_ptr(), dX.data_ptr(), R, rtol=rtol, atol=0.0, mixed=mixed,
-                                      inner_rtol=args.inner_rtol, maxit=200000)
+                                      inner_rtol=args.inner_rtol, max_inner=args.segment, maxit=200000)
 
     # warm-up: autotuner, graph capture
     for _ in range(max(1, args.warmup - 2)):
@@ -440,8 +446,9 @@ def run_batched(args, w, rank, world, local_rank):
            "ms_per_step": 1e3 * sum(tm) / args.steps, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32 inner (batched) / f64 residual", "data": "synthetic",
            "config": {"workload": w["desc"], "n_dofs": n, "n_elements": m.n_elem, "nrhs": R, "rtol": rtol,
-                      "inner_rtol": args.inner_rtol, "loads": "N(0,1) per DoF, seed %d" % w["seed"],
-                      "tuning (cols_per_thread, groups, ms)": tuning},
+                      "inner_rtol": args.inner_rtol, "segment": args.segment,
+                      "loads": "N(0,1) per DoF, seed %d" % w["seed"],
+                      "tuning (tile columns, tile rows, ms)": tuning},
            "batched_mixed": {"solves_per_s": smx, "inner_iterations": stm.iterations,
                              "refinements": stm.refinements, "worst_rel_residual": stm.rel_residual,
                              "max_rel_diff_vs_fp64_single": err},
@@ -458,6 +465,134 @@ def run_batched(args, w, rank, world, local_rank):
     return out if rank == 0 else None
 
 
+SERVE_KINDS = [(0, "hex8 Poisson"), (1, "hex8 elasticity"), (2, "hex20 elasticity")]
+
+
+def serve_requests(args, seed):
+    """Seeded request set: element type uniform over SERVE_KINDS, edge log-uniform in [8, edge_max],
+    coordinates jittered 0.1 h, loads N(0,1) per DoF (prescribed values on constrained DoFs)."""
+    from amat_gb300 import Maps, aMatFree
+    from amat_gb300 import problems as P
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for i in range(args.requests):
+        kind, name = SERVE_KINDS[int(rng.integers(len(SERVE_KINDS)))]
+        edge = int(round(np.exp(rng.uniform(np.log(8), np.log(args.edge_max)))))
+        if kind != 0:
+            edge += edge % 2  # the elastic bar's constraints sit on centre nodes (even edge)
+        m = P.Mesh(kind, edge, jitter=0.1, seed=seed * 1000 + i)
+        ke = m.element_matrices(ngt=3 if kind == P.HEX20_ELASTIC else 2)
+        dofs, vals = m.boundary_conditions()
+        maps = Maps()
+        maps.set_map(m.n_elem, m.dof_map(), m.ndpe, m.n_dofs)
+        maps.set_bdr_map(dofs, vals)
+        A = aMatFree(maps)
+        A.set_element_matrices(0, ke)
+        b = rng.normal(size=m.n_dofs)
+        b[dofs.astype(np.int64)] = vals
+        reqs.append(dict(A=A, b=b, kind=name, edge=edge, n_dofs=m.n_dofs, n_elem=m.n_elem))
+    return reqs
+
+
+def run_serve(args, w, rank, world, local_rank):
+    """Served CG solves: Poisson arrivals at each rate, admission by HBM, mixed-precision solves to rtol,
+    p50/p99 latency (arrival to result) beside solves/s; against the plain path (finalize + FP64 CG, one
+    request after another) on the same requests."""
+    import torch
+    from amat_gb300.serve import Server
+    dev = local_rank
+    torch.cuda.set_device(dev)
+    rates = [float(r) for r in args.rates.split(",")]
+    seed = 4
+    # plain FP64 GPU path, sequential
+    reqs = serve_requests(args, seed)
+    t0 = time.perf_counter()
+    its, t_fin, t_dev = 0, 0.0, 0.0
+    for r in reqs:
+        tf = time.perf_counter()
+        r["A"].finalize()
+        t_fin += time.perf_counter() - tf
+        x, st = r["A"].solve(r["b"], rtol=args.rtol, atol=0.0, maxit=1000000)
+        its += st.iterations
+        t_dev += st.seconds
+        r["A"].close()
+    t_plain = time.perf_counter() - t0
+    plain = {"solves_per_s": len(reqs) / t_plain, "total_s": t_plain, "finalize_s": t_fin, "solve_device_s": t_dev,
+             "fp64_iterations": its, "dtype": "f64 (split arena)"}
+    log("plain: %d solves in %.2f s" % (len(reqs), t_plain))
+    # the same requests one at a time through the server (mixed precision, no overlap)
+    reqs = serve_requests(args, seed)
+    srv = Server(dev)
+    t0 = time.perf_counter()
+    for r in reqs:
+        rid = srv.submit(r["A"], r["b"], rtol=args.rtol, inner_rtol=args.serve_inner)
+        while srv.take(rid) is None:
+            srv.poll()
+    t_alone = time.perf_counter() - t0
+    srv.close()
+    alone = {"solves_per_s": len(reqs) / t_alone, "total_s": t_alone}
+    log("served one at a time: %d solves in %.2f s" % (len(reqs), t_alone))
+    lines = []
+    clk = ClockSampler(dev)
+    with clk:
+        for rate in rates:
+            reqs = serve_requests(args, seed)
+            arr = np.cumsum(np.random.default_rng(seed + int(rate)).exponential(1.0 / rate, len(reqs)))
+            srv = Server(dev)
+            ids, lat, res, brk = {}, [], [], []
+            k = 0
+            t0 = time.monotonic()
+            last = t0
+            while len(lat) < len(reqs):
+                now = time.monotonic() - t0
+                while k < len(reqs) and arr[k] <= now:
+                    ids[srv.submit(reqs[k]["A"], reqs[k]["b"], rtol=args.rtol, inner_rtol=args.serve_inner)] = k
+                    k += 1
+                srv.poll()
+                for rid in list(ids):
+                    out = srv.take(rid)
+                    if out is None:
+                        continue
+                    j = ids.pop(rid)
+                    x, st, tt = out
+                    lat.append(tt[3] - (t0 + arr[j]))
+                    res.append(st.rel_residual)
+                    brk.append((tt[1] - tt[0], tt[2] - tt[1], tt[3] - tt[2], st.seconds))
+                    last = max(last, tt[3])
+                if k < len(reqs) and not ids:
+                    time.sleep(max(0.0, min(arr[k] - (time.monotonic() - t0), 0.001)))
+            srv.close()
+            span = last - (t0 + arr[0])
+            lat = np.array(lat)
+            brk = np.array(brk)
+            lines.append({"rate_req_s": rate, "solves_per_s": len(reqs) / span, "p50_ms": 1e3 * np.percentile(lat, 50),
+                          "p99_ms": 1e3 * np.percentile(lat, 99), "max_rel_residual": float(max(res)),
+                          "median_ms": {"queued": 1e3 * float(np.median(brk[:, 0])),
+                                        "finalize": 1e3 * float(np.median(brk[:, 1])),
+                                        "solve_wall": 1e3 * float(np.median(brk[:, 2])),
+                                        "solve_device": 1e3 * float(np.median(brk[:, 3]))}})
+            log("rate %g: %.2f solves/s, p50 %.1f ms, p99 %.1f ms" % (rate, lines[-1]["solves_per_s"],
+                                                                     lines[-1]["p50_ms"], lines[-1]["p99_ms"]))
+    best = max(lines, key=lambda d: d["solves_per_s"])
+    sizes = [r["n_dofs"] for r in reqs]
+    out = {"metric": "served CG solves/s at %g rel. residual (FP64-checked)" % args.rtol,
+           "value": best["solves_per_s"], "unit": "solves/s", "n_gpus": world, "steps": len(rates),
+           "warmup": 0, "ms_per_step": 1e3 / best["solves_per_s"], "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32 inner / f64 reliable updates", "data": "synthetic",
+           "config": {"workload": "serving: Poisson arrivals, %d requests, types %s, edge log-uniform 8..%d, "
+                                  "jitter 0.1h, loads N(0,1)" % (args.requests, [k[1] for k in SERVE_KINDS],
+                                                                  args.edge_max),
+                      "n_dofs_range": [int(min(sizes)), int(max(sizes))], "rtol": args.rtol,
+                      "inner_rtol": args.serve_inner, "admission": "FIFO by HBM budget (85% of free), 32 slots"},
+           "rates": lines, "p50_ms": best["p50_ms"], "p99_ms": best["p99_ms"], "plain_fp64_sequential": plain,
+           "served_one_at_a_time": alone,
+           "speedup_vs_plain": best["solves_per_s"] / plain["solves_per_s"]}
+    cs = clk.summary()
+    if cs:
+        out["clocks"] = cs
+    return out if rank == 0 else None
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -468,10 +603,15 @@ def main():
     ap.add_argument("--precision", default="auto", choices=sorted(PREC_NAMES))
     ap.add_argument("--also-native", type=int, default=1, help="also time native FP64 when the split path runs")
     ap.add_argument("--cpu-sample-elems", type=int, default=32768)
-    ap.add_argument("--mode", default="matvec", choices=["matvec", "solve", "batched"])
+    ap.add_argument("--mode", default="matvec", choices=["matvec", "solve", "batched", "serve"])
+    ap.add_argument("--rates", default="20,100,500", help="serve: arrival rates (requests/s)")
+    ap.add_argument("--requests", type=int, default=48, help="serve: requests per rate")
+    ap.add_argument("--edge-max", type=int, default=32, help="serve: largest mesh edge")
+    ap.add_argument("--serve-inner", type=float, default=0.1, help="serve: FP32 reduction between FP64 updates")
     ap.add_argument("--nrhs", type=int, default=64)
     ap.add_argument("--single-cols", type=int, default=2, help="columns solved one by one for the FP64 comparison")
     ap.add_argument("--batched-fp64", type=int, default=0, help="also time the FP64 batched block CG")
+    ap.add_argument("--segment", type=int, default=64, help="FP32 iterations between FP64 updates (batched)")
     ap.add_argument("--rtol", type=float, default=1e-8)
     ap.add_argument("--inner-rtol", type=float, default=1e-2)
     args = ap.parse_args()
@@ -487,7 +627,7 @@ def main():
             import torch
             torch.cuda.set_device(local_rank)
             torch.distributed.init_process_group("nccl")
-        run = {"matvec": run_ours, "solve": run_solve, "batched": run_batched}[args.mode]
+        run = {"matvec": run_ours, "solve": run_solve, "batched": run_batched, "serve": run_serve}[args.mode]
         out = run(args, w, rank, world, local_rank)
         if world > 1:
             import torch

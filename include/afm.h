@@ -127,7 +127,7 @@ int afm_set_matfree_type(afm_operator* op, int matfree_type);
 int afm_set_precision(afm_operator* op, int precision);
 /* Execution of small elements (no counterpart in the reference). enable = 1
  * (default): when every element has the same size n <= 12 and lists no DoF
- * twice, the matvec runs over patches, compact groups of up to 256 elements
+ * twice, the matvec runs over patches, compact groups of up to 128 elements
  * whose vector entries are staged in shared memory; patches of one colour
  * share no DoF. enable = 0: one launch per element colour, as for larger
  * elements. Both are deterministic and agree within rounding. Takes effect at
@@ -222,7 +222,7 @@ int afm_solve_cg_device(afm_operator* op, const double* d_b, double* d_x, double
  * in FP64 with the split element matrices (MatMult_mf semantics) and replaces
  * the FP32 residual, and the recursion continues with its search direction.
  * The solve stops at ||b - A x|| <= max(rtol ||b||, atol), after max_outer
- * updates, or after three updates in a row without a new smallest residual.
+ * updates, or after ten updates in a row without a new smallest residual.
  * Needs an FP64_SPLIT operator (AFM_PREC_AUTO with in-range Ke). stats:
  * iterations = FP32 iterations, refinements = FP64 residual updates. */
 int afm_solve_cg_mixed(afm_operator* op, const double* b, double* x, double rtol, double atol, int max_outer,
@@ -234,13 +234,14 @@ int afm_matmult_bc_device_f32(afm_operator* op, float* d_v, const float* d_u, vo
 
 /* ---- batched: many right-hand sides at once -------------------------------
  * Blocks are n_dofs x ld row-major device arrays (the nrhs values of one DoF
- * are contiguous); nrhs is a multiple of 4, at most 256; every element must
- * have more than 16 DoFs. Each element matrix is streamed once per call and
- * applied to all columns (for example hex8 elasticity with 64 right-hand
- * sides). The first call for a given (nrhs, ld,
- * arithmetic) runs the autotuner, which times the kernel's tile shapes on the
- * caller's data and keeps the fastest for the operator. No counterpart in the
- * reference, whose matvec takes one vector. */
+ * are contiguous), 16-byte aligned; nrhs is a multiple of 4, at most 256, ld
+ * >= nrhs a multiple of 4; every element must have more than 16 DoFs. Each
+ * element matrix is streamed once per call and applied to all columns (for
+ * example hex8 elasticity with 64 right-hand sides): a warp per element, a
+ * register tile of V_e per lane. The first call for a given (nrhs, ld,
+ * arithmetic) runs the autotuner, which times the lane tile shapes on the
+ * caller's data and keeps the fastest for the operator. No counterpart in
+ * the reference, whose matvec takes one vector. */
 int afm_matvec_batched_device(afm_operator* op, double* d_V, const double* d_U, uint32_t nrhs, uint32_t ld,
                               void* stream);
 int afm_matvec_batched_device_f32(afm_operator* op, float* d_V, const float* d_U, uint32_t nrhs, uint32_t ld,
@@ -250,22 +251,27 @@ int afm_matmult_bc_batched_device(afm_operator* op, double* d_V, const double* d
                                   void* stream);
 int afm_matmult_bc_batched_device_f32(afm_operator* op, float* d_V, const float* d_U, uint32_t nrhs, uint32_t ld,
                                       void* stream);
-/* The autotuner's choice for (nrhs, ld, f32): columns per thread tile,
- * element groups per CTA, and the time of one product in ms. */
+/* The autotuner's choice for (nrhs, ld, f32): columns and rows of the lane
+ * tile, and the time of one product in ms. */
 int afm_get_batch_tuning(afm_operator* op, uint32_t nrhs, uint32_t ld, int f32, int* cols_per_thread,
-                         int* groups_per_cta, float* ms);
-/* Pins the batched kernel configuration for (nrhs, ld, f32) instead of the
- * autotuner's choice: cols_per_thread 4 or 8, groups_per_cta 1..4. */
+                         int* rows_per_thread, float* ms);
+/* Pins the lane tile for (nrhs, ld, f32) instead of the autotuner's choice:
+ * (columns, rows) one of (8, 2), (8, 4), (8, 6), (4, 4). */
 int afm_set_batch_tuning(afm_operator* op, uint32_t nrhs, uint32_t ld, int f32, int cols_per_thread,
-                         int groups_per_cta);
+                         int rows_per_thread);
 /* Batched Jacobi-PCG: one CG per column (own scalars and stopping test
  * ||b_j - A x_j|| <= max(rtol ||b_j||, atol)), all advanced together, the
  * iterations captured in CUDA graphs. FP64 arithmetic of the operator. ld =
  * nrhs. stats->rel_residual: worst column. */
 int afm_solve_cg_batched_device(afm_operator* op, const double* d_B, double* d_X, uint32_t nrhs, double rtol,
                                 double atol, int maxit, afm_solve_stats* stats);
-/* Batched mixed-precision refinement: FP64 residual block on the split arena,
- * inner batched Jacobi-PCG in FP32 (FP64 scalars) to inner_rtol per column. */
+/* Batched mixed-precision solve: one FP32 block Jacobi-PCG recursion (FP64
+ * scalars) on the hi plane of the split arena, with FP64 reliable updates of
+ * every column from the FP64 residual block (as afm_solve_cg_mixed). A segment
+ * ends once every running column's FP32 residual fell by inner_rtol or after
+ * max_inner iterations; columns wait for the slowest, so a short max_inner
+ * (tens of iterations) keeps all columns busy. Columns that meet rtol are
+ * frozen. */
 int afm_solve_cg_batched_mixed_device(afm_operator* op, const double* d_B, double* d_X, uint32_t nrhs, double rtol,
                                       double atol, int max_outer, double inner_rtol, int max_inner,
                                       afm_solve_stats* stats);
@@ -280,6 +286,37 @@ int afm_solve_cg_batched_mixed_device(afm_operator* op, const double* d_B, doubl
 int afm_patch_plan_host_matvec(uint32_t n_elem, uint32_t n_dofs, const uint32_t* offsets, const uint32_t* map,
                                const double* ke, const double* u, double* v, uint32_t* n_patches,
                                uint32_t* n_patch_colors);
+
+/* ---- serving: many CG solves on different operators ----------------------
+ * No counterpart in the reference. A request is an operator whose maps and
+ * element matrices are set on the host (finalize not needed) and a load b
+ * (host, n_dofs, boundary conditions applied). Requests wait in a FIFO queue
+ * and are admitted while the HBM budget, the device's free memory and the
+ * slot limit allow; admission finalises the operator on a worker thread. An
+ * admitted request keeps Ke, maps, b, x and its Krylov vectors on the device
+ * and is solved by the mixed-precision solve (afm_solve_cg_mixed, to rtol,
+ * FP64-checked). afm_server_poll never blocks: it admits, and takes the next
+ * step of every request whose previous step has finished on the GPU. Each
+ * request runs on its own stream, so the work of all running requests
+ * overlaps on the device, and requests arriving meanwhile join as slots and
+ * memory free up. A request's result does not depend on the others: it is
+ * the same, bit for bit, alone and in any mix. One thread drives a server. */
+typedef struct afm_server afm_server;
+/* hbm_budget_bytes 0: 85% of the device memory free now; max_active 0: 32. */
+int afm_server_create(afm_server** out, int device, uint64_t hbm_budget_bytes, uint32_t max_active);
+/* Takes ownership of op (destroyed when the request finishes). inner_rtol:
+ * FP32 residual reduction between FP64 updates (0 < inner_rtol < 1). */
+int afm_server_submit(afm_server* s, afm_operator* op, const double* b, double rtol, double inner_rtol,
+                      uint64_t* id);
+/* Non-blocking progress; optional counts of queued and admitted requests. */
+int afm_server_poll(afm_server* s, uint32_t* n_queued, uint32_t* n_active);
+/* *finished = 0 (and AFM_SUCCESS) while the request is queued or running.
+ * Once it has finished: *finished = 1, x (host, n_dofs), stats and times[4]
+ * (submit, admit, start of the solve, done; steady-clock seconds) are filled,
+ * the request is forgotten, and the solve's status is returned. */
+int afm_server_take(afm_server* s, uint64_t id, int* finished, double* x, afm_solve_stats* stats, double* times);
+/* Waits for running work and releases everything. */
+int afm_server_destroy(afm_server* s);
 
 /* Largest operator (DoFs) afm_solve_cg_device_noalloc accepts. */
 #define AFM_NOALLOC_MAX_DOFS 262144u
