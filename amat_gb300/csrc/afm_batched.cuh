@@ -170,7 +170,7 @@ __global__ void __launch_bounds__(9 * 32, 1) afm_batched_kernel(BatchArgs a, Rin
         const uint32_t* mp = reinterpret_cast<const uint32_t*>(b);
         const VT* ub = reinterpret_cast<const VT*>(b + batch_map_bytes(n));
         const uint32_t s = i % S;
-        const bool ok = ring_wait(full, tag, s, i, S, abort);
+        const bool ok = ring_wait(&full[s], &tag[s], i, (i / S) & 1, abort);
         const unsigned char* ks = smem + (size_t)s * L.slot_bytes;
         const uint32_t ub_end = (uint32_t)(reinterpret_cast<const unsigned char*>(ub) - smem) + n * R * sizeof(VT);
         if (ub_end > a.smem_total || s >= S) report_bad(a.err, 6, ub_end, s, i);

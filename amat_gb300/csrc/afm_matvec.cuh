@@ -277,26 +277,32 @@ struct RingLayout {
     __host__ __device__ uint32_t total() const { return ubuf_offset() + extra_bytes; }
 };
 
-// Waits until ring slot s holds ring index ii. A parity test alone cannot tell
-// round r of a slot from round r - 2 (a consumer that reaches a slot while its
-// previous round is still loading would pass at once), so the producer
-// writes the slot's tag = ring index before the arrive that completes the
-// phase, and the consumer accepts the phase only with the matching tag.
-// Bounded like mbar_wait_abortable.
-__device__ __forceinline__ bool ring_wait(uint64_t* full, const volatile uint32_t* tag, uint32_t s, uint32_t ii,
-                                          uint32_t S, volatile int* abort) {
-    const uint32_t par = (ii / S) & 1;
-    if (mbar_try_wait(&full[s], par) && tag[s] == ii) return true;
+// Waits until ring slot s holds ring index ii (parity = (ii / S) & 1). A
+// parity test alone cannot tell round r of a slot from round r - 2 (a consumer
+// that reaches a slot while its previous round is still loading would pass at
+// once), so the producer writes the slot's tag = ring index before the arrive
+// that completes the phase, and the consumer accepts the phase only with the
+// matching tag. The polling loop is out of line: inlined, it costs the hot
+// loops of the element kernels registers and spills. Bounded like
+// mbar_wait_abortable.
+static __device__ __noinline__ bool ring_wait_slow(uint64_t* bar, const volatile uint32_t* tag, uint32_t ii, uint32_t parity,
+                                                   volatile int* abort) {
     const unsigned long long t0 = globaltimer_ns();
     for (;;) {
         for (int k = 0; k < 64; k++)
-            if (mbar_try_wait(&full[s], par) && tag[s] == ii) return true;
+            if (mbar_try_wait(bar, parity) && *tag == ii) return true;
         if (*abort) return false;
         if (globaltimer_ns() - t0 > kWaitLimitNs) {
             *abort = 1;
             return false;
         }
     }
+}
+
+__device__ __forceinline__ bool ring_wait(uint64_t* bar, const volatile uint32_t* tag, uint32_t ii, uint32_t parity,
+                                          volatile int* abort) {
+    if (mbar_try_wait(bar, parity) && *tag == ii) return true;
+    return ring_wait_slow(bar, tag, ii, parity, abort);
 }
 
 // ---- warp per element (n > 16) --------------------------------------------
@@ -564,7 +570,7 @@ __global__ void __launch_bounds__(17 * 32, 1) afm_wpg_kernel(SegArgs a, RingLayo
         }
         const uint32_t s = i % S;
         Acc acc = A::zero();
-        if (ring_wait(full, tag, s, i, S, abort)) {
+        if (ring_wait(&full[s], &tag[s], i, (i / S) & 1, abort)) {
             const unsigned char* ks = smem + (size_t)s * L.slot_bytes;
             const UT* uu = ubuf(par);
             if (rvalid) {

@@ -189,22 +189,26 @@ cudaError_t BATCH_FN(const Segment& s, const BatchArgs& a, int sm_count, int ct,
 // ---- patch path (small elements) -----------------------------------------
 
 namespace {
+// consumer groups of the patch kernel for this arithmetic (see afm_patch.cuh)
+constexpr int kGroups = sizeof(typename ARITH::VT) == 4 ? 4 : 2;
+
 void* pick_patch_kernel(uint32_t n) {
     switch (n) {
-        case 4: return (void*)afm_patch_kernel<4, ARITH>;
-        case 8: return (void*)afm_patch_kernel<8, ARITH>;
-        case 10: return (void*)afm_patch_kernel<10, ARITH>;
-        default: return (void*)afm_patch_kernel<0, ARITH>;
+        case 4: return (void*)afm_patch_kernel<4, ARITH, kGroups>;
+        case 8: return (void*)afm_patch_kernel<8, ARITH, kGroups>;
+        case 10: return (void*)afm_patch_kernel<10, ARITH, kGroups>;
+        default: return (void*)afm_patch_kernel<0, ARITH, kGroups>;
     }
 }
 
 PatchLayout patch_layout(const PatchPlanGeom& pg, uint32_t copy_bytes) {
     PatchLayout L;
+    L.groups = kGroups;
     L.slot_bytes = (copy_bytes + kSlotAlign - 1) / kSlotAlign * kSlotAlign;
     L.idx_bytes = patch_r16(pg.max_idx);
     L.us_bytes = patch_r16(pg.max_ndof * (uint32_t)sizeof(typename ARITH::UT));
     L.ve_bytes = patch_r16(pg.n * pg.max_slots * (uint32_t)sizeof(typename ARITH::VT));
-    const uint32_t fixed = 16 * kPatchGroups + 16 + 16 + kPatchGroups * L.group_bytes();
+    const uint32_t fixed = 16 * kPatchMaxGroups + 16 + 16 + L.groups * L.group_bytes();
     L.stages = 0;
     if (fixed < kSmemBudget) {
         const uint32_t st = (kSmemBudget - fixed) / (L.slot_bytes + 20);

@@ -12,10 +12,9 @@
 // and the patch's Ke as units of 32 element slots in the thread-per-element
 // layout (entry (r, c) of slot l at (r n + c) 32 + l; empty slots are zero).
 //
-// CTA = kPatchGroups consumer groups of kPatchGroupWarps warps + 1 producer
-// warp; group g takes the CTA's patches g, g + G, ... (G patches in flight
-// per SM, so one patch's gather and reduce latency hides behind the others'
-// products). The producer's elected lane copies each
+// CTA = G consumer groups of 8 / G warps + 1 producer warp; group g takes the
+// CTA's patches g, g + G, ... (G patches in flight per SM, so one patch's
+// gather and reduce latency hides behind the others' products). The producer's elected lane copies each
 // patch's index block into the group's buffer (one bulk copy) and streams
 // its Ke units through the shared ring. A group: gathers u of the patch's
 // DoFs into shared memory once; each lane multiplies one element slot and
@@ -30,27 +29,34 @@
 
 namespace afm {
 
-constexpr uint32_t kPatchGroups = 4;
-constexpr uint32_t kPatchGroupWarps = 2;
-constexpr uint32_t kPatchGroupThreads = kPatchGroupWarps * 32;
-constexpr uint32_t kPatchThreads = kPatchGroups * kPatchGroupThreads + 32;
+// 8 consumer warps in G groups: G = 4 groups of 2 warps when a unit is small
+// enough (FP32, 12.8 KB for n = 10) that the ring holds several patches; G = 2
+// groups of 4 warps for 8-byte entries, whose ring holds about two patches.
+constexpr uint32_t kPatchConsumerWarps = 8;
+constexpr uint32_t kPatchThreads = kPatchConsumerWarps * 32 + 32;
+constexpr uint32_t kPatchMaxGroups = 4;
 constexpr int kBatch = 8;  // global loads a thread keeps in flight in the gather and the update
 
-// Shared-memory layout: ring slots, mbarriers (full[S], empty[S], idx_full[G],
-// idx_empty[G]) and the abort flag, the slot tags (ring_wait), then per group:
+// Shared-memory layout: ring slots, mbarriers (full[S], empty[S], idx_full[4],
+// idx_empty[4]) and the abort flag, the slot tags (ring_wait), then per group:
 // index block, staged u, element products.
 struct PatchLayout {
-    uint32_t slot_bytes, stages;
+    uint32_t slot_bytes, stages, groups;
     uint32_t idx_bytes, us_bytes, ve_bytes;  // per group, 16-byte multiples
     __host__ __device__ uint32_t bars_offset() const { return slot_bytes * stages; }
-    __host__ __device__ uint32_t tags_offset() const { return bars_offset() + 16u * stages + 16u * kPatchGroups + 16u; }
+    __host__ __device__ uint32_t tags_offset() const {
+        return bars_offset() + 16u * stages + 16u * kPatchMaxGroups + 16u;
+    }
     __host__ __device__ uint32_t group_offset() const { return tags_offset() + ((4u * stages + 15u) & ~15u); }
     __host__ __device__ uint32_t group_bytes() const { return idx_bytes + us_bytes + ve_bytes; }
-    __host__ __device__ uint32_t total() const { return group_offset() + kPatchGroups * group_bytes(); }
+    __host__ __device__ uint32_t total() const { return group_offset() + groups * group_bytes(); }
 };
 
-template <int NT, typename A>
+template <int NT, typename A, int G>
 __global__ void __launch_bounds__(kPatchThreads, 1) afm_patch_kernel(PatchArgs a, PatchLayout L, uint32_t n_rt) {
+    constexpr uint32_t kPatchGroups = G;
+    constexpr uint32_t kPatchGroupWarps = kPatchConsumerWarps / G;
+    constexpr uint32_t kPatchGroupThreads = kPatchGroupWarps * 32;
     using KT = typename A::KT;
     using UT = typename A::UT;
     using VT = typename A::VT;
@@ -60,8 +66,8 @@ __global__ void __launch_bounds__(kPatchThreads, 1) afm_patch_kernel(PatchArgs a
     uint64_t* full = reinterpret_cast<uint64_t*>(smem + L.bars_offset());
     uint64_t* empty = full + L.stages;
     uint64_t* idx_full = empty + L.stages;
-    uint64_t* idx_empty = idx_full + kPatchGroups;
-    volatile int* abort = reinterpret_cast<volatile int*>(idx_empty + kPatchGroups);
+    uint64_t* idx_empty = idx_full + kPatchMaxGroups;
+    volatile int* abort = reinterpret_cast<volatile int*>(idx_empty + kPatchMaxGroups);
     volatile uint32_t* tag = reinterpret_cast<volatile uint32_t*>(smem + L.tags_offset());
     const uint32_t tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const uint32_t S = L.stages;
@@ -179,7 +185,7 @@ __global__ void __launch_bounds__(kPatchThreads, 1) afm_patch_kernel(PatchArgs a
         // element products: lane l of warp w takes slot (unit w + W i, lane l)
         for (uint32_t un = wg; un < d.units; un += kPatchGroupWarps) {
             const uint32_t ii = base + un, s = ii % S;
-            const bool ok = iok && ring_wait(full, tag, s, ii, S, abort);
+            const bool ok = iok && ring_wait(&full[s], &tag[s], ii, (ii / S) & 1, abort);
             if (ok) {
                 const unsigned char* ks = smem + (size_t)s * L.slot_bytes;
                 UT ul[NM];

@@ -134,7 +134,7 @@ void finish(afm_server* s, Request* r, int status, const char* msg) {
 
 // At most this many operators are finalised at once: each finalize runs
 // OpenMP loops over all host cores, and more in parallel only contend.
-constexpr int kMaxFinalizing = 2;
+constexpr int kMaxFinalizing = 4;
 
 // admission: FIFO while the budget, free device memory and slots allow
 void admit(afm_server* s) {
@@ -201,7 +201,7 @@ int afm_server_create(afm_server** out, int device, uint64_t hbm_budget_bytes, u
     s->device = device;
     s->budget = hbm_budget_bytes ? hbm_budget_bytes : (uint64_t)(free_b * 0.85);
     s->reserve = std::min<uint64_t>(total_b / 50, 2ull << 30);
-    s->max_active = max_active ? max_active : 32;
+    s->max_active = max_active ? max_active : 64;
     s->reaper = std::thread(reap, s);
     *out = s;
     return afm::set_error(AFM_SUCCESS, "");

@@ -168,10 +168,11 @@ def cpu_sample(w, m, dmap, max_elems):
     return pr, u, v, ne, sample_bytes
 
 
-def time_cpu(pr, u, v, reps):
+def time_cpu(pr, u, v, reps, seconds=0.0):
+    """reps matvecs, continued until `seconds` of CPU time have been timed."""
     ts = []
     threads = 1
-    for _ in range(reps):
+    while len(ts) < reps or sum(ts) < seconds:
         t0 = time.perf_counter()
         _, threads = pr.matvec_omp(u, v)
         ts.append(time.perf_counter() - t0)
@@ -189,7 +190,7 @@ def run_reference(args, w, rank):
     ts, threads = time_cpu(pr, u, v, args.steps)
     t = sum(ts)
     value = sbytes * args.steps / t / 1e9
-    sample = "%d of %d elements (%s), %d matvecs" % (ne, m.n_elem, w["desc"], args.steps)
+    sample = "%d of %d elements (%s) per step, %d steps" % (ne, m.n_elem, w["desc"], args.steps)
     return {
         "impl": "reference", "metric": "AFM matvec GB/s", "value": value, "unit": "GB/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True,
@@ -313,7 +314,9 @@ def run_ours(args, w, rank, world, local_rank):
                    "l2": "no flush: inputs %.2f GB > 129 MB L2" % (alg / 1e9)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": ncu_traffic(key), "peak_kind": peak_kind,
-                     "kernel": "afm_wpg_kernel, one launch per colour + v zero fill (%d launches/step)"
+                     "kernel": ("afm_patch_kernel, one launch per patch colour + v zero fill (%d launches/step)"
+                                if info["n_patches"] else
+                                "afm_wpg_kernel, one launch per colour + v zero fill (%d launches/step)")
                                % info["n_launches"],
                      "algorithmic_bytes_per_step": alg},
         "e2e": e2e,
@@ -326,11 +329,11 @@ def run_ours(args, w, rank, world, local_rank):
         out["clocks"] = clk_sum
     if args.cpu_sample_elems > 0:
         pr, uc, vc, ne, sbytes = cpu_sample(w, m, dmap, args.cpu_sample_elems)
-        ts, threads = time_cpu(pr, uc, vc, 5)
+        ts, threads = time_cpu(pr, uc, vc, 5, args.cpu_seconds)
         out["cpu_baseline"] = {"value": sbytes * len(ts) / sum(ts) / 1e9, "unit": "GB/s", "cores": threads,
                                "kind": "port",
-                               "sample": "%d of %d elements, 5 matvecs, oracle port of matvec_ghosted_OMP"
-                                         % (ne, m.n_elem)}
+                               "sample": "%d of %d elements, %d matvecs (%.1f s), oracle port of matvec_ghosted_OMP"
+                                         % (ne, m.n_elem, len(ts), sum(ts))}
     return out
 
 
@@ -583,7 +586,7 @@ def run_serve(args, w, rank, world, local_rank):
                                   "jitter 0.1h, loads N(0,1)" % (args.requests, [k[1] for k in SERVE_KINDS],
                                                                   args.edge_max),
                       "n_dofs_range": [int(min(sizes)), int(max(sizes))], "rtol": args.rtol,
-                      "inner_rtol": args.serve_inner, "admission": "FIFO by HBM budget (85% of free), 32 slots"},
+                      "inner_rtol": args.serve_inner, "admission": "FIFO by HBM budget (85% of free), 64 slots"},
            "rates": lines, "p50_ms": best["p50_ms"], "p99_ms": best["p99_ms"], "plain_fp64_sequential": plain,
            "served_one_at_a_time": alone,
            "speedup_vs_plain": best["solves_per_s"] / plain["solves_per_s"]}
@@ -602,7 +605,8 @@ def main():
     ap.add_argument("--workload", default="hex20_elastic_64", choices=sorted(WORKLOADS))
     ap.add_argument("--precision", default="auto", choices=sorted(PREC_NAMES))
     ap.add_argument("--also-native", type=int, default=1, help="also time native FP64 when the split path runs")
-    ap.add_argument("--cpu-sample-elems", type=int, default=32768)
+    ap.add_argument("--cpu-sample-elems", type=int, default=65536)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU time the baseline sample is timed for")
     ap.add_argument("--mode", default="matvec", choices=["matvec", "solve", "batched", "serve"])
     ap.add_argument("--rates", default="20,100,500", help="serve: arrival rates (requests/s)")
     ap.add_argument("--requests", type=int, default=48, help="serve: requests per rate")

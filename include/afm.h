@@ -302,7 +302,7 @@ int afm_patch_plan_host_matvec(uint32_t n_elem, uint32_t n_dofs, const uint32_t*
  * memory free up. A request's result does not depend on the others: it is
  * the same, bit for bit, alone and in any mix. One thread drives a server. */
 typedef struct afm_server afm_server;
-/* hbm_budget_bytes 0: 85% of the device memory free now; max_active 0: 32. */
+/* hbm_budget_bytes 0: 85% of the device memory free now; max_active 0: 64. */
 int afm_server_create(afm_server** out, int device, uint64_t hbm_budget_bytes, uint32_t max_active);
 /* Takes ownership of op (destroyed when the request finishes). inner_rtol:
  * FP32 residual reduction between FP64 updates (0 < inner_rtol < 1). */
