@@ -207,7 +207,7 @@ PatchLayout patch_layout(const PatchPlanGeom& pg, uint32_t copy_bytes) {
     L.slot_bytes = (copy_bytes + kSlotAlign - 1) / kSlotAlign * kSlotAlign;
     L.idx_bytes = patch_r16(pg.max_idx);
     L.us_bytes = patch_r16(pg.max_ndof * (uint32_t)sizeof(typename ARITH::UT));
-    L.ve_bytes = patch_r16(pg.n * pg.max_slots * (uint32_t)sizeof(typename ARITH::VT));
+    L.ve_bytes = patch_r16(pg.n * pg.max_slots * (uint32_t)sizeof(typename ARITH::Acc));
     const uint32_t fixed = 16 * kPatchMaxGroups + 16 + 16 + L.groups * L.group_bytes();
     L.stages = 0;
     if (fixed < kSmemBudget) {

@@ -142,7 +142,11 @@ __global__ void __launch_bounds__(kPatchThreads, 1) afm_patch_kernel(PatchArgs a
     const uint32_t bar_id = 1 + g;
     unsigned char* gbase = smem + L.group_offset() + g * L.group_bytes();
     UT* us = reinterpret_cast<UT*>(gbase + L.idx_bytes);
-    VT* ve = reinterpret_cast<VT*>(gbase + L.idx_bytes + L.us_bytes);
+    // element products stay in the accumulator format (a double-float pair
+    // for the split arithmetic) until one finish per DoF: on GB300 every FP64
+    // instruction costs as much as 64 FP32 ones
+    using Acc = typename A::Acc;
+    Acc* ve = reinterpret_cast<Acc*>(gbase + L.idx_bytes + L.us_bytes);
     const VT* __restrict__ u = static_cast<const VT*>(a.u);
     VT* __restrict__ v = static_cast<VT*>(a.v);
     const uint64_t keep = l2_evict_last_policy();
@@ -200,7 +204,7 @@ __global__ void __launch_bounds__(kPatchThreads, 1) afm_patch_kernel(PatchArgs a
 #pragma unroll
                         for (int c = 0; c < NM; c++)
                             if (c < (int)n) A::fma(acc, A::kload(ks, (size_t)(r * n + c) * 32u + lane, a.plane), ul[c]);
-                        ve[r * cap + e] = A::finish(acc);
+                        ve[r * cap + e] = acc;
                     }
                 }
             }
@@ -228,10 +232,10 @@ __global__ void __launch_bounds__(kPatchThreads, 1) afm_patch_kernel(PatchArgs a
                 for (int q = 0; q < kBatch; q++) {
                     const uint32_t i = i0 + q * kPatchGroupThreads;
                     if (i < d.ndof) {
-                        VT sum = VT(0);
+                        Acc sum = A::zero();
                         const uint32_t q1 = coff[i + 1];
-                        for (uint32_t c = coff[i]; c < q1; c++) sum += ve[slot[c]];
-                        st_hint(v + gi[q], old[q] + sum, keep);
+                        for (uint32_t c = coff[i]; c < q1; c++) A::combine(sum, ve[slot[c]]);
+                        st_hint(v + gi[q], old[q] + A::finish(sum), keep);
                     }
                 }
             }

@@ -7,9 +7,10 @@
 // Admission finalises the operator on a worker thread (colouring, patch plan,
 // upload of Ke and maps), so the polling thread never blocks on host work.
 // An admitted request keeps all of its state on the device: Ke, maps, b, x
-// and the Krylov vectors of its mixed-precision solve (afm_mixed.hpp). Every
-// poll takes the next step of each request whose previous step has finished
-// on the GPU; each request runs on its own stream, so the kernels of all
+// and the Krylov vectors of its mixed-precision solve (afm_mixed.hpp). The
+// server's progress thread keeps taking the next step of each request whose
+// previous step has finished on the GPU (so progress never waits for the
+// caller); each request runs on its own stream, so the kernels of all
 // running requests overlap on the device, and requests that arrive while
 // others run are admitted as soon as slots and memory free up (continuous
 // batching). A finished request copies x back asynchronously, releases its
@@ -22,6 +23,7 @@
 #include <stdint.h>
 #include <string.h>
 
+#include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <deque>
@@ -92,6 +94,11 @@ struct afm_server {
     std::condition_variable cv;
     std::deque<afm_operator*> graveyard;
     bool stop = false;
+    // requests advance on a progress thread of the server's own; state_mu
+    // guards the queue, the active list and the request table
+    std::thread progress;
+    std::mutex state_mu;
+    std::atomic<bool> running{false};
 };
 
 namespace {
@@ -137,7 +144,8 @@ void finish(afm_server* s, Request* r, int status, const char* msg) {
 constexpr int kMaxFinalizing = 4;
 
 // admission: FIFO while the budget, free device memory and slots allow
-void admit(afm_server* s) {
+int admit(afm_server* s) {
+    int admitted = 0;
     int finalizing = 0;
     for (const Request* r : s->active) finalizing += (r->state == RQ_ADMITTING);
     while (!s->queue.empty() && s->active.size() < s->max_active && finalizing < kMaxFinalizing) {
@@ -158,7 +166,9 @@ void admit(afm_server* s) {
         });
         s->active.push_back(r);
         finalizing++;
+        admitted++;
     }
+    return admitted;
 }
 
 int start(afm_server* s, Request* r) {
@@ -185,52 +195,14 @@ int start(afm_server* s, Request* r) {
 
 }  // namespace
 
-extern "C" {
+namespace {
 
-int afm_server_create(afm_server** out, int device, uint64_t hbm_budget_bytes, uint32_t max_active) {
-    if (!out) return afm::set_error(AFM_ERR_INVALID_ARG, "out is null");
-    *out = nullptr;
-    int ndev = 0;
-    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return afm::set_error(AFM_ERR_CUDA, "no CUDA device");
-    if (device < 0) cudaGetDevice(&device);
-    if (device >= ndev) return afm::set_error(AFM_ERR_INVALID_ARG, "device %d of %d", device, ndev);
-    if (cudaSetDevice(device) != cudaSuccess) return afm::set_error(AFM_ERR_CUDA, "cudaSetDevice(%d)", device);
-    size_t free_b = 0, total_b = 0;
-    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return afm::set_error(AFM_ERR_CUDA, "cudaMemGetInfo");
-    auto* s = new afm_server();
-    s->device = device;
-    s->budget = hbm_budget_bytes ? hbm_budget_bytes : (uint64_t)(free_b * 0.85);
-    s->reserve = std::min<uint64_t>(total_b / 50, 2ull << 30);
-    s->max_active = max_active ? max_active : 64;
-    s->reaper = std::thread(reap, s);
-    *out = s;
-    return afm::set_error(AFM_SUCCESS, "");
-}
-
-int afm_server_submit(afm_server* s, afm_operator* op, const double* b, double rtol, double inner_rtol, uint64_t* id) {
-    if (!s || !op || !b || !id) return afm::set_error(AFM_ERR_INVALID_ARG, "null argument");
-    if (!op->have_map) return afm::set_error(AFM_ERR_STATE, "operator without a map");
-    if (op->device != s->device) return afm::set_error(AFM_ERR_INVALID_ARG, "operator on device %d", op->device);
-    if (!(rtol > 0.0) || !(inner_rtol > 0.0) || inner_rtol >= 1.0)
-        return afm::set_error(AFM_ERR_INVALID_ARG, "rtol %g, inner_rtol %g", rtol, inner_rtol);
-    auto* r = new Request();
-    r->id = s->next_id++;
-    r->op = op;
-    r->b.assign(b, b + op->n_dofs);
-    r->rtol = rtol;
-    r->inner_rtol = inner_rtol;
-    r->est_bytes = estimate_bytes(op);
-    r->t_submit = now_s();
-    s->queue.push_back(r);
-    s->all[r->id] = r;
-    *id = r->id;
-    return afm::set_error(AFM_SUCCESS, "");
-}
-
-int afm_server_poll(afm_server* s, uint32_t* n_queued, uint32_t* n_active) {
-    if (!s) return afm::set_error(AFM_ERR_INVALID_ARG, "null server");
+// One round of progress (caller holds state_mu): admit, then take the next step
+// of every admitted request whose previous step has finished on the GPU.
+// Returns how many things changed.
+int step(afm_server* s) {
     cudaSetDevice(s->device);
-    admit(s);
+    int changes = admit(s);
     std::vector<Request*> still;
     still.reserve(s->active.size());
     for (Request* r : s->active) {
@@ -247,11 +219,14 @@ int afm_server_poll(afm_server* s, uint32_t* n_queued, uint32_t* n_active) {
                 continue;
             }
             r->state = RQ_RUNNING;
+            changes++;
         }
         if (r->state == RQ_RUNNING) {
             int st = AFM_SUCCESS;
-            while (st == AFM_SUCCESS && r->ms.phase != afm::MS_DONE && afm::mixed_ready(r->ms))
+            while (st == AFM_SUCCESS && r->ms.phase != afm::MS_DONE && afm::mixed_ready(r->ms)) {
                 st = afm::mixed_advance(r->ms);
+                changes++;
+            }
             if (st != AFM_SUCCESS) {
                 afm::mixed_end(r->ms, nullptr);
                 finish(s, r, st, afm_last_error());
@@ -274,7 +249,73 @@ int afm_server_poll(afm_server* s, uint32_t* n_queued, uint32_t* n_active) {
         still.push_back(r);
     }
     s->active.swap(still);
-    admit(s);
+    changes += admit(s);
+    return changes;
+}
+
+void run_progress(afm_server* s) {
+    cudaSetDevice(s->device);
+    while (s->running.load()) {
+        int changes;
+        {
+            std::lock_guard<std::mutex> lk(s->state_mu);
+            changes = step(s);
+        }
+        if (!changes) std::this_thread::sleep_for(std::chrono::microseconds(20));
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int afm_server_create(afm_server** out, int device, uint64_t hbm_budget_bytes, uint32_t max_active) {
+    if (!out) return afm::set_error(AFM_ERR_INVALID_ARG, "out is null");
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return afm::set_error(AFM_ERR_CUDA, "no CUDA device");
+    if (device < 0) cudaGetDevice(&device);
+    if (device >= ndev) return afm::set_error(AFM_ERR_INVALID_ARG, "device %d of %d", device, ndev);
+    if (cudaSetDevice(device) != cudaSuccess) return afm::set_error(AFM_ERR_CUDA, "cudaSetDevice(%d)", device);
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return afm::set_error(AFM_ERR_CUDA, "cudaMemGetInfo");
+    auto* s = new afm_server();
+    s->device = device;
+    s->budget = hbm_budget_bytes ? hbm_budget_bytes : (uint64_t)(free_b * 0.85);
+    s->reserve = std::min<uint64_t>(total_b / 50, 2ull << 30);
+    s->max_active = max_active ? max_active : 64;
+    s->reaper = std::thread(reap, s);
+    s->running = true;
+    s->progress = std::thread(run_progress, s);
+    *out = s;
+    return afm::set_error(AFM_SUCCESS, "");
+}
+
+int afm_server_submit(afm_server* s, afm_operator* op, const double* b, double rtol, double inner_rtol, uint64_t* id) {
+    if (!s || !op || !b || !id) return afm::set_error(AFM_ERR_INVALID_ARG, "null argument");
+    if (!op->have_map) return afm::set_error(AFM_ERR_STATE, "operator without a map");
+    if (op->device != s->device) return afm::set_error(AFM_ERR_INVALID_ARG, "operator on device %d", op->device);
+    if (!(rtol > 0.0) || !(inner_rtol > 0.0) || inner_rtol >= 1.0)
+        return afm::set_error(AFM_ERR_INVALID_ARG, "rtol %g, inner_rtol %g", rtol, inner_rtol);
+    std::lock_guard<std::mutex> lk(s->state_mu);
+    auto* r = new Request();
+    r->id = s->next_id++;
+    r->op = op;
+    r->b.assign(b, b + op->n_dofs);
+    r->rtol = rtol;
+    r->inner_rtol = inner_rtol;
+    r->est_bytes = estimate_bytes(op);
+    r->t_submit = now_s();
+    s->queue.push_back(r);
+    s->all[r->id] = r;
+    *id = r->id;
+    return afm::set_error(AFM_SUCCESS, "");
+}
+
+int afm_server_poll(afm_server* s, uint32_t* n_queued, uint32_t* n_active) {
+    if (!s) return afm::set_error(AFM_ERR_INVALID_ARG, "null server");
+    std::lock_guard<std::mutex> lk(s->state_mu);
+    step(s);
     if (n_queued) *n_queued = (uint32_t)s->queue.size();
     if (n_active) *n_active = (uint32_t)s->active.size();
     return afm::set_error(AFM_SUCCESS, "");
@@ -283,6 +324,7 @@ int afm_server_poll(afm_server* s, uint32_t* n_queued, uint32_t* n_active) {
 int afm_server_take(afm_server* s, uint64_t id, int* finished, double* x, afm_solve_stats* stats, double* times) {
     if (!s || !finished) return afm::set_error(AFM_ERR_INVALID_ARG, "null argument");
     *finished = 0;
+    std::lock_guard<std::mutex> lk(s->state_mu);
     auto it = s->all.find(id);
     if (it == s->all.end()) return afm::set_error(AFM_ERR_INVALID_ARG, "unknown request %llu", (unsigned long long)id);
     Request* r = it->second;
@@ -306,6 +348,8 @@ int afm_server_take(afm_server* s, uint64_t id, int* finished, double* x, afm_so
 
 int afm_server_destroy(afm_server* s) {
     if (!s) return AFM_SUCCESS;
+    s->running = false;
+    if (s->progress.joinable()) s->progress.join();
     cudaSetDevice(s->device);
     for (Request* r : s->active)
         if (r->state == RQ_ADMITTING) r->fin.wait();

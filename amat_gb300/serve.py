@@ -1,6 +1,6 @@
 """Serving loop for many CG solves on different operators (afm_server_* in
 include/afm.h): FIFO admission by HBM budget, device-resident state, every
-admitted request advanced by non-blocking polls on its own stream."""
+admitted request advanced on its own stream by the server's progress thread."""
 import ctypes as C
 
 import numpy as np
@@ -31,7 +31,7 @@ class Server:
         return rid.value
 
     def poll(self):
-        """Admits and advances without blocking; returns (queued, admitted)."""
+        """One more round of progress without blocking; returns (queued, admitted)."""
         q, a = C.c_uint32(), C.c_uint32()
         check(self._lib.afm_server_poll(self._h, C.byref(q), C.byref(a)), "afm_server_poll")
         return q.value, a.value

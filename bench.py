@@ -43,6 +43,8 @@ WORKLOADS = {
                              desc="tet10 Poisson 48^3 x 6 (663k tets), 10x10 Ke"),
     "tet10_poisson_64": dict(kind=3, n=64, ngt=2, jitter=0.15, seed=2,
                              desc="tet10 Poisson 64^3 x 6 (1.57M tets), 10x10 Ke"),
+    "tet10_elastic_64": dict(kind=4, n=64, ngt=2, jitter=0.15, seed=2,
+                             desc="tet10 elasticity 64^3 x 6 (1.57M tets), 30x30 Ke, E=1, nu=0.3"),
     "hex8_poisson_96": dict(kind=0, n=96, ngt=2, jitter=0.1, seed=0,
                             desc="hex8 Poisson 96^3, 8x8 FP64 Ke, 2x2x2 Gauss, jitter 0.1h"),
 }
@@ -468,6 +470,56 @@ def run_batched(args, w, rank, world, local_rank):
     return out if rank == 0 else None
 
 
+def run_product(args, w, rank, world, local_rank):
+    """The batched product alone (V = K U on nrhs columns, the inner kernel of the batched solves): FP32 on the
+    hi plane of the split arena and FP64 (double-float) on the whole arena; autotuned or pinned lane tile,
+    CUDA-event time per product."""
+    import torch
+    dev = local_rank
+    torch.cuda.set_device(dev)
+    m, dofs, vals, A = build_bc_problem(w, dev)
+    R = args.nrhs
+    info = A.info()
+    flops = info["algorithmic_flops"] * R
+    stream_ptr = A.stream()
+    stream = torch.cuda.ExternalStream(stream_ptr)
+    out = {}
+    for f32 in (True, False):
+        key = "fp32" if f32 else "fp64_split"
+        dt = torch.float32 if f32 else torch.float64
+        U = torch.empty((m.n_dofs, R), dtype=dt, device="cuda").uniform_(-1, 1)
+        V = torch.empty_like(U)
+        if args.tile:  # pin the lane tile (columns, rows) instead of the autotuner's choice
+            ct, rt = (int(x) for x in args.tile.split(","))
+            A.set_batch_tuning(R, ct, rt, f32=f32)
+        torch.cuda.synchronize()
+        for _ in range(max(args.warmup, 3)):  # the first call runs the autotuner
+            A.matvec_batched_device(V.data_ptr(), U.data_ptr(), R, f32=f32, stream=stream_ptr)
+        A.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            A.matvec_batched_device(V.data_ptr(), U.data_ptr(), R, f32=f32, stream=stream_ptr)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        ke_bytes = info["ke_bytes"] // 2 if f32 else info["ke_bytes"]
+        vec_bytes = 3 * m.n_dofs * R * (4 if f32 else 8)
+        out[key] = {"ms": ms, "tflops": flops / (ms * 1e-3) / 1e12,
+                    "tile (columns, rows)": A.batch_tuning(R, f32=f32)[:2],
+                    "streamed_gbs": (ke_bytes + vec_bytes) / (ms * 1e-3) / 1e9}
+        log("batched product %s: %.3f ms, %.2f TFLOP/s" % (key, ms, out[key]["tflops"]))
+    best = out["fp32"]
+    res = {"metric": "batched AFM product TFLOP/s (%d right-hand sides)" % R, "value": best["tflops"],
+           "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps, "warmup": max(args.warmup, 3),
+           "ms_per_step": best["ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32 (hi plane of the split arena)", "data": "synthetic",
+           "config": {"workload": w["desc"], "n_dofs": m.n_dofs, "n_elements": m.n_elem, "nrhs": R,
+                      "flops_per_product": flops},
+           "products": out}
+    return res if rank == 0 else None
+
+
 SERVE_KINDS = [(0, "hex8 Poisson"), (1, "hex8 elasticity"), (2, "hex20 elasticity")]
 
 
@@ -530,7 +582,7 @@ def run_serve(args, w, rank, world, local_rank):
     for r in reqs:
         rid = srv.submit(r["A"], r["b"], rtol=args.rtol, inner_rtol=args.serve_inner)
         while srv.take(rid) is None:
-            srv.poll()
+            time.sleep(0.0002)
     t_alone = time.perf_counter() - t0
     srv.close()
     alone = {"solves_per_s": len(reqs) / t_alone, "total_s": t_alone}
@@ -551,19 +603,21 @@ def run_serve(args, w, rank, world, local_rank):
                 while k < len(reqs) and arr[k] <= now:
                     ids[srv.submit(reqs[k]["A"], reqs[k]["b"], rtol=args.rtol, inner_rtol=args.serve_inner)] = k
                     k += 1
-                srv.poll()
+                got = 0
                 for rid in list(ids):
                     out = srv.take(rid)
                     if out is None:
                         continue
+                    got += 1
                     j = ids.pop(rid)
                     x, st, tt = out
                     lat.append(tt[3] - (t0 + arr[j]))
                     res.append(st.rel_residual)
                     brk.append((tt[1] - tt[0], tt[2] - tt[1], tt[3] - tt[2], st.seconds))
                     last = max(last, tt[3])
-                if k < len(reqs) and not ids:
-                    time.sleep(max(0.0, min(arr[k] - (time.monotonic() - t0), 0.001)))
+                if not got:  # the server's progress thread does the work; wait a little
+                    nxt = arr[k] - (time.monotonic() - t0) if k < len(reqs) else 0.0005
+                    time.sleep(max(0.0, min(nxt, 0.0005)))
             srv.close()
             span = last - (t0 + arr[0])
             lat = np.array(lat)
@@ -607,15 +661,16 @@ def main():
     ap.add_argument("--also-native", type=int, default=1, help="also time native FP64 when the split path runs")
     ap.add_argument("--cpu-sample-elems", type=int, default=65536)
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU time the baseline sample is timed for")
-    ap.add_argument("--mode", default="matvec", choices=["matvec", "solve", "batched", "serve"])
+    ap.add_argument("--mode", default="matvec", choices=["matvec", "solve", "batched", "product", "serve"])
     ap.add_argument("--rates", default="20,100,500", help="serve: arrival rates (requests/s)")
-    ap.add_argument("--requests", type=int, default=48, help="serve: requests per rate")
+    ap.add_argument("--requests", type=int, default=160, help="serve: requests per rate")
     ap.add_argument("--edge-max", type=int, default=32, help="serve: largest mesh edge")
     ap.add_argument("--serve-inner", type=float, default=0.1, help="serve: FP32 reduction between FP64 updates")
     ap.add_argument("--nrhs", type=int, default=64)
     ap.add_argument("--single-cols", type=int, default=2, help="columns solved one by one for the FP64 comparison")
     ap.add_argument("--batched-fp64", type=int, default=0, help="also time the FP64 batched block CG")
     ap.add_argument("--segment", type=int, default=64, help="FP32 iterations between FP64 updates (batched)")
+    ap.add_argument("--tile", default="", help="product: pin the batched lane tile 'columns,rows'")
     ap.add_argument("--rtol", type=float, default=1e-8)
     ap.add_argument("--inner-rtol", type=float, default=1e-2)
     args = ap.parse_args()
@@ -631,7 +686,8 @@ def main():
             import torch
             torch.cuda.set_device(local_rank)
             torch.distributed.init_process_group("nccl")
-        run = {"matvec": run_ours, "solve": run_solve, "batched": run_batched, "serve": run_serve}[args.mode]
+        run = {"matvec": run_ours, "solve": run_solve, "batched": run_batched, "product": run_product,
+               "serve": run_serve}[args.mode]
         out = run(args, w, rank, world, local_rank)
         if world > 1:
             import torch

@@ -295,12 +295,13 @@ int afm_patch_plan_host_matvec(uint32_t n_elem, uint32_t n_dofs, const uint32_t*
  * slot limit allow; admission finalises the operator on a worker thread. An
  * admitted request keeps Ke, maps, b, x and its Krylov vectors on the device
  * and is solved by the mixed-precision solve (afm_solve_cg_mixed, to rtol,
- * FP64-checked). afm_server_poll never blocks: it admits, and takes the next
- * step of every request whose previous step has finished on the GPU. Each
- * request runs on its own stream, so the work of all running requests
- * overlaps on the device, and requests arriving meanwhile join as slots and
- * memory free up. A request's result does not depend on the others: it is
- * the same, bit for bit, alone and in any mix. One thread drives a server. */
+ * FP64-checked). A progress thread of the server's own keeps admitting and
+ * taking the next step of every request whose previous step has finished on
+ * the GPU, so progress never waits for the caller. Each request runs on its
+ * own stream, so the work of all running requests overlaps on the device, and
+ * requests arriving meanwhile join as slots and memory free up. A request's
+ * result does not depend on the others: it is the same, bit for bit, alone
+ * and in any mix. The calls below are thread-safe. */
 typedef struct afm_server afm_server;
 /* hbm_budget_bytes 0: 85% of the device memory free now; max_active 0: 64. */
 int afm_server_create(afm_server** out, int device, uint64_t hbm_budget_bytes, uint32_t max_active);
@@ -308,7 +309,8 @@ int afm_server_create(afm_server** out, int device, uint64_t hbm_budget_bytes, u
  * FP32 residual reduction between FP64 updates (0 < inner_rtol < 1). */
 int afm_server_submit(afm_server* s, afm_operator* op, const double* b, double rtol, double inner_rtol,
                       uint64_t* id);
-/* Non-blocking progress; optional counts of queued and admitted requests. */
+/* Non-blocking: one more round of progress, and the counts of queued and
+ * admitted requests (optional). */
 int afm_server_poll(afm_server* s, uint32_t* n_queued, uint32_t* n_active);
 /* *finished = 0 (and AFM_SUCCESS) while the request is queued or running.
  * Once it has finished: *finished = 1, x (host, n_dofs), stats and times[4]
