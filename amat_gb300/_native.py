@@ -26,7 +26,8 @@ class AfmInfo(C.Structure):
         ("max_dofs_per_element", C.c_uint32), ("precision", C.c_int), ("ke_bytes", C.c_uint64),
         ("map_bytes", C.c_uint64), ("algorithmic_bytes", C.c_uint64), ("algorithmic_flops", C.c_double),
         ("n_launches", C.c_uint32), ("device", C.c_int), ("n_patches", C.c_uint32),
-        ("n_patch_colors", C.c_uint32), ("patch_index_bytes", C.c_uint64),
+        ("n_patch_colors", C.c_uint32), ("patch_index_bytes", C.c_uint64), ("ke_symmetric", C.c_int),
+        ("sym_available", C.c_int), ("sym_bytes", C.c_uint64),
     ]
 
 
@@ -63,6 +64,7 @@ AFM_SIGNATURES = {
     "afm_set_matfree_type": (I, [P, I]),
     "afm_set_precision": (I, [P, I]),
     "afm_set_patch_mode": (I, [P, I]),
+    "afm_set_symmetric_inner": (I, [P, I]),
     "afm_server_create": (I, [P, I, U64, U32]),
     "afm_server_submit": (I, [P, P, P, D, D, P]),
     "afm_server_poll": (I, [P, P, P]),

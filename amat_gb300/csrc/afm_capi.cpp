@@ -48,6 +48,13 @@ cudaError_t configure_kernels_fp32();
 cudaError_t launch_patches_fp64(const PatchPlanGeom& pg, const PatchArgs& a, int sm_count, bool pdl, cudaStream_t st);
 cudaError_t launch_patches_split(const PatchPlanGeom& pg, const PatchArgs& a, int sm_count, bool pdl, cudaStream_t st);
 cudaError_t launch_patches_fp32(const PatchPlanGeom& pg, const PatchArgs& a, int sm_count, bool pdl, cudaStream_t st);
+cudaError_t launch_segment_f32sym(const Segment& s, const SegArgs& a, int sm_count, bool dup, bool pdl,
+                                  cudaStream_t st);
+cudaError_t launch_patches_f32sym(const PatchPlanGeom& pg, const PatchArgs& a, int sm_count, bool pdl,
+                                  cudaStream_t st);
+cudaError_t configure_kernels_f32sym();
+size_t patch_smem_f32sym(const PatchPlanGeom& pg, uint32_t copy_bytes);
+size_t segment_smem_f32sym(const Segment& s);
 size_t patch_smem_fp64(const PatchPlanGeom& pg, uint32_t copy_bytes);
 size_t patch_smem_split(const PatchPlanGeom& pg, uint32_t copy_bytes);
 size_t patch_smem_fp32(const PatchPlanGeom& pg, uint32_t copy_bytes);
@@ -57,6 +64,7 @@ cudaError_t launch_patches(int prec, const PatchPlanGeom& pg, const PatchArgs& a
     switch (prec) {
         case AFM_PREC_FP64: return launch_patches_fp64(pg, a, sm_count, pdl, stream);
         case AFM_PREC_FP64_SPLIT: return launch_patches_split(pg, a, sm_count, pdl, stream);
+        case kPrecF32Sym: return launch_patches_f32sym(pg, a, sm_count, pdl, stream);
         default: return launch_patches_fp32(pg, a, sm_count, pdl, stream);
     }
 }
@@ -65,6 +73,7 @@ size_t patch_smem_bytes(int prec, const PatchPlanGeom& pg, uint32_t copy_bytes) 
     switch (prec) {
         case AFM_PREC_FP64: return patch_smem_fp64(pg, copy_bytes);
         case AFM_PREC_FP64_SPLIT: return patch_smem_split(pg, copy_bytes);
+        case kPrecF32Sym: return patch_smem_f32sym(pg, copy_bytes);
         default: return patch_smem_fp32(pg, copy_bytes);
     }
 }
@@ -78,6 +87,7 @@ cudaError_t launch_segment(const Segment& s, int prec, const SegArgs& a, int sm_
     switch (prec) {
         case AFM_PREC_FP64: return launch_segment_fp64(s, a, sm_count, dup, pdl, stream);
         case AFM_PREC_FP64_SPLIT: return launch_segment_split(s, a, sm_count, dup, pdl, stream);
+        case kPrecF32Sym: return launch_segment_f32sym(s, a, sm_count, dup, pdl, stream);
         default: return launch_segment_fp32(s, a, sm_count, dup, pdl, stream);
     }
 }
@@ -86,6 +96,7 @@ size_t segment_smem_bytes(const Segment& s, int prec) {
     switch (prec) {
         case AFM_PREC_FP64: return segment_smem_fp64(s);
         case AFM_PREC_FP64_SPLIT: return segment_smem_split(s);
+        case kPrecF32Sym: return segment_smem_f32sym(s);
         default: return segment_smem_fp32(s);
     }
 }
@@ -190,6 +201,7 @@ void free_device(afm_operator* op) {
     dfree(op, op->d_work32);
     dfree(op, op->d_patch_desc);
     dfree(op, op->d_patch_idx);
+    dfree(op, op->d_sym);
     op->work_elems = 0;
     op->work32_elems = 0;
 }
@@ -405,6 +417,8 @@ bool build_patch_plan(afm_operator* op, uint32_t n, int prec, std::vector<PatchD
     G.n = n;
     uint64_t units = 0, ib = 0;
     for (PatchDesc& d : desc) {
+        d.unit0 = (uint32_t)units;
+        d.pad_ = 0;
         d.ke_off = units * s.unit_bytes;
         d.idx_off = ib;
         units += d.units;
@@ -418,6 +432,8 @@ bool build_patch_plan(afm_operator* op, uint32_t n, int prec, std::vector<PatchD
     s.count = (uint32_t)(units * kTpeWidth);
     s.ke_offset = 0;
     s.map_offset = 0;
+    s.sym_offset = 0;
+    s.sym_unit_bytes = (uint64_t)n * (n + 1) / 2 * kTpeWidth * 4;  // packed triangle, 16-byte multiple
 
     // element slots and index blocks
     std::vector<uint8_t> is_bc(ND, 0);
@@ -480,7 +496,7 @@ void build_segments(afm_operator* op, int prec) {
 
     op->segs.clear();
     const size_t eb = entry_bytes(prec);
-    uint64_t ke_off = 0, map_off = 0;
+    uint64_t ke_off = 0, map_off = 0, sym_off = 0;
     for (uint32_t p = 0; p < op->n_elem;) {
         const uint32_t e = op->perm[p];
         Segment s;
@@ -512,6 +528,10 @@ void build_segments(afm_operator* op, int prec) {
         }
         s.ke_offset = ke_off;
         s.map_offset = map_off;
+        // symmetric inner arena: n/2 + 1 wrapped diagonals per element (warp-group kernel only)
+        s.sym_unit_bytes = s.regime == REG_WPE ? round16((uint64_t)(s.n / 2 + 1) * s.n * 4) : 0;
+        s.sym_offset = sym_off;
+        sym_off += s.sym_unit_bytes * s.units;
         ke_off += s.unit_bytes * s.units;
         map_off += (uint64_t)s.units * (s.regime == REG_TPE ? kTpeWidth : 1) * s.n;
         map_off = (map_off + 3) / 4 * 4;  // keep 16-byte alignment of each segment's map
@@ -520,6 +540,52 @@ void build_segments(afm_operator* op, int prec) {
     }
     op->ke_bytes = ke_off;
     op->map_bytes = map_off * sizeof(uint32_t);
+}
+
+// True when every element matrix is symmetric to within 1e-6 of its largest
+// diagonal entry (exactly, for an element whose diagonal is zero).
+bool ke_is_symmetric(const afm_operator* op) {
+    int sym = 1;
+#pragma omp parallel for schedule(static) reduction(&& : sym)
+    for (int64_t e = 0; e < (int64_t)op->n_elem; e++) {
+        if (!sym) continue;
+        const uint32_t n = op->offsets[e + 1] - op->offsets[e];
+        const double* k = op->ke.data() + op->kofs[e];
+        double dmax = 0.0;
+        for (uint32_t r = 0; r < n; r++) dmax = std::max(dmax, std::fabs(k[(size_t)r * n + r]));
+        const double tol = 1e-6 * dmax;
+        for (uint32_t r = 0; r < n && sym; r++)
+            for (uint32_t c = r + 1; c < n; c++)
+                if (!(std::fabs(k[(size_t)r * n + c] - k[(size_t)c * n + r]) <= tol)) {
+                    sym = 0;
+                    break;
+                }
+    }
+    return sym != 0;
+}
+
+// Builds the symmetric inner arena on the operator's stream (once); work
+// enqueued afterwards on `st` is ordered after it. Call outside stream capture.
+int ensure_sym(afm_operator* op, cudaStream_t st) {
+    if (!op->sym_ok || !op->sym_mode || op->d_sym) return AFM_SUCCESS;
+    AFM_CUDA(dalloc(op, &op->d_sym, op->sym_bytes));
+    AFM_CUDA(cudaMemsetAsync(op->d_sym, 0, op->sym_bytes, op->stream));
+    for (const Segment& s : op->segs) {
+        const cudaError_t e = build_sym_segment(s, op->d_ke, op->d_sym, op->sm_count, op->stream);
+        if (e != cudaSuccess) {
+            dfree(op, op->d_sym);
+            return fail(AFM_ERR_CUDA, "symmetric arena: %s", cudaGetErrorString(e));
+        }
+    }
+    op->generation++;  // captured FP32 iterations switch to the new arena
+    if (st != op->stream) {
+        cudaEvent_t ev;
+        AFM_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        cudaEventRecord(ev, op->stream);
+        cudaStreamWaitEvent(st, ev, 0);
+        cudaEventDestroy(ev);
+    }
+    return AFM_SUCCESS;
 }
 
 int upload_arena(afm_operator* op) {
@@ -611,10 +677,12 @@ int check_device_error(afm_operator* op) {
 // v = K u (bc_mode 0) or the product of MatMult_mf without the final v_c = u_c
 // (bc_mode 1: constrained columns of u read as zero), device arrays.
 int enqueue_matvec(afm_operator* op, void* d_v, const void* d_u, int bc_mode, cudaStream_t st, bool f32 = false) {
-    // f32: FP32 product on float vectors, from an FP32 arena or from the hi
-    // plane of a split arena (half of each unit is copied)
-    const int kprec = f32 ? AFM_PREC_FP32 : op->precision;
-    const size_t vbytes = (size_t)op->n_dofs * (kprec == AFM_PREC_FP32 ? 4 : 8);
+    // f32: FP32 product on float vectors, from the symmetric inner arena once
+    // built, else from an FP32 arena or the hi plane of a split arena (half of
+    // each unit is copied)
+    const bool sym = f32 && op->d_sym != nullptr;
+    const int kprec = sym ? kPrecF32Sym : f32 ? AFM_PREC_FP32 : op->precision;
+    const size_t vbytes = (size_t)op->n_dofs * (f32 || kprec == AFM_PREC_FP32 ? 4 : 8);
     AFM_CUDA(cudaMemsetAsync(d_v, 0, vbytes, st));
     bool first = true;
     if (op->use_patches) {
@@ -623,14 +691,14 @@ int enqueue_matvec(afm_operator* op, void* d_v, const void* d_u, int bc_mode, cu
             PatchArgs a;
             a.desc = op->d_patch_desc + op->patch_color_first[c];
             a.count = op->patch_color_first[c + 1] - op->patch_color_first[c];
-            a.ke = op->d_ke;
+            a.ke = sym ? op->d_sym : op->d_ke;
             a.idx = op->d_patch_idx;
             a.u = d_u;
             a.v = d_v;
-            a.unit_bytes = s.unit_bytes;
-            a.copy_bytes = (uint32_t)s.unit_bytes;
-            a.plane = s.plane;
-            if (f32 && op->precision == AFM_PREC_FP64_SPLIT) a.copy_bytes = s.plane * 4;
+            a.unit_bytes = sym ? s.sym_unit_bytes : s.unit_bytes;
+            a.copy_bytes = (uint32_t)a.unit_bytes;
+            a.plane = sym ? 0 : s.plane;
+            if (f32 && !sym && op->precision == AFM_PREC_FP64_SPLIT) a.copy_bytes = s.plane * 4;
             a.bc_mode = bc_mode;
             a.err = op->d_err;
             AFM_CUDA(launch_patches(kprec, op->patch_geom, a, op->sm_count, !first, st));
@@ -641,16 +709,16 @@ int enqueue_matvec(afm_operator* op, void* d_v, const void* d_u, int bc_mode, cu
     for (const Segment& s : op->segs) {
         if (s.units == 0) continue;
         SegArgs a;
-        a.ke = op->d_ke + s.ke_offset;
+        a.ke = sym ? op->d_sym + s.sym_offset : op->d_ke + s.ke_offset;
         a.map = op->d_map + s.map_offset;
         a.u = d_u;
         a.v = d_v;
         a.units = s.units;
         a.count = s.count;
-        a.unit_bytes = s.unit_bytes;
-        a.copy_bytes = (uint32_t)s.unit_bytes;
-        a.plane = s.plane;
-        if (f32 && op->precision == AFM_PREC_FP64_SPLIT) a.copy_bytes = s.plane * 4;
+        a.unit_bytes = sym ? s.sym_unit_bytes : s.unit_bytes;
+        a.copy_bytes = (uint32_t)a.unit_bytes;
+        a.plane = sym ? 0 : s.plane;
+        if (f32 && !sym && op->precision == AFM_PREC_FP64_SPLIT) a.copy_bytes = s.plane * 4;
         a.bc_mode = bc_mode;
         a.err = op->d_err;
         // every launch after the first may overlap its prologue with the previous one's tail
@@ -1125,6 +1193,8 @@ int mixed_begin(MixedSolve& m) {
     if (s) return s;
     s = ensure_work32(op, 7);
     if (s) return s;
+    s = ensure_sym(op, op->stream);  // once per operator, before the timed solve
+    if (s) return s;
     AFM_CUDA(cudaEventCreateWithFlags(&m.ev, cudaEventDisableTiming));
     AFM_CUDA(cudaEventCreate(&m.e0));
     AFM_CUDA(cudaEventCreate(&m.e1));
@@ -1287,7 +1357,7 @@ int afm_create(afm_operator** out, int bc_method, int device) {
                     prop.major, prop.minor);
     DeviceGuard g(device);
     // kernels' shared-memory limits, before any launch or graph capture
-    if (configure_kernels_fp64() != cudaSuccess || configure_kernels_split() != cudaSuccess ||
+    if (configure_kernels_fp64() != cudaSuccess || configure_kernels_split() != cudaSuccess || configure_kernels_f32sym() != cudaSuccess ||
         configure_kernels_fp32() != cudaSuccess)
         return fail(AFM_ERR_CUDA, "kernel configuration failed on device %d", device);
     auto* op = new afm_operator();
@@ -1346,6 +1416,17 @@ int afm_set_patch_mode(afm_operator* op, int enable) {
     AFM_CHECK_OP(op);
     op->patch_mode = enable ? 1 : 0;
     op->finalized = false;
+    return ok();
+}
+
+int afm_set_symmetric_inner(afm_operator* op, int enable) {
+    AFM_CHECK_OP(op);
+    op->sym_mode = enable ? 1 : 0;
+    if (!op->sym_mode && op->d_sym) {
+        DeviceGuard g(op->device);
+        dfree(op, op->d_sym);
+        op->generation++;  // captured FP32 iterations return to the hi plane
+    }
     return ok();
 }
 
@@ -1568,6 +1649,22 @@ int afm_finalize(afm_operator* op) {
     AFM_CUDA(cudaStreamSynchronize(op->stream));
     int st = upload_arena(op);
     if (st != AFM_SUCCESS) return st;
+
+    // symmetric inner arena (built on the first FP32 product): split arena,
+    // symmetric Ke, and elements that run as patches or on the warp-group kernel
+    op->ke_symmetric = false;
+    op->sym_ok = false;
+    op->sym_bytes = 0;
+    if (prec == AFM_PREC_FP64_SPLIT && !op->dup_in_element && op->n_elem > 0) {
+        op->ke_symmetric = ke_is_symmetric(op);
+        bool covered = true;
+        for (const Segment& s : op->segs) {
+            if (s.units && s.sym_unit_bytes == 0) covered = false;
+            op->sym_bytes = std::max<size_t>(op->sym_bytes, s.sym_offset + s.sym_unit_bytes * s.units);
+        }
+        op->sym_ok = op->ke_symmetric && covered;
+        if (!op->sym_ok) op->sym_bytes = 0;
+    }
     op->ke_dirty = false;
     op->finalized = true;
     return ok();
@@ -1591,7 +1688,10 @@ int afm_matvec_device_f32(afm_operator* op, float* d_v, const float* d_u, void* 
         return fail(AFM_ERR_STATE, "FP32 product needs an FP32 or FP64_SPLIT operator");
     if (!d_v || !d_u || (void*)d_v == (const void*)d_u) return fail(AFM_ERR_INVALID_ARG, "bad vectors");
     DeviceGuard g(op->device);
-    int s = enqueue_matvec(op, d_v, d_u, 0, pick_stream(op, stream), true);
+    cudaStream_t st = pick_stream(op, stream);
+    int s = ensure_sym(op, st);
+    if (s) return s;
+    s = enqueue_matvec(op, d_v, d_u, 0, st, true);
     return s == AFM_SUCCESS ? ok() : s;
 }
 
@@ -1654,7 +1754,9 @@ int afm_matmult_bc_device_f32(afm_operator* op, float* d_v, const float* d_u, vo
     if (!d_v || !d_u || (void*)d_v == (const void*)d_u) return fail(AFM_ERR_INVALID_ARG, "bad vectors");
     DeviceGuard g(op->device);
     cudaStream_t st = pick_stream(op, stream);
-    int s = enqueue_matvec(op, d_v, d_u, 1, st, true);
+    int s = ensure_sym(op, st);
+    if (s) return s;
+    s = enqueue_matvec(op, d_v, d_u, 1, st, true);
     if (s) return s;
     AFM_CUDA(launch_set_constrained(d_v, d_u, op->d_bc_idx, op->n_bc, st));
     return ok();
@@ -2178,6 +2280,9 @@ int afm_get_info(afm_operator* op, afm_info* info) {
     info->n_patches = op->n_patches;
     info->n_patch_colors = op->use_patches ? (uint32_t)op->patch_color_first.size() - 1 : 0;
     info->patch_index_bytes = op->use_patches ? op->patch_idx_bytes : 0;
+    info->ke_symmetric = op->ke_symmetric ? 1 : 0;
+    info->sym_available = (op->sym_ok && op->sym_mode) ? 1 : 0;
+    info->sym_bytes = op->d_sym ? op->sym_bytes : 0;
     info->device = op->device;
     return ok();
 }

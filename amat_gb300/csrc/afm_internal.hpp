@@ -43,6 +43,8 @@ struct Segment {
     uint64_t unit_bytes = 0;  // arena bytes per unit (16-byte multiple)
     uint64_t map_offset = 0;  // uint32 offset of the first unit in the map
     uint32_t plane = 0;       // FP64_SPLIT: entries per plane of a unit (the lo plane follows the hi plane)
+    uint64_t sym_offset = 0;     // byte offset of the first unit in the symmetric inner arena
+    uint64_t sym_unit_bytes = 0; // its bytes per unit (0: no symmetric form)
 };
 
 // Arguments of one segment launch.
@@ -104,12 +106,14 @@ AFM_HD inline uint32_t patch_slot_off(uint32_t ndof, uint32_t units, uint32_t n)
 
 // One patch: its Ke units and its index block (both 16-byte aligned).
 struct PatchDesc {
-    uint64_t ke_off;     // bytes into the Ke arena
+    uint64_t ke_off;     // bytes into the Ke arena (unit0 x its unit size)
     uint64_t idx_off;    // bytes into the index arena
     uint32_t units;      // units of 32 element slots
     uint32_t ndof;       // local DoFs
     uint32_t idx_bytes;  // size of the index block (16-byte multiple)
     uint32_t elems;      // elements (the rest of the slots are empty)
+    uint32_t unit0;      // first unit of the patch, in units of any arena
+    uint32_t pad_;
 };
 
 // Arguments of one patch-colour launch.
@@ -140,7 +144,17 @@ cudaError_t launch_patches(int prec, const PatchPlanGeom& pg, const PatchArgs& a
 // Shared memory of a patch launch (0 if it does not fit).
 size_t patch_smem_bytes(int prec, const PatchPlanGeom& pg, uint32_t copy_bytes);
 
-// Launches one segment on stream. prec: afm_precision (FP64, FP64_SPLIT, FP32).
+// Kernel arithmetic for FP32 products from the symmetric inner arena (an
+// internal value beside the afm_precision codes).
+constexpr int kPrecF32Sym = 16;
+
+// Fills segment s's part of the symmetric inner arena from its split-arena
+// units (afm_mv_f32sym.cu).
+cudaError_t build_sym_segment(const Segment& s, const unsigned char* ke, unsigned char* sym, int sm_count,
+                              cudaStream_t st);
+
+// Launches one segment on stream. prec: afm_precision (FP64, FP64_SPLIT, FP32)
+// or kPrecF32Sym.
 // pdl: allow the launch to begin while the previous kernel on the stream
 // drains (programmatic dependent launch; v is touched only after it ends).
 cudaError_t launch_segment(const Segment& s, int prec, const SegArgs& a, int sm_count, bool dup_in_element, bool pdl,
@@ -218,6 +232,14 @@ struct afm_operator {
     };
     CgGraph cg64, cg32, bcg64, bcg32;
     uint64_t generation = 0;  // bumped whenever device buffers are released
+
+    // symmetric inner arena: FP32 element matrices with each symmetric pair of
+    // entries stored once, built from the split arena on the first FP32 product
+    bool ke_symmetric = false;      // every Ke symmetric to 1e-6 of its largest diagonal entry
+    bool sym_ok = false;            // symmetric, split arena, and a layout the symmetric kernels cover
+    int sym_mode = 1;               // afm_set_symmetric_inner
+    unsigned char* d_sym = nullptr;
+    size_t sym_bytes = 0;
 
     // patch path (small elements): patches in colour order
     bool use_patches = false;

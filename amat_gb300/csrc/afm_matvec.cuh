@@ -129,6 +129,8 @@ __device__ __forceinline__ void report_bad(int* err, int kind, uint32_t a0, uint
 // KT: stored Ke entry, UT: staged u entry, VT: vector entry, Acc: accumulator.
 
 struct ArithF64 {
+    static constexpr bool kSym = false;
+    static constexpr uint32_t kWpgWarps = 16;  // consumer warps of the warp-group kernel
     using KT = double;
     using UT = double;
     using VT = double;
@@ -150,6 +152,8 @@ struct ArithF64 {
 // "Accurate sum and dot product", SIAM J. Sci. Comput. 26(6), 2005, Dot2).
 // The _rn intrinsics keep the compiler from fusing the steps.
 struct ArithSplit {
+    static constexpr bool kSym = false;
+    static constexpr uint32_t kWpgWarps = 16;
     using KT = float2;
     using UT = float2;
     using VT = double;
@@ -187,6 +191,8 @@ struct ArithSplit {
 };
 
 struct ArithF32 {
+    static constexpr bool kSym = false;
+    static constexpr uint32_t kWpgWarps = 24;  // more elements in flight: see wpg_gc
     using KT = float;
     using UT = float;
     using VT = float;
@@ -200,6 +206,28 @@ struct ArithF32 {
     static __device__ __forceinline__ VT finish(const Acc& a) { return a.s; }
     static __device__ __forceinline__ void combine(Acc& a, const Acc& b) { a.s += b.s; }
 };
+
+// FP32 products from the symmetric inner arena: each pair of entries K(i, j),
+// K(j, i) of a symmetric element matrix is stored once, which cuts the bytes
+// streamed per product to about 55%. Thread-per-element units (patches) hold
+// the packed upper triangle, entry (i, j), i <= j, at j (j + 1) / 2 + i;
+// element units (warp-group kernel) hold the n/2 + 1 wrapped diagonals,
+// D[d][j] = K(j, (j + d) mod n) at d n + j, so that both the row and the
+// transposed reads of a warp touch consecutive words.
+struct ArithF32Sym : ArithF32 {
+    static constexpr bool kSym = true;
+};
+
+// Entry index of (r, c) in a thread-per-element unit.
+template <typename A>
+__host__ __device__ __forceinline__ uint32_t tpe_entry(uint32_t r, uint32_t c, uint32_t n) {
+    if constexpr (A::kSym) {
+        const uint32_t i = r < c ? r : c, j = r < c ? c : r;
+        return j * (j + 1) / 2 + i;
+    } else {
+        return r * n + c;
+    }
+}
 
 __device__ __forceinline__ uint64_t l2_evict_last_policy() {
     uint64_t p;
@@ -468,8 +496,40 @@ struct GroupGeom {
 
 __host__ __device__ inline uint32_t wpg_ubuf_bytes(uint32_t n, uint32_t ut) { return (n * ut + 15) / 16 * 16; }
 
+// Column groups of the warp-group kernel for gr row groups: four warps per
+// element when the products are expensive (8-byte staged u: FP64 and split
+// arithmetic), two for FP32, whose element takes little time to multiply and
+// whose throughput comes from having more elements in flight per SM.
+__host__ __device__ constexpr uint32_t wpg_gc(uint32_t gr, uint32_t ut_bytes) {
+    return gr >= 3 ? 1u : (ut_bytes == 4 ? (gr >= 2 ? 1u : 2u) : 4u / gr);
+}
+
+// Terms [T0, T1) of row r of a symmetric element in the wrapped-diagonal
+// layout (D[d][j] = K(j, (j + d) mod n) at d n + j): term t <= n/2 is
+// D[t][r] u[r + t], term t > n/2 (d = t - n/2) is K(r, r - d) =
+// D[d][(r - d) mod n] u[r - d]. kr = the unit + r, ur = the staged u + r,
+// where u is staged twice in a row (u[j + n] = u[j]) so that no u index
+// wraps. Every offset is a compile-time constant but the wrap of the
+// transposed read (one select).
+template <typename A, int NT, int T0, int T1>
+__device__ __forceinline__ void sym_terms(typename A::Acc& acc, const float* kr, const typename A::UT* ur,
+                                          uint32_t r) {
+    constexpr int H = NT / 2;
+#pragma unroll
+    for (int t = T0; t < T1; t++) {
+        if (t <= H) {
+            A::fma(acc, kr[t * NT], ur[t]);
+        } else {
+            const int d = t - H;
+            const float kv = kr[d * NT - d + ((int)r < d ? NT : 0)];
+            A::fma(acc, kv, ur[NT - d]);
+        }
+    }
+}
+
 template <int NT, typename A>
-__global__ void __launch_bounds__(17 * 32, 1) afm_wpg_kernel(SegArgs a, RingLayout L, GroupGeom G, uint32_t n_rt) {
+__global__ void __launch_bounds__((A::kWpgWarps + 1) * 32, 1)
+    afm_wpg_kernel(SegArgs a, RingLayout L, GroupGeom G, uint32_t n_rt) {
     using KT = typename A::KT;
     using UT = typename A::UT;
     using VT = typename A::VT;
@@ -480,7 +540,7 @@ __global__ void __launch_bounds__(17 * 32, 1) afm_wpg_kernel(SegArgs a, RingLayo
     uint64_t* empty = full + L.stages;
     volatile int* abort = reinterpret_cast<volatile int*>(empty + L.stages);
     volatile uint32_t* tag = reinterpret_cast<volatile uint32_t*>(smem + L.tags_offset());
-    const uint32_t ub = wpg_ubuf_bytes(n, sizeof(UT));
+    const uint32_t ub = wpg_ubuf_bytes(A::kSym ? 2 * n : n, sizeof(UT));
     unsigned char* ubase = smem + L.ubuf_offset();                 // [ng][2] u buffers
     Acc* pbase = reinterpret_cast<Acc*>(ubase + (size_t)G.ng * 2 * ub);  // [ng][2][gc-1][n] partials
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -553,7 +613,11 @@ __global__ void __launch_bounds__(17 * 32, 1) afm_wpg_kernel(SegArgs a, RingLayo
     uint32_t i = grp;
     if (gatherer && i < cnt) {
         dof_c = map_at(i);
-        if (rvalid) ubuf(0)[r] = A::stage(load_u_hint(u, dof_c, a.bc_mode, keep));
+        if (rvalid) {
+            const UT x = A::stage(load_u_hint(u, dof_c, a.bc_mode, keep));
+            ubuf(0)[r] = x;
+            if constexpr (A::kSym) ubuf(0)[r + n] = x;
+        }
         if (i + G.ng < cnt) dof_n = map_at(i + G.ng);
     }
     wait_prior_grid();
@@ -574,9 +638,54 @@ __global__ void __launch_bounds__(17 * 32, 1) afm_wpg_kernel(SegArgs a, RingLayo
             const unsigned char* ks = smem + (size_t)s * L.slot_bytes;
             const UT* uu = ubuf(par);
             if (rvalid) {
-                if constexpr (NT != 0) {
+                if constexpr (A::kSym && NT != 0) {
+                    // the column group's terms, with compile-time bounds
+                    constexpr int GR = (NT + 31) / 32;
+                    constexpr int GC = (int)wpg_gc(GR, sizeof(UT));
+                    const float* kr = reinterpret_cast<const float*>(ks) + r;
+                    const UT* ur = uu + r;
+                    if constexpr (GC == 1) {
+                        sym_terms<A, NT, 0, NT>(acc, kr, ur, r);
+                    } else if constexpr (GC == 2) {
+                        if (cg == 0)
+                            sym_terms<A, NT, 0, NT / 2>(acc, kr, ur, r);
+                        else
+                            sym_terms<A, NT, NT / 2, NT>(acc, kr, ur, r);
+                    } else {
+                        switch (cg) {
+                            case 0: sym_terms<A, NT, 0, NT / 4>(acc, kr, ur, r); break;
+                            case 1: sym_terms<A, NT, NT / 4, 2 * NT / 4>(acc, kr, ur, r); break;
+                            case 2: sym_terms<A, NT, 2 * NT / 4, 3 * NT / 4>(acc, kr, ur, r); break;
+                            default: sym_terms<A, NT, 3 * NT / 4, NT>(acc, kr, ur, r); break;
+                        }
+                    }
+                } else if constexpr (A::kSym) {
+                    // run-time n: term t <= n/2: D[t][r] u[r + t]; term t > n/2, d = t - n/2:
+                    // K(r, r - d) = D[d][(r - d) mod n] times u[r - d + n]
+                    constexpr uint32_t NS = kMaxN;
+                    constexpr uint32_t GR = (NS + 31) / 32;
+                    constexpr uint32_t GC = wpg_gc(GR, sizeof(UT));
+                    constexpr uint32_t TRIP = (NS + GC - 1) / GC;
+                    const uint32_t h = n / 2;
+#pragma unroll 4
+                    for (uint32_t j = 0; j < TRIP; j++) {
+                        const uint32_t t = cb + j;
+                        if (t < ce) {
+                            uint32_t col, k;
+                            if (t <= h) {
+                                col = r + t;
+                                k = t * n + r;
+                            } else {
+                                const uint32_t d = t - h;
+                                col = r + n - d;
+                                k = d * n + (r >= d ? r - d : r + n - d);
+                            }
+                            A::fma(acc, A::kload(ks, k, a.plane), uu[col]);
+                        }
+                    }
+                } else if constexpr (NT != 0) {
                     constexpr uint32_t GR = (NT + 31) / 32;
-                    constexpr uint32_t GC = GR >= 3 ? 1 : 4 / GR;
+                    constexpr uint32_t GC = wpg_gc(GR, sizeof(UT));
                     constexpr uint32_t TRIP = (NT + GC - 1) / GC;
 #pragma unroll
                     for (uint32_t j = 0; j < TRIP; j++) {
@@ -592,7 +701,11 @@ __global__ void __launch_bounds__(17 * 32, 1) afm_wpg_kernel(SegArgs a, RingLayo
             if (lane == 0) mbar_arrive(&empty[s]);
         }
         if (!gatherer && rvalid) pbuf(par)[(cg - 1) * n + r] = acc;
-        if (gatherer && rvalid && i + G.ng < cnt) ubuf(par ^ 1)[r] = A::stage(u_n);
+        if (gatherer && rvalid && i + G.ng < cnt) {
+            const UT x = A::stage(u_n);
+            ubuf(par ^ 1)[r] = x;
+            if constexpr (A::kSym) ubuf(par ^ 1)[r + n] = x;
+        }
         named_barrier(bar_id, bar_threads);
         if (gatherer) {
             for (uint32_t c2 = 1; c2 < G.gc; c2++) {

@@ -1,6 +1,7 @@
 // Instantiation and dispatch of the matvec kernels for one arithmetic policy
-// (included by afm_mv_fp64.cu, afm_mv_split.cu, afm_mv_fp32.cu, which define
-// ARITH and LAUNCH_FN so that the three compile in parallel).
+// (included by afm_mv_fp64.cu, afm_mv_split.cu, afm_mv_fp32.cu and
+// afm_mv_f32sym.cu, which define ARITH and LAUNCH_FN so that they compile in
+// parallel; BATCH_FN is left undefined where there is no batched product).
 #include <algorithm>
 
 #include "afm_batched.cuh"
@@ -14,7 +15,9 @@ namespace {
 // or <= kMaxN (WPE) runs the run-time-n instance (template argument 0).
 template <int NT, bool WPE, bool DUP>
 void* kernel_ptr() {
-    if constexpr (WPE) {
+    if constexpr (ARITH::kSym && (!WPE || DUP)) {
+        return nullptr;  // the symmetric arena has element units for the warp-group kernel only
+    } else if constexpr (WPE) {
         if constexpr (DUP)
             return (void*)afm_wpe_kernel<NT, ARITH, true>;
         else
@@ -47,11 +50,15 @@ void* pick_kernel(int regime, uint32_t n, bool dup) {
 }  // namespace
 
 // Ring stages that fit beside `extra` bytes: per stage the slot, two
-// mbarriers and a tag; 32 bytes for the flag word and the tags' padding.
+// mbarriers and a tag; 32 bytes for the flag word and the tags' padding. Up to
+// kMaxStages: under full load an element matrix copy takes microseconds to
+// land, and each SM needs ~200 KB of copies in flight to keep HBM busy, which
+// small slots reach only with many stages.
+constexpr uint32_t kMaxStages = 32;
 static uint32_t stages_for(uint32_t slot_bytes, uint32_t extra) {
     if (extra + 32 >= kSmemBudget) return 0;
     uint32_t st = (kSmemBudget - extra - 32) / (slot_bytes + 20);
-    return st > 16 ? 16 : st;
+    return st > kMaxStages ? kMaxStages : st;
 }
 
 // Ring layout and (for the warp-group kernel) group geometry of a segment.
@@ -64,11 +71,12 @@ static RingLayout ring_layout(const Segment& s, uint64_t copy_bytes, bool dup, G
     if (s.regime == REG_WPE && !dup) {
         GroupGeom G;
         G.gr = (s.n + 31) / 32;
-        G.gc = G.gr >= 3 ? 1 : 4 / G.gr;
+        G.gc = wpg_gc(G.gr, (uint32_t)ut);
         G.g = G.gr * G.gc;
-        const uint32_t ub = wpg_ubuf_bytes(s.n, (uint32_t)ut);
+        const uint32_t ub = wpg_ubuf_bytes(ARITH::kSym ? 2 * s.n : s.n, (uint32_t)ut);  // u staged twice (symmetric)
         const uint32_t pstride = (G.gc > 1 ? G.gc - 1 : 1) * s.n;
-        for (G.ng = 16 / G.g; G.ng >= 1; G.ng--) {
+        // element groups: up to ARITH::kWpgWarps consumer warps, at most 15 groups (one named barrier each)
+        for (G.ng = std::min<uint32_t>(ARITH::kWpgWarps / G.g, 15u); G.ng >= 1; G.ng--) {
             L.extra_bytes = G.ng * 2 * ub + G.ng * 2 * pstride * (uint32_t)acc;
             L.stages = stages_for(L.slot_bytes, L.extra_bytes);
             if (L.stages >= G.ng + 2 || G.ng == 1) break;
@@ -97,6 +105,7 @@ cudaError_t LAUNCH_FN(const Segment& s, const SegArgs& a, int sm_count, bool dup
     const RingLayout L = ring_layout(s, a.copy_bytes, dup, &G);
     if (L.stages < 2) return cudaErrorInvalidConfiguration;
     void* fn = pick_kernel(s.regime, s.n, dup);
+    if (!fn) return cudaErrorInvalidValue;
     const uint32_t smem = L.total();
     // at least 4 elements (2 thread-per-element units) per CTA: a small segment occupies few SMs
     // and leaves the rest to concurrent work (other operators' streams)
@@ -125,6 +134,7 @@ cudaError_t LAUNCH_FN(const Segment& s, const SegArgs& a, int sm_count, bool dup
     return cudaLaunchKernelExC(&cfg, fn, params);
 }
 
+#ifdef BATCH_FN
 // ---- batched (multi right-hand side) product, warp per element -------------
 
 namespace {
@@ -186,24 +196,35 @@ cudaError_t BATCH_FN(const Segment& s, const BatchArgs& a, int sm_count, int ct,
     return cudaLaunchKernelExC(&cfg, fn, params);
 }
 
+#endif  // BATCH_FN
+
 // ---- patch path (small elements) -----------------------------------------
 
 namespace {
-// consumer groups of the patch kernel for this arithmetic (see afm_patch.cuh)
-constexpr int kGroups = sizeof(typename ARITH::VT) == 4 ? 4 : 2;
+// consumer groups (G) of GW warps of the patch kernel for this arithmetic
+// (see afm_patch.cuh): FP32 tries 8 groups, then 4; 8-byte entries use 2.
+constexpr bool kF32Patch = sizeof(typename ARITH::VT) == 4;
+constexpr int kPatchGW = kF32Patch ? 2 : 4;
+constexpr uint32_t kMinPatchStages = 6;  // ring slots below which fewer groups are used
 
-void* pick_patch_kernel(uint32_t n) {
+template <int G>
+void* patch_kernel_g(uint32_t n) {
     switch (n) {
-        case 4: return (void*)afm_patch_kernel<4, ARITH, kGroups>;
-        case 8: return (void*)afm_patch_kernel<8, ARITH, kGroups>;
-        case 10: return (void*)afm_patch_kernel<10, ARITH, kGroups>;
-        default: return (void*)afm_patch_kernel<0, ARITH, kGroups>;
+        case 4: return (void*)afm_patch_kernel<4, ARITH, G, kPatchGW>;
+        case 8: return (void*)afm_patch_kernel<8, ARITH, G, kPatchGW>;
+        case 10: return (void*)afm_patch_kernel<10, ARITH, G, kPatchGW>;
+        default: return (void*)afm_patch_kernel<0, ARITH, G, kPatchGW>;
     }
 }
 
-PatchLayout patch_layout(const PatchPlanGeom& pg, uint32_t copy_bytes) {
+void* pick_patch_kernel(uint32_t n, uint32_t groups) {
+    if constexpr (kF32Patch) return groups == 8 ? patch_kernel_g<8>(n) : patch_kernel_g<4>(n);
+    else return patch_kernel_g<2>(n);
+}
+
+PatchLayout patch_layout_g(const PatchPlanGeom& pg, uint32_t copy_bytes, uint32_t groups) {
     PatchLayout L;
-    L.groups = kGroups;
+    L.groups = groups;
     L.slot_bytes = (copy_bytes + kSlotAlign - 1) / kSlotAlign * kSlotAlign;
     L.idx_bytes = patch_r16(pg.max_idx);
     L.us_bytes = patch_r16(pg.max_ndof * (uint32_t)sizeof(typename ARITH::UT));
@@ -212,9 +233,19 @@ PatchLayout patch_layout(const PatchPlanGeom& pg, uint32_t copy_bytes) {
     L.stages = 0;
     if (fixed < kSmemBudget) {
         const uint32_t st = (kSmemBudget - fixed) / (L.slot_bytes + 20);
-        L.stages = st > 16 ? 16 : st;
+        L.stages = st > kMaxStages ? kMaxStages : st;
     }
     return L;
+}
+
+PatchLayout patch_layout(const PatchPlanGeom& pg, uint32_t copy_bytes) {
+    if constexpr (kF32Patch) {
+        const PatchLayout L8 = patch_layout_g(pg, copy_bytes, 8);
+        if (L8.stages >= kMinPatchStages) return L8;
+        return patch_layout_g(pg, copy_bytes, 4);
+    } else {
+        return patch_layout_g(pg, copy_bytes, 2);
+    }
 }
 }  // namespace
 
@@ -224,7 +255,7 @@ cudaError_t PATCH_FN(const PatchPlanGeom& pg, const PatchArgs& a, int sm_count, 
     if (L.stages < 2 || pg.n == 0 || pg.n > kPatchMaxN) return cudaErrorInvalidConfiguration;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(a.count < (uint32_t)sm_count ? a.count : (uint32_t)sm_count);
-    cfg.blockDim = dim3(kPatchThreads);
+    cfg.blockDim = dim3((L.groups * kPatchGW + 1) * 32);
     cfg.dynamicSmemBytes = L.total();
     cfg.stream = stream;
     cudaLaunchAttribute attr[1];
@@ -235,7 +266,7 @@ cudaError_t PATCH_FN(const PatchPlanGeom& pg, const PatchArgs& a, int sm_count, 
     PatchArgs args = a;
     uint32_t n_rt = pg.n;
     void* params[] = {&args, &L, &n_rt};
-    return cudaLaunchKernelExC(&cfg, pick_patch_kernel(pg.n), params);
+    return cudaLaunchKernelExC(&cfg, pick_patch_kernel(pg.n, L.groups), params);
 }
 
 size_t PATCH_SMEM_FN(const PatchPlanGeom& pg, uint32_t copy_bytes) {
@@ -252,15 +283,18 @@ cudaError_t CONFIG_FN() {
         for (uint32_t nn : {4u, 8u, 10u, 20u, 24u, 30u, 60u, 0u})
             for (int d = 0; d < 2; d++) {
                 void* f = pick_kernel(reg, nn == 0 ? 7u : nn, d != 0);
+                if (!f) continue;
                 cudaError_t e =
                     cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kSmemBudget + 1024));
                 if (e != cudaSuccess) return e;
             }
-    for (uint32_t nn : {4u, 8u, 10u, 0u}) {
-        cudaError_t e = cudaFuncSetAttribute(pick_patch_kernel(nn), cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)(kSmemBudget + 1024));
-        if (e != cudaSuccess) return e;
-    }
+    for (uint32_t nn : {4u, 8u, 10u, 0u})
+        for (uint32_t gg : {2u, 4u, 8u}) {
+            cudaError_t e = cudaFuncSetAttribute(pick_patch_kernel(nn, gg),
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kSmemBudget + 1024));
+            if (e != cudaSuccess) return e;
+        }
+#ifdef BATCH_FN
     const int tiles[4][2] = {{2, 8}, {4, 4}, {4, 8}, {6, 8}};
     for (const auto& t : tiles)
         for (uint32_t nn : {24u, 7u}) {
@@ -268,6 +302,7 @@ cudaError_t CONFIG_FN() {
                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kSmemBudget + 1024));
             if (e != cudaSuccess) return e;
         }
+#endif
     return cudaSuccess;
 }
 

@@ -10,32 +10,36 @@
 //   slot[...]            slot[csr_off[d] .. csr_off[d+1]), each r * cap + e
 //                        (row r of element slot e; cap = 32 units)
 // and the patch's Ke as units of 32 element slots in the thread-per-element
-// layout (entry (r, c) of slot l at (r n + c) 32 + l; empty slots are zero).
+// layout (entry (r, c) of slot l at (r n + c) 32 + l, or at the packed
+// triangle index for the symmetric inner arena; empty slots are zero). The
+// patch's units start at unit0 of whichever arena the launch streams.
 //
-// CTA = G consumer groups of 8 / G warps + 1 producer warp; group g takes the
+// CTA = G consumer groups of GW warps + 1 producer warp; group g takes the
 // CTA's patches g, g + G, ... (G patches in flight per SM, so one patch's
 // gather and reduce latency hides behind the others' products). The producer's elected lane copies each
 // patch's index block into the group's buffer (one bulk copy) and streams
 // its Ke units through the shared ring. A group: gathers u of the patch's
 // DoFs into shared memory once; each lane multiplies one element slot and
 // writes its n products to a shared buffer; then each DoF sums its
-// contributions in the stored order and does one v = v_old + sum. No atomics;
-// the order of every sum is fixed by the index block, so v is
-// bit-reproducible. u and v cross HBM about once per patch instead of once
-// per element colour.
+// contributions in the stored order and adds the sum to v at L2 (red.add,
+// one per DoF and colour: no two patches of a colour share a DoF, so no
+// update races). The order of every sum is fixed by the index block and the
+// colour order, so v is bit-reproducible. u and v cross HBM about once per
+// patch instead of once per element colour.
 #pragma once
 
 #include "afm_matvec.cuh"
 
 namespace afm {
 
-// 8 consumer warps in G groups: G = 4 groups of 2 warps when a unit is small
-// enough (FP32, 12.8 KB for n = 10) that the ring holds several patches; G = 2
-// groups of 4 warps for 8-byte entries, whose ring holds about two patches.
-constexpr uint32_t kPatchConsumerWarps = 8;
-constexpr uint32_t kPatchThreads = kPatchConsumerWarps * 32 + 32;
-constexpr uint32_t kPatchMaxGroups = 4;
-constexpr int kBatch = 8;  // global loads a thread keeps in flight in the gather and the update
+// G consumer groups of GW warps: FP32 runs 8 groups of 2 warps (or 4 when
+// the shared memory of 8 would leave the ring too few slots), 8-byte entries
+// 2 groups of 4 warps, whose 25.6 KB units fill the ring with about two
+// patches. A group's patch passes through phases bound by memory latency
+// (the index block, the gather of u), so the patches in flight per SM, not
+// the multiply, set the kernel's pace.
+constexpr uint32_t kPatchMaxGroups = 8;
+constexpr int kBatch = 8;  // global loads a thread keeps in flight in the gather
 
 // Shared-memory layout: ring slots, mbarriers (full[S], empty[S], idx_full[4],
 // idx_empty[4]) and the abort flag, the slot tags (ring_wait), then per group:
@@ -52,10 +56,19 @@ struct PatchLayout {
     __host__ __device__ uint32_t total() const { return group_offset() + groups * group_bytes(); }
 };
 
-template <int NT, typename A, int G>
-__global__ void __launch_bounds__(kPatchThreads, 1) afm_patch_kernel(PatchArgs a, PatchLayout L, uint32_t n_rt) {
+// v[i] += x at L2, round to nearest (the f32 form flushes subnormal values
+// to zero)
+__device__ __forceinline__ void red_add(float* p, float x) {
+    asm volatile("red.global.add.f32 [%0], %1;" ::"l"(p), "f"(x) : "memory");
+}
+__device__ __forceinline__ void red_add(double* p, double x) {
+    asm volatile("red.global.add.f64 [%0], %1;" ::"l"(p), "d"(x) : "memory");
+}
+
+template <int NT, typename A, int G, int GW>
+__global__ void __launch_bounds__((G * GW + 1) * 32, 1) afm_patch_kernel(PatchArgs a, PatchLayout L, uint32_t n_rt) {
     constexpr uint32_t kPatchGroups = G;
-    constexpr uint32_t kPatchGroupWarps = kPatchConsumerWarps / G;
+    constexpr uint32_t kPatchGroupWarps = GW;
     constexpr uint32_t kPatchGroupThreads = kPatchGroupWarps * 32;
     using KT = typename A::KT;
     using UT = typename A::UT;
@@ -114,7 +127,7 @@ __global__ void __launch_bounds__(kPatchThreads, 1) afm_patch_kernel(PatchArgs a
                     }
                     tag[s] = issued;
                     mbar_arrive_expect_tx(&full[s], a.copy_bytes);
-                    bulk_load(smem + (size_t)s * L.slot_bytes, a.ke + d.ke_off + (uint64_t)u * a.unit_bytes,
+                    bulk_load(smem + (size_t)s * L.slot_bytes, a.ke + (uint64_t)(d.unit0 + u) * a.unit_bytes,
                               a.copy_bytes, &full[s], pol);
                     issued++;
                 }
@@ -203,7 +216,8 @@ __global__ void __launch_bounds__(kPatchThreads, 1) afm_patch_kernel(PatchArgs a
                         typename A::Acc acc = A::zero();
 #pragma unroll
                         for (int c = 0; c < NM; c++)
-                            if (c < (int)n) A::fma(acc, A::kload(ks, (size_t)(r * n + c) * 32u + lane, a.plane), ul[c]);
+                            if (c < (int)n) A::fma(acc, A::kload(ks, (size_t)tpe_entry<A>(r, c, n) * 32u + lane, a.plane),
+                                              ul[c]);
                         ve[r * cap + e] = acc;
                     }
                 }
@@ -213,31 +227,20 @@ __global__ void __launch_bounds__(kPatchThreads, 1) afm_patch_kernel(PatchArgs a
         }
         named_barrier(bar_id, kPatchGroupThreads);
 
-        // each DoF sums its contributions in stored order; one v update
+        // each DoF sums its contributions in stored order; one v update, as
+        // a reduction performed at L2 (red.add: no load, no wait). Patches of
+        // one colour share no DoF and colour launches are ordered, so every v
+        // entry still receives v + sum once per colour, in colour order.
         if (!waited_prior) {
             wait_prior_grid();
             waited_prior = true;
         }
         if (iok && !*abort)
-            for (uint32_t i0 = t; i0 < d.ndof; i0 += kPatchGroupThreads * kBatch) {
-                uint32_t gi[kBatch];
-                VT old[kBatch];
-#pragma unroll
-                for (int q = 0; q < kBatch; q++) {
-                    const uint32_t i = i0 + q * kPatchGroupThreads;
-                    gi[q] = i < d.ndof ? (glob[i] & kDofMask) : 0u;
-                    old[q] = i < d.ndof ? ld_hint(v + gi[q], keep) : VT(0);
-                }
-#pragma unroll
-                for (int q = 0; q < kBatch; q++) {
-                    const uint32_t i = i0 + q * kPatchGroupThreads;
-                    if (i < d.ndof) {
-                        Acc sum = A::zero();
-                        const uint32_t q1 = coff[i + 1];
-                        for (uint32_t c = coff[i]; c < q1; c++) A::combine(sum, ve[slot[c]]);
-                        st_hint(v + gi[q], old[q] + A::finish(sum), keep);
-                    }
-                }
+            for (uint32_t i = t; i < d.ndof; i += kPatchGroupThreads) {
+                Acc sum = A::zero();
+                const uint32_t q1 = coff[i + 1];
+                for (uint32_t c = coff[i]; c < q1; c++) A::combine(sum, ve[slot[c]]);
+                red_add(v + (glob[i] & kDofMask), A::finish(sum));
             }
         named_barrier(bar_id, kPatchGroupThreads);
         if (t == 0) mbar_arrive(&idx_empty[g]);

@@ -18,15 +18,22 @@ namespace afm {
 
 namespace {
 
+// Sum over the block in a fixed tree: shuffles within each warp, then over
+// the warps' sums (sh holds at least 33 doubles).
 __device__ __forceinline__ double block_sum(double x, double* sh) {
-    const int t = threadIdx.x;
-    sh[t] = x;
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if (lane == 0) sh[w] = x;
     __syncthreads();
-    for (int s = kRedThreads / 2; s > 0; s >>= 1) {
-        if (t < s) sh[t] += sh[t + s];
-        __syncthreads();
+    if (w == 0) {
+        double r = lane < kRedThreads / 32 ? sh[lane] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(0xffffffffu, r, o);
+        if (lane == 0) sh[32] = r;
     }
-    const double r = sh[0];
+    __syncthreads();
+    const double r = sh[32];
     __syncthreads();
     return r;
 }
@@ -39,32 +46,68 @@ __device__ __forceinline__ double final_sum(const double* part, double* sh, uint
 
 #define kStride ((size_t)gridDim.x * kRedThreads)
 
+// Dot-product accumulators of one thread. FP64 vectors: FP64 fused
+// multiply-adds. FP32 vectors: compensated FP32 arithmetic (Ogita, Rump &
+// Oishi, "Accurate sum and dot product", 2005, Dot2: TwoProduct by FMA and
+// TwoSum, about twice FP32 precision per thread), which keeps the FP32
+// recursion off GB300's FP64 pipe (1/64 of the FP32 rate). The _rn intrinsics
+// keep the compiler from fusing the steps.
+template <typename T>
+struct DotAcc;
+template <>
+struct DotAcc<double> {
+    double s = 0.0;
+    __device__ __forceinline__ void add(double x, double y) { s = __fma_rn(x, y, s); }
+    __device__ __forceinline__ double value() const { return s; }
+};
+template <>
+struct DotAcc<float> {
+    float hi = 0.0f, lo = 0.0f;
+    __device__ __forceinline__ void add(float x, float y) {
+        const float p = __fmul_rn(x, y);
+        const float e = __fmaf_rn(x, y, -p);
+        const float t = __fadd_rn(hi, p);
+        const float bp = __fsub_rn(t, hi);
+        const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+        hi = t;
+        lo = __fadd_rn(lo, __fadd_rn(err, e));
+    }
+    __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+
+// Strided loops visit i = i0, i0 + stride, ... in index order; kUnroll of
+// them load before any is used, so that each thread keeps several memory
+// requests in flight (the order of every sum is unchanged).
+constexpr int kUnroll = 4;
+
+
+
 template <typename T>
 __global__ void __launch_bounds__(kRedThreads) k_set_constrained(T* v, const T* u, const uint32_t* idx, uint32_t n) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k < n) v[idx[k]] = u[idx[k]];
 }
 
-// part[j*kRedBlocks + block]: partial sums of a.b, a.a, b.b
+// part[block]: partial sums of a.b
 template <typename T>
-__global__ void __launch_bounds__(kRedThreads) k_dots(const T* __restrict__ a, const T* __restrict__ b, size_t n,
-                                                      double* part) {
+__global__ void __launch_bounds__(kRedThreads) k_dot(const T* __restrict__ a, const T* __restrict__ b, size_t n,
+                                                     double* part) {
     __shared__ double sh[kRedThreads];
-    double ab = 0.0, aa = 0.0, bb = 0.0;
-    for (size_t i = (size_t)blockIdx.x * kRedThreads + threadIdx.x; i < n; i += kStride) {
-        const double x = a[i], y = b[i];
-        ab = __fma_rn(x, y, ab);
-        aa = __fma_rn(x, x, aa);
-        bb = __fma_rn(y, y, bb);
+    DotAcc<T> ab;
+    size_t i = (size_t)blockIdx.x * kRedThreads + threadIdx.x;
+    for (; i + (kUnroll - 1) * kStride < n; i += kUnroll * kStride) {
+        T x[kUnroll], y[kUnroll];
+#pragma unroll
+        for (int q = 0; q < kUnroll; q++) {
+            x[q] = a[i + q * kStride];
+            y[q] = b[i + q * kStride];
+        }
+#pragma unroll
+        for (int q = 0; q < kUnroll; q++) ab.add(x[q], y[q]);
     }
-    ab = block_sum(ab, sh);
-    aa = block_sum(aa, sh);
-    bb = block_sum(bb, sh);
-    if (threadIdx.x == 0) {
-        part[blockIdx.x] = ab;
-        part[kRedBlocks + blockIdx.x] = aa;
-        part[2 * kRedBlocks + blockIdx.x] = bb;
-    }
+    for (; i < n; i += kStride) ab.add(a[i], b[i]);
+    const double s = block_sum(ab.value(), sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = s;
 }
 
 // r = b - q, z = dinv r, p = z; partials of r.z, r.r, z.z, b.b, (dinv b).(dinv b)
@@ -205,24 +248,33 @@ __global__ void __launch_bounds__(kRedThreads) k_cg_update(T* __restrict__ x, T*
                                                            double* part) {
     __shared__ double sh[kRedThreads];
     const T alpha = (T)sc[S_ALPHA];
-    double rz = 0, rr = 0, zz = 0;
-    for (size_t i = (size_t)blockIdx.x * kRedThreads + threadIdx.x; i < n; i += kStride) {
-        x[i] = alpha * p[i] + x[i];
-        const T ri = -alpha * q[i] + r[i];
-        const T zi = dinv[i] * ri;
+    DotAcc<T> rz, rr, zz;
+    auto step = [&](size_t i, T xi, T pi, T qi, T ri0, T di) {
+        x[i] = alpha * pi + xi;
+        const T ri = -alpha * qi + ri0;
+        const T zi = di * ri;
         r[i] = ri;
         z[i] = zi;
-        rz = __fma_rn((double)ri, (double)zi, rz);
-        rr = __fma_rn((double)ri, (double)ri, rr);
-        zz = __fma_rn((double)zi, (double)zi, zz);
+        rz.add(ri, zi);
+        rr.add(ri, ri);
+        zz.add(zi, zi);
+    };
+    size_t i = (size_t)blockIdx.x * kRedThreads + threadIdx.x;
+    for (; i + (kUnroll - 1) * kStride < n; i += kUnroll * kStride) {
+        T xv[kUnroll], pv[kUnroll], qv[kUnroll], rv[kUnroll], dv[kUnroll];
+#pragma unroll
+        for (int k = 0; k < kUnroll; k++) {
+            const size_t j = i + k * kStride;
+            xv[k] = x[j], pv[k] = p[j], qv[k] = q[j], rv[k] = r[j], dv[k] = dinv[j];
+        }
+#pragma unroll
+        for (int k = 0; k < kUnroll; k++) step(i + k * kStride, xv[k], pv[k], qv[k], rv[k], dv[k]);
     }
-    rz = block_sum(rz, sh);
-    rr = block_sum(rr, sh);
-    zz = block_sum(zz, sh);
-    if (threadIdx.x == 0) {
-        part[blockIdx.x] = rz;
-        part[kRedBlocks + blockIdx.x] = rr;
-        part[2 * kRedBlocks + blockIdx.x] = zz;
+    for (; i < n; i += kStride) step(i, x[i], p[i], q[i], r[i], dinv[i]);
+    const double v[3] = {rz.value(), rr.value(), zz.value()};
+    for (int j = 0; j < 3; j++) {
+        const double t = block_sum(v[j], sh);
+        if (threadIdx.x == 0) part[j * kRedBlocks + blockIdx.x] = t;
     }
 }
 
@@ -313,12 +365,6 @@ cudaError_t launch_set_constrained(T* v, const T* u, const uint32_t* idx, uint32
 }
 
 template <typename T>
-cudaError_t launch_dots(const T* a, const T* b, size_t n, double* part, cudaStream_t st) {
-    k_dots<T><<<red_blocks(n), kRedThreads, 0, st>>>(a, b, n, part);
-    return cudaGetLastError();
-}
-
-template <typename T>
 cudaError_t launch_cg_init(const T* b, const T* q, const T* dinv, T* r, T* z, T* p, size_t n, double* sc,
                            double* part, cudaStream_t st) {
     const uint32_t nb = red_blocks(n);
@@ -330,7 +376,7 @@ cudaError_t launch_cg_init(const T* b, const T* q, const T* dinv, T* r, T* z, T*
 template <typename T>
 cudaError_t launch_cg_alpha(const T* p, const T* q, size_t n, double* sc, double* part, cudaStream_t st) {
     const uint32_t nb = red_blocks(n);
-    k_dots<T><<<nb, kRedThreads, 0, st>>>(p, q, n, part);
+    k_dot<T><<<nb, kRedThreads, 0, st>>>(p, q, n, part);
     k_cg_alpha<<<1, kRedThreads, 0, st>>>(sc, part, nb);
     return cudaGetLastError();
 }
@@ -354,7 +400,7 @@ cudaError_t launch_invert(T* dinv, const double* d, size_t n, cudaStream_t st) {
 template <typename T>
 cudaError_t launch_norm2(const T* a, size_t n, double* sc, double* part, cudaStream_t st) {
     const uint32_t nb = red_blocks(n);
-    k_dots<T><<<nb, kRedThreads, 0, st>>>(a, a, n, part);
+    k_dot<T><<<nb, kRedThreads, 0, st>>>(a, a, n, part);
     k_sum<<<1, kRedThreads, 0, st>>>(sc, part, nb);
     return cudaGetLastError();
 }
@@ -385,7 +431,6 @@ cudaError_t launch_add_f32(double* x, float* d, size_t n, cudaStream_t st) {
 
 #define AFM_SOLVER_INSTANCES(T)                                                                                       \
     template cudaError_t launch_set_constrained<T>(T*, const T*, const uint32_t*, uint32_t, cudaStream_t);            \
-    template cudaError_t launch_dots<T>(const T*, const T*, size_t, double*, cudaStream_t);                           \
     template cudaError_t launch_cg_init<T>(const T*, const T*, const T*, T*, T*, T*, size_t, double*, double*,        \
                                            cudaStream_t);                                                             \
     template cudaError_t launch_cg_alpha<T>(const T*, const T*, size_t, double*, double*, cudaStream_t);              \

@@ -35,11 +35,10 @@ enum : int {
 constexpr int kPartialSlots = 5 * kRedBlocks;
 
 // T = double (FP64 CG) or float (inner CG of the mixed-precision solve);
-// dot products and scalars are FP64 in both.
+// step scalars are FP64 in both; dot products accumulate in FP64 (double) or
+// in compensated FP32 (float) and are reduced across threads in FP64.
 template <typename T>
 cudaError_t launch_set_constrained(T* v, const T* u, const uint32_t* idx, uint32_t n, cudaStream_t st);
-template <typename T>
-cudaError_t launch_dots(const T* a, const T* b, size_t n, double* part, cudaStream_t st);
 template <typename T>
 cudaError_t launch_cg_init(const T* b, const T* q, const T* dinv, T* r, T* z, T* p, size_t n, double* sc,
                            double* part, cudaStream_t st);

@@ -274,6 +274,38 @@ def measure_e2e(A, u_host, v_dev, steps, world):
     return e2e_s
 
 
+def measure_inner_f32(A, m, steps, warmup):
+    """FP32 products of the split operator (the inner matvec of the mixed-precision solve): from the
+    symmetric copy (each pair of entries once) and from the hi plane; GB/s over the bytes streamed."""
+    import torch
+    stream_ptr = A.stream()
+    stream = torch.cuda.ExternalStream(stream_ptr)
+    u = torch.tensor(np.random.default_rng(99).uniform(-1, 1, m.n_dofs), dtype=torch.float32, device="cuda")
+    v = torch.empty_like(u)
+    base = 4 * m.n_elem * m.ndpe + 8 * m.n_dofs  # map entries, u read, v written
+    out = {}
+    for sym in (1, 0):
+        A.set_symmetric_inner(sym)
+        for _ in range(warmup):
+            A.matvec_device_f32(v.data_ptr(), u.data_ptr(), stream_ptr)
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(steps):
+            A.matvec_device_f32(v.data_ptr(), u.data_ptr(), stream_ptr)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        ms = ev0.elapsed_time(ev1) / steps
+        info = A.info()
+        ke = info["sym_bytes"] if sym else info["ke_bytes"] // 2
+        if sym and not ke:
+            continue  # no symmetric copy for this operator
+        out["symmetric_copy" if sym else "hi_plane"] = {
+            "ms": ms, "ke_bytes": ke, "streamed_gbs": (ke + base) / (ms * 1e-3) / 1e9}
+    A.set_symmetric_inner(1)
+    return out
+
+
 def run_ours(args, w, rank, world, local_rank):
     import torch
     dev = local_rank
@@ -291,6 +323,7 @@ def run_ours(args, w, rank, world, local_rank):
         e2e_s = measure_e2e(A, u_host, v, args.steps, world)
         e2e = {"value": alg * world * args.steps / e2e_s / 1e9, "unit": "GB/s", "h2d_bytes_per_step": 8 * n,
                "d2h_bytes_per_step": 8 * n}
+    inner = measure_inner_f32(A, m, args.steps, args.warmup) if info["precision"] == 1 else None
     native = None
     if args.also_native and info["precision"] == 1:
         # the same workload in native FP64 arithmetic, for comparison
@@ -326,6 +359,8 @@ def run_ours(args, w, rank, world, local_rank):
     }
     if native:
         out["fp64_native"] = native
+    if inner:
+        out["fp32_inner_products"] = inner
     clk_sum = clk.summary() if clk else None
     if clk_sum:
         out["clocks"] = clk_sum
@@ -391,6 +426,8 @@ def run_solve(args, w, rank, world, local_rank):
            "config": {"workload": w["desc"], "n_dofs": m.n_dofs, "n_elements": m.n_elem, "rtol": rtol,
                       "inner_rtol": args.inner_rtol},
            "mixed": {"solves_per_s": smx, "inner_iterations": stm.iterations, "refinements": stm.refinements,
+                     "inner_ke_bytes": A.info()["sym_bytes"] or A.info()["ke_bytes"] // 2,
+                     "inner_arena": "symmetric FP32 copy" if A.info()["sym_bytes"] else "hi plane",
                      "rel_residual": stm.rel_residual,
                      "rel_error_vs_fp64_solution": float(np.linalg.norm(xm - x64) / np.linalg.norm(x64))},
            "fp64": {"solves_per_s": s64, "iterations": st.iterations, "rel_residual": st.rel_residual,

@@ -101,6 +101,9 @@ typedef struct afm_info {
     uint32_t n_patches;         /* small-element patches (0: colour segments) */
     uint32_t n_patch_colors;    /* colours of the patch conflict graph */
     uint64_t patch_index_bytes; /* device bytes of the patch index blocks */
+    int ke_symmetric;           /* every Ke symmetric (FP64_SPLIT operators; 0 otherwise) */
+    int sym_available;          /* the symmetric inner arena can serve FP32 products */
+    uint64_t sym_bytes;         /* device bytes of that arena once built (0: not built) */
 } afm_info;
 
 typedef struct afm_solve_stats {
@@ -133,6 +136,17 @@ int afm_set_precision(afm_operator* op, int precision);
  * elements. Both are deterministic and agree within rounding. Takes effect at
  * the next afm_finalize. */
 int afm_set_patch_mode(afm_operator* op, int enable);
+/* FP32 products of an FP64_SPLIT operator (no counterpart in the reference):
+ * enable = 1 (default) lets them stream a symmetric copy of the FP32 element
+ * matrices that stores each pair K(i, j), K(j, i) once, about 55% of the
+ * bytes of the hi plane, when every Ke is symmetric (to 1e-6 of its largest
+ * diagonal entry; the copy holds the rounded symmetric part) and the elements
+ * run as patches or have more than 16 DoFs. The copy is built on the device
+ * from the split arena by the first FP32 product or mixed-precision solve
+ * (outside any stream capture) and costs another ~28% of the split arena's
+ * memory. FP64 products never use it. enable = 0: FP32 products read the hi
+ * plane. Takes effect at the next FP32 product. */
+int afm_set_symmetric_inner(afm_operator* op, int enable);
 
 /* ---- maps (par::Maps) --------------------------------------------------- */
 

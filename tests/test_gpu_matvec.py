@@ -316,3 +316,59 @@ def test_patch_path_against_oracle(gpu, kind, shape, jitter, prec):
         A.matvec_device_f32(dv32.data_ptr(), du32.data_ptr())
         A.synchronize()
         assert rel(dv32.double().cpu().numpy(), vo) < FP32_RTOL
+
+
+@pytest.mark.parametrize("kind,n,ngt", [
+    (P.HEX8_POISSON, 20, 2), (P.TET10_POISSON, 12, 2), (P.HEX8_ELASTIC, 10, 2), (P.TET10_ELASTIC, 6, 2),
+    (P.HEX20_ELASTIC, 6, 3),
+])
+def test_symmetric_inner_arena(gpu, kind, n, ngt):
+    """FP32 products of a split operator stream the symmetric copy (each pair
+    of entries once) when every Ke is symmetric: against the FP64 product, the
+    hi-plane product, and itself on a second call."""
+    import torch
+    m = P.Mesh(kind, n, jitter=0.12, seed=6)
+    ke = m.element_matrices(ngt=ngt)
+    maps = Maps()
+    maps.set_map(m.n_elem, m.dof_map(), m.ndpe, m.n_dofs)
+    A = aMatFree(maps)
+    A.set_precision(PRECISION.FP64_SPLIT)
+    A.set_element_matrices(0, ke)
+    A.finalize()
+    info = A.info()
+    assert info["ke_symmetric"] == 1 and info["sym_available"] == 1 and info["sym_bytes"] == 0
+    u = np.random.default_rng(7).uniform(-1, 1, m.n_dofs)
+    v64 = np.empty(m.n_dofs)
+    A.matvec(v64, u, True)
+    du = torch.tensor(u, dtype=torch.float32, device="cuda")
+    dv1, dv2, dh = torch.empty_like(du), torch.empty_like(du), torch.empty_like(du)
+    torch.cuda.synchronize()
+    A.matvec_device_f32(dv1.data_ptr(), du.data_ptr())
+    A.matvec_device_f32(dv2.data_ptr(), du.data_ptr())
+    A.synchronize()
+    # the hi plane is half of the split arena; the symmetric copy about 55% of that
+    assert 0 < A.info()["sym_bytes"] < 0.29 * info["ke_bytes"]
+    assert torch.equal(dv1, dv2)
+    assert rel(dv1.double().cpu().numpy(), v64) < FP32_RTOL
+    A.set_symmetric_inner(0)
+    assert A.info()["sym_available"] == 0 and A.info()["sym_bytes"] == 0
+    A.matvec_device_f32(dh.data_ptr(), du.data_ptr())
+    A.synchronize()
+    assert rel(dh.double().cpu().numpy(), v64) < FP32_RTOL
+    assert rel(dv1.double().cpu().numpy(), dh.double().cpu().numpy()) < 2e-6
+
+
+def test_symmetric_inner_needs_symmetric_ke(gpu):
+    """A non-symmetric element matrix keeps FP32 products on the hi plane."""
+    import torch
+    g = load("mixed_random")
+    A = make_operator(g, 0, PRECISION.FP64_SPLIT)
+    info = A.info()
+    assert info["ke_symmetric"] == 0 and info["sym_available"] == 0
+    u = torch.tensor(g["u"], dtype=torch.float32, device="cuda")
+    v = torch.empty_like(u)
+    torch.cuda.synchronize()
+    A.matvec_device_f32(v.data_ptr(), u.data_ptr())
+    A.synchronize()
+    assert A.info()["sym_bytes"] == 0
+    assert rel(v.cpu().double().numpy(), g["matvec"]) < FP32_RTOL
