@@ -132,9 +132,10 @@ class aMatFree:
         """Small elements as shared-memory patches (1, default) or one launch per colour (0)."""
         check(self._lib.afm_set_patch_mode(self._h, int(bool(enable))), "afm_set_patch_mode")
 
-    def set_symmetric_inner(self, enable):
-        """FP32 products stream the symmetric copy of the element matrices (1, default) or the hi plane (0)."""
-        check(self._lib.afm_set_symmetric_inner(self._h, int(bool(enable))), "afm_set_symmetric_inner")
+    def set_symmetric_inner(self, fmt):
+        """Inner format of FP32 products: 1 (default) symmetric copy in FP32, 2 symmetric copy in FP32 + BF16
+        correction with FP64 sums, 0 the hi plane."""
+        check(self._lib.afm_set_symmetric_inner(self._h, int(fmt)), "afm_set_symmetric_inner")
 
     def set_element_matrix(self, eid, e_mat, block_i=0, block_j=0, blocks_dim=1):
         """aMatFree::set_element_matrix (include/aMatFree.hpp:856-880)."""

@@ -53,6 +53,13 @@ cudaError_t launch_segment_f32sym(const Segment& s, const SegArgs& a, int sm_cou
 cudaError_t launch_patches_f32sym(const PatchPlanGeom& pg, const PatchArgs& a, int sm_count, bool pdl,
                                   cudaStream_t st);
 cudaError_t configure_kernels_f32sym();
+cudaError_t launch_segment_f32symx(const Segment& s, const SegArgs& a, int sm_count, bool dup, bool pdl,
+                                   cudaStream_t st);
+cudaError_t launch_patches_f32symx(const PatchPlanGeom& pg, const PatchArgs& a, int sm_count, bool pdl,
+                                   cudaStream_t st);
+cudaError_t configure_kernels_f32symx();
+size_t patch_smem_f32symx(const PatchPlanGeom& pg, uint32_t copy_bytes);
+size_t segment_smem_f32symx(const Segment& s);
 size_t patch_smem_f32sym(const PatchPlanGeom& pg, uint32_t copy_bytes);
 size_t segment_smem_f32sym(const Segment& s);
 size_t patch_smem_fp64(const PatchPlanGeom& pg, uint32_t copy_bytes);
@@ -65,6 +72,7 @@ cudaError_t launch_patches(int prec, const PatchPlanGeom& pg, const PatchArgs& a
         case AFM_PREC_FP64: return launch_patches_fp64(pg, a, sm_count, pdl, stream);
         case AFM_PREC_FP64_SPLIT: return launch_patches_split(pg, a, sm_count, pdl, stream);
         case kPrecF32Sym: return launch_patches_f32sym(pg, a, sm_count, pdl, stream);
+        case kPrecF32SymX: return launch_patches_f32symx(pg, a, sm_count, pdl, stream);
         default: return launch_patches_fp32(pg, a, sm_count, pdl, stream);
     }
 }
@@ -74,6 +82,7 @@ size_t patch_smem_bytes(int prec, const PatchPlanGeom& pg, uint32_t copy_bytes) 
         case AFM_PREC_FP64: return patch_smem_fp64(pg, copy_bytes);
         case AFM_PREC_FP64_SPLIT: return patch_smem_split(pg, copy_bytes);
         case kPrecF32Sym: return patch_smem_f32sym(pg, copy_bytes);
+        case kPrecF32SymX: return patch_smem_f32symx(pg, copy_bytes);
         default: return patch_smem_fp32(pg, copy_bytes);
     }
 }
@@ -88,6 +97,7 @@ cudaError_t launch_segment(const Segment& s, int prec, const SegArgs& a, int sm_
         case AFM_PREC_FP64: return launch_segment_fp64(s, a, sm_count, dup, pdl, stream);
         case AFM_PREC_FP64_SPLIT: return launch_segment_split(s, a, sm_count, dup, pdl, stream);
         case kPrecF32Sym: return launch_segment_f32sym(s, a, sm_count, dup, pdl, stream);
+        case kPrecF32SymX: return launch_segment_f32symx(s, a, sm_count, dup, pdl, stream);
         default: return launch_segment_fp32(s, a, sm_count, dup, pdl, stream);
     }
 }
@@ -97,6 +107,7 @@ size_t segment_smem_bytes(const Segment& s, int prec) {
         case AFM_PREC_FP64: return segment_smem_fp64(s);
         case AFM_PREC_FP64_SPLIT: return segment_smem_split(s);
         case kPrecF32Sym: return segment_smem_f32sym(s);
+        case kPrecF32SymX: return segment_smem_f32symx(s);
         default: return segment_smem_fp32(s);
     }
 }
@@ -202,6 +213,7 @@ void free_device(afm_operator* op) {
     dfree(op, op->d_patch_desc);
     dfree(op, op->d_patch_idx);
     dfree(op, op->d_sym);
+    dfree(op, op->d_vx);
     op->work_elems = 0;
     op->work32_elems = 0;
 }
@@ -432,8 +444,6 @@ bool build_patch_plan(afm_operator* op, uint32_t n, int prec, std::vector<PatchD
     s.count = (uint32_t)(units * kTpeWidth);
     s.ke_offset = 0;
     s.map_offset = 0;
-    s.sym_offset = 0;
-    s.sym_unit_bytes = (uint64_t)n * (n + 1) / 2 * kTpeWidth * 4;  // packed triangle, 16-byte multiple
 
     // element slots and index blocks
     std::vector<uint8_t> is_bc(ND, 0);
@@ -496,7 +506,7 @@ void build_segments(afm_operator* op, int prec) {
 
     op->segs.clear();
     const size_t eb = entry_bytes(prec);
-    uint64_t ke_off = 0, map_off = 0, sym_off = 0;
+    uint64_t ke_off = 0, map_off = 0;
     for (uint32_t p = 0; p < op->n_elem;) {
         const uint32_t e = op->perm[p];
         Segment s;
@@ -528,10 +538,6 @@ void build_segments(afm_operator* op, int prec) {
         }
         s.ke_offset = ke_off;
         s.map_offset = map_off;
-        // symmetric inner arena: n/2 + 1 wrapped diagonals per element (warp-group kernel only)
-        s.sym_unit_bytes = s.regime == REG_WPE ? round16((uint64_t)(s.n / 2 + 1) * s.n * 4) : 0;
-        s.sym_offset = sym_off;
-        sym_off += s.sym_unit_bytes * s.units;
         ke_off += s.unit_bytes * s.units;
         map_off += (uint64_t)s.units * (s.regime == REG_TPE ? kTpeWidth : 1) * s.n;
         map_off = (map_off + 3) / 4 * 4;  // keep 16-byte alignment of each segment's map
@@ -564,10 +570,41 @@ bool ke_is_symmetric(const afm_operator* op) {
     return sym != 0;
 }
 
-// Builds the symmetric inner arena on the operator's stream (once); work
-// enqueued afterwards on `st` is ordered after it. Call outside stream capture.
+// Layout of the symmetric inner arena in format `mode` (1: FP32, 2: FP32 +
+// BF16 correction plane): patch units hold the packed triangle of 32 element
+// slots (S = n (n + 1) / 2 x 32 entries), element units the n/2 + 1 wrapped
+// diagonals (S = (n/2 + 1) n); the correction plane follows the FP32 plane
+// at a 16-byte boundary.
+void layout_sym(afm_operator* op, int mode) {
+    uint64_t off = 0;
+    for (Segment& s : op->segs) {
+        const uint64_t S = s.regime == REG_TPE ? (uint64_t)s.n * (s.n + 1) / 2 * kTpeWidth
+                                               : (uint64_t)(s.n / 2 + 1) * s.n;
+        const uint64_t P = (S + 3) / 4 * 4;
+        s.sym_plane = mode == 2 ? (uint32_t)P : 0;
+        s.sym_unit_bytes = mode == 2 ? round16(P * 4 + S * 2) : round16(S * 4);
+        s.sym_offset = off;
+        off += s.sym_unit_bytes * s.units;
+    }
+    op->sym_bytes = off;
+}
+
+// Format of the symmetric inner arena the operator's FP32 products use (0:
+// none, they read the hi plane).
+int sym_format(const afm_operator* op) { return op->sym_ok ? op->sym_mode : 0; }
+
+// Builds the symmetric inner arena in the operator's format on its stream
+// (once per format); work enqueued afterwards on `st` is ordered after it.
+// Call outside stream capture.
 int ensure_sym(afm_operator* op, cudaStream_t st) {
-    if (!op->sym_ok || !op->sym_mode || op->d_sym) return AFM_SUCCESS;
+    const int fmt = sym_format(op);
+    if (!fmt) return AFM_SUCCESS;
+    if (op->d_sym && op->sym_built == fmt) return AFM_SUCCESS;
+    dfree(op, op->d_sym);
+    dfree(op, op->d_vx);
+    op->sym_built = 0;
+    layout_sym(op, fmt);
+    if (fmt == 2) AFM_CUDA(dalloc(op, &op->d_vx, sizeof(double) * std::max<uint32_t>(op->n_dofs, 1)));
     AFM_CUDA(dalloc(op, &op->d_sym, op->sym_bytes));
     AFM_CUDA(cudaMemsetAsync(op->d_sym, 0, op->sym_bytes, op->stream));
     for (const Segment& s : op->segs) {
@@ -577,6 +614,7 @@ int ensure_sym(afm_operator* op, cudaStream_t st) {
             return fail(AFM_ERR_CUDA, "symmetric arena: %s", cudaGetErrorString(e));
         }
     }
+    op->sym_built = fmt;
     op->generation++;  // captured FP32 iterations switch to the new arena
     if (st != op->stream) {
         cudaEvent_t ev;
@@ -681,9 +719,13 @@ int enqueue_matvec(afm_operator* op, void* d_v, const void* d_u, int bc_mode, cu
     // built, else from an FP32 arena or the hi plane of a split arena (half of
     // each unit is copied)
     const bool sym = f32 && op->d_sym != nullptr;
-    const int kprec = sym ? kPrecF32Sym : f32 ? AFM_PREC_FP32 : op->precision;
+    const bool symx = sym && op->sym_built == 2;
+    const int kprec = sym ? (symx ? kPrecF32SymX : kPrecF32Sym) : f32 ? AFM_PREC_FP32 : op->precision;
     const size_t vbytes = (size_t)op->n_dofs * (f32 || kprec == AFM_PREC_FP32 ? 4 : 8);
-    AFM_CUDA(cudaMemsetAsync(d_v, 0, vbytes, st));
+    // the corrected format sums into an FP64 vector, rounded to FP32 at the end
+    float* const d_v32 = static_cast<float*>(d_v);
+    if (symx) d_v = op->d_vx;
+    AFM_CUDA(cudaMemsetAsync(d_v, 0, symx ? (size_t)op->n_dofs * 8 : vbytes, st));
     bool first = true;
     if (op->use_patches) {
         const Segment& s = op->segs[0];
@@ -697,13 +739,14 @@ int enqueue_matvec(afm_operator* op, void* d_v, const void* d_u, int bc_mode, cu
             a.v = d_v;
             a.unit_bytes = sym ? s.sym_unit_bytes : s.unit_bytes;
             a.copy_bytes = (uint32_t)a.unit_bytes;
-            a.plane = sym ? 0 : s.plane;
+            a.plane = sym ? s.sym_plane : s.plane;
             if (f32 && !sym && op->precision == AFM_PREC_FP64_SPLIT) a.copy_bytes = s.plane * 4;
             a.bc_mode = bc_mode;
             a.err = op->d_err;
             AFM_CUDA(launch_patches(kprec, op->patch_geom, a, op->sm_count, !first, st));
             first = false;
         }
+        if (symx) AFM_CUDA(launch_to_f32(d_v32, op->d_vx, op->n_dofs, st));
         return AFM_SUCCESS;
     }
     for (const Segment& s : op->segs) {
@@ -717,7 +760,7 @@ int enqueue_matvec(afm_operator* op, void* d_v, const void* d_u, int bc_mode, cu
         a.count = s.count;
         a.unit_bytes = sym ? s.sym_unit_bytes : s.unit_bytes;
         a.copy_bytes = (uint32_t)a.unit_bytes;
-        a.plane = sym ? 0 : s.plane;
+        a.plane = sym ? s.sym_plane : s.plane;
         if (f32 && !sym && op->precision == AFM_PREC_FP64_SPLIT) a.copy_bytes = s.plane * 4;
         a.bc_mode = bc_mode;
         a.err = op->d_err;
@@ -725,6 +768,7 @@ int enqueue_matvec(afm_operator* op, void* d_v, const void* d_u, int bc_mode, cu
         AFM_CUDA(launch_segment(s, kprec, a, op->sm_count, op->dup_in_element, !first, st));
         first = false;
     }
+    if (symx) AFM_CUDA(launch_to_f32(d_v32, op->d_vx, op->n_dofs, st));
     return AFM_SUCCESS;
 }
 
@@ -1357,8 +1401,9 @@ int afm_create(afm_operator** out, int bc_method, int device) {
                     prop.major, prop.minor);
     DeviceGuard g(device);
     // kernels' shared-memory limits, before any launch or graph capture
-    if (configure_kernels_fp64() != cudaSuccess || configure_kernels_split() != cudaSuccess || configure_kernels_f32sym() != cudaSuccess ||
-        configure_kernels_fp32() != cudaSuccess)
+    if (configure_kernels_fp64() != cudaSuccess || configure_kernels_split() != cudaSuccess ||
+        configure_kernels_fp32() != cudaSuccess || configure_kernels_f32sym() != cudaSuccess ||
+        configure_kernels_f32symx() != cudaSuccess)
         return fail(AFM_ERR_CUDA, "kernel configuration failed on device %d", device);
     auto* op = new afm_operator();
     op->device = device;
@@ -1419,13 +1464,16 @@ int afm_set_patch_mode(afm_operator* op, int enable) {
     return ok();
 }
 
-int afm_set_symmetric_inner(afm_operator* op, int enable) {
+int afm_set_symmetric_inner(afm_operator* op, int format) {
     AFM_CHECK_OP(op);
-    op->sym_mode = enable ? 1 : 0;
-    if (!op->sym_mode && op->d_sym) {
+    if (format < 0 || format > 2) return fail(AFM_ERR_INVALID_ARG, "symmetric inner format %d (0, 1 or 2)", format);
+    op->sym_mode = format;
+    if (op->d_sym && op->sym_built != sym_format(op)) {
         DeviceGuard g(op->device);
         dfree(op, op->d_sym);
-        op->generation++;  // captured FP32 iterations return to the hi plane
+        dfree(op, op->d_vx);
+        op->sym_built = 0;
+        op->generation++;  // captured FP32 iterations leave the old arena
     }
     return ok();
 }
@@ -1655,15 +1703,14 @@ int afm_finalize(afm_operator* op) {
     op->ke_symmetric = false;
     op->sym_ok = false;
     op->sym_bytes = 0;
+    op->sym_built = 0;
     if (prec == AFM_PREC_FP64_SPLIT && !op->dup_in_element && op->n_elem > 0) {
         op->ke_symmetric = ke_is_symmetric(op);
         bool covered = true;
-        for (const Segment& s : op->segs) {
-            if (s.units && s.sym_unit_bytes == 0) covered = false;
-            op->sym_bytes = std::max<size_t>(op->sym_bytes, s.sym_offset + s.sym_unit_bytes * s.units);
-        }
+        if (!op->use_patches)
+            for (const Segment& s : op->segs)
+                if (s.units && s.regime != REG_WPE) covered = false;
         op->sym_ok = op->ke_symmetric && covered;
-        if (!op->sym_ok) op->sym_bytes = 0;
     }
     op->ke_dirty = false;
     op->finalized = true;
@@ -2281,7 +2328,7 @@ int afm_get_info(afm_operator* op, afm_info* info) {
     info->n_patch_colors = op->use_patches ? (uint32_t)op->patch_color_first.size() - 1 : 0;
     info->patch_index_bytes = op->use_patches ? op->patch_idx_bytes : 0;
     info->ke_symmetric = op->ke_symmetric ? 1 : 0;
-    info->sym_available = (op->sym_ok && op->sym_mode) ? 1 : 0;
+    info->sym_available = sym_format(op);
     info->sym_bytes = op->d_sym ? op->sym_bytes : 0;
     info->device = op->device;
     return ok();

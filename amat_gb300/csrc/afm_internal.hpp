@@ -45,6 +45,7 @@ struct Segment {
     uint32_t plane = 0;       // FP64_SPLIT: entries per plane of a unit (the lo plane follows the hi plane)
     uint64_t sym_offset = 0;     // byte offset of the first unit in the symmetric inner arena
     uint64_t sym_unit_bytes = 0; // its bytes per unit (0: no symmetric form)
+    uint32_t sym_plane = 0;      // entries of a unit's FP32 plane before its BF16 correction plane (0: none)
 };
 
 // Arguments of one segment launch.
@@ -147,6 +148,8 @@ size_t patch_smem_bytes(int prec, const PatchPlanGeom& pg, uint32_t copy_bytes);
 // Kernel arithmetic for FP32 products from the symmetric inner arena (an
 // internal value beside the afm_precision codes).
 constexpr int kPrecF32Sym = 16;
+// ... and from the symmetric inner arena with its BF16 correction plane.
+constexpr int kPrecF32SymX = 17;
 
 // Fills segment s's part of the symmetric inner arena from its split-arena
 // units (afm_mv_f32sym.cu).
@@ -237,9 +240,11 @@ struct afm_operator {
     // entries stored once, built from the split arena on the first FP32 product
     bool ke_symmetric = false;      // every Ke symmetric to 1e-6 of its largest diagonal entry
     bool sym_ok = false;            // symmetric, split arena, and a layout the symmetric kernels cover
-    int sym_mode = 1;               // afm_set_symmetric_inner
+    int sym_mode = 1;               // afm_set_symmetric_inner: 0 off, 1 FP32, 2 FP32 + BF16 correction
+    int sym_built = 0;              // format of d_sym (1 or 2; 0: not built)
     unsigned char* d_sym = nullptr;
     size_t sym_bytes = 0;
+    double* d_vx = nullptr;         // format 2: FP64 product before its rounding to FP32 (n_dofs)
 
     // patch path (small elements): patches in colour order
     bool use_patches = false;

@@ -134,6 +134,7 @@ struct ArithF64 {
     using KT = double;
     using UT = double;
     using VT = double;
+    using VO = double;  // the product vector v (VT but for ArithF32SymX)
     struct Acc { double s; };
     static __device__ __forceinline__ KT kload(const unsigned char* slot, size_t i, uint32_t) {
         return reinterpret_cast<const double*>(slot)[i];
@@ -157,6 +158,7 @@ struct ArithSplit {
     using KT = float2;
     using UT = float2;
     using VT = double;
+    using VO = double;
     struct Acc { float hi, lo; };
     // planar unit: hi plane, then the lo plane `plane` entries further on
     static __device__ __forceinline__ KT kload(const unsigned char* slot, size_t i, uint32_t plane) {
@@ -196,6 +198,7 @@ struct ArithF32 {
     using KT = float;
     using UT = float;
     using VT = float;
+    using VO = float;
     struct Acc { float s; };
     static __device__ __forceinline__ KT kload(const unsigned char* slot, size_t i, uint32_t) {
         return reinterpret_cast<const float*>(slot)[i];
@@ -216,6 +219,52 @@ struct ArithF32 {
 // transposed reads of a warp touch consecutive words.
 struct ArithF32Sym : ArithF32 {
     static constexpr bool kSym = true;
+};
+
+// The symmetric inner arena with a correction plane: each stored entry is
+// hi + lo, hi = fl32(K) in the first plane and lo = bf16(K - hi) in the
+// plane `plane` entries further on (2 bytes each), which represents K to
+// about 2^-32 instead of 2^-24 for 1.5x the bytes. Products are accumulated
+// as double-float pairs in FP32 arithmetic (TwoProduct by FMA, TwoSum), and
+// the element rows are summed into v in FP64 (VO = double), so that neither
+// the correction nor the cancellation between element contributions is lost
+// to FP32 rounding. Rounding the element matrices, or the sums, to FP32
+// perturbs the product by about 2^-24 |K| |u|, far more than 2^-24 |K u| for
+// smooth u, which slows the inner CG of ill-conditioned systems (elasticity)
+// markedly; this arithmetic removes both.
+struct ArithF32SymX {
+    static constexpr bool kSym = true;
+    static constexpr uint32_t kWpgWarps = 24;
+    using KT = float2;  // (hi, lo)
+    using UT = float;
+    using VT = float;
+    using VO = double;  // v sums the element products across colours without FP32 cancellation
+    struct Acc { float hi, lo; };
+    static __device__ __forceinline__ KT kload(const unsigned char* slot, size_t i, uint32_t plane) {
+        const float h = reinterpret_cast<const float*>(slot)[i];
+        const unsigned short b = reinterpret_cast<const unsigned short*>(slot + (size_t)plane * 4)[i];
+        return make_float2(h, __uint_as_float((uint32_t)b << 16));
+    }
+    static __device__ __forceinline__ Acc zero() { return {0.0f, 0.0f}; }
+    static __device__ __forceinline__ UT stage(VT x) { return x; }
+    static __device__ __forceinline__ void fma(Acc& a, KT k, UT u) {
+        const float p = __fmul_rn(k.x, u);
+        const float e = __fmaf_rn(k.x, u, -p);
+        const float t = __fmaf_rn(k.y, u, e);
+        const float s = __fadd_rn(a.hi, p);
+        const float bp = __fsub_rn(s, a.hi);
+        const float err = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bp)), __fsub_rn(p, bp));
+        a.hi = s;
+        a.lo = __fadd_rn(a.lo, __fadd_rn(err, t));
+    }
+    static __device__ __forceinline__ VO finish(const Acc& a) { return (double)a.hi + (double)a.lo; }
+    static __device__ __forceinline__ void combine(Acc& a, const Acc& b) {
+        const float s = __fadd_rn(a.hi, b.hi);
+        const float bp = __fsub_rn(s, a.hi);
+        const float err = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bp)), __fsub_rn(b.hi, bp));
+        a.hi = s;
+        a.lo = __fadd_rn(a.lo, __fadd_rn(b.lo, err));
+    }
 };
 
 // Entry index of (r, c) in a thread-per-element unit.
@@ -512,17 +561,16 @@ __host__ __device__ constexpr uint32_t wpg_gc(uint32_t gr, uint32_t ut_bytes) {
 // wraps. Every offset is a compile-time constant but the wrap of the
 // transposed read (one select).
 template <typename A, int NT, int T0, int T1>
-__device__ __forceinline__ void sym_terms(typename A::Acc& acc, const float* kr, const typename A::UT* ur,
-                                          uint32_t r) {
+__device__ __forceinline__ void sym_terms(typename A::Acc& acc, const unsigned char* ks, uint32_t plane,
+                                          const typename A::UT* ur, uint32_t r) {
     constexpr int H = NT / 2;
 #pragma unroll
     for (int t = T0; t < T1; t++) {
         if (t <= H) {
-            A::fma(acc, kr[t * NT], ur[t]);
+            A::fma(acc, A::kload(ks, r + t * NT, plane), ur[t]);
         } else {
             const int d = t - H;
-            const float kv = kr[d * NT - d + ((int)r < d ? NT : 0)];
-            A::fma(acc, kv, ur[NT - d]);
+            A::fma(acc, A::kload(ks, r + d * NT - d + ((int)r < d ? NT : 0), plane), ur[NT - d]);
         }
     }
 }
@@ -533,6 +581,7 @@ __global__ void __launch_bounds__((A::kWpgWarps + 1) * 32, 1)
     using KT = typename A::KT;
     using UT = typename A::UT;
     using VT = typename A::VT;
+    using VO = typename A::VO;
     using Acc = typename A::Acc;
     const uint32_t n = NT ? NT : n_rt;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -596,7 +645,7 @@ __global__ void __launch_bounds__((A::kWpgWarps + 1) * 32, 1)
     const bool gatherer = (cg == 0);
     const uint32_t bar_id = 1 + grp, bar_threads = G.g * 32;
     const VT* __restrict__ u = static_cast<const VT*>(a.u);
-    VT* __restrict__ v = static_cast<VT*>(a.v);
+    VO* __restrict__ v = static_cast<VO*>(a.v);
     unsigned char* ubuf0 = ubase + (size_t)(grp * 2) * ub;
     const uint32_t pstride = (G.gc > 1 ? G.gc - 1 : 1) * n;
     Acc* pbuf0 = pbase + (size_t)(grp * 2) * pstride;
@@ -604,7 +653,8 @@ __global__ void __launch_bounds__((A::kWpgWarps + 1) * 32, 1)
     auto pbuf = [&](uint32_t p) { return pbuf0 + (size_t)p * pstride; };
 
     uint32_t dof_c = 0, dof_n = 0, dof_nn = 0;
-    VT vold_c = VT(0), vold_n = VT(0), u_n = VT(0);
+    VO vold_c = VO(0), vold_n = VO(0);
+    VT u_n = VT(0);
     const uint64_t keep = l2_evict_last_policy(), stream_pol = l2_evict_first_policy();
     auto map_at = [&](uint32_t i) {
         return rvalid ? ld_nc_hint(a.map + (size_t)(begin + i) * n + r, stream_pol) : 0u;
@@ -642,21 +692,21 @@ __global__ void __launch_bounds__((A::kWpgWarps + 1) * 32, 1)
                     // the column group's terms, with compile-time bounds
                     constexpr int GR = (NT + 31) / 32;
                     constexpr int GC = (int)wpg_gc(GR, sizeof(UT));
-                    const float* kr = reinterpret_cast<const float*>(ks) + r;
                     const UT* ur = uu + r;
+                    const uint32_t pl = a.plane;
                     if constexpr (GC == 1) {
-                        sym_terms<A, NT, 0, NT>(acc, kr, ur, r);
+                        sym_terms<A, NT, 0, NT>(acc, ks, pl, ur, r);
                     } else if constexpr (GC == 2) {
                         if (cg == 0)
-                            sym_terms<A, NT, 0, NT / 2>(acc, kr, ur, r);
+                            sym_terms<A, NT, 0, NT / 2>(acc, ks, pl, ur, r);
                         else
-                            sym_terms<A, NT, NT / 2, NT>(acc, kr, ur, r);
+                            sym_terms<A, NT, NT / 2, NT>(acc, ks, pl, ur, r);
                     } else {
                         switch (cg) {
-                            case 0: sym_terms<A, NT, 0, NT / 4>(acc, kr, ur, r); break;
-                            case 1: sym_terms<A, NT, NT / 4, 2 * NT / 4>(acc, kr, ur, r); break;
-                            case 2: sym_terms<A, NT, 2 * NT / 4, 3 * NT / 4>(acc, kr, ur, r); break;
-                            default: sym_terms<A, NT, 3 * NT / 4, NT>(acc, kr, ur, r); break;
+                            case 0: sym_terms<A, NT, 0, NT / 4>(acc, ks, pl, ur, r); break;
+                            case 1: sym_terms<A, NT, NT / 4, 2 * NT / 4>(acc, ks, pl, ur, r); break;
+                            case 2: sym_terms<A, NT, 2 * NT / 4, 3 * NT / 4>(acc, ks, pl, ur, r); break;
+                            default: sym_terms<A, NT, 3 * NT / 4, NT>(acc, ks, pl, ur, r); break;
                         }
                     }
                 } else if constexpr (A::kSym) {

@@ -1,5 +1,6 @@
 // Matvec kernels, ArithF32Sym instances (FP32 products from the symmetric
-// inner arena), and the kernels that build that arena from a split arena.
+// inner arena), and the kernels that build that arena (with or without its
+// BF16 correction plane) from a split arena.
 #define ARITH ArithF32Sym
 #define LAUNCH_FN launch_segment_f32sym
 #define SMEM_FN segment_smem_f32sym
@@ -8,22 +9,35 @@
 #define PATCH_SMEM_FN patch_smem_f32sym
 #include "afm_mv_launch.inl"
 
+#include <cuda_bf16.h>
+
 namespace afm {
 
 namespace {
 
-// Symmetric part of an element pair from the hi + lo planes, rounded once.
-__device__ __forceinline__ float sym_entry(const float* h, uint32_t plane, size_t a, size_t b) {
+// Symmetric part of an element pair from the split arena's hi + lo planes.
+__device__ __forceinline__ double sym_entry(const float* h, uint32_t plane, size_t a, size_t b) {
     const double x = (double)h[a] + (double)h[a + plane];
     const double y = (double)h[b] + (double)h[b + plane];
-    return __double2float_rn(0.5 * (x + y));
+    return 0.5 * (x + y);
+}
+
+// Writes entry q of a unit: hi = fl32(x); with a correction plane (lo_plane >
+// 0 entries after the start of the unit, in floats), lo = bf16(x - hi).
+__device__ __forceinline__ void put_sym(float* unit, uint64_t q, uint32_t lo_plane, double x) {
+    const float h = __double2float_rn(x);
+    unit[q] = h;
+    if (lo_plane) {
+        const __nv_bfloat16 l = __float2bfloat16_rn(__double2float_rn(x - (double)h));
+        reinterpret_cast<unsigned short*>(unit + lo_plane)[q] = __bfloat16_as_ushort(l);
+    }
 }
 
 // Patch units (32 element slots, entry (r, c) of slot l at (r n + c) 32 + l in
 // each plane) -> packed upper triangle, entry k = j (j + 1) / 2 + i at k 32 + l.
 __global__ void __launch_bounds__(256) k_sym_tpe(const unsigned char* __restrict__ src, uint64_t src_unit_bytes,
                                                  uint32_t plane, uint32_t n, uint64_t units, float* __restrict__ dst,
-                                                 uint64_t dst_unit_floats) {
+                                                 uint64_t dst_unit_floats, uint32_t lo_plane) {
     const uint32_t np = n * (n + 1) / 2;
     const uint64_t total = units * np * kTpeWidth;
     for (uint64_t x = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; x < total;
@@ -36,8 +50,8 @@ __global__ void __launch_bounds__(256) k_sym_tpe(const unsigned char* __restrict
         while ((j + 1) * (j + 2) / 2 <= k) j++;
         const uint32_t i = k - j * (j + 1) / 2;
         const float* h = reinterpret_cast<const float*>(src + u * src_unit_bytes);
-        dst[u * dst_unit_floats + (uint64_t)k * kTpeWidth + l] =
-            sym_entry(h, plane, ((size_t)i * n + j) * kTpeWidth + l, ((size_t)j * n + i) * kTpeWidth + l);
+        put_sym(dst + u * dst_unit_floats, (uint64_t)k * kTpeWidth + l, lo_plane,
+                sym_entry(h, plane, ((size_t)i * n + j) * kTpeWidth + l, ((size_t)j * n + i) * kTpeWidth + l));
     }
 }
 
@@ -45,7 +59,7 @@ __global__ void __launch_bounds__(256) k_sym_tpe(const unsigned char* __restrict
 // diagonals, D[d][j] = K(j, (j + d) mod n) at d n + j, d = 0 .. n/2.
 __global__ void __launch_bounds__(256) k_sym_wpe(const unsigned char* __restrict__ src, uint64_t src_unit_bytes,
                                                  uint32_t plane, uint32_t n, uint64_t units, float* __restrict__ dst,
-                                                 uint64_t dst_unit_floats) {
+                                                 uint64_t dst_unit_floats, uint32_t lo_plane) {
     const uint32_t per = (n / 2 + 1) * n;
     const uint64_t total = units * per;
     for (uint64_t x = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; x < total;
@@ -55,14 +69,15 @@ __global__ void __launch_bounds__(256) k_sym_wpe(const unsigned char* __restrict
         const uint32_t d = q / n, j = q % n;
         const uint32_t c = j + d >= n ? j + d - n : j + d;
         const float* h = reinterpret_cast<const float*>(src + u * src_unit_bytes);
-        dst[u * dst_unit_floats + q] = sym_entry(h, plane, (size_t)c * n + j, (size_t)j * n + c);
+        put_sym(dst + u * dst_unit_floats, q, lo_plane, sym_entry(h, plane, (size_t)c * n + j, (size_t)j * n + c));
     }
 }
 
 }  // namespace
 
 // Fills the symmetric inner arena of segment s (sym must be zeroed: unit
-// padding stays zero) from its split-arena units.
+// padding stays zero) from its split-arena units; s.sym_plane > 0 adds the
+// BF16 correction plane.
 cudaError_t build_sym_segment(const Segment& s, const unsigned char* ke, unsigned char* sym, int sm_count,
                               cudaStream_t st) {
     if (s.units == 0 || s.sym_unit_bytes == 0) return cudaSuccess;
@@ -74,9 +89,11 @@ cudaError_t build_sym_segment(const Segment& s, const unsigned char* ke, unsigne
     float* dst = reinterpret_cast<float*>(sym + s.sym_offset);
     const unsigned char* src = ke + s.ke_offset;
     if (tpe)
-        k_sym_tpe<<<grid, 256, 0, st>>>(src, s.unit_bytes, s.plane, s.n, s.units, dst, s.sym_unit_bytes / 4);
+        k_sym_tpe<<<grid, 256, 0, st>>>(src, s.unit_bytes, s.plane, s.n, s.units, dst, s.sym_unit_bytes / 4,
+                                        s.sym_plane);
     else
-        k_sym_wpe<<<grid, 256, 0, st>>>(src, s.unit_bytes, s.plane, s.n, s.units, dst, s.sym_unit_bytes / 4);
+        k_sym_wpe<<<grid, 256, 0, st>>>(src, s.unit_bytes, s.plane, s.n, s.units, dst, s.sym_unit_bytes / 4,
+                                        s.sym_plane);
     return cudaGetLastError();
 }
 

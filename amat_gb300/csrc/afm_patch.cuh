@@ -73,6 +73,7 @@ __global__ void __launch_bounds__((G * GW + 1) * 32, 1) afm_patch_kernel(PatchAr
     using KT = typename A::KT;
     using UT = typename A::UT;
     using VT = typename A::VT;
+    using VO = typename A::VO;
     constexpr int NM = NT ? NT : 12;
     const uint32_t n = NT ? NT : n_rt;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -161,7 +162,7 @@ __global__ void __launch_bounds__((G * GW + 1) * 32, 1) afm_patch_kernel(PatchAr
     using Acc = typename A::Acc;
     Acc* ve = reinterpret_cast<Acc*>(gbase + L.idx_bytes + L.us_bytes);
     const VT* __restrict__ u = static_cast<const VT*>(a.u);
-    VT* __restrict__ v = static_cast<VT*>(a.v);
+    VO* __restrict__ v = static_cast<VO*>(a.v);
     const uint64_t keep = l2_evict_last_policy();
 
     // ring index of this group's first unit: units of the patches before it

@@ -64,14 +64,14 @@ double now_s() {
 }
 
 // Device bytes a request holds once admitted: element matrices (8 bytes per
-// entry in every arena but FP32, plus the symmetric FP32 copy of about 2.2
-// bytes per entry), maps or patch index blocks, diagonal, the solver's FP64
-// and FP32 work vectors, b and x; 10% and 1 MB of slack.
+// entry in every arena but FP32, plus the symmetric inner copy of at most 6
+// bytes per stored pair), maps or patch index blocks, diagonal, the solver's
+// FP64 and FP32 work vectors, b and x; 10% and 1 MB of slack.
 uint64_t estimate_bytes(const afm_operator* op) {
     uint64_t ke = 0;
     for (uint32_t e = 0; e < op->n_elem; e++) {
         const uint64_t n = op->offsets[e + 1] - op->offsets[e];
-        ke += n * n * 8 + 8 * n + 2 * n * (n / 2 + 1) * 2;
+        ke += n * n * 8 + 8 * n + 6 * n * (n / 2 + 1);
     }
     const uint64_t vec = (uint64_t)op->n_dofs * (8 * 8 + 7 * 4 + 3 * 8);
     return (ke + vec) * 11 / 10 + (1u << 20);

@@ -276,7 +276,8 @@ def measure_e2e(A, u_host, v_dev, steps, world):
 
 def measure_inner_f32(A, m, steps, warmup):
     """FP32 products of the split operator (the inner matvec of the mixed-precision solve): from the
-    symmetric copy (each pair of entries once) and from the hi plane; GB/s over the bytes streamed."""
+    symmetric copy (each pair of entries once) with and without its BF16 correction plane, and from the
+    hi plane; GB/s over the bytes streamed."""
     import torch
     stream_ptr = A.stream()
     stream = torch.cuda.ExternalStream(stream_ptr)
@@ -284,7 +285,8 @@ def measure_inner_f32(A, m, steps, warmup):
     v = torch.empty_like(u)
     base = 4 * m.n_elem * m.ndpe + 8 * m.n_dofs  # map entries, u read, v written
     out = {}
-    for sym in (1, 0):
+    names = {2: "symmetric_copy_bf16_correction", 1: "symmetric_copy", 0: "hi_plane"}
+    for sym in (2, 1, 0):
         A.set_symmetric_inner(sym)
         for _ in range(warmup):
             A.matvec_device_f32(v.data_ptr(), u.data_ptr(), stream_ptr)
@@ -300,7 +302,7 @@ def measure_inner_f32(A, m, steps, warmup):
         ke = info["sym_bytes"] if sym else info["ke_bytes"] // 2
         if sym and not ke:
             continue  # no symmetric copy for this operator
-        out["symmetric_copy" if sym else "hi_plane"] = {
+        out[names[sym]] = {
             "ms": ms, "ke_bytes": ke, "streamed_gbs": (ke + base) / (ms * 1e-3) / 1e9}
     A.set_symmetric_inner(1)
     return out
@@ -427,7 +429,8 @@ def run_solve(args, w, rank, world, local_rank):
                       "inner_rtol": args.inner_rtol},
            "mixed": {"solves_per_s": smx, "inner_iterations": stm.iterations, "refinements": stm.refinements,
                      "inner_ke_bytes": A.info()["sym_bytes"] or A.info()["ke_bytes"] // 2,
-                     "inner_arena": "symmetric FP32 copy" if A.info()["sym_bytes"] else "hi plane",
+                     "inner_arena": {0: "hi plane", 1: "symmetric copy, FP32",
+                                     2: "symmetric copy, FP32 + BF16 correction"}[A.info()["sym_available"]],
                      "rel_residual": stm.rel_residual,
                      "rel_error_vs_fp64_solution": float(np.linalg.norm(xm - x64) / np.linalg.norm(x64))},
            "fp64": {"solves_per_s": s64, "iterations": st.iterations, "rel_residual": st.rel_residual,
@@ -702,7 +705,7 @@ def main():
     ap.add_argument("--rates", default="20,100,500", help="serve: arrival rates (requests/s)")
     ap.add_argument("--requests", type=int, default=160, help="serve: requests per rate")
     ap.add_argument("--edge-max", type=int, default=32, help="serve: largest mesh edge")
-    ap.add_argument("--serve-inner", type=float, default=0.1, help="serve: FP32 reduction between FP64 updates")
+    ap.add_argument("--serve-inner", type=float, default=0.3, help="serve: FP32 reduction between FP64 updates")
     ap.add_argument("--nrhs", type=int, default=64)
     ap.add_argument("--single-cols", type=int, default=2, help="columns solved one by one for the FP64 comparison")
     ap.add_argument("--batched-fp64", type=int, default=0, help="also time the FP64 batched block CG")

@@ -102,7 +102,7 @@ typedef struct afm_info {
     uint32_t n_patch_colors;    /* colours of the patch conflict graph */
     uint64_t patch_index_bytes; /* device bytes of the patch index blocks */
     int ke_symmetric;           /* every Ke symmetric (FP64_SPLIT operators; 0 otherwise) */
-    int sym_available;          /* the symmetric inner arena can serve FP32 products */
+    int sym_available;          /* format of the symmetric inner arena FP32 products use (0: none) */
     uint64_t sym_bytes;         /* device bytes of that arena once built (0: not built) */
 } afm_info;
 
@@ -136,17 +136,23 @@ int afm_set_precision(afm_operator* op, int precision);
  * elements. Both are deterministic and agree within rounding. Takes effect at
  * the next afm_finalize. */
 int afm_set_patch_mode(afm_operator* op, int enable);
-/* FP32 products of an FP64_SPLIT operator (no counterpart in the reference):
- * enable = 1 (default) lets them stream a symmetric copy of the FP32 element
- * matrices that stores each pair K(i, j), K(j, i) once, about 55% of the
- * bytes of the hi plane, when every Ke is symmetric (to 1e-6 of its largest
- * diagonal entry; the copy holds the rounded symmetric part) and the elements
- * run as patches or have more than 16 DoFs. The copy is built on the device
- * from the split arena by the first FP32 product or mixed-precision solve
- * (outside any stream capture) and costs another ~28% of the split arena's
- * memory. FP64 products never use it. enable = 0: FP32 products read the hi
- * plane. Takes effect at the next FP32 product. */
-int afm_set_symmetric_inner(afm_operator* op, int enable);
+/* FP32 products of an FP64_SPLIT operator (no counterpart in the reference),
+ * which the mixed-precision solves use: when every Ke is symmetric (to 1e-6
+ * of its largest diagonal entry; the copy holds the symmetric part) and the
+ * elements run as patches or have more than 16 DoFs, they can stream a
+ * symmetric copy of the element matrices that stores each pair K(i, j),
+ * K(j, i) once. format = 1 (default): the pairs in FP32, about 55% of the
+ * bytes of the hi plane, FP32 sums. format = 2: FP32 plus a BF16 correction
+ * plane (about 83% of the hi plane's bytes), which represents Ke to about
+ * 2^-32, with compensated sums in FP32 arithmetic and the element rows summed
+ * in FP64 before v is rounded to FP32. FP32 rounding of Ke or of the sums
+ * perturbs the product by ~2^-24 |K| |u|, which costs the inner CG of
+ * ill-conditioned systems (elasticity under rough loads) up to ~1.9x the
+ * iterations of FP64 CG; format 2 brings that to ~1.1-1.2x, at a higher cost
+ * per product. format = 0: FP32 products read the hi plane. The copy is built on the device from the split arena by the first
+ * FP32 product or mixed-precision solve after a change (outside any stream
+ * capture). FP64 products never use it. */
+int afm_set_symmetric_inner(afm_operator* op, int format);
 
 /* ---- maps (par::Maps) --------------------------------------------------- */
 

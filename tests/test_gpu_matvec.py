@@ -324,8 +324,9 @@ def test_patch_path_against_oracle(gpu, kind, shape, jitter, prec):
 ])
 def test_symmetric_inner_arena(gpu, kind, n, ngt):
     """FP32 products of a split operator stream the symmetric copy (each pair
-    of entries once) when every Ke is symmetric: against the FP64 product, the
-    hi-plane product, and itself on a second call."""
+    of entries once) when every Ke is symmetric, in FP32 (format 1) or FP32
+    with a BF16 correction plane and FP64 sums (format 2): against the FP64
+    product, the hi-plane product, and themselves on a second call."""
     import torch
     m = P.Mesh(kind, n, jitter=0.12, seed=6)
     ke = m.element_matrices(ngt=ngt)
@@ -341,21 +342,30 @@ def test_symmetric_inner_arena(gpu, kind, n, ngt):
     v64 = np.empty(m.n_dofs)
     A.matvec(v64, u, True)
     du = torch.tensor(u, dtype=torch.float32, device="cuda")
-    dv1, dv2, dh = torch.empty_like(du), torch.empty_like(du), torch.empty_like(du)
-    torch.cuda.synchronize()
-    A.matvec_device_f32(dv1.data_ptr(), du.data_ptr())
-    A.matvec_device_f32(dv2.data_ptr(), du.data_ptr())
-    A.synchronize()
-    # the hi plane is half of the split arena; the symmetric copy about 55% of that
-    assert 0 < A.info()["sym_bytes"] < 0.29 * info["ke_bytes"]
-    assert torch.equal(dv1, dv2)
-    assert rel(dv1.double().cpu().numpy(), v64) < FP32_RTOL
+    # v64 of the FP32-rounded u: the products' own error, apart from rounding u
+    u32 = du.double().cpu().numpy()
+    A.matvec(v64, u32, True)
+    dh = torch.empty_like(du)
     A.set_symmetric_inner(0)
-    assert A.info()["sym_available"] == 0 and A.info()["sym_bytes"] == 0
     A.matvec_device_f32(dh.data_ptr(), du.data_ptr())
     A.synchronize()
-    assert rel(dh.double().cpu().numpy(), v64) < FP32_RTOL
-    assert rel(dv1.double().cpu().numpy(), dh.double().cpu().numpy()) < 2e-6
+    assert A.info()["sym_available"] == 0 and A.info()["sym_bytes"] == 0
+    vh = dh.double().cpu().numpy()
+    assert rel(vh, v64) < FP32_RTOL
+    # format: (bytes below this fraction of the split arena, error bound against FP64)
+    for fmt, frac, tol in [(1, 0.29, FP32_RTOL), (2, 0.43, 3e-7)]:
+        A.set_symmetric_inner(fmt)
+        dv1, dv2 = torch.empty_like(du), torch.empty_like(du)
+        A.matvec_device_f32(dv1.data_ptr(), du.data_ptr())
+        A.matvec_device_f32(dv2.data_ptr(), du.data_ptr())
+        A.synchronize()
+        # the hi plane is half of the split arena; the symmetric copy about 55% (83% with the correction) of that
+        assert 0 < A.info()["sym_bytes"] < frac * info["ke_bytes"]
+        assert torch.equal(dv1, dv2)
+        v1 = dv1.double().cpu().numpy()
+        assert rel(v1, v64) < tol
+        if fmt == 1:
+            assert rel(v1, vh) < 2e-6
 
 
 def test_symmetric_inner_needs_symmetric_ke(gpu):
