@@ -415,10 +415,15 @@ def run_solve(args, w, rank, world, local_rank):
     if stm.status != 0:
         raise SystemExit("mixed-precision solve did not converge")
     t64, tmx = [], []
+    nvtx = torch.cuda.nvtx
     for _ in range(args.steps):
+        nvtx.range_push("fp64_solve")  # ranges for profiler filters (ncu --nvtx-include)
         x64, st = A.solve(rhs, rtol=rtol, atol=0.0, maxit=100000)
+        nvtx.range_pop()
         t64.append(st.seconds)
+        nvtx.range_push("mixed_solve")
         xm, stm = A.solve_mixed(rhs, rtol=rtol, atol=0.0, inner_rtol=args.inner_rtol)
+        nvtx.range_pop()
         tmx.append(stm.seconds)
     s64 = args.steps / sum(t64)
     smx = args.steps / sum(tmx)
