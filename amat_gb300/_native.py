@@ -27,7 +27,7 @@ class AfmInfo(C.Structure):
         ("map_bytes", C.c_uint64), ("algorithmic_bytes", C.c_uint64), ("algorithmic_flops", C.c_double),
         ("n_launches", C.c_uint32), ("device", C.c_int), ("n_patches", C.c_uint32),
         ("n_patch_colors", C.c_uint32), ("patch_index_bytes", C.c_uint64), ("ke_symmetric", C.c_int),
-        ("sym_available", C.c_int), ("sym_bytes", C.c_uint64),
+        ("sym_available", C.c_int), ("sym_bytes", C.c_uint64), ("csr_nnz", C.c_uint64),
     ]
 
 
@@ -65,6 +65,10 @@ AFM_SIGNATURES = {
     "afm_set_precision": (I, [P, I]),
     "afm_set_patch_mode": (I, [P, I]),
     "afm_set_symmetric_inner": (I, [P, I]),
+    "afm_assemble_csr_host": (I, [U32, U32, P, P, P, P, U32, I, I, P, P, P, P]),
+    "afm_assemble": (I, [P, I]),
+    "afm_matvec_assembled_device": (I, [P, P, P, P]),
+    "afm_get_assembled_csr": (I, [P, P, P, P, P]),
     "afm_server_create": (I, [P, I, U64, U32]),
     "afm_server_submit": (I, [P, P, P, D, D, P]),
     "afm_server_poll": (I, [P, P, P]),

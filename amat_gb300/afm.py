@@ -279,3 +279,45 @@ class aMatFree:
 
     def synchronize(self):
         check(self._lib.afm_synchronize(self._h), "afm_synchronize")
+
+    # ---- assembled operator (par::aMatBased) ----
+    def assemble(self, apply_bc=True):
+        """The matrix aMatBased assembles (include/aMatBased.hpp:214-352), kept on the device as CSR."""
+        check(self._lib.afm_assemble(self._h, int(bool(apply_bc))), "afm_assemble")
+
+    def matvec_assembled_device(self, v_ptr, u_ptr, stream=None):
+        """aMatBased::matmult on device vectors (CSR SpMV)."""
+        check(self._lib.afm_matvec_assembled_device(self._h, C.c_void_p(v_ptr), C.c_void_p(u_ptr),
+                                                    C.c_void_p(stream)), "afm_matvec_assembled_device")
+
+    def assembled_csr(self):
+        """dump_mat: (row_ptr, cols, vals) of the assembled matrix."""
+        nnz = C.c_uint64(0)
+        check(self._lib.afm_get_assembled_csr(self._h, C.byref(nnz), None, None, None), "afm_get_assembled_csr")
+        n = self.info()["n_dofs"]
+        rp = np.empty(n + 1, np.uint64)
+        cols = np.empty(nnz.value, np.uint32)
+        vals = np.empty(nnz.value)
+        check(self._lib.afm_get_assembled_csr(self._h, C.byref(nnz), _ptr(rp), _ptr(cols), _ptr(vals)),
+              "afm_get_assembled_csr")
+        return rp, cols, vals
+
+
+def assemble_csr_host(n_dofs, offsets, dof_map, ke, constrained=(), bc_method=BC_METH.BC_IMATRIX, apply_bc=True):
+    """Host-only aMatBased assembly (afm_assemble_csr_host): ke is the concatenation of the row-major element
+    matrices, offsets/dof_map the flattened map. Returns (row_ptr, cols, vals)."""
+    offsets = np.ascontiguousarray(offsets, dtype=np.uint32)
+    dof_map = np.ascontiguousarray(dof_map, dtype=np.uint32)
+    ke = np.ascontiguousarray(ke, dtype=np.float64).ravel()
+    cons = np.ascontiguousarray(constrained, dtype=np.uint64)
+    n_elem = len(offsets) - 1
+    nnz = C.c_uint64(0)
+    args = (n_elem, int(n_dofs), _ptr(offsets), _ptr(dof_map), _ptr(ke), _ptr(cons) if len(cons) else None,
+            len(cons), int(bc_method), int(bool(apply_bc)))
+    check(libafm().afm_assemble_csr_host(*args, C.byref(nnz), None, None, None), "afm_assemble_csr_host")
+    rp = np.empty(int(n_dofs) + 1, np.uint64)
+    cols = np.empty(nnz.value, np.uint32)
+    vals = np.empty(nnz.value)
+    check(libafm().afm_assemble_csr_host(*args, C.byref(nnz), _ptr(rp), _ptr(cols), _ptr(vals)),
+          "afm_assemble_csr_host")
+    return rp, cols, vals

@@ -214,6 +214,10 @@ void free_device(afm_operator* op) {
     dfree(op, op->d_patch_idx);
     dfree(op, op->d_sym);
     dfree(op, op->d_vx);
+    dfree(op, op->d_csr_rp);
+    dfree(op, op->d_csr_cols);
+    dfree(op, op->d_csr_vals);
+    op->csr_nnz = 0;
     op->work_elems = 0;
     op->work32_elems = 0;
 }
@@ -2330,6 +2334,7 @@ int afm_get_info(afm_operator* op, afm_info* info) {
     info->ke_symmetric = op->ke_symmetric ? 1 : 0;
     info->sym_available = sym_format(op);
     info->sym_bytes = op->d_sym ? op->sym_bytes : 0;
+    info->csr_nnz = op->csr_nnz;
     info->device = op->device;
     return ok();
 }

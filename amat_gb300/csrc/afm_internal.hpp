@@ -246,6 +246,13 @@ struct afm_operator {
     size_t sym_bytes = 0;
     double* d_vx = nullptr;         // format 2: FP64 product before its rounding to FP32 (n_dofs)
 
+    // assembled operator (afm_assembled.cpp): CSR on the device
+    uint64_t* d_csr_rp = nullptr;
+    uint32_t* d_csr_cols = nullptr;
+    double* d_csr_vals = nullptr;
+    uint64_t csr_nnz = 0;
+    int csr_width = 32;             // threads per row of the SpMV
+
     // patch path (small elements): patches in colour order
     bool use_patches = false;
     afm::PatchPlanGeom patch_geom;

@@ -376,6 +376,55 @@ def run_ours(args, w, rank, world, local_rank):
     return out
 
 
+def run_assembled(args, w, rank, world, local_rank):
+    """The aMatBased baseline: the same operator assembled into CSR (element-order sums, as the reference's
+    PETSc assembly) and multiplied by the hand-written CSR SpMV, against the assembly-free product."""
+    import torch
+    dev = local_rank
+    torch.cuda.set_device(dev)
+    prec = PREC_NAMES[args.precision]
+    m, dmap, A = build_problem(w, prec, dev)
+    t0 = time.time()
+    A.assemble(apply_bc=False)
+    t_asm = time.time() - t0
+    info = A.info()
+    n, nnz = m.n_dofs, info["csr_nnz"]
+    stream_ptr = A.stream()
+    stream = torch.cuda.ExternalStream(stream_ptr)
+    du = torch.tensor(np.random.default_rng(3).uniform(-1, 1, n), device="cuda")
+    va, vf = torch.empty_like(du), torch.empty_like(du)
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / args.steps
+
+    ms_csr = timed(lambda: A.matvec_assembled_device(va.data_ptr(), du.data_ptr(), stream_ptr))
+    ms_afm = timed(lambda: A.matvec_device(vf.data_ptr(), du.data_ptr(), stream_ptr))
+    diff = float(torch.linalg.norm(va - vf) / torch.linalg.norm(vf))
+    csr_bytes = nnz * 12 + 8 * (n + 1) + 16 * n
+    peak, peak_kind = measured_peak()
+    gbs = csr_bytes / (ms_csr * 1e-3) / 1e9
+    return {"metric": "assembled (CSR) matvec GB/s", "value": gbs, "unit": "GB/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_csr, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": w["desc"], "n_dofs": n, "n_elements": m.n_elem, "csr_nnz": nnz,
+                       "csr_bytes": csr_bytes, "host_assembly_s": t_asm},
+            "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                         "peak_kind": peak_kind, "kernel": "k_csr_spmv (%d threads per row)" % (
+                             8 if nnz / n <= 32 else 16 if nnz / n <= 96 else 32)},
+            "afm": {"ms": ms_afm, "algorithmic_bytes": info["algorithmic_bytes"],
+                    "precision": PREC_KEYS[info["precision"]]},
+            "afm_speedup_vs_assembled": ms_csr / ms_afm, "rel_diff_vs_afm": diff} if rank == 0 else None
+
+
 def build_bc_problem(w, dev):
     """Operator with the workload's boundary conditions (FP64_SPLIT arena: FP64 residual + FP32 view)."""
     from amat_gb300 import Maps, aMatFree
@@ -706,7 +755,8 @@ def main():
     ap.add_argument("--also-native", type=int, default=1, help="also time native FP64 when the split path runs")
     ap.add_argument("--cpu-sample-elems", type=int, default=65536)
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU time the baseline sample is timed for")
-    ap.add_argument("--mode", default="matvec", choices=["matvec", "solve", "batched", "product", "serve"])
+    ap.add_argument("--mode", default="matvec", choices=["matvec", "solve", "batched", "product", "serve",
+                                                         "assembled"])
     ap.add_argument("--rates", default="20,100,500", help="serve: arrival rates (requests/s)")
     ap.add_argument("--requests", type=int, default=160, help="serve: requests per rate")
     ap.add_argument("--edge-max", type=int, default=32, help="serve: largest mesh edge")
@@ -732,6 +782,7 @@ def main():
             torch.cuda.set_device(local_rank)
             torch.distributed.init_process_group("nccl")
         run = {"matvec": run_ours, "solve": run_solve, "batched": run_batched, "product": run_product,
+               "assembled": run_assembled,
                "serve": run_serve}[args.mode]
         out = run(args, w, rank, world, local_rank)
         if world > 1:

@@ -104,6 +104,7 @@ typedef struct afm_info {
     int ke_symmetric;           /* every Ke symmetric (FP64_SPLIT operators; 0 otherwise) */
     int sym_available;          /* format of the symmetric inner arena FP32 products use (0: none) */
     uint64_t sym_bytes;         /* device bytes of that arena once built (0: not built) */
+    uint64_t csr_nnz;           /* entries of the assembled matrix (0: afm_assemble not called) */
 } afm_info;
 
 typedef struct afm_solve_stats {
@@ -306,6 +307,32 @@ int afm_solve_cg_batched_mixed_device(afm_operator* op, const double* d_B, doubl
 int afm_patch_plan_host_matvec(uint32_t n_elem, uint32_t n_dofs, const uint32_t* offsets, const uint32_t* map,
                                const double* ke, const double* u, double* v, uint32_t* n_patches,
                                uint32_t* n_patch_colors);
+
+/* ---- assembled operator (par::aMatBased) ----------------------------------
+ * The matrix aMatBased assembles through PETSc, as CSR (row_ptr[n_dofs + 1],
+ * cols ascending per row, FP64 values): set_element_matrix with ADD_VALUES in
+ * element order (include/aMatBased.hpp:214-258), so every entry is summed in
+ * the reference's order and matches its matrix bit for bit; apply_bc = 1 also
+ * applies apply_bc_mat (294-352): identity method, constrained rows become
+ * unit rows and constrained columns zero; penalty method, constrained
+ * diagonals become 100 tr(K). The sparsity pattern is the union of the
+ * element patterns (entries set to zero are kept, as in the reference). */
+/* Host-only assembly (no device needed); ke holds the element matrices row
+ * by row, one after another (offsets as afm_set_map). Call with row_ptr,
+ * cols and vals NULL to get *nnz, then with arrays of that size (*nnz in:
+ * their capacity). */
+int afm_assemble_csr_host(uint32_t n_elem, uint32_t n_dofs, const uint32_t* offsets, const uint32_t* map,
+                          const double* ke, const uint64_t* constrained, uint32_t n_constrained, int bc_method,
+                          int apply_bc, uint64_t* nnz, uint64_t* row_ptr, uint32_t* cols, double* vals);
+/* Assembles the finalized operator's matrix (its element matrices, boundary
+ * conditions and method) and keeps it on the device. */
+int afm_assemble(afm_operator* op, int apply_bc);
+/* aMatBased::matmult (include/aMatBased.hpp:458-460) on device vectors: a
+ * hand-written CSR SpMV, bit-reproducible. */
+int afm_matvec_assembled_device(afm_operator* op, double* d_v, const double* d_u, void* stream);
+/* dump_mat (include/aMatBased.hpp:262-292): the assembled matrix as CSR
+ * (same calling convention as afm_assemble_csr_host). */
+int afm_get_assembled_csr(afm_operator* op, uint64_t* nnz, uint64_t* row_ptr, uint32_t* cols, double* vals);
 
 /* ---- serving: many CG solves on different operators ----------------------
  * No counterpart in the reference. A request is an operator whose maps and

@@ -41,6 +41,7 @@ _REF_SIGS = {
     "ref_based_matmult": (I, [P, P, P]),
     "ref_based_apply_bc": (I, [P, P]),
     "ref_based_destroy": (None, [P]),
+    "ref_based_csr": (C.c_uint64, [P, P, P, P]),
     "ref_mesh_coloring": (I, [U32, U32, P, P, P, P]),
     "ref_gauss": (None, [U32, P]),
     "ref_ke_hex8": (None, [P, U32, P]),
@@ -175,7 +176,8 @@ class Problem:
         return dict(matvec=v, diag=d, rhs_bc=r, matmult_bc=w)
 
     def ref_assembled(self, u, rhs, bc_method=0):
-        """Reference aMatBased (PETSc-assembled) K u before BCs, then K_bc u and rhs after apply_bc."""
+        """Reference aMatBased (PETSc-assembled) K u before BCs, then K_bc u, rhs and the matrix (CSR) after
+        apply_bc."""
         R = ref()
         h = R.ref_based_create(self.n_elem, self.n_dofs, _p(self.offsets), _p(self.map), _p(self.ke), 1,
                                _p(self.constrained), _p(self.values), len(self.constrained), bc_method)
@@ -186,8 +188,13 @@ class Problem:
         R.ref_based_apply_bc(h, _p(r))
         w = np.empty(self.n_dofs)
         R.ref_based_matmult(h, _p(w), _p(u))
+        nnz = int(R.ref_based_csr(h, None, None, None))
+        rp = np.empty(self.n_dofs + 1, np.uint64)
+        cols = np.empty(nnz, np.uint32)
+        vals = np.empty(nnz)
+        R.ref_based_csr(h, _p(rp), _p(cols), _p(vals))
         R.ref_based_destroy(h)
-        return dict(matvec=v, rhs_bc=r, matmult_bc=w)
+        return dict(matvec=v, rhs_bc=r, matmult_bc=w, csr_row_ptr=rp, csr_cols=cols, csr_vals=vals)
 
     def ref_coloring(self):
         c = np.empty(self.n_elem, dtype=np.uint32)

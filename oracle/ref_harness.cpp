@@ -198,6 +198,25 @@ int ref_based_apply_bc(void* h, double* rhs) {
     return 0;
 }
 
+// The assembled matrix as CSR, rows in order, columns ascending (the shim's
+// row maps; PETSc's MatView of dump_mat, include/aMatBased.hpp:262-292, lists
+// the same entries). Returns the entry count; fills the arrays when given.
+uint64_t ref_based_csr(void* h, uint64_t* row_ptr, uint32_t* cols, double* vals) {
+    auto* r = (RefBased*)h;
+    Mat A = r->A->get_matrix();
+    uint64_t k = 0;
+    for (size_t i = 0; i < A->rows.size(); i++) {
+        if (row_ptr) row_ptr[i] = k;
+        for (const auto& e : A->rows[i]) {
+            if (cols) cols[k] = (uint32_t)e.first;
+            if (vals) vals[k] = e.second;
+            k++;
+        }
+    }
+    if (row_ptr) row_ptr[A->rows.size()] = k;
+    return k;
+}
+
 void ref_based_destroy(void* h) { delete (RefBased*)h; }
 
 // meshGraph::mesh2Graph + greedyColoring (include/meshGraph.hpp:132-155, 59-109)

@@ -6,7 +6,8 @@ reference sources in place (oracle/build_ref.sh) and records, for small seeded
 problems, the reference's own outputs:
   - aMatFree (method 1) matvec, MatMult_mf, MatGetDiagonal_mf, apply_bc rhs
     (identity and penalty), for blocks_dim 1 and 2;
-  - aMatBased (assembled) K u, K_bc u and rhs;
+  - aMatBased (assembled) K u, K_bc u and rhs, and the assembled matrix after the
+    identity and penalty BCs (CSR);
   - meshGraph greedy colouring;
   - element matrices of ke_matrix.cpp for jittered elements of each kind;
   - the Gauss-Legendre rule of integration.hpp.
@@ -87,7 +88,12 @@ def record(case, out):
                 diag_penalty=rpen["diag"], rhs_bc_penalty=rpen["rhs_bc"], matmult_bc_penalty=rpen["matmult_bc"])
     if bd == 1:
         a = prob.ref_assembled(u, rhs, bc_method=0)
-        data.update(asm_matvec=a["matvec"], asm_matmult_bc=a["matmult_bc"], asm_rhs_bc=a["rhs_bc"])
+        data.update(asm_matvec=a["matvec"], asm_matmult_bc=a["matmult_bc"], asm_rhs_bc=a["rhs_bc"],
+                    asm_row_ptr=a["csr_row_ptr"], asm_cols=a["csr_cols"], asm_vals=a["csr_vals"])
+        a = prob.ref_assembled(u, rhs, bc_method=1)
+        data.update(asm_matmult_bc_penalty=a["matmult_bc"], asm_rhs_bc_penalty=a["rhs_bc"],
+                    asm_vals_penalty=a["csr_vals"])
+        assert np.array_equal(a["csr_row_ptr"], data["asm_row_ptr"]) and np.array_equal(a["csr_cols"], data["asm_cols"])
     if "coords" in case:
         data.update(coords=case["coords"], elem_nodes=case["elem_nodes"])
     np.savez_compressed(out, **data)
