@@ -216,9 +216,9 @@ int afm_assemble(afm_operator* op, int apply_bc) {
                           cudaGetErrorString(e));
         } else {
             op->csr_nnz = nnz;
-            // threads per row: about a quarter of the mean row length, 8 to 32
+            // threads per row: about a quarter of the mean row length, 4 to 32
             const double mean = op->n_dofs ? (double)nnz / op->n_dofs : 0.0;
-            op->csr_width = mean <= 32.0 ? 8 : mean <= 96.0 ? 16 : 32;
+            op->csr_width = mean <= 32.0 ? 4 : mean <= 64.0 ? 8 : mean <= 128.0 ? 16 : 32;
             s = set_error(AFM_SUCCESS, "");
         }
     }

@@ -1,8 +1,8 @@
 // CSR SpMV of the assembled operator (afm_assembled.cpp): y = A x in FP64.
-// W threads per row (W = 8, 16 or 32 by the mean row length); each thread
-// sums the row's entries j = start + lane, start + lane + W, ... in order
-// (loading four of them ahead),
-// then the W partial sums meet in a fixed shuffle tree, so y is
+// W threads per row (4 to 32: about a quarter of the mean row length, so
+// that each thread has four entries to load ahead); each thread sums the
+// row's entries j = start + lane, start + lane + W, ... in order, then the W
+// partial sums meet in a fixed shuffle tree, so y is
 // bit-reproducible. Values and column indices are read once per product
 // (streaming loads); x is gathered through the L1/L2 caches.
 #include <cuda_runtime.h>
@@ -51,6 +51,7 @@ cudaError_t launch_csr_spmv(const uint64_t* rp, const uint32_t* cols, const doub
     const uint64_t want = (threads + 255) / 256;
     const uint32_t grid = (uint32_t)(want < (uint64_t)sm_count * 8 ? want : (uint64_t)sm_count * 8);
     switch (width) {
+        case 4: k_csr_spmv<4><<<grid, 256, 0, st>>>(rp, cols, vals, x, y, n_rows); break;
         case 8: k_csr_spmv<8><<<grid, 256, 0, st>>>(rp, cols, vals, x, y, n_rows); break;
         case 16: k_csr_spmv<16><<<grid, 256, 0, st>>>(rp, cols, vals, x, y, n_rows); break;
         default: k_csr_spmv<32><<<grid, 256, 0, st>>>(rp, cols, vals, x, y, n_rows); break;

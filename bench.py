@@ -419,7 +419,7 @@ def run_assembled(args, w, rank, world, local_rank):
                        "csr_bytes": csr_bytes, "host_assembly_s": t_asm},
             "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
                          "peak_kind": peak_kind, "kernel": "k_csr_spmv (%d threads per row)" % (
-                             8 if nnz / n <= 32 else 16 if nnz / n <= 96 else 32)},
+                             4 if nnz / n <= 32 else 8 if nnz / n <= 64 else 16 if nnz / n <= 128 else 32)},
             "afm": {"ms": ms_afm, "algorithmic_bytes": info["algorithmic_bytes"],
                     "precision": PREC_KEYS[info["precision"]]},
             "afm_speedup_vs_assembled": ms_csr / ms_afm, "rel_diff_vs_afm": diff} if rank == 0 else None
