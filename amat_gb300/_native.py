@@ -65,6 +65,8 @@ AFM_SIGNATURES = {
     "afm_set_precision": (I, [P, I]),
     "afm_set_patch_mode": (I, [P, I]),
     "afm_set_symmetric_inner": (I, [P, I]),
+    "afm_set_element_kind": (I, [P, I, D, D, U32]),
+    "afm_set_element_coords": (I, [P, U32, U32, P]),
     "afm_assemble_csr_host": (I, [U32, U32, P, P, P, P, U32, I, I, P, P, P, P]),
     "afm_assemble": (I, [P, I]),
     "afm_matvec_assembled_device": (I, [P, P, P, P]),

@@ -21,8 +21,10 @@ class BC_METH(enum.IntEnum):
 
 
 class MATFREE_TYPE(enum.IntEnum):
-    """par::MATFREE_TYPE (include/enums.hpp:56); 1 and 3 run the stored-Ke device operator."""
+    """par::MATFREE_TYPE (include/enums.hpp:56); 1 and 3 run the stored-Ke device operator, 2 the matrix-free one
+    (element kernels on the device from node coordinates)."""
     QUASI_FREE = 1
+    FREE = 2
     GPU_PURE = 3
 
 
@@ -136,6 +138,18 @@ class aMatFree:
         """Inner format of FP32 products: 1 (default) symmetric copy in FP32, 2 symmetric copy in FP32 + BF16
         correction with FP64 sums, 0 the hi plane."""
         check(self._lib.afm_set_symmetric_inner(self._h, int(fmt)), "afm_set_symmetric_inner")
+
+    def set_element_kind(self, kind, E=1.0, nu=0.3, ngt=2):
+        """Element kernels of the matrix-free operator (method 2), the counterpart of
+        set_element_matrix_function (include/aMat.hpp:114-116); kind as problems.HEX8_POISSON etc."""
+        check(self._lib.afm_set_element_kind(self._h, int(kind), float(E), float(nu), int(ngt)),
+              "afm_set_element_kind")
+
+    def set_element_coords(self, first_eid, xe):
+        """Node coordinates (count x nodes x 3) of elements first_eid, first_eid + 1, ..."""
+        x = np.ascontiguousarray(xe, dtype=np.float64)
+        check(self._lib.afm_set_element_coords(self._h, int(first_eid), int(x.shape[0]), _ptr(x)),
+              "afm_set_element_coords")
 
     def set_element_matrix(self, eid, e_mat, block_i=0, block_j=0, blocks_dim=1):
         """aMatFree::set_element_matrix (include/aMatFree.hpp:856-880)."""

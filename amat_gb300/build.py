@@ -26,10 +26,10 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fopenmp", "--expt-relaxed-constexpr"] + ARCH
 CU_SOURCES = ["afm_mv_fp64.cu", "afm_mv_split.cu", "afm_mv_fp32.cu", "afm_mv_f32sym.cu", "afm_mv_f32symx.cu",
               "afm_solver.cu",
-              "afm_batched_solver.cu", "afm_noalloc.cu", "afm_spmv.cu", "afm_capi.cpp", "afm_server.cpp",
+              "afm_batched_solver.cu", "afm_noalloc.cu", "afm_spmv.cu", "afm_free.cu", "afm_capi.cpp", "afm_server.cpp",
               "afm_assembled.cpp"]
 HEADERS = ["afm_internal.hpp", "afm_matvec.cuh", "afm_batched.cuh", "afm_patch.cuh", "afm_mv_launch.inl",
-           "afm_solver.hpp", "afm_batched_solver.hpp", "afm_mixed.hpp"]
+           "afm_solver.hpp", "afm_batched_solver.hpp", "afm_mixed.hpp", "afm_shape.hpp"]
 
 
 def _nvcc():
@@ -82,7 +82,7 @@ def build_problems():
     hdr = os.path.join(ROOT, "include", "afm_problems.h")
     if not os.path.exists(src):
         return None
-    if not _newer(PROBLEMS_LIB, [src, hdr]):
+    if not _newer(PROBLEMS_LIB, [src, hdr, os.path.join(CSRC, "afm_shape.hpp")]):
         cxx = shutil.which("g++") or "g++"
         _run([cxx, "-O3", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-I" + os.path.join(ROOT, "include"),
               src, "-o", PROBLEMS_LIB])

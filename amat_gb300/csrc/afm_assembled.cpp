@@ -184,6 +184,8 @@ int afm_assemble_csr_host(uint32_t n_elem, uint32_t n_dofs, const uint32_t* offs
 int afm_assemble(afm_operator* op, int apply_bc) {
     if (!op) return set_error(AFM_ERR_INVALID_ARG, "null operator");
     if (!op->finalized) return set_error(AFM_ERR_STATE, "assemble before finalize");
+    if (op->ke.size() != op->kofs[op->n_elem])
+        return set_error(AFM_ERR_STATE, "assembly needs the element matrices (set_element_matrix)");
     int prev = -1;
     cudaGetDevice(&prev);
     cudaSetDevice(op->device);

@@ -27,6 +27,7 @@
 #include "afm_batched_solver.hpp"
 #include "afm_internal.hpp"
 #include "afm_mixed.hpp"
+#include "afm_shape.hpp"
 #include "afm_solver.hpp"
 
 namespace afm {
@@ -218,6 +219,10 @@ void free_device(afm_operator* op) {
     dfree(op, op->d_csr_cols);
     dfree(op, op->d_csr_vals);
     op->csr_nnz = 0;
+    dfree(op, op->d_free_xe64);
+    dfree(op, op->d_free_xe32);
+    dfree(op, op->d_free_ref64);
+    dfree(op, op->d_free_ref32);
     op->work_elems = 0;
     op->work32_elems = 0;
 }
@@ -718,7 +723,30 @@ int check_device_error(afm_operator* op) {
 
 // v = K u (bc_mode 0) or the product of MatMult_mf without the final v_c = u_c
 // (bc_mode 1: constrained columns of u read as zero), device arrays.
+// Matrix-free product (method 2): one launch per colour.
+int enqueue_free(afm_operator* op, void* d_v, const void* d_u, int bc_mode, cudaStream_t st, bool f32) {
+    AFM_CUDA(cudaMemsetAsync(d_v, 0, (size_t)op->n_dofs * (f32 ? 4 : 8), st));
+    const double E = op->elem_E, nu = op->elem_nu;
+    FreeArgs a;
+    a.xe = f32 ? (const void*)op->d_free_xe32 : (const void*)op->d_free_xe64;
+    a.map = op->d_map;
+    a.ref = f32 ? (const void*)op->d_free_ref32 : (const void*)op->d_free_ref64;
+    a.u = d_u;
+    a.v = d_v;
+    a.nq = op->free_nq;
+    a.bc_mode = bc_mode;
+    a.lam = E * nu / (1.0 + nu) / (1.0 - 2.0 * nu);
+    a.mu = 0.5 * E / (1.0 + nu);
+    for (size_t c = 0; c + 1 < op->free_color_first.size(); c++) {
+        a.first = op->free_color_first[c];
+        a.count = op->free_color_first[c + 1] - a.first;
+        AFM_CUDA(launch_free(op->elem_kind, f32, a, op->sm_count, st));
+    }
+    return AFM_SUCCESS;
+}
+
 int enqueue_matvec(afm_operator* op, void* d_v, const void* d_u, int bc_mode, cudaStream_t st, bool f32 = false) {
+    if (op->matfree_type == 2) return enqueue_free(op, d_v, d_u, bc_mode, st, f32);
     // f32: FP32 product on float vectors, from the symmetric inner arena once
     // built, else from an FP32 arena or the hi plane of a split arena (half of
     // each unit is copied)
@@ -822,6 +850,7 @@ int enqueue_matvec_batched(afm_operator* op, void* d_V, const void* d_U, uint32_
 
 int check_batched(afm_operator* op, uint32_t nrhs, uint32_t ld) {
     if (!op->finalized) return fail(AFM_ERR_STATE, "batched product before finalize");
+    if (op->matfree_type == 2) return fail(AFM_NOT_IMPLEMENTED, "batched product of a matrix-free (method 2) operator");
     if (nrhs == 0 || nrhs > 256 || nrhs % 4 != 0 || ld < nrhs || ld % 4 != 0)
         return fail(AFM_ERR_INVALID_ARG, "nrhs %u (multiple of 4, <= 256), ld %u (>= nrhs, multiple of 4)", nrhs, ld);
     for (const Segment& s : op->segs)
@@ -1233,7 +1262,7 @@ int mixed_begin(MixedSolve& m) {
     afm_operator* op = m.op;
     AFM_CHECK_OP(op);
     if (!op->finalized) return fail(AFM_ERR_STATE, "solve before finalize");
-    if (op->precision != AFM_PREC_FP64_SPLIT)
+    if (op->precision != AFM_PREC_FP64_SPLIT && op->matfree_type != 2)
         return fail(AFM_ERR_STATE, "mixed-precision solve needs the FP64_SPLIT arena (hi plane = FP32 matrix)");
     if (!m.d_b || !m.d_x) return fail(AFM_ERR_INVALID_ARG, "null vector");
     DeviceGuard g(op->device);
@@ -1448,7 +1477,8 @@ int afm_destroy(afm_operator* op) {
 
 int afm_set_matfree_type(afm_operator* op, int t) {
     AFM_CHECK_OP(op);
-    if (t != 1 && t != 3) return fail(AFM_UNKNOWN_MAT_TYPE, "MATFREE_TYPE %d not provided (1 or 3)", t);
+    if (t != 1 && t != 2 && t != 3) return fail(AFM_UNKNOWN_MAT_TYPE, "MATFREE_TYPE %d not provided (1, 2 or 3)", t);
+    if ((t == 2) != (op->matfree_type == 2)) op->finalized = false;
     op->matfree_type = t;
     return ok();
 }
@@ -1527,11 +1557,11 @@ int afm_set_map(afm_operator* op, uint32_t n_elements, const uint32_t* dof_offse
         std::sort(tmp.begin(), tmp.end());
         if (std::adjacent_find(tmp.begin(), tmp.end()) != tmp.end()) op->dup_in_element = true;
     }
-    try {
-        op->ke.assign(op->kofs[n_elements], 0.0);
-    } catch (...) {
-        return fail(AFM_ERR_OOM, "host element-matrix store of %llu entries", (unsigned long long)op->kofs[n_elements]);
-    }
+    // the host element-matrix store is allocated by the first set_element_matrix (a matrix-free
+    // operator never needs it)
+    op->ke.clear();
+    op->ke.shrink_to_fit();
+    op->xe.clear();
     op->have_map = true;
     op->finalized = false;
     op->ke_dirty = true;
@@ -1554,10 +1584,25 @@ int afm_set_bdr_map(afm_operator* op, const uint64_t* constrained, const double*
     return ok();
 }
 
+namespace {
+// Host store of the element matrices (zeros until set), n_elem blocks of n^2 entries.
+int ensure_ke_store(afm_operator* op) {
+    const uint64_t need = op->kofs.empty() ? 0 : op->kofs[op->n_elem];
+    if (op->ke.size() == need) return AFM_SUCCESS;
+    try {
+        op->ke.assign(need, 0.0);
+    } catch (...) {
+        return fail(AFM_ERR_OOM, "host element-matrix store of %llu entries", (unsigned long long)need);
+    }
+    return AFM_SUCCESS;
+}
+}  // namespace
+
 int afm_set_element_matrix(afm_operator* op, uint32_t eid, const double* e_mat, uint32_t bi, uint32_t bj,
                            uint32_t bd) {
     AFM_CHECK_OP(op);
     if (!op->have_map) return fail(AFM_ERR_STATE, "set_element_matrix before set_map");
+    if (int st = ensure_ke_store(op)) return st;
     if (eid >= op->n_elem) return fail(AFM_INDEX_OUT_OF_BOUNDS, "element %u >= %u", eid, op->n_elem);
     if (!e_mat || bd == 0 || bi >= bd || bj >= bd) return fail(AFM_ERR_INVALID_ARG, "bad block (%u,%u) of %u", bi, bj, bd);
     const uint32_t n = op->offsets[eid + 1] - op->offsets[eid];
@@ -1576,6 +1621,7 @@ int afm_set_element_matrices(afm_operator* op, uint32_t first, uint32_t count, c
     if (!op->have_map) return fail(AFM_ERR_STATE, "set_element_matrices before set_map");
     if ((uint64_t)first + count > op->n_elem) return fail(AFM_INDEX_OUT_OF_BOUNDS, "elements %u+%u > %u", first, count, op->n_elem);
     if (count && !ke) return fail(AFM_ERR_INVALID_ARG, "ke is null");
+    if (int st = ensure_ke_store(op)) return st;
     const uint64_t a = op->kofs[first], b = op->kofs[(size_t)first + count];
     memcpy(op->ke.data() + a, ke, (size_t)(b - a) * sizeof(double));
     op->ke_dirty = true;
@@ -1583,9 +1629,180 @@ int afm_set_element_matrices(afm_operator* op, uint32_t first, uint32_t count, c
     return ok();
 }
 
+namespace {
+
+// Matrix-free finalize (method 2): colours, the colour-sorted element order
+// with its DoF map and node coordinates (FP64 and FP32), the reference-element
+// tables, and the Jacobi diagonal and trace from the element kernels on the
+// host (each diagonal entry summed exactly as the stored-Ke element kernel
+// sums it, so both operators give the same diagonal).
+int finalize_free(afm_operator* op) {
+    if (op->elem_kind < 0) return fail(AFM_ERR_STATE, "MATFREE_TYPE::FREE needs afm_set_element_kind");
+    afm_shape::Kind K;
+    if (!afm_shape::kind_info(op->elem_kind, &K)) return fail(AFM_UNKNOWN_ELEMENT_TYPE, "kind %d", op->elem_kind);
+    const uint32_t nn = (uint32_t)K.nodes, n = nn * (uint32_t)K.dpn;
+    for (uint32_t e = 0; e < op->n_elem; e++)
+        if (op->offsets[e + 1] - op->offsets[e] != n)
+            return fail(AFM_ERR_INVALID_ARG, "element %u has %u DoFs, kind %d needs %u", e,
+                        op->offsets[e + 1] - op->offsets[e], op->elem_kind, n);
+    if (op->xe.size() != (size_t)op->n_elem * nn * 3) return fail(AFM_ERR_STATE, "element coordinates not set");
+    DeviceGuard g(op->device);
+    AFM_CUDA(cudaStreamSynchronize(op->stream));
+    free_device(op);
+    op->finalized = false;
+    op->precision = AFM_PREC_FP64;  // FP64 products in FP64 arithmetic, _f32 products in FP32
+    op->use_patches = false;
+    op->n_patches = 0;
+    op->patch_color_first.clear();
+    op->segs.clear();
+    op->sym_ok = false;
+    op->ke_symmetric = false;
+    op->n_colors = color_elements(op->n_dofs, op->n_elem, op->offsets, op->map, op->colors);
+    op->perm.resize(op->n_elem);
+    std::iota(op->perm.begin(), op->perm.end(), 0u);
+    std::stable_sort(op->perm.begin(), op->perm.end(),
+                     [&](uint32_t a, uint32_t b) { return op->colors[a] < op->colors[b]; });
+    op->free_color_first.assign(op->n_colors + 1, 0);
+    for (uint32_t e = 0; e < op->n_elem; e++) op->free_color_first[op->colors[e] + 1]++;
+    for (uint32_t c = 0; c < op->n_colors; c++) op->free_color_first[c + 1] += op->free_color_first[c];
+    std::vector<uint8_t> is_bc(op->n_dofs, 0);
+    for (uint32_t d : op->bc_unique) is_bc[d] = 1;
+    std::vector<uint32_t> hmap((size_t)op->n_elem * n);
+    std::vector<double> x64((size_t)op->n_elem * nn * 3);
+    std::vector<float> x32(x64.size());
+#pragma omp parallel for schedule(static)
+    for (int64_t p = 0; p < (int64_t)op->n_elem; p++) {
+        const uint32_t e = op->perm[p];
+        for (uint32_t i = 0; i < n; i++) {
+            const uint32_t d = op->map[op->offsets[e] + i];
+            hmap[(size_t)p * n + i] = d | (is_bc[d] ? kBcFlag : 0u);
+        }
+        for (uint32_t k = 0; k < nn * 3; k++) {
+            x64[(size_t)p * nn * 3 + k] = op->xe[(size_t)e * nn * 3 + k];
+            x32[(size_t)p * nn * 3 + k] = (float)op->xe[(size_t)e * nn * 3 + k];
+        }
+    }
+    // reference tables: dN of every node at every quadrature point, then the weights
+    std::vector<double> q;
+    afm_shape::quadrature(K.tet, op->elem_ngt, q);
+    const uint32_t nq = (uint32_t)(q.size() / 4);
+    std::vector<double> r64((size_t)nq * (nn * 3 + 1));
+    for (uint32_t t = 0; t < nq; t++) {
+        K.shape(&q[4 * t], nullptr, &r64[(size_t)t * nn * 3]);
+        r64[(size_t)nq * nn * 3 + t] = q[4 * t + 3];
+    }
+    std::vector<float> r32(r64.begin(), r64.end());
+    op->free_nq = nq;
+    // Jacobi diagonal and trace in element order (mat_get_diagonal, include/aMatFree.hpp:998-1056)
+    const double E = op->elem_E, nu = op->elem_nu;
+    const double lam = E * nu / (1.0 + nu) / (1.0 - 2.0 * nu), mu = 0.5 * E / (1.0 + nu);
+    std::vector<double> kd((size_t)op->n_elem * n, 0.0);
+    int bad = 0;
+#pragma omp parallel for schedule(static) reduction(| : bad)
+    for (int64_t e = 0; e < (int64_t)op->n_elem; e++) {
+        double dNx[3 * 20], detJ;
+        double* k = kd.data() + (size_t)e * n;
+        const double* xe = op->xe.data() + (size_t)e * nn * 3;
+        for (size_t t = 0; t < q.size(); t += 4) {
+            if (!afm_shape::gradients(K, xe, &q[t], nullptr, dNx, &detJ)) {
+                bad = 1;
+                break;
+            }
+            const double w = detJ * q[t + 3];
+            for (uint32_t a = 0; a < nn; a++) {
+                const double* ga = dNx + 3 * a;
+                const double gg = ga[0] * ga[0] + ga[1] * ga[1] + ga[2] * ga[2];
+                if (K.dpn == 1) {
+                    k[a] += gg * w;
+                } else {
+                    for (int i = 0; i < 3; i++) {
+                        double v = lam * ga[i] * ga[i] + mu * ga[i] * ga[i];
+                        v += mu * gg;
+                        k[3 * a + i] += v * w;
+                    }
+                }
+            }
+        }
+    }
+    if (bad) return fail(AFM_ERR_INVALID_ARG, "an element has a non-positive Jacobian");
+    op->diag_host.assign(op->n_dofs, 0.0);
+    op->trace = 0.0;
+    for (uint32_t e = 0; e < op->n_elem; e++)
+        for (uint32_t r = 0; r < n; r++) {
+            op->diag_host[op->map[op->offsets[e] + r]] += kd[(size_t)e * n + r];
+            op->trace += kd[(size_t)e * n + r];
+        }
+    const double bc_diag = (op->bc_method == AFM_BC_PENALTY) ? 100.0 * op->trace : 1.0;
+    for (uint32_t d : op->map)
+        if (is_bc[d]) op->diag_host[d] = bc_diag;
+    // uploads
+    op->ke_bytes = 0;
+    op->map_bytes = hmap.size() * sizeof(uint32_t);
+    op->n_bc = (uint32_t)op->constrained.size();
+    AFM_CUDA(dalloc(op, &op->d_map, std::max<size_t>(op->map_bytes, 16)));
+    AFM_CUDA(dalloc(op, &op->d_diag, sizeof(double) * std::max<uint32_t>(op->n_dofs, 1)));
+    AFM_CUDA(dalloc(op, &op->d_bc_idx, sizeof(uint32_t) * std::max<uint32_t>(op->n_bc, 1)));
+    AFM_CUDA(dalloc(op, &op->d_bc_val, sizeof(double) * std::max<uint32_t>(op->n_bc, 1)));
+    AFM_CUDA(dalloc(op, &op->d_free_xe64, sizeof(double) * std::max<size_t>(x64.size(), 1)));
+    AFM_CUDA(dalloc(op, &op->d_free_xe32, sizeof(float) * std::max<size_t>(x32.size(), 1)));
+    AFM_CUDA(dalloc(op, &op->d_free_ref64, sizeof(double) * r64.size()));
+    AFM_CUDA(dalloc(op, &op->d_free_ref32, sizeof(float) * r32.size()));
+    std::vector<uint32_t> bci(op->constrained.begin(), op->constrained.end());
+    cudaStream_t st = op->stream;
+    AFM_CUDA(cudaMemcpyAsync(op->d_map, hmap.data(), op->map_bytes, cudaMemcpyHostToDevice, st));
+    AFM_CUDA(cudaMemcpyAsync(op->d_diag, op->diag_host.data(), sizeof(double) * op->n_dofs, cudaMemcpyHostToDevice,
+                             st));
+    if (op->n_bc) {
+        AFM_CUDA(cudaMemcpyAsync(op->d_bc_idx, bci.data(), sizeof(uint32_t) * op->n_bc, cudaMemcpyHostToDevice, st));
+        AFM_CUDA(cudaMemcpyAsync(op->d_bc_val, op->values.data(), sizeof(double) * op->n_bc, cudaMemcpyHostToDevice,
+                                 st));
+    }
+    AFM_CUDA(cudaMemcpyAsync(op->d_free_xe64, x64.data(), sizeof(double) * x64.size(), cudaMemcpyHostToDevice, st));
+    AFM_CUDA(cudaMemcpyAsync(op->d_free_xe32, x32.data(), sizeof(float) * x32.size(), cudaMemcpyHostToDevice, st));
+    AFM_CUDA(cudaMemcpyAsync(op->d_free_ref64, r64.data(), sizeof(double) * r64.size(), cudaMemcpyHostToDevice, st));
+    AFM_CUDA(cudaMemcpyAsync(op->d_free_ref32, r32.data(), sizeof(float) * r32.size(), cudaMemcpyHostToDevice, st));
+    AFM_CUDA(cudaStreamSynchronize(st));
+    op->ke_dirty = false;
+    op->finalized = true;
+    return ok();
+}
+
+}  // namespace
+
+int afm_set_element_kind(afm_operator* op, int kind, double E, double nu, uint32_t ngt) {
+    AFM_CHECK_OP(op);
+    afm_shape::Kind K;
+    if (!afm_shape::kind_info(kind, &K)) return fail(AFM_UNKNOWN_ELEMENT_TYPE, "element kind %d", kind);
+    if (ngt < 1 || ngt > 3) return fail(AFM_ERR_INVALID_ARG, "%u Gauss points per direction (1 to 3)", ngt);
+    if (K.dpn == 3 && !(E > 0.0 && nu > -1.0 && nu < 0.5)) return fail(AFM_ERR_INVALID_ARG, "E %g, nu %g", E, nu);
+    if ((uint32_t)K.nodes != op->elem_nodes) op->xe.clear();
+    op->elem_kind = kind;
+    op->elem_E = E;
+    op->elem_nu = nu;
+    op->elem_ngt = ngt;
+    op->elem_nodes = (uint32_t)K.nodes;
+    op->finalized = false;
+    return ok();
+}
+
+int afm_set_element_coords(afm_operator* op, uint32_t first, uint32_t count, const double* xe) {
+    AFM_CHECK_OP(op);
+    if (!op->have_map) return fail(AFM_ERR_STATE, "set_element_coords before set_map");
+    if (op->elem_kind < 0) return fail(AFM_ERR_STATE, "set_element_coords before set_element_kind");
+    if ((uint64_t)first + count > op->n_elem) return fail(AFM_INDEX_OUT_OF_BOUNDS, "elements %u+%u > %u", first, count, op->n_elem);
+    if (count && !xe) return fail(AFM_ERR_INVALID_ARG, "xe is null");
+    const size_t per = (size_t)op->elem_nodes * 3;
+    if (op->xe.size() != (size_t)op->n_elem * per) op->xe.assign((size_t)op->n_elem * per, 0.0);
+    memcpy(op->xe.data() + (size_t)first * per, xe, sizeof(double) * per * count);
+    op->finalized = false;
+    return ok();
+}
+
 int afm_finalize(afm_operator* op) {
     AFM_CHECK_OP(op);
     if (!op->have_map) return fail(AFM_ERR_STATE, "finalize before set_map");
+    if (op->matfree_type == 2) return finalize_free(op);
+    if (int st = ensure_ke_store(op)) return st;
     DeviceGuard g(op->device);
     AFM_CUDA(cudaStreamSynchronize(op->stream));
     free_device(op);
@@ -1735,8 +1952,8 @@ int afm_matvec_device(afm_operator* op, double* d_v, const double* d_u, void* st
 int afm_matvec_device_f32(afm_operator* op, float* d_v, const float* d_u, void* stream) {
     AFM_CHECK_OP(op);
     if (!op->finalized) return fail(AFM_ERR_STATE, "matvec before finalize");
-    if (op->precision != AFM_PREC_FP32 && op->precision != AFM_PREC_FP64_SPLIT)
-        return fail(AFM_ERR_STATE, "FP32 product needs an FP32 or FP64_SPLIT operator");
+    if (op->precision != AFM_PREC_FP32 && op->precision != AFM_PREC_FP64_SPLIT && op->matfree_type != 2)
+        return fail(AFM_ERR_STATE, "FP32 product needs an FP32, FP64_SPLIT or matrix-free operator");
     if (!d_v || !d_u || (void*)d_v == (const void*)d_u) return fail(AFM_ERR_INVALID_ARG, "bad vectors");
     DeviceGuard g(op->device);
     cudaStream_t st = pick_stream(op, stream);
@@ -1800,8 +2017,8 @@ int afm_matmult_bc(afm_operator* op, double* v, const double* u) {
 int afm_matmult_bc_device_f32(afm_operator* op, float* d_v, const float* d_u, void* stream) {
     AFM_CHECK_OP(op);
     if (!op->finalized) return fail(AFM_ERR_STATE, "matmult before finalize");
-    if (op->precision != AFM_PREC_FP32 && op->precision != AFM_PREC_FP64_SPLIT)
-        return fail(AFM_ERR_STATE, "FP32 product needs an FP32 or FP64_SPLIT operator");
+    if (op->precision != AFM_PREC_FP32 && op->precision != AFM_PREC_FP64_SPLIT && op->matfree_type != 2)
+        return fail(AFM_ERR_STATE, "FP32 product needs an FP32, FP64_SPLIT or matrix-free operator");
     if (!d_v || !d_u || (void*)d_v == (const void*)d_u) return fail(AFM_ERR_INVALID_ARG, "bad vectors");
     DeviceGuard g(op->device);
     cudaStream_t st = pick_stream(op, stream);
@@ -2108,7 +2325,7 @@ int afm_solve_cg_batched_mixed_device(afm_operator* op, const double* d_B, doubl
     AFM_CHECK_OP(op);
     int s = check_batched(op, nrhs, nrhs);
     if (s) return s;
-    if (op->precision != AFM_PREC_FP64_SPLIT)
+    if (op->precision != AFM_PREC_FP64_SPLIT && op->matfree_type != 2)
         return fail(AFM_ERR_STATE, "mixed-precision solve needs the FP64_SPLIT arena (hi plane = FP32 matrix)");
     if (!d_B || !d_X) return fail(AFM_ERR_INVALID_ARG, "null block");
     if (((uintptr_t)d_B | (uintptr_t)d_X) % 16) return fail(AFM_ERR_INVALID_ARG, "blocks must be 16-byte aligned");

@@ -145,6 +145,20 @@ cudaError_t launch_patches(int prec, const PatchPlanGeom& pg, const PatchArgs& a
 // Shared memory of a patch launch (0 if it does not fit).
 size_t patch_smem_bytes(int prec, const PatchPlanGeom& pg, uint32_t copy_bytes);
 
+// Arguments of one matrix-free (method 2) launch: the elements first ..
+// first + count - 1 of the colour-sorted order (one colour).
+struct FreeArgs {
+    const void* xe;        // node coordinates, element-major (nodes x 3), double or float
+    const uint32_t* map;   // n DoFs per element (kBcFlag on constrained DoFs)
+    const void* ref;       // dN of every node at every quadrature point ([q][node][3]), then the q weights
+    const void* u;
+    void* v;
+    uint32_t first, count, nq;
+    int bc_mode;
+    double lam, mu;        // Lame parameters (elasticity)
+};
+cudaError_t launch_free(int kind, bool f32, const FreeArgs& a, int sm_count, cudaStream_t st);
+
 // Kernel arithmetic for FP32 products from the symmetric inner arena (an
 // internal value beside the afm_precision codes).
 constexpr int kPrecF32Sym = 16;
@@ -245,6 +259,19 @@ struct afm_operator {
     unsigned char* d_sym = nullptr;
     size_t sym_bytes = 0;
     double* d_vx = nullptr;         // format 2: FP64 product before its rounding to FP32 (n_dofs)
+
+    // matrix-free operator (method 2, MATFREE_TYPE::FREE): element kind, material, quadrature and
+    // node coordinates; on the device, coordinates and maps in colour order and the reference tables
+    int elem_kind = -1;
+    double elem_E = 1.0, elem_nu = 0.3;
+    uint32_t elem_ngt = 2, elem_nodes = 0;
+    std::vector<double> xe;         // n_elem x nodes x 3
+    std::vector<uint32_t> free_color_first;  // colour offsets into the colour-sorted elements
+    uint32_t free_nq = 0;
+    double* d_free_xe64 = nullptr;
+    float* d_free_xe32 = nullptr;
+    double* d_free_ref64 = nullptr;
+    float* d_free_ref32 = nullptr;
 
     // assembled operator (afm_assembled.cpp): CSR on the device
     uint64_t* d_csr_rp = nullptr;

@@ -124,9 +124,33 @@ int afm_create(afm_operator** out, int bc_method, int device);
 /* ~aMatFree */
 int afm_destroy(afm_operator* op);
 
-/* aMat::set_matfree_type (include/aMat.hpp:184-187). Accepts QUASI_FREE (1)
- * and GPU_PURE (3): both select the stored-Ke device operator here. */
+/* aMat::set_matfree_type (include/aMat.hpp:184-187). QUASI_FREE (1) and
+ * GPU_PURE (3) select the stored-Ke device operator; FREE (2) the matrix-free
+ * one (afm_set_element_kind, afm_set_element_coords). */
 int afm_set_matfree_type(afm_operator* op, int matfree_type);
+/* Element kernels of the matrix-free operator (method 2): the device
+ * counterpart of aMat::set_element_matrix_function (include/aMat.hpp:114-116)
+ * for the element kinds of the reference's examples (afm_element_kind, the
+ * kernels of examples/src/ke_matrix.cpp: Gauss-Legendre rules of ngt points
+ * per direction, 1 to 3; E and nu for elasticity). */
+typedef enum afm_element_kind {
+    AFM_ELEM_HEX8_POISSON = 0,
+    AFM_ELEM_HEX8_ELASTIC = 1,
+    AFM_ELEM_HEX20_ELASTIC = 2,
+    AFM_ELEM_TET10_POISSON = 3,
+    AFM_ELEM_TET10_ELASTIC = 4
+} afm_element_kind;
+int afm_set_element_kind(afm_operator* op, int kind, double E, double nu, uint32_t ngt);
+/* Node coordinates of elements first .. first + count - 1: count x nodes x 3
+ * doubles, node order of the kind (what the reference's callback gathers
+ * into xe, e.g. examples/src/example07a.cpp:54-71). With
+ * afm_set_matfree_type(op, 2) (MATFREE_TYPE::FREE, include/aMatFree.hpp:
+ * 2241-2745) every product integrates each element's stiffness from these
+ * coordinates on the device instead of reading stored Ke: one warp per
+ * element, one launch per colour, FP64 for afm_matvec(_device), FP32 for the
+ * _f32 products and the inner CG of afm_solve_cg_mixed; the Jacobi diagonal
+ * and trace come from the same kernels on the host at afm_finalize. */
+int afm_set_element_coords(afm_operator* op, uint32_t first, uint32_t count, const double* xe);
 /* Arithmetic of the stored Ke; call before afm_finalize. Default AUTO. */
 int afm_set_precision(afm_operator* op, int precision);
 /* Execution of small elements (no counterpart in the reference). enable = 1
