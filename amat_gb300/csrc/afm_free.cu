@@ -7,9 +7,10 @@
 // up to the order of the sums. It trades the Ke bytes for arithmetic: in FP32
 // it needs ~0.5 KB per hex20 element instead of 7-29 KB of stored Ke.
 //
-// One warp per element, elements of one colour per launch (they share no
-// DoF, so v = v_old + v_e needs no atomics and is bit-reproducible). Phase 1,
-// lane = quadrature point: Jacobian J = sum_a xe_a (x) dN_a, its inverse, the
+// G = 8, 16 or 32 lanes per element (32 / G elements per warp), elements of
+// one colour per launch (they share no DoF, so v += v_e is a reduction at L2
+// with no read of the old v, and bit-reproducible). Phase 1, lane =
+// quadrature point: Jacobian J = sum_a xe_a (x) dN_a, its inverse, the
 // gradient of u (Poisson: grad u; elasticity: H = du/dx), and the weighted
 // flux / stress w |J| (lam tr(H) I + mu (H + H^T)), kept in shared memory with
 // J^-1. Phase 2, lane = node: v_a = sum_q (J_q^-T dN_a(q)) . flux_q.
@@ -39,14 +40,28 @@ struct FreeKind<4> { static constexpr int NODES = 10, DPN = 3; };
 constexpr int kFreeWarps = 8;
 constexpr int kFreeMaxQ = 27;
 
-template <int KIND, typename T>
+// v[i] += x at L2, no load and no wait (round to nearest; the f32 form
+// flushes subnormal values to zero). Elements of a launch share no DoF and
+// launches are ordered, so each entry gets one add per colour, in colour order.
+__device__ __forceinline__ void red_add(float* p, float x) {
+    asm volatile("red.global.add.f32 [%0], %1;" ::"l"(p), "f"(x) : "memory");
+}
+__device__ __forceinline__ void red_add(double* p, double x) {
+    asm volatile("red.global.add.f64 [%0], %1;" ::"l"(p), "d"(x) : "memory");
+}
+
+// G lanes per element (8, 16 or 32: at least the quadrature points and the
+// nodes), 32 / G elements per warp side by side.
+template <int KIND, typename T, int G>
 __global__ void __launch_bounds__(kFreeWarps * 32) k_free(FreeArgs a) {
     constexpr int NN = FreeKind<KIND>::NODES, DPN = FreeKind<KIND>::DPN, N = NN * DPN;
     constexpr int QS = 9 + (DPN == 3 ? 6 : 3);  // per quadrature point: J^-1, weighted stress / flux
-    __shared__ T ref[kFreeMaxQ * (NN * 3 + 1)];  // dN of every node at every point, then the weights
-    __shared__ T ue[kFreeWarps][N];
-    __shared__ T xs[kFreeWarps][NN * 3];
-    __shared__ T qb[kFreeWarps][kFreeMaxQ][QS];
+    constexpr int EPW = 32 / G, SLOTS = kFreeWarps * EPW, QM = G < kFreeMaxQ ? G : kFreeMaxQ;
+    static_assert(NN <= G, "a lane per node");
+    __shared__ T ref[QM * (NN * 3 + 1)];  // dN of every node at every point, then the weights
+    __shared__ T ue[SLOTS][N];
+    __shared__ T xs[SLOTS][NN * 3];
+    __shared__ T qb[SLOTS][QM][QS];
     const int nq = (int)a.nq;
     const T* gref = static_cast<const T*>(a.ref);
     for (int i = threadIdx.x; i < nq * (NN * 3 + 1); i += blockDim.x) ref[i] = gref[i];
@@ -54,24 +69,30 @@ __global__ void __launch_bounds__(kFreeWarps * 32) k_free(FreeArgs a) {
     const T* dNref = ref;             // [q][a][p]
     const T* wq = ref + nq * NN * 3;  // [q]
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int slot = warp * EPW + lane / G, sl = lane % G;
     const T* __restrict__ u = static_cast<const T*>(a.u);
     T* __restrict__ v = static_cast<T*>(a.v);
     const T* __restrict__ xe = static_cast<const T*>(a.xe);
     const T lam = (T)a.lam, mu = (T)a.mu;
-    const uint32_t stride = gridDim.x * kFreeWarps;
-    for (uint32_t el = blockIdx.x * kFreeWarps + warp; el < a.count; el += stride) {
-        const uint32_t e = a.first + el;
+    const uint32_t stride = gridDim.x * SLOTS;
+    // every lane of the warp runs the same number of rounds (the __syncwarp calls); a slot past the end idles
+    for (uint32_t base = blockIdx.x * SLOTS + warp * EPW; base < a.count; base += stride) {
+        const uint32_t el = base + lane / G;
+        const bool live = el < a.count;
+        const uint32_t e = a.first + (live ? el : 0u);
         const uint32_t* m = a.map + (size_t)e * N;
-        for (int i = lane; i < N; i += 32) {
-            const uint32_t d = m[i];
-            T x = u[d & kDofMask];
-            if (a.bc_mode && (d & kBcFlag)) x = T(0);
-            ue[warp][i] = x;
+        if (live) {
+            for (int i = sl; i < N; i += G) {
+                const uint32_t d = m[i];
+                T x = u[d & kDofMask];
+                if (a.bc_mode && (d & kBcFlag)) x = T(0);
+                ue[slot][i] = x;
+            }
+            for (int i = sl; i < NN * 3; i += G) xs[slot][i] = xe[(size_t)e * NN * 3 + i];
         }
-        for (int i = lane; i < NN * 3; i += 32) xs[warp][i] = xe[(size_t)e * NN * 3 + i];
         __syncwarp();
-        if (lane < nq) {
-            const int q = lane;
+        if (live && sl < nq) {
+            const int q = sl;
             const T* dN = dNref + q * NN * 3;
             T J[3][3] = {};  // J[i][p] = d x_i / d xi_p
 #pragma unroll
@@ -79,7 +100,7 @@ __global__ void __launch_bounds__(kFreeWarps * 32) k_free(FreeArgs a) {
 #pragma unroll
                 for (int i = 0; i < 3; i++)
 #pragma unroll
-                    for (int p = 0; p < 3; p++) J[i][p] += xs[warp][3 * b + i] * dN[3 * b + p];
+                    for (int p = 0; p < 3; p++) J[i][p] += xs[slot][3 * b + i] * dN[3 * b + p];
             const T det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
                           J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
                           J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
@@ -94,7 +115,7 @@ __global__ void __launch_bounds__(kFreeWarps * 32) k_free(FreeArgs a) {
             Ji[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) * id;
             Ji[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * id;
             Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
-            T* o = qb[warp][q];
+            T* o = qb[slot][q];
 #pragma unroll
             for (int k = 0; k < 9; k++) o[k] = Ji[k / 3][k % 3];
             const T w = wq[q] * det;
@@ -102,7 +123,7 @@ __global__ void __launch_bounds__(kFreeWarps * 32) k_free(FreeArgs a) {
                 T gu[3] = {};
 #pragma unroll
                 for (int b = 0; b < NN; b++) {
-                    const T ub = ue[warp][b];
+                    const T ub = ue[slot][b];
 #pragma unroll
                     for (int i = 0; i < 3; i++)
                         gu[i] += ub * (dN[3 * b] * Ji[0][i] + dN[3 * b + 1] * Ji[1][i] + dN[3 * b + 2] * Ji[2][i]);
@@ -120,7 +141,7 @@ __global__ void __launch_bounds__(kFreeWarps * 32) k_free(FreeArgs a) {
 #pragma unroll
                     for (int i = 0; i < 3; i++)
 #pragma unroll
-                        for (int j = 0; j < 3; j++) H[i][j] += ue[warp][3 * b + i] * g[j];
+                        for (int j = 0; j < 3; j++) H[i][j] += ue[slot][3 * b + i] * g[j];
                 }
                 const T tr = lam * (H[0][0] + H[1][1] + H[2][2]);
                 o[9] = w * (tr + mu * (H[0][0] + H[0][0]));   // s_xx
@@ -132,11 +153,11 @@ __global__ void __launch_bounds__(kFreeWarps * 32) k_free(FreeArgs a) {
             }
         }
         __syncwarp();
-        if (lane < NN) {
-            const int b = lane;
+        if (live && sl < NN) {
+            const int b = sl;
             T acc[DPN] = {};
             for (int q = 0; q < nq; q++) {
-                const T* o = qb[warp][q];
+                const T* o = qb[slot][q];
                 const T* dN = dNref + (q * NN + b) * 3;
                 T g[3];
 #pragma unroll
@@ -150,23 +171,32 @@ __global__ void __launch_bounds__(kFreeWarps * 32) k_free(FreeArgs a) {
                 }
             }
 #pragma unroll
-            for (int i = 0; i < DPN; i++) {
-                const uint32_t d = m[DPN * b + i] & kDofMask;
-                v[d] = v[d] + acc[i];
-            }
+            for (int i = 0; i < DPN; i++) red_add(v + (m[DPN * b + i] & kDofMask), acc[i]);
         }
         __syncwarp();
     }
 }
 
+template <int KIND, typename T>
+void* free_kernel_g(int g) {
+    constexpr int NN = FreeKind<KIND>::NODES;
+    if constexpr (NN <= 8) {
+        if (g == 8) return (void*)k_free<KIND, T, 8>;
+    }
+    if constexpr (NN <= 16) {
+        if (g == 16) return (void*)k_free<KIND, T, 16>;
+    }
+    return g == 32 ? (void*)k_free<KIND, T, 32> : nullptr;
+}
+
 template <typename T>
-void* free_kernel(int kind) {
+void* free_kernel(int kind, int g) {
     switch (kind) {
-        case 0: return (void*)k_free<0, T>;
-        case 1: return (void*)k_free<1, T>;
-        case 2: return (void*)k_free<2, T>;
-        case 3: return (void*)k_free<3, T>;
-        case 4: return (void*)k_free<4, T>;
+        case 0: return free_kernel_g<0, T>(g);
+        case 1: return free_kernel_g<1, T>(g);
+        case 2: return free_kernel_g<2, T>(g);
+        case 3: return free_kernel_g<3, T>(g);
+        case 4: return free_kernel_g<4, T>(g);
         default: return nullptr;
     }
 }
@@ -176,9 +206,14 @@ void* free_kernel(int kind) {
 cudaError_t launch_free(int kind, bool f32, const FreeArgs& a, int sm_count, cudaStream_t st) {
     if (a.count == 0) return cudaSuccess;
     if (a.nq == 0 || a.nq > (uint32_t)kFreeMaxQ) return cudaErrorInvalidValue;
-    void* fn = f32 ? free_kernel<float>(kind) : free_kernel<double>(kind);
+    static const int nodes[5] = {8, 8, 20, 10, 10};
+    if (kind < 0 || kind > 4) return cudaErrorInvalidValue;
+    const uint32_t need = a.nq > (uint32_t)nodes[kind] ? a.nq : (uint32_t)nodes[kind];
+    const int g = need <= 8 ? 8 : need <= 16 ? 16 : 32;
+    void* fn = f32 ? free_kernel<float>(kind, g) : free_kernel<double>(kind, g);
     if (!fn) return cudaErrorInvalidValue;
-    const uint32_t want = (a.count + kFreeWarps - 1) / kFreeWarps;
+    const uint32_t slots = kFreeWarps * (32 / g);
+    const uint32_t want = (a.count + slots - 1) / slots;
     const uint32_t grid = want < (uint32_t)sm_count * 4 ? want : (uint32_t)sm_count * 4;
     FreeArgs args = a;
     void* params[] = {&args};

@@ -425,6 +425,70 @@ def run_assembled(args, w, rank, world, local_rank):
             "afm_speedup_vs_assembled": ms_csr / ms_afm, "rel_diff_vs_afm": diff} if rank == 0 else None
 
 
+def run_free(args, w, rank, world, local_rank):
+    """Method 2 (MATFREE_TYPE::FREE): element stiffness integrated on the device from node coordinates every
+    product, FP64 and FP32, against the stored-Ke products (FP64-split, and the FP32 symmetric copy the inner CG
+    uses) of the same operator; then the mixed-precision solve on each."""
+    import torch
+    from amat_gb300 import MATFREE_TYPE, Maps, aMatFree
+    from amat_gb300 import problems as P
+    dev = local_rank
+    torch.cuda.set_device(dev)
+    m, dmap, S = build_problem(w, PREC_NAMES["fp64_split"], dev)
+    xe = m.coords[m.elem_nodes]
+    maps = Maps()
+    maps.set_map(m.n_elem, dmap, m.ndpe, m.n_dofs)
+    F = aMatFree(maps, 0, dev)
+    F.set_matfree_type(MATFREE_TYPE.FREE)
+    F.set_element_kind(w["kind"], E=1.0, nu=0.3, ngt=w["ngt"])
+    F.set_element_coords(0, xe)
+    t0 = time.time()
+    F.finalize()
+    t_fin = time.time() - t0
+    n = m.n_dofs
+    u = np.random.default_rng(5).uniform(-1, 1, n)
+    d64 = torch.tensor(u, device="cuda")
+    d32 = d64.float()
+    o64, o32 = torch.empty_like(d64), torch.empty_like(d32)
+
+    def timed(A, fn):
+        st = torch.cuda.ExternalStream(A.stream())
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(args.steps):
+            fn()
+        e1.record(st)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / args.steps
+
+    fs = F.stream()
+    ss = S.stream()
+    ms_f64 = timed(F, lambda: F.matvec_device(o64.data_ptr(), d64.data_ptr(), fs))
+    ref64 = o64.clone()
+    ms_f32 = timed(F, lambda: F.matvec_device_f32(o32.data_ptr(), d32.data_ptr(), fs))
+    ms_s64 = timed(S, lambda: S.matvec_device(o64.data_ptr(), d64.data_ptr(), ss))
+    diff = float(torch.linalg.norm(o64 - ref64) / torch.linalg.norm(o64))
+    S.set_symmetric_inner(1)
+    ms_s32 = timed(S, lambda: S.matvec_device_f32(o32.data_ptr(), d32.data_ptr(), ss))
+    info = S.info()
+    nn = m.elem_nodes.shape[1]
+    # FP32 bytes the matrix-free product moves per element: coordinates, map, u and v entries
+    free_bytes = m.n_elem * (nn * 3 * 4 + m.ndpe * 4) + 8 * n
+    return {"metric": "matrix-free (method 2) FP32 product ms", "value": ms_f32, "unit": "ms", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_f32, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": w["desc"], "n_dofs": n, "n_elements": m.n_elem, "free_finalize_s": t_fin},
+            "free": {"fp64_ms": ms_f64, "fp32_ms": ms_f32, "fp32_bytes_per_product": free_bytes,
+                     "rel_diff_fp64_vs_stored": diff, "device_ke_bytes": F.info()["ke_bytes"]},
+            "stored": {"fp64_split_ms": ms_s64, "fp32_symmetric_copy_ms": ms_s32, "ke_bytes": info["ke_bytes"],
+                       "symmetric_copy_bytes": info["sym_bytes"]},
+            "fp32_speedup_vs_stored_fp32": ms_s32 / ms_f32, "fp64_speedup_vs_stored_fp64": ms_s64 / ms_f64} \
+        if rank == 0 else None
+
+
 def build_bc_problem(w, dev):
     """Operator with the workload's boundary conditions (FP64_SPLIT arena: FP64 residual + FP32 view)."""
     from amat_gb300 import Maps, aMatFree
@@ -756,7 +820,7 @@ def main():
     ap.add_argument("--cpu-sample-elems", type=int, default=65536)
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU time the baseline sample is timed for")
     ap.add_argument("--mode", default="matvec", choices=["matvec", "solve", "batched", "product", "serve",
-                                                         "assembled"])
+                                                         "assembled", "free"])
     ap.add_argument("--rates", default="20,100,500", help="serve: arrival rates (requests/s)")
     ap.add_argument("--requests", type=int, default=160, help="serve: requests per rate")
     ap.add_argument("--edge-max", type=int, default=32, help="serve: largest mesh edge")
@@ -782,7 +846,7 @@ def main():
             torch.cuda.set_device(local_rank)
             torch.distributed.init_process_group("nccl")
         run = {"matvec": run_ours, "solve": run_solve, "batched": run_batched, "product": run_product,
-               "assembled": run_assembled,
+               "assembled": run_assembled, "free": run_free,
                "serve": run_serve}[args.mode]
         out = run(args, w, rank, world, local_rank)
         if world > 1:
