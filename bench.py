@@ -522,7 +522,19 @@ def run_solve(args, w, rank, world, local_rank):
     rtol = args.rtol
     x64, st = A.solve(rhs, rtol=rtol, atol=0.0, maxit=100000)  # warm-up (captures the graphs)
     log("fp64 CG: %d iterations, rel residual %.3e, %.3f s" % (st.iterations, st.rel_residual, st.seconds))
-    xm, stm = A.solve_mixed(rhs, rtol=rtol, atol=0.0, inner_rtol=args.inner_rtol, raise_on_fail=False)
+    M = A
+    if args.free:
+        # the mixed solve on the matrix-free operator (method 2): no element matrix on the device
+        from amat_gb300 import MATFREE_TYPE, Maps, aMatFree
+        maps = Maps()
+        maps.set_map(m.n_elem, m.dof_map(), m.ndpe, m.n_dofs)
+        maps.set_bdr_map(dofs, vals)
+        M = aMatFree(maps, 0, dev)
+        M.set_matfree_type(MATFREE_TYPE.FREE)
+        M.set_element_kind(w["kind"], E=1.0, nu=0.3, ngt=w["ngt"])
+        M.set_element_coords(0, m.coords[m.elem_nodes])
+        M.finalize()
+    xm, stm = M.solve_mixed(rhs, rtol=rtol, atol=0.0, inner_rtol=args.inner_rtol, raise_on_fail=False)
     log("mixed: status %d, %d refinements, %d inner iterations, rel residual %.3e, %.3f s" % (
         stm.status, stm.refinements, stm.iterations, stm.rel_residual, stm.seconds))
     if stm.status != 0:
@@ -535,7 +547,7 @@ def run_solve(args, w, rank, world, local_rank):
         nvtx.range_pop()
         t64.append(st.seconds)
         nvtx.range_push("mixed_solve")
-        xm, stm = A.solve_mixed(rhs, rtol=rtol, atol=0.0, inner_rtol=args.inner_rtol)
+        xm, stm = M.solve_mixed(rhs, rtol=rtol, atol=0.0, inner_rtol=args.inner_rtol)
         nvtx.range_pop()
         tmx.append(stm.seconds)
     s64 = args.steps / sum(t64)
@@ -546,8 +558,9 @@ def run_solve(args, w, rank, world, local_rank):
            "config": {"workload": w["desc"], "n_dofs": m.n_dofs, "n_elements": m.n_elem, "rtol": rtol,
                       "inner_rtol": args.inner_rtol},
            "mixed": {"solves_per_s": smx, "inner_iterations": stm.iterations, "refinements": stm.refinements,
-                     "inner_ke_bytes": A.info()["sym_bytes"] or A.info()["ke_bytes"] // 2,
-                     "inner_arena": {0: "hi plane", 1: "symmetric copy, FP32",
+                     "inner_ke_bytes": 0 if args.free else A.info()["sym_bytes"] or A.info()["ke_bytes"] // 2,
+                     "inner_arena": "matrix-free (method 2): Ke integrated from coordinates" if args.free else
+                                    {0: "hi plane", 1: "symmetric copy, FP32",
                                      2: "symmetric copy, FP32 + BF16 correction"}[A.info()["sym_available"]],
                      "rel_residual": stm.rel_residual,
                      "rel_error_vs_fp64_solution": float(np.linalg.norm(xm - x64) / np.linalg.norm(x64))},
@@ -831,6 +844,7 @@ def main():
     ap.add_argument("--segment", type=int, default=64, help="FP32 iterations between FP64 updates (batched)")
     ap.add_argument("--tile", default="", help="product: pin the batched lane tile 'columns,rows'")
     ap.add_argument("--rtol", type=float, default=1e-8)
+    ap.add_argument("--free", type=int, default=0, help="solve: mixed solve on the matrix-free operator (method 2)")
     ap.add_argument("--inner-rtol", type=float, default=1e-2)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
