@@ -1263,7 +1263,7 @@ int mixed_begin(MixedSolve& m) {
     AFM_CHECK_OP(op);
     if (!op->finalized) return fail(AFM_ERR_STATE, "solve before finalize");
     if (op->precision != AFM_PREC_FP64_SPLIT && op->matfree_type != 2)
-        return fail(AFM_ERR_STATE, "mixed-precision solve needs the FP64_SPLIT arena (hi plane = FP32 matrix)");
+        return fail(AFM_ERR_STATE, "mixed-precision solve needs an FP64_SPLIT or matrix-free operator");
     if (!m.d_b || !m.d_x) return fail(AFM_ERR_INVALID_ARG, "null vector");
     DeviceGuard g(op->device);
     int s = ensure_work(op, 8);
@@ -2326,7 +2326,7 @@ int afm_solve_cg_batched_mixed_device(afm_operator* op, const double* d_B, doubl
     int s = check_batched(op, nrhs, nrhs);
     if (s) return s;
     if (op->precision != AFM_PREC_FP64_SPLIT && op->matfree_type != 2)
-        return fail(AFM_ERR_STATE, "mixed-precision solve needs the FP64_SPLIT arena (hi plane = FP32 matrix)");
+        return fail(AFM_ERR_STATE, "mixed-precision solve needs an FP64_SPLIT or matrix-free operator");
     if (!d_B || !d_X) return fail(AFM_ERR_INVALID_ARG, "null block");
     if (((uintptr_t)d_B | (uintptr_t)d_X) % 16) return fail(AFM_ERR_INVALID_ARG, "blocks must be 16-byte aligned");
     DeviceGuard g(op->device);

@@ -1,5 +1,6 @@
 // Resumable mixed-precision solve (afm_solve_cg_mixed_device): FP32
-// Jacobi-PCG recursion on the hi plane of the split arena with FP64 reliable
+// Jacobi-PCG recursion on the operator's FP32 products (symmetric FP32 copy,
+// hi plane of the split arena, or matrix-free kernels) with FP64 reliable
 // updates, written as a state machine whose every step only enqueues work on
 // the operator's stream and records an event. afm_solve_cg_mixed_device
 // drives it by waiting on the event; the serving loop (afm_server.cpp) drives

@@ -174,9 +174,10 @@ int afm_set_patch_mode(afm_operator* op, int enable);
  * perturbs the product by ~2^-24 |K| |u|, which costs the inner CG of
  * ill-conditioned systems (elasticity under rough loads) up to ~1.9x the
  * iterations of FP64 CG; format 2 brings that to ~1.1-1.2x, at a higher cost
- * per product. format = 0: FP32 products read the hi plane. The copy is built on the device from the split arena by the first
- * FP32 product or mixed-precision solve after a change (outside any stream
- * capture). FP64 products never use it. */
+ * per product. format = 0: FP32 products read the hi plane. The copy is
+ * built on the device from the split arena by the first FP32 product or
+ * mixed-precision solve after a change (outside any stream capture). FP64
+ * products never use it. */
 int afm_set_symmetric_inner(afm_operator* op, int format);
 
 /* ---- maps (par::Maps) --------------------------------------------------- */
@@ -224,8 +225,10 @@ int afm_matvec(afm_operator* op, double* v, const double* u, int is_ghosted);
 /* v = K u on device arrays, enqueued on stream (NULL: the operator's stream)
  * and returned without waiting. */
 int afm_matvec_device(afm_operator* op, double* d_v, const double* d_u, void* stream);
-/* FP32 product on float device vectors: from an AFM_PREC_FP32 arena, or from
- * the hi plane (the FP32-rounded Ke) of an AFM_PREC_FP64_SPLIT arena. */
+/* FP32 product on float device vectors: from an AFM_PREC_FP32 arena; from an
+ * AFM_PREC_FP64_SPLIT arena's symmetric FP32 copy (afm_set_symmetric_inner)
+ * or its hi plane (the FP32-rounded Ke); or, for the matrix-free operator,
+ * by the element kernels in FP32. */
 int afm_matvec_device_f32(afm_operator* op, float* d_v, const float* d_u, void* stream);
 
 /* aMatFree::MatMult_mf (include/aMatFree.hpp:3894-3941): u_c taken as zero
@@ -259,16 +262,19 @@ int afm_solve_cg_device(afm_operator* op, const double* d_b, double* d_x, double
                         int norm_type, afm_solve_stats* stats);
 
 /* Mixed-precision solve of the same system (no counterpart in the
- * reference): Jacobi-PCG whose recursion runs in FP32 (the FP32 matrix, the
- * hi plane of the FP64_SPLIT arena at half the bytes; FP32 vectors; FP64 dot
- * products and step scalars) with reliable updates in FP64: once the FP32
+ * reference): Jacobi-PCG whose recursion runs in FP32 (the FP32 products of
+ * afm_matvec_device_f32: the symmetric FP32 copy of the element matrices at
+ * ~28% of the split arena's bytes, or the hi plane, or the matrix-free
+ * kernels; FP32 vectors; dot products in compensated FP32 reduced in FP64;
+ * FP64 step scalars) with reliable updates in FP64: once the FP32
  * residual has dropped by inner_rtol (or after max_inner iterations), the FP32
  * increment is added to x in FP64, the true residual r = b - A x is computed
- * in FP64 with the split element matrices (MatMult_mf semantics) and replaces
+ * in FP64 (MatMult_mf semantics) and replaces
  * the FP32 residual, and the recursion continues with its search direction.
  * The solve stops at ||b - A x|| <= max(rtol ||b||, atol), after max_outer
  * updates, or after ten updates in a row without a new smallest residual.
- * Needs an FP64_SPLIT operator (AFM_PREC_AUTO with in-range Ke). stats:
+ * Needs an FP64_SPLIT operator (AFM_PREC_AUTO with in-range Ke) or the
+ * matrix-free operator. stats:
  * iterations = FP32 iterations, refinements = FP64 residual updates. */
 int afm_solve_cg_mixed(afm_operator* op, const double* b, double* x, double rtol, double atol, int max_outer,
                        double inner_rtol, int max_inner, afm_solve_stats* stats);
