@@ -2539,11 +2539,17 @@ int afm_get_info(afm_operator* op, afm_info* info) {
     info->algorithmic_bytes = alg + 2 * vb * (uint64_t)op->n_dofs;
     info->algorithmic_flops = fl;
     uint32_t launches = 1;  // the zero fill of v
-    if (op->use_patches)
+    if (op->matfree_type == 2 && op->finalized) {
+        // matrix-free: node coordinates and the map per element instead of Ke
+        info->algorithmic_bytes = (uint64_t)op->n_elem * (op->elem_nodes * 3 * 8 + (uint64_t)op->nmax * 4) +
+                                  16 * (uint64_t)op->n_dofs;
+        launches += (uint32_t)op->free_color_first.size() - 1;
+    } else if (op->use_patches) {
         launches += (uint32_t)op->patch_color_first.size() - 1;
-    else
+    } else {
         for (const Segment& s : op->segs)
             if (s.units) launches++;
+    }
     info->n_launches = launches;
     info->n_patches = op->n_patches;
     info->n_patch_colors = op->use_patches ? (uint32_t)op->patch_color_first.size() - 1 : 0;

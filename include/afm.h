@@ -94,7 +94,8 @@ typedef struct afm_info {
     int precision;              /* effective afm_precision after finalize */
     uint64_t ke_bytes;          /* device bytes of the element-matrix arena */
     uint64_t map_bytes;         /* device bytes of the DoF map */
-    uint64_t algorithmic_bytes; /* per matvec: sum_e (n_e^2 * entry + 4 n_e) + 16 n_dofs */
+    uint64_t algorithmic_bytes; /* per matvec: sum_e (n_e^2 * entry + 4 n_e) + 16 n_dofs (matrix-free:
+                                   sum_e (24 nodes_e + 4 n_e) + 16 n_dofs) */
     double algorithmic_flops;   /* per matvec: sum_e 2 n_e^2 */
     uint32_t n_launches;        /* kernel launches per matvec */
     int device;
