@@ -202,24 +202,28 @@ cudaError_t BATCH_FN(const Segment& s, const BatchArgs& a, int sm_count, int ct,
 
 namespace {
 // consumer groups (G) of GW warps of the patch kernel for this arithmetic
-// (see afm_patch.cuh): FP32 tries 8 groups, then 4; 8-byte entries use 2.
+// (see afm_patch.cuh): FP32 tries 8 groups of 2 warps, then 4; 8-byte entries
+// 4 groups of 2 warps, then 2 of 4 (their 25.6 KB units leave few ring slots).
 constexpr bool kF32Patch = sizeof(typename ARITH::VT) == 4;
-constexpr int kPatchGW = kF32Patch ? 2 : 4;
-constexpr uint32_t kMinPatchStages = 6;  // ring slots below which fewer groups are used
+constexpr uint32_t kMinPatchStages = kF32Patch ? 6 : 5;  // ring slots below which fewer groups are used
+
+// warps per group for G groups
+constexpr int patch_gw(int G) { return kF32Patch ? 2 : (G == 4 ? 2 : 4); }
 
 template <int G>
 void* patch_kernel_g(uint32_t n) {
+    constexpr int GW = patch_gw(G);
     switch (n) {
-        case 4: return (void*)afm_patch_kernel<4, ARITH, G, kPatchGW>;
-        case 8: return (void*)afm_patch_kernel<8, ARITH, G, kPatchGW>;
-        case 10: return (void*)afm_patch_kernel<10, ARITH, G, kPatchGW>;
-        default: return (void*)afm_patch_kernel<0, ARITH, G, kPatchGW>;
+        case 4: return (void*)afm_patch_kernel<4, ARITH, G, GW>;
+        case 8: return (void*)afm_patch_kernel<8, ARITH, G, GW>;
+        case 10: return (void*)afm_patch_kernel<10, ARITH, G, GW>;
+        default: return (void*)afm_patch_kernel<0, ARITH, G, GW>;
     }
 }
 
 void* pick_patch_kernel(uint32_t n, uint32_t groups) {
     if constexpr (kF32Patch) return groups == 8 ? patch_kernel_g<8>(n) : patch_kernel_g<4>(n);
-    else return patch_kernel_g<2>(n);
+    else return groups == 4 ? patch_kernel_g<4>(n) : patch_kernel_g<2>(n);
 }
 
 PatchLayout patch_layout_g(const PatchPlanGeom& pg, uint32_t copy_bytes, uint32_t groups) {
@@ -239,13 +243,10 @@ PatchLayout patch_layout_g(const PatchPlanGeom& pg, uint32_t copy_bytes, uint32_
 }
 
 PatchLayout patch_layout(const PatchPlanGeom& pg, uint32_t copy_bytes) {
-    if constexpr (kF32Patch) {
-        const PatchLayout L8 = patch_layout_g(pg, copy_bytes, 8);
-        if (L8.stages >= kMinPatchStages) return L8;
-        return patch_layout_g(pg, copy_bytes, 4);
-    } else {
-        return patch_layout_g(pg, copy_bytes, 2);
-    }
+    const uint32_t more = kF32Patch ? 8 : 4, fewer = kF32Patch ? 4 : 2;
+    const PatchLayout L = patch_layout_g(pg, copy_bytes, more);
+    if (L.stages >= kMinPatchStages) return L;
+    return patch_layout_g(pg, copy_bytes, fewer);
 }
 }  // namespace
 
@@ -255,7 +256,7 @@ cudaError_t PATCH_FN(const PatchPlanGeom& pg, const PatchArgs& a, int sm_count, 
     if (L.stages < 2 || pg.n == 0 || pg.n > kPatchMaxN) return cudaErrorInvalidConfiguration;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(a.count < (uint32_t)sm_count ? a.count : (uint32_t)sm_count);
-    cfg.blockDim = dim3((L.groups * kPatchGW + 1) * 32);
+    cfg.blockDim = dim3((L.groups * patch_gw((int)L.groups) + 1) * 32);
     cfg.dynamicSmemBytes = L.total();
     cfg.stream = stream;
     cudaLaunchAttribute attr[1];

@@ -32,12 +32,12 @@
 
 namespace afm {
 
-// G consumer groups of GW warps: FP32 runs 8 groups of 2 warps (or 4 when
-// the shared memory of 8 would leave the ring too few slots), 8-byte entries
-// 2 groups of 4 warps, whose 25.6 KB units fill the ring with about two
-// patches. A group's patch passes through phases bound by memory latency
-// (the index block, the gather of u), so the patches in flight per SM, not
-// the multiply, set the kernel's pace.
+// G consumer groups of GW warps: 8 groups of 2 warps for FP32 (or 4 when the
+// shared memory of 8 would leave the ring too few slots), 4 groups of 2 warps
+// for 8-byte entries (or 2 groups of 4 when their 25.6 KB units would leave
+// the ring too few slots). A group's patch passes through phases bound by
+// memory latency (the index block, the gather of u), so the patches in flight
+// per SM, not the multiply, set the kernel's pace.
 constexpr uint32_t kPatchMaxGroups = 8;
 constexpr int kBatch = 8;  // global loads a thread keeps in flight in the gather
 
