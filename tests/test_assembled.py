@@ -96,3 +96,28 @@ def test_device_assembled_against_afm_at_scale(gpu, kind, n):
     A.synchronize()
     assert torch.equal(v1, v2)
     assert rel(v1.cpu().numpy(), va.cpu().numpy()) < FP64_RTOL
+
+
+def test_host_assembly_order_with_repeated_dofs():
+    """Elements that list a DoF twice add both rows and columns into the same entry, in element, row,
+    column order (MatSetValues with ADD_VALUES): the same sums as a plain loop in that order, bit for bit."""
+    rng = np.random.default_rng(21)
+    n_dofs, sizes = 40, [3, 5, 7, 4, 6] * 6
+    maps = [rng.integers(0, n_dofs, size=s).astype(np.uint32) for s in sizes]  # repeats allowed
+    kes = [rng.normal(size=(len(m), len(m))) for m in maps]
+    offsets = np.concatenate([[0], np.cumsum([len(m) for m in maps])]).astype(np.uint32)
+    dense = {}
+    for m, k in zip(maps, kes):
+        for r in range(len(m)):
+            for c in range(len(m)):
+                key = (int(m[r]), int(m[c]))
+                dense[key] = dense.get(key, 0.0) + k[r, c]
+    rp, cols, vals = assemble_csr_host(n_dofs, offsets, np.concatenate(maps), np.concatenate([k.ravel() for k in kes]),
+                                       (), BC_METH.BC_IMATRIX, False)
+    got = {}
+    for i in range(n_dofs):
+        for j in range(int(rp[i]), int(rp[i + 1])):
+            got[(i, int(cols[j]))] = vals[j]
+    assert got.keys() == dense.keys()
+    for key, v in dense.items():
+        assert got[key] == v  # bit for bit
