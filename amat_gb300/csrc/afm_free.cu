@@ -76,21 +76,58 @@ __global__ void __launch_bounds__(kFreeWarps * 32) k_free(FreeArgs a) {
     const T lam = (T)a.lam, mu = (T)a.mu;
     const uint32_t stride = gridDim.x * SLOTS;
     // every lane of the warp runs the same number of rounds (the __syncwarp calls); a slot past the end idles
-    for (uint32_t base = blockIdx.x * SLOTS + warp * EPW; base < a.count; base += stride) {
+    // Gather pipeline: the element of the next round has its u entries and coordinates loaded (and the one
+    // after it its map) while the current element is integrated, so a round waits on no load of its own.
+    constexpr int CN = (N + G - 1) / G, CX = (NN * 3 + G - 1) / G;
+    uint32_t mc[CN], mn[CN];  // maps of the next round and of the one after
+    T uc[CN], xc[CX];         // u entries and coordinates of the next round
+    auto load_map = [&](uint32_t base_r, uint32_t* out) {
+        const uint32_t el_r = base_r + lane / G;
+#pragma unroll
+        for (int k = 0; k < CN; k++) {
+            const int i = sl + k * G;
+            out[k] = (el_r < a.count && i < N) ? a.map[(size_t)(a.first + el_r) * N + i] : 0u;
+        }
+    };
+    auto load_ux = [&](uint32_t base_r, const uint32_t* mp) {
+        const uint32_t el_r = base_r + lane / G;
+        const bool ok = el_r < a.count;
+#pragma unroll
+        for (int k = 0; k < CN; k++) {
+            const int i = sl + k * G;
+            T x = (ok && i < N) ? u[mp[k] & kDofMask] : T(0);
+            if (a.bc_mode && (mp[k] & kBcFlag)) x = T(0);
+            uc[k] = x;
+        }
+#pragma unroll
+        for (int k = 0; k < CX; k++) {
+            const int i = sl + k * G;
+            xc[k] = (ok && i < NN * 3) ? xe[(size_t)(a.first + el_r) * NN * 3 + i] : T(0);
+        }
+    };
+    uint32_t base = blockIdx.x * SLOTS + warp * EPW;
+    load_map(base, mc);
+    load_ux(base, mc);
+    load_map(base + stride, mn);
+    for (; base < a.count; base += stride) {
         const uint32_t el = base + lane / G;
         const bool live = el < a.count;
         const uint32_t e = a.first + (live ? el : 0u);
         const uint32_t* m = a.map + (size_t)e * N;
         if (live) {
-            for (int i = sl; i < N; i += G) {
-                const uint32_t d = m[i];
-                T x = u[d & kDofMask];
-                if (a.bc_mode && (d & kBcFlag)) x = T(0);
-                ue[slot][i] = x;
-            }
-            for (int i = sl; i < NN * 3; i += G) xs[slot][i] = xe[(size_t)e * NN * 3 + i];
+#pragma unroll
+            for (int k = 0; k < CN; k++)
+                if (sl + k * G < N) ue[slot][sl + k * G] = uc[k];
+#pragma unroll
+            for (int k = 0; k < CX; k++)
+                if (sl + k * G < NN * 3) xs[slot][sl + k * G] = xc[k];
         }
         __syncwarp();
+        // next round: its u and coordinates from the map loaded a round ago; the map of the round after
+#pragma unroll
+        for (int k = 0; k < CN; k++) mc[k] = mn[k];
+        load_ux(base + stride, mc);
+        load_map(base + 2 * stride, mn);
         if (live && sl < nq) {
             const int q = sl;
             const T* dN = dNref + q * NN * 3;
