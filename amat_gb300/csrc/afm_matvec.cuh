@@ -111,6 +111,12 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t b
         : "memory");
 }
 
+// Prefetch of bytes (16-byte aligned, a multiple of 16) from global memory
+// into L2, no completion to wait for.
+__device__ __forceinline__ void bulk_prefetch_l2(const void* src, uint32_t bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+}
+
 // Records a failed bounds check (the access is skipped by the caller): the
 // first failure's kind, block, thread and three values in err[1..6], and
 // kErrBounds in err[0]; the host reports AFM_ERR_INTERNAL.
