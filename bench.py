@@ -13,6 +13,15 @@ matvec over the whole mesh with u resident in HBM. The inputs (7.66 GB) are
 loop (the oracle's port of matvec_ghosted_OMP: OpenMP parallel-for over
 elements, row-major GEMV, atomic scatter) on all host cores, on a bounded
 sample of the same workload. One JSON line on stdout (rank 0).
+
+Other measurements (`--mode`, each one JSON line):
+  solve      CG solves/s to --rtol: FP64 Jacobi-PCG against the mixed-precision
+             solve (--free 1: on the matrix-free operator)
+  batched    block CG over --nrhs load cases against one-at-a-time FP64 CG
+  product    the batched multi-RHS product in FP32 and FP64-split, TFLOP/s
+  serve      served solves/s and p50/p99 latency under Poisson arrivals
+  assembled  the aMatBased CSR SpMV against the assembly-free product
+  free       the matrix-free (method 2) products against the stored-Ke ones
 """
 import argparse
 import json
