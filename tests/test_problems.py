@@ -116,3 +116,15 @@ def test_boundary_conditions():
     m = P.Mesh(P.HEX20_ELASTIC, 2)
     d, v = m.boundary_conditions()
     assert len(d) == 6 and np.all(np.diff(d.astype(np.int64)) > 0)
+
+
+@pytest.mark.parametrize("kind,ngt", [(P.HEX8_POISSON, 2), (P.HEX8_ELASTIC, 2), (P.HEX20_ELASTIC, 3),
+                                      (P.TET10_POISSON, 2), (P.TET10_ELASTIC, 2)])
+def test_element_matrices_are_symmetric(kind, ngt):
+    """Every generated Ke is symmetric well inside the 1e-6 (of the largest diagonal entry) bound under which
+    FP32 products may stream the symmetric copy of the element matrices."""
+    m = P.Mesh(kind, 3, jitter=0.15, seed=5)
+    ke = m.element_matrices(ngt=ngt)
+    dmax = np.abs(np.diagonal(ke, axis1=1, axis2=2)).max(axis=1)
+    asym = np.abs(ke - np.transpose(ke, (0, 2, 1))).max(axis=(1, 2))
+    assert np.all(asym <= 1e-12 * dmax)
