@@ -28,6 +28,7 @@ class AfmInfo(C.Structure):
         ("n_launches", C.c_uint32), ("device", C.c_int), ("n_patches", C.c_uint32),
         ("n_patch_colors", C.c_uint32), ("patch_index_bytes", C.c_uint64), ("ke_symmetric", C.c_int),
         ("sym_available", C.c_int), ("sym_bytes", C.c_uint64), ("csr_nnz", C.c_uint64),
+        ("work_bytes", C.c_uint64),
     ]
 
 
@@ -48,8 +49,20 @@ class AfmMesh(C.Structure):
     ]
 
 
-# include/afm.h: largest operator of afm_solve_cg_device_noalloc
-NOALLOC_MAX_DOFS = 262144
+
+
+def _header_define(name):
+    """Value of an integer #define of include/afm.h (the header is the one statement of such limits)."""
+    import re
+    with open(os.path.join(os.path.dirname(HERE), "include", "afm.h")) as f:
+        m = re.search(r"^#define\s+%s\s+(\d+)u?\s*$" % name, f.read(), re.M)
+    if not m:
+        raise RuntimeError("include/afm.h defines no %s" % name)
+    return int(m.group(1))
+
+
+# largest operator of afm_solve_cg_device_noalloc
+NOALLOC_MAX_DOFS = _header_define("AFM_NOALLOC_MAX_DOFS")
 
 P = C.c_void_p
 U32 = C.c_uint32
@@ -65,6 +78,8 @@ AFM_SIGNATURES = {
     "afm_set_precision": (I, [P, I]),
     "afm_set_patch_mode": (I, [P, I]),
     "afm_set_symmetric_inner": (I, [P, I]),
+    "afm_set_wait_limit": (I, [P, D]),
+    "afm_set_wait_probe": (I, [P, I]),
     "afm_set_element_kind": (I, [P, I, D, D, U32]),
     "afm_set_element_coords": (I, [P, U32, U32, P]),
     "afm_assemble_csr_host": (I, [U32, U32, P, P, P, P, U32, I, I, P, P, P, P]),

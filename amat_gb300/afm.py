@@ -139,6 +139,15 @@ class aMatFree:
         correction with FP64 sums, 0 the hi plane."""
         check(self._lib.afm_set_symmetric_inner(self._h, int(fmt)), "afm_set_symmetric_inner")
 
+    def set_wait_limit(self, seconds):
+        """Limit of each wait inside the element kernels (4 s by default); past it a call reports ERR_TIMEOUT."""
+        check(self._lib.afm_set_wait_limit(self._h, float(seconds)), "afm_set_wait_limit")
+
+    def set_wait_probe(self, enable):
+        """Test hook: one warp of every element kernel waits on a flag nothing sets, so that its wait
+        runs out after the wait limit and calls report ERR_TIMEOUT."""
+        check(self._lib.afm_set_wait_probe(self._h, int(bool(enable))), "afm_set_wait_probe")
+
     def set_element_kind(self, kind, E=1.0, nu=0.3, ngt=2):
         """Element kernels of the matrix-free operator (method 2), the counterpart of
         set_element_matrix_function (include/aMat.hpp:114-116); kind as problems.HEX8_POISSON etc."""

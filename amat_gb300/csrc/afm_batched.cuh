@@ -101,7 +101,7 @@ __global__ void __launch_bounds__(9 * 32, 1) afm_batched_kernel(BatchArgs a, Rin
             uint32_t issued = 0;
             for (uint32_t i = 0; i < cnt; i++) {
                 const uint32_t s = i % S;
-                if (i >= S && !mbar_wait_abortable(&empty[s], ((i / S) - 1) & 1, abort)) break;
+                if (i >= S && !mbar_wait_abortable(&empty[s], ((i / S) - 1) & 1, abort, a.wait_ns)) break;
                 tag[s] = i;
                 mbar_arrive_expect_tx(&full[s], a.copy_bytes);
                 bulk_load(smem + (size_t)s * L.slot_bytes, a.ke + (size_t)(begin + i) * a.unit_bytes, a.copy_bytes,
@@ -109,18 +109,13 @@ __global__ void __launch_bounds__(9 * 32, 1) afm_batched_kernel(BatchArgs a, Rin
                 issued = i + 1;
             }
             allow_dependent_launch();
-            if (*abort) {
-                atomicOr(a.err, kErrTimeout);
-                const uint32_t first = issued > S ? issued - S : 0;
-                const unsigned long long t0 = globaltimer_ns();
-                for (uint32_t i = first; i < issued; i++)
-                    while (!mbar_try_wait(&full[i % S], (i / S) & 1) && globaltimer_ns() - t0 < kWaitLimitNs) {
-                    }
-            }
+            if (*abort) atomicOr(a.err, kErrTimeout);
+            drain_ring(full, S, issued);
         }
         return;
     }
 
+    if (a.probe && blockIdx.x == 0 && warp == 0 && !probe_wait(a.probe, a.wait_ns)) *abort = 1;
     const uint32_t R = a.nrhs, ld = a.ld;
     const uint32_t ctiles = R / CT, tiles = ((n + RT - 1) / RT) * ctiles;
     constexpr uint32_t kChunk = 16 / sizeof(VT);  // values per 16-byte copy
@@ -170,12 +165,15 @@ __global__ void __launch_bounds__(9 * 32, 1) afm_batched_kernel(BatchArgs a, Rin
         const uint32_t* mp = reinterpret_cast<const uint32_t*>(b);
         const VT* ub = reinterpret_cast<const VT*>(b + batch_map_bytes(n));
         const uint32_t s = i % S;
-        const bool ok = ring_wait(&full[s], &tag[s], i, (i / S) & 1, abort);
+        const bool ok = __all_sync(0xffffffffu, ring_wait(&full[s], &tag[s], i, (i / S) & 1, abort, a.wait_ns));
         const unsigned char* ks = smem + (size_t)s * L.slot_bytes;
         const uint32_t ub_end = (uint32_t)(reinterpret_cast<const unsigned char*>(ub) - smem) + n * R * sizeof(VT);
         if (ub_end > a.smem_total || s >= S) report_bad(a.err, 6, ub_end, s, i);
         for (uint32_t t = lane; t < tiles && ok && ub_end <= a.smem_total; t += 32) {
             const uint32_t r0 = (t / ctiles) * RT, j0 = (t % ctiles) * CT;
+            int usk[CT];  // per-column u scale of the split arithmetic
+#pragma unroll
+            for (int y = 0; y < CT; y++) usk[y] = load_uscale<A>(a.umax + j0 + y);
             typename A::Acc acc[RT][CT];
 #pragma unroll
             for (int x = 0; x < RT; x++)
@@ -192,7 +190,7 @@ __global__ void __launch_bounds__(9 * 32, 1) afm_batched_kernel(BatchArgs a, Rin
                 const bool zero = a.bc_mode && (mp[c] & kBcFlag);
                 UT us[CT];
 #pragma unroll
-                for (int y = 0; y < CT; y++) us[y] = A::stage(zero ? VT(0) : uv[y]);
+                for (int y = 0; y < CT; y++) us[y] = stage_s<A>(zero ? VT(0) : uv[y], usk[y]);
 #pragma unroll
                 for (int x = 0; x < RT; x++)
 #pragma unroll
@@ -211,7 +209,7 @@ __global__ void __launch_bounds__(9 * 32, 1) afm_batched_kernel(BatchArgs a, Rin
                         VT old[CT];
                         RowVec<VT, CT>::load(row, old);
 #pragma unroll
-                        for (int y = 0; y < CT; y++) old[y] = old[y] + A::finish(acc[x][y]);
+                        for (int y = 0; y < CT; y++) old[y] = old[y] + finish_s<A>(acc[x][y], usk[y]);
                         RowVec<VT, CT>::store(row, old);
                     }
                 }

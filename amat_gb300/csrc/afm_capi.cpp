@@ -41,6 +41,8 @@ cudaError_t launch_batched_fp64(const Segment& s, const BatchArgs& a, int sm_cou
                                 cudaStream_t st);
 cudaError_t launch_batched_split(const Segment& s, const BatchArgs& a, int sm_count, int tr, int ng, bool pdl,
                                  cudaStream_t st);
+bool batched_tc_supported(uint32_t n, uint32_t nrhs);
+cudaError_t launch_batched_tc(const Segment& s, const BatchArgs& a, int sm_count, bool pdl, cudaStream_t stream);
 cudaError_t launch_batched_fp32(const Segment& s, const BatchArgs& a, int sm_count, int tr, int ng, bool pdl,
                                 cudaStream_t st);
 cudaError_t configure_kernels_fp64();
@@ -209,6 +211,7 @@ void free_device(afm_operator* op) {
     dfree(op, op->d_diag);
     dfree(op, op->d_bc_idx);
     dfree(op, op->d_bc_val);
+    dfree(op, op->d_bcmask);
     dfree(op, op->d_work);
     dfree(op, op->d_work32);
     dfree(op, op->d_patch_desc);
@@ -757,7 +760,14 @@ int enqueue_matvec(afm_operator* op, void* d_v, const void* d_u, int bc_mode, cu
     // the corrected format sums into an FP64 vector, rounded to FP32 at the end
     float* const d_v32 = static_cast<float*>(d_v);
     if (symx) d_v = op->d_vx;
-    AFM_CUDA(cudaMemsetAsync(d_v, 0, symx ? (size_t)op->n_dofs * 8 : vbytes, st));
+    // split arithmetic: max|u| for the launches' power-of-two u scale (and v = 0) in one launch, before
+    // the first element launch, which waits for it in full; other arithmetic: v = 0
+    const bool scaled = kprec == AFM_PREC_FP64_SPLIT;
+    if (scaled)
+        AFM_CUDA(launch_umax(static_cast<const double*>(d_u), bc_mode ? op->d_bcmask : nullptr, op->n_dofs,
+                             static_cast<double*>(d_v), op->n_dofs, op->d_usc, st));
+    else
+        AFM_CUDA(cudaMemsetAsync(d_v, 0, symx ? (size_t)op->n_dofs * 8 : vbytes, st));
     bool first = true;
     if (op->use_patches) {
         const Segment& s = op->segs[0];
@@ -775,6 +785,9 @@ int enqueue_matvec(afm_operator* op, void* d_v, const void* d_u, int bc_mode, cu
             if (f32 && !sym && op->precision == AFM_PREC_FP64_SPLIT) a.copy_bytes = s.plane * 4;
             a.bc_mode = bc_mode;
             a.err = op->d_err;
+            a.umax = op->d_usc;
+            a.wait_ns = op->wait_ns;
+            a.probe = op->wait_probe ? op->d_err + (kErrWords - 1) : nullptr;
             AFM_CUDA(launch_patches(kprec, op->patch_geom, a, op->sm_count, !first, st));
             first = false;
         }
@@ -796,6 +809,9 @@ int enqueue_matvec(afm_operator* op, void* d_v, const void* d_u, int bc_mode, cu
         if (f32 && !sym && op->precision == AFM_PREC_FP64_SPLIT) a.copy_bytes = s.plane * 4;
         a.bc_mode = bc_mode;
         a.err = op->d_err;
+        a.umax = op->d_usc;
+        a.wait_ns = op->wait_ns;
+        a.probe = op->wait_probe ? op->d_err + (kErrWords - 1) : nullptr;
         // every launch after the first may overlap its prologue with the previous one's tail
         AFM_CUDA(launch_segment(s, kprec, a, op->sm_count, op->dup_in_element, !first, st));
         first = false;
@@ -815,6 +831,10 @@ int enqueue_matvec_batched(afm_operator* op, void* d_V, const void* d_U, uint32_
     const int kprec = f32 ? AFM_PREC_FP32 : op->precision;
     const size_t vb = (kprec == AFM_PREC_FP32 ? 4 : 8);
     AFM_CUDA(cudaMemsetAsync(d_V, 0, (size_t)op->n_dofs * ld * vb, st));
+    // split arithmetic: max|U(:, j)| of every column for the per-column u scale
+    if (kprec == AFM_PREC_FP64_SPLIT)
+        AFM_CUDA(launch_umax_cols(static_cast<const double*>(d_U), bc_mode ? op->d_bcmask : nullptr, op->n_dofs,
+                                  nrhs, ld, op->d_usc + kUscColsOffset, st));
     bool first = true;
     for (const Segment& s : op->segs) {
         if (s.units == 0) continue;
@@ -834,11 +854,16 @@ int enqueue_matvec_batched(afm_operator* op, void* d_V, const void* d_U, uint32_
         a.bc_mode = bc_mode;
         a.err = op->d_err;
         a.n_dofs = op->n_dofs;
+        a.umax = op->d_usc + kUscColsOffset;
+        a.wait_ns = op->wait_ns;
+        a.probe = op->wait_probe ? op->d_err + (kErrWords - 1) : nullptr;
         cudaError_t e;
         if (kprec == AFM_PREC_FP64)
             e = launch_batched_fp64(s, a, op->sm_count, tr, ng, !first, st);
         else if (kprec == AFM_PREC_FP64_SPLIT)
             e = launch_batched_split(s, a, op->sm_count, tr, ng, !first, st);
+        else if (tr == 0)  // the tensor-core kernel
+            e = launch_batched_tc(s, a, op->sm_count, !first, st);
         else
             e = launch_batched_fp32(s, a, op->sm_count, tr, ng, !first, st);
         if (e != cudaSuccess) return fail(AFM_ERR_CUDA, "batched launch (n=%u, tr=%d, ng=%d): %s", s.n, tr, ng,
@@ -860,6 +885,13 @@ int check_batched(afm_operator* op, uint32_t nrhs, uint32_t ld) {
     return AFM_SUCCESS;
 }
 
+// Every segment of the operator can run the tensor-core FP32 kernel for nrhs.
+bool batched_tc_all(afm_operator* op, uint32_t nrhs) {
+    for (const Segment& s : op->segs)
+        if (s.units && !batched_tc_supported(s.n, nrhs)) return false;
+    return true;
+}
+
 // The project's autotuner: the first batched call for (nrhs, ld, arithmetic)
 // times every (columns per thread tile, element groups per CTA) candidate on
 // the caller's data, three runs each, and keeps the fastest for the operator.
@@ -873,8 +905,9 @@ int batch_tuning(afm_operator* op, void* d_V, const void* d_U, uint32_t nrhs, ui
             *ng = t.ng;
             return AFM_SUCCESS;
         }
-    // (columns, rows) of the lane tile
-    const std::vector<std::pair<int, int>> cand = {{8, 6}, {8, 4}, {8, 2}, {4, 4}};
+    // (columns, rows) of the lane tile; (0, 0): the tensor-core kernel (FP32 products)
+    std::vector<std::pair<int, int>> cand = {{8, 6}, {8, 4}, {8, 2}, {4, 4}};
+    if (f32 && batched_tc_all(op, nrhs)) cand.insert(cand.begin(), {0, 0});
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -1188,6 +1221,16 @@ int run_cg_iterations(afm_operator* op, afm_operator::CgGraph& gc, const CgVecto
 // the rest.
 constexpr int kIrMaxStall = 10;
 
+// Power of two sigma with sigma x in [0.5, 1) for x > 0 (1 otherwise), its
+// exponent clamped so that sigma and 1 / sigma stay normal doubles.
+double residual_scale(double x) {
+    if (!(x > 0.0) || !std::isfinite(x)) return 1.0;
+    int e = 0;
+    std::frexp(x, &e);
+    e = std::max(-1000, std::min(1000, e));
+    return std::ldexp(1.0, -e);
+}
+
 bool ir_progress(double rn, double* best, int* stall) {
     if (rn < *best) {
         *best = rn;
@@ -1251,7 +1294,7 @@ int mixed_finish(MixedSolve& m, int status) {
 int mixed_segment_end(MixedSolve& m, int iters, int seg_status) {
     m.inner_total += iters;
     m.fresh = (seg_status == AFM_ERR_BREAKDOWN);
-    AFM_CUDA(launch_add_f32(m.d_x, mixed_vectors(m.op).V.x, m.op->n_dofs, m.op->stream));
+    AFM_CUDA(launch_add_f32(m.d_x, mixed_vectors(m.op).V.x, m.op->n_dofs, m.op->stream, 1.0 / m.sigma));
     m.outer++;
     return mixed_residual(m);
 }
@@ -1308,26 +1351,30 @@ int mixed_advance(MixedSolve& m) {
             if (m.rn <= m.tol) return mixed_finish(m, AFM_SUCCESS);
             if (!ir_progress(m.rn, &m.best, &m.stall) || m.outer >= m.max_outer)
                 return mixed_finish(m, AFM_ERR_MAXIT);
+            // the segment's scale: a power of two that brings ||r|| into [0.5, 1) (exact)
+            const double sigma = residual_scale(m.rn);
             if (m.fresh) {
-                // FP32 Jacobi-PCG on A d = r from d = 0
-                AFM_CUDA(launch_to_f32(W.b32, W.r64, n, st));
+                // FP32 Jacobi-PCG on A d = sigma r from d = 0
+                AFM_CUDA(launch_to_f32(W.b32, W.r64, n, st, sigma));
                 AFM_CUDA(cudaMemsetAsync(W.V.q, 0, n * sizeof(float), st));
                 AFM_CUDA(launch_cg_init(W.b32, W.V.q, W.V.dinv, W.V.r, W.V.z, W.V.p, n, sc, part, st));
             } else {
                 // reliable update: the recursion continues from the true residual
-                AFM_CUDA(launch_cg_reliable(W.r64, W.V.r, W.V.z, W.V.p, W.V.dinv, n, sc, part, st));
+                AFM_CUDA(launch_cg_reliable(W.r64, W.V.r, W.V.z, W.V.p, W.V.dinv, n, sc, part, sigma,
+                                            sigma / m.sigma, st));
             }
+            m.sigma = sigma;
             // the segment ends once the FP32 residual has dropped by inner_rtol
             m.inner_tol = std::max(m.inner_rtol * m.rn, m.tol);
             m.phase = MS_SEGSTART;
             return mixed_record(m);
         }
         case MS_SEGSTART: {
-            const double n0 = std::sqrt(h[S_RR]);
+            const double n0 = std::sqrt(h[S_RR]) / m.sigma;
             if (h[S_FLAG] != 0.0 || std::isnan(n0)) return mixed_segment_end(m, 0, AFM_ERR_BREAKDOWN);
             if (n0 <= m.inner_tol) return mixed_segment_end(m, 0, AFM_SUCCESS);
             if (m.max_inner <= 0) return mixed_segment_end(m, 0, AFM_ERR_MAXIT);
-            h[S_TOL] = m.inner_tol;
+            h[S_TOL] = m.inner_tol * m.sigma;
             h[S_MAXIT] = (double)m.max_inner;
             h[S_NORM] = 0.0;
             AFM_CUDA(cudaMemcpyAsync(sc + S_DONE, h + S_DONE, sizeof(double) * (S_NORM - S_DONE + 1),
@@ -1345,7 +1392,7 @@ int mixed_advance(MixedSolve& m) {
                 AFM_CUDA(cudaEventRecord(m.ev, st));
                 return AFM_SUCCESS;
             }
-            const double nrm = std::sqrt(h[S_RR]);
+            const double nrm = std::sqrt(h[S_RR]) / m.sigma;
             const int seg = h[S_FLAG] != 0.0 ? AFM_ERR_BREAKDOWN : (nrm <= m.inner_tol ? AFM_SUCCESS : AFM_ERR_MAXIT);
             return mixed_segment_end(m, (int)h[S_ITER], seg);
         }
@@ -1444,12 +1491,14 @@ int afm_create(afm_operator** out, int bc_method, int device) {
     op->sm_count = prop.multiProcessorCount;
     if (cudaStreamCreateWithFlags(&op->stream, cudaStreamNonBlocking) != cudaSuccess ||
         dalloc(op, &op->d_err, sizeof(int) * kErrWords) != cudaSuccess ||
+        dalloc(op, &op->d_usc, sizeof(unsigned long long) * kUscWords) != cudaSuccess ||
         dalloc(op, &op->d_scalars, sizeof(double) * (kScalarSlots + kPartialSlots)) != cudaSuccess ||
         cudaMallocHost((void**)&op->h_scalars, sizeof(double) * kScalarSlots) != cudaSuccess) {
         afm_destroy(op);
         return fail(AFM_ERR_CUDA, "afm_create: stream or buffer allocation failed");
     }
     cudaMemsetAsync(op->d_err, 0, sizeof(int) * kErrWords, op->stream);
+    cudaMemsetAsync(op->d_usc, 0, sizeof(unsigned long long) * kUscWords, op->stream);
     cudaStreamSynchronize(op->stream);
     *out = op;
     return ok();
@@ -1463,6 +1512,7 @@ int afm_destroy(afm_operator* op) {
         free_device(op);
         if (op->stream) {
             dfree(op, op->d_err);
+            dfree(op, op->d_usc);
             dfree(op, op->d_scalars);
             dfree(op, op->d_bremain);
             cudaStreamSynchronize(op->stream);
@@ -1495,6 +1545,27 @@ int afm_set_patch_mode(afm_operator* op, int enable) {
     AFM_CHECK_OP(op);
     op->patch_mode = enable ? 1 : 0;
     op->finalized = false;
+    return ok();
+}
+
+int afm_set_wait_limit(afm_operator* op, double seconds) {
+    AFM_CHECK_OP(op);
+    if (!(seconds >= 1e-9 && seconds <= 600.0)) return fail(AFM_ERR_INVALID_ARG, "wait limit %g s (1e-9 .. 600)", seconds);
+    const unsigned long long ns = (unsigned long long)std::llround(seconds * 1e9);
+    if (ns != op->wait_ns) {
+        op->wait_ns = ns;
+        op->generation++;  // captured iterations hold the old limit in their launch arguments
+    }
+    return ok();
+}
+
+int afm_set_wait_probe(afm_operator* op, int enable) {
+    AFM_CHECK_OP(op);
+    if (enable != 0 && enable != 1) return fail(AFM_ERR_INVALID_ARG, "wait probe %d (0 or 1)", enable);
+    if (op->wait_probe != (enable == 1)) {
+        op->wait_probe = enable == 1;
+        op->generation++;  // captured iterations hold the hook in their launch arguments
+    }
     return ok();
 }
 
@@ -1822,6 +1893,12 @@ int afm_finalize(afm_operator* op) {
         prec = fits ? AFM_PREC_FP64_SPLIT : AFM_PREC_FP64;
     }
     op->precision = prec;
+    if (prec == AFM_PREC_FP64_SPLIT) {
+        // the pair hi + lo of every entry must be FP32 numbers
+        for (double x : op->ke)
+            if (!std::isfinite(x) || std::fabs(x) > 1e38)
+                return fail(AFM_ERR_INVALID_ARG, "FP64_SPLIT: element matrix entry %g outside the FP32 range", x);
+    }
 
     // colouring (the reference's greedy colouring, also the segment order)
     op->n_colors = color_elements(op->n_dofs, op->n_elem, op->offsets, op->map, op->colors);
@@ -1901,6 +1978,10 @@ int afm_finalize(afm_operator* op) {
     AFM_CUDA(cudaMemcpyAsync(op->d_map, hmap.data(), op->map_bytes, cudaMemcpyHostToDevice, op->stream));
     AFM_CUDA(cudaMemcpyAsync(op->d_diag, op->diag_host.data(), sizeof(double) * op->n_dofs, cudaMemcpyHostToDevice,
                              op->stream));
+    if (!op->bc_unique.empty()) {
+        AFM_CUDA(dalloc(op, &op->d_bcmask, std::max<uint32_t>(op->n_dofs, 1)));
+        AFM_CUDA(cudaMemcpyAsync(op->d_bcmask, is_bc.data(), op->n_dofs, cudaMemcpyHostToDevice, op->stream));
+    }
     if (op->n_bc) {
         AFM_CUDA(cudaMemcpyAsync(op->d_bc_idx, bci.data(), sizeof(uint32_t) * op->n_bc, cudaMemcpyHostToDevice,
                                  op->stream));
@@ -2243,9 +2324,12 @@ int afm_set_batch_tuning(afm_operator* op, uint32_t nrhs, uint32_t ld, int f32, 
                          int rows_per_thread) {
     AFM_CHECK_OP(op);
     if (!op->finalized) return fail(AFM_ERR_STATE, "before finalize");
-    const bool tile_ok = (cols_per_thread == 4 && rows_per_thread == 4) ||
+    const bool tc = cols_per_thread == 0 && rows_per_thread == 0;
+    if (tc && !(f32 && batched_tc_all(op, nrhs)))
+        return fail(AFM_ERR_INVALID_ARG, "the tensor-core kernel takes FP32 products with nrhs 32, 64 or 128");
+    const bool tile_ok = tc || (cols_per_thread == 4 && rows_per_thread == 4) ||
                          (cols_per_thread == 8 && (rows_per_thread == 2 || rows_per_thread == 4 || rows_per_thread == 6));
-    if (!tile_ok || nrhs % (uint32_t)cols_per_thread)
+    if (!tile_ok || (!tc && nrhs % (uint32_t)cols_per_thread))
         return fail(AFM_ERR_INVALID_ARG, "tile %d rows x %d columns for nrhs %u", rows_per_thread, cols_per_thread, nrhs);
     const int groups_per_cta = rows_per_thread;
     const int kprec = f32 ? AFM_PREC_FP32 : op->precision;
@@ -2558,6 +2642,8 @@ int afm_get_info(afm_operator* op, afm_info* info) {
     info->sym_available = sym_format(op);
     info->sym_bytes = op->d_sym ? op->sym_bytes : 0;
     info->csr_nnz = op->csr_nnz;
+    info->work_bytes = op->work_elems * sizeof(double) + op->work32_elems * sizeof(float) +
+                       op->bwork_elems * sizeof(double) + op->bsc_elems * sizeof(double);
     info->device = op->device;
     return ok();
 }

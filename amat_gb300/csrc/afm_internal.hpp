@@ -29,7 +29,7 @@ constexpr uint32_t kDofMask = 0x7fffffffu;
 // bounds check (kind, block, thread and three values); kErrWords ints in all.
 constexpr int kErrTimeout = 1;
 constexpr int kErrBounds = 2;
-constexpr int kErrWords = 8;
+constexpr int kErrWords = 8;  // the last word is never written: the flag of afm_set_wait_probe
 
 // One launch of the matvec: the elements of one colour that share n.
 struct Segment {
@@ -61,6 +61,9 @@ struct SegArgs {
     uint32_t plane;           // entries per plane (split arena)
     int bc_mode;              // 1: constrained columns read as zero (MatMult_mf)
     int* err;
+    const unsigned long long* umax;  // split arithmetic: max|u| (bits of a non-negative double)
+    unsigned long long wait_ns;  // limit of each pipeline wait (afm_set_wait_limit)
+    const int* probe;         // test hook: a flag nothing sets, or null (afm_set_wait_probe)
 };
 
 // Arguments of one batched (multi right-hand side) segment launch.
@@ -77,6 +80,9 @@ struct BatchArgs {
     int* err;
     uint32_t n_dofs;      // rows of U and V (bounds checks)
     uint32_t smem_total;  // dynamic shared memory of the launch (bounds checks)
+    const unsigned long long* umax;  // split arithmetic: max|U(:, j)| per column j (double bits)
+    unsigned long long wait_ns;  // limit of each pipeline wait
+    const int* probe;         // test hook: a flag nothing sets, or null (afm_set_wait_probe)
 };
 
 // ---- patch path (small elements) -----------------------------------------
@@ -130,6 +136,9 @@ struct PatchArgs {
     uint32_t plane;           // entries per plane (split arena)
     int bc_mode;
     int* err;
+    const unsigned long long* umax;  // split arithmetic: max|u| (double bits)
+    unsigned long long wait_ns;  // limit of each pipeline wait
+    const int* probe;         // test hook: a flag nothing sets, or null (afm_set_wait_probe)
 };
 
 // Patch launch geometry shared by all colours of an operator.
@@ -233,6 +242,10 @@ struct afm_operator {
     double* d_bc_val = nullptr;
     uint32_t n_bc = 0;
     int* d_err = nullptr;
+    unsigned long long wait_ns = 4000000000ull;  // limit of each kernel pipeline wait (afm_set_wait_limit)
+    bool wait_probe = false;         // afm_set_wait_probe
+    unsigned long long* d_usc = nullptr;  // u-scale words of the split products (kUscWords, afm_solver.hpp)
+    uint8_t* d_bcmask = nullptr;     // 1 per constrained DoF (null without constraints)
     double* d_work = nullptr;        // host-API staging and solver vectors
     size_t work_elems = 0;
     double* d_scalars = nullptr;     // solver scalars / reduction partials

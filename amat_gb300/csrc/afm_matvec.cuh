@@ -13,9 +13,13 @@
 // atomics, and each v entry receives its element contributions in colour
 // order, independent of scheduling (bit-reproducible).
 //
-// Every mbarrier wait is bounded by wall time (globaltimer); on expiry the
-// warp sets kErrTimeout in *err and leaves its loop, and the host reports
-// AFM_ERR_TIMEOUT.
+// Every mbarrier wait is bounded by wall time (globaltimer): the operator's
+// wait limit (afm_set_wait_limit, 4 s by default) for the pipeline's waits;
+// on expiry the warp sets kErrTimeout in *err and leaves its loop, and the
+// host reports AFM_ERR_TIMEOUT. Before its CTA exits, the producer waits for
+// every bulk copy it issued to land (drain_ring, bounded by kDrainLimitNs
+// whatever the operator's limit), so that no copy writes into the shared
+// memory of an exited CTA however short the limit.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -25,7 +29,8 @@
 
 namespace afm {
 
-constexpr unsigned long long kWaitLimitNs = 4000000000ull;  // 4 s per wait
+constexpr unsigned long long kDefaultWaitNs = 4000000000ull;  // 4 s per wait unless the operator sets another
+constexpr unsigned long long kDrainLimitNs = 4000000000ull;   // copies in flight at exit: always 4 s
 constexpr uint32_t kSmemBudget = 220 * 1024;
 constexpr uint32_t kSlotAlign = 128;
 
@@ -62,28 +67,75 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
     return ok != 0;
 }
 
-// Bounded wait for the phase with the given parity; false on timeout.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-    if (mbar_try_wait(bar, parity)) return true;
+// Non-blocking test of the phase with the given parity.
+__device__ __forceinline__ bool mbar_test_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Limits below this are polled with non-blocking tests: try_wait may suspend
+// the thread for a hardware-chosen while before it reports an incomplete
+// phase, which would stretch a short limit.
+constexpr unsigned long long kSpinBelowNs = 100000ull;
+
+__device__ __forceinline__ bool mbar_poll(uint64_t* bar, uint32_t parity, bool spin) {
+    return spin ? mbar_test_wait(bar, parity) : mbar_try_wait(bar, parity);
+}
+
+// Bounded wait for the phase with the given parity; false on timeout. The
+// first test does not block; after it the timer is read after every poll.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, unsigned long long limit) {
+    if (mbar_test_wait(bar, parity)) return true;
+    const bool spin = limit < kSpinBelowNs;
     const unsigned long long t0 = globaltimer_ns();
     for (;;) {
-        for (int k = 0; k < 64; k++)
-            if (mbar_try_wait(bar, parity)) return true;
-        if (globaltimer_ns() - t0 > kWaitLimitNs) return false;
+        if (mbar_poll(bar, parity, spin)) return true;
+        if (globaltimer_ns() - t0 > limit) return false;
     }
+}
+
+// The producer's last step: waits until each of the last min(issued, S) ring
+// copies (the latest round of every slot) has landed, bounded by
+// kDrainLimitNs. Consumers that gave up early leave copies in flight; the CTA
+// must not exit before they land.
+__device__ __forceinline__ void drain_ring(uint64_t* full, uint32_t S, uint32_t issued) {
+    const unsigned long long t0 = globaltimer_ns();
+    for (uint32_t i = issued > S ? issued - S : 0; i < issued; i++)
+        while (!mbar_try_wait(&full[i % S], (i / S) & 1) && globaltimer_ns() - t0 < kDrainLimitNs) {
+        }
+}
+
+// Test hook of the timeout path (afm_set_wait_probe): when `flag` is set in
+// the launch arguments, one consumer warp of block 0 waits for *flag to
+// become non-zero, which nothing ever makes it; the wait runs out after
+// `limit` and the caller takes its timeout path. Returns false on expiry
+// (the same verdict in every lane).
+__device__ __forceinline__ bool probe_wait(const int* flag, unsigned long long limit) {
+    const unsigned long long t0 = globaltimer_ns();
+    bool set = false;
+    while (!(set = (*(const volatile int*)flag != 0)) && globaltimer_ns() - t0 <= limit) __nanosleep(256);
+    return __all_sync(0xffffffffu, set);
 }
 
 // Bounded wait that also gives up as soon as another warp of the CTA has set
 // *abort (after a timeout), so that the whole CTA drains quickly and keeps
 // meeting its named barriers.
-__device__ __forceinline__ bool mbar_wait_abortable(uint64_t* bar, uint32_t parity, volatile int* abort) {
-    if (mbar_try_wait(bar, parity)) return true;
+__device__ __forceinline__ bool mbar_wait_abortable(uint64_t* bar, uint32_t parity, volatile int* abort,
+                                                    unsigned long long limit) {
+    if (mbar_test_wait(bar, parity)) return true;
+    const bool spin = limit < kSpinBelowNs;
     const unsigned long long t0 = globaltimer_ns();
     for (;;) {
-        for (int k = 0; k < 64; k++)
-            if (mbar_try_wait(bar, parity)) return true;
+        if (mbar_poll(bar, parity, spin)) return true;
         if (*abort) return false;
-        if (globaltimer_ns() - t0 > kWaitLimitNs) {
+        if (globaltimer_ns() - t0 > limit) {
             *abort = 1;
             return false;
         }
@@ -136,6 +188,7 @@ __device__ __forceinline__ void report_bad(int* err, int kind, uint32_t a0, uint
 
 struct ArithF64 {
     static constexpr bool kSym = false;
+    static constexpr bool kScaled = false;  // u scaled by a power of two per launch (stage_s, finish_s)
     static constexpr uint32_t kWpgWarps = 16;  // consumer warps of the warp-group kernel
     using KT = double;
     using UT = double;
@@ -160,6 +213,7 @@ struct ArithF64 {
 // The _rn intrinsics keep the compiler from fusing the steps.
 struct ArithSplit {
     static constexpr bool kSym = false;
+    static constexpr bool kScaled = true;
     static constexpr uint32_t kWpgWarps = 16;
     using KT = float2;
     using UT = float2;
@@ -200,6 +254,7 @@ struct ArithSplit {
 
 struct ArithF32 {
     static constexpr bool kSym = false;
+    static constexpr bool kScaled = false;
     static constexpr uint32_t kWpgWarps = 24;  // more elements in flight: see wpg_gc
     using KT = float;
     using UT = float;
@@ -240,6 +295,7 @@ struct ArithF32Sym : ArithF32 {
 // markedly; this arithmetic removes both.
 struct ArithF32SymX {
     static constexpr bool kSym = true;
+    static constexpr bool kScaled = false;
     static constexpr uint32_t kWpgWarps = 24;
     using KT = float2;  // (hi, lo)
     using UT = float;
@@ -272,6 +328,79 @@ struct ArithF32SymX {
         a.lo = __fadd_rn(a.lo, __fadd_rn(b.lo, err));
     }
 };
+
+// Range guard of the double-float arithmetic. Its u pairs and products live in
+// FP32's exponent range: unscaled, |u| above 3.4e38 would overflow and small
+// entries would fall into FP32 subnormals and lose their low bits. So every
+// launch scales u by 2^k with k = -eu, max|u| = f 2^eu (f in [0.5, 1)), over
+// the DoFs the product reads: the largest scaled entry lies in [0.5, 1), and
+// with max|Ke| in [1e-30, 1e30] (checked at finalize) every product of a
+// scaled u entry and a Ke entry stays within FP32's normal range. The element
+// sums are scaled back by 2^-k in FP64. Both steps only move exponents, so
+// they are exact, and they run on the integer pipe (GB300 issues FP64 at 1/64
+// of the FP32 rate): the staged pair (hi, lo) of 2^k x is cut from the bits of
+// x directly, hi = the leading 24 significant bits, lo = the next 29 rounded
+// to FP32 (together 2^-47 of |x|). A scaled entry below 2^-126 becomes 0 and
+// one below 2^-74 keeps only hi, i.e. changes of at most 2^-98 of max|u|:
+// the norm-wise bound |v - K u| <= c 2^-44 |K| |u| holds for every finite u.
+// A non-finite max|u| leaves k = 0 (the product is then non-finite, as in FP64).
+__device__ __forceinline__ int uscale_of(unsigned long long mbits) {
+    if (mbits == 0ull || mbits >= 0x7ff0000000000000ull) return 0;
+    const int e = (int)(mbits >> 52);  // biased exponent of max|u| (0: subnormal)
+    int eu = e - 1022;                 // frexp exponent of a normal max|u|
+    if (e == 0) eu = -1022;            // a subnormal maximum: scale as the smallest normal
+    return eu > 1000 ? -1000 : (eu < -1000 ? 1000 : -eu);
+}
+
+// u scale exponent k of a launch: from the max|u| word for a scaled
+// arithmetic, 0 otherwise.
+template <typename A>
+__device__ __forceinline__ int load_uscale(const unsigned long long* umax) {
+    if constexpr (A::kScaled) return uscale_of(*umax);
+    return 0;
+}
+
+// (hi, lo) of 2^k x as above, with integer and FP32 operations only (the FP64
+// pipe only for non-finite x).
+__device__ __forceinline__ float2 split_scaled(double x, int k) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int e = (int)((b >> 52) & 0x7ff);
+    const unsigned sgn = (unsigned)(b >> 32) & 0x80000000u;
+    if (e == 0x7ff) return make_float2(__double2float_rn(x), 0.0f);
+    const int E = e - 1023 + k;  // unbiased exponent of 2^k x
+    if (e == 0 || E < -126) return make_float2(__uint_as_float(sgn), 0.0f);
+    if (E > 127) return make_float2(__uint_as_float(sgn | 0x7f800000u), 0.0f);
+    const unsigned long long m = b & 0x000fffffffffffffull;
+    const float h = __uint_as_float(sgn | ((unsigned)(E + 127) << 23) | (unsigned)(m >> 29));
+    float l = 0.0f;
+    const unsigned mlo = (unsigned)(m & 0x1fffffffu);
+    if (mlo && E >= -74) {
+        // mlo units of 2^(E - 52), a normal FP32 power of two for E >= -74
+        const float unit = __uint_as_float((unsigned)(E - 52 + 127) << 23);
+        l = __uint_as_float(__float_as_uint(__uint2float_rn(mlo) * unit) | sgn);
+    }
+    return make_float2(h, l);
+}
+
+// 2^k y through the exponent field (y normal and the result normal), else in FP64.
+__device__ __forceinline__ double scale_pow2(double y, int k) {
+    const long long b = __double_as_longlong(y);
+    const int e = (int)((b >> 52) & 0x7ff);
+    if (e != 0 && e != 0x7ff && e + k > 0 && e + k < 0x7ff) return __longlong_as_double(b + ((long long)k << 52));
+    return y * __longlong_as_double((long long)(1023 + k) << 52);
+}
+
+template <typename A>
+__device__ __forceinline__ typename A::UT stage_s(typename A::VT x, int k) {
+    if constexpr (A::kScaled) return split_scaled(x, k);
+    else return A::stage(x);
+}
+
+template <typename A>
+__device__ __forceinline__ typename A::VO finish_s(const typename A::Acc& acc, int k) {
+    if constexpr (A::kScaled) return scale_pow2(A::finish(acc), -k);
+    else return A::finish(acc);
+}
 
 // Entry index of (r, c) in a thread-per-element unit.
 template <typename A>
@@ -369,13 +498,13 @@ struct RingLayout {
 // loops of the element kernels registers and spills. Bounded like
 // mbar_wait_abortable.
 static __device__ __noinline__ bool ring_wait_slow(uint64_t* bar, const volatile uint32_t* tag, uint32_t ii, uint32_t parity,
-                                                   volatile int* abort) {
+                                                   volatile int* abort, unsigned long long limit) {
+    const bool spin = limit < kSpinBelowNs;
     const unsigned long long t0 = globaltimer_ns();
     for (;;) {
-        for (int k = 0; k < 64; k++)
-            if (mbar_try_wait(bar, parity) && *tag == ii) return true;
+        if (mbar_poll(bar, parity, spin) && *tag == ii) return true;
         if (*abort) return false;
-        if (globaltimer_ns() - t0 > kWaitLimitNs) {
+        if (globaltimer_ns() - t0 > limit) {
             *abort = 1;
             return false;
         }
@@ -383,9 +512,9 @@ static __device__ __noinline__ bool ring_wait_slow(uint64_t* bar, const volatile
 }
 
 __device__ __forceinline__ bool ring_wait(uint64_t* bar, const volatile uint32_t* tag, uint32_t ii, uint32_t parity,
-                                          volatile int* abort) {
-    if (mbar_try_wait(bar, parity) && *tag == ii) return true;
-    return ring_wait_slow(bar, tag, ii, parity, abort);
+                                          volatile int* abort, unsigned long long limit) {
+    if (mbar_test_wait(bar, parity) && *tag == ii) return true;
+    return ring_wait_slow(bar, tag, ii, parity, abort, limit);
 }
 
 // ---- warp per element (n > 16) --------------------------------------------
@@ -420,22 +549,30 @@ __global__ void __launch_bounds__(9 * 32, 1) afm_wpe_kernel(SegArgs a, RingLayou
     if (warp == NW) {  // producer
         if (lane == 0) {
             const uint64_t pol = l2_evict_first_policy();
+            uint32_t issued = 0;
             for (uint32_t i = 0; i < cnt; i++) {
                 const uint32_t s = i % S;
-                if (i >= S && !mbar_wait(&empty[s], ((i / S) - 1) & 1)) {
+                if (i >= S && !mbar_wait(&empty[s], ((i / S) - 1) & 1, a.wait_ns)) {
                     atomicOr(a.err, kErrTimeout);
                     break;
                 }
                 mbar_arrive_expect_tx(&full[s], a.copy_bytes);
                 bulk_load(smem + (size_t)s * L.slot_bytes, a.ke + (size_t)(begin + i) * a.unit_bytes, a.copy_bytes,
                           &full[s], pol);
+                issued = i + 1;
             }
             allow_dependent_launch();
+            drain_ring(full, S, issued);
         }
         return;
     }
     wait_prior_grid();
+    if (a.probe && blockIdx.x == 0 && warp == 0 && !probe_wait(a.probe, a.wait_ns)) {
+        if (lane == 0) atomicOr(a.err, kErrTimeout);
+        return;  // this warp's elements are left out; the producer's waits for their slots run out too
+    }
 
+    const int usk = load_uscale<A>(a.umax);
     const VT* __restrict__ u = static_cast<const VT*>(a.u);
     VT* __restrict__ v = static_cast<VT*>(a.v);
     UT* us = reinterpret_cast<UT*>(smem + L.ubuf_offset() + warp * L.ubuf_bytes);
@@ -475,7 +612,7 @@ __global__ void __launch_bounds__(9 * 32, 1) afm_wpe_kernel(SegArgs a, RingLayou
         load_uv(dof_c, u_c, vold_c);
 #pragma unroll
         for (int t = 0; t < RMAX; t++)
-            if (lane + 32 * t < n) us[lane + 32 * t] = A::stage(u_c[t]);
+            if (lane + 32 * t < n) us[lane + 32 * t] = stage_s<A>(u_c[t], usk);
         if (i + NW < cnt) load_map(i + NW, dof_n);
     }
     for (; i < cnt; i += NW) {
@@ -484,7 +621,7 @@ __global__ void __launch_bounds__(9 * 32, 1) afm_wpe_kernel(SegArgs a, RingLayou
         __syncwarp();
 
         const uint32_t s = i % S;
-        if (!mbar_wait(&full[s], (i / S) & 1)) {
+        if (!__all_sync(0xffffffffu, mbar_wait(&full[s], (i / S) & 1, a.wait_ns))) {  // one verdict per warp
             if (lane == 0) atomicOr(a.err, kErrTimeout);
             break;
         }
@@ -508,14 +645,14 @@ __global__ void __launch_bounds__(9 * 32, 1) afm_wpe_kernel(SegArgs a, RingLayou
 #pragma unroll
             for (int t = 0; t < RMAX; t++) {
                 const uint32_t r = lane + 32 * t;
-                if (r < n) v[dof_c[t] & kDofMask] = vold_c[t] + A::finish(acc[t]);
+                if (r < n) v[dof_c[t] & kDofMask] = vold_c[t] + finish_s<A>(acc[t], usk);
             }
         } else {
             // an element lists a DoF more than once: add row by row in order
             for (uint32_t r = 0; r < n; r++) {
                 if ((r & 31) == lane) {
                     const uint32_t d = dof_c[r >> 5] & kDofMask;
-                    v[d] = v[d] + A::finish(acc[r >> 5]);
+                    v[d] = v[d] + finish_s<A>(acc[r >> 5], usk);
                 }
                 __syncwarp();
             }
@@ -530,7 +667,7 @@ __global__ void __launch_bounds__(9 * 32, 1) afm_wpe_kernel(SegArgs a, RingLayou
         if (i + NW < cnt) {
 #pragma unroll
             for (int t = 0; t < RMAX; t++)
-                if (lane + 32 * t < n) us[lane + 32 * t] = A::stage(u_n[t]);
+                if (lane + 32 * t < n) us[lane + 32 * t] = stage_s<A>(u_n[t], usk);
         }
     }
 }
@@ -622,7 +759,7 @@ __global__ void __launch_bounds__((A::kWpgWarps + 1) * 32, 1)
             uint32_t issued = 0;
             for (uint32_t i = 0; i < cnt; i++) {
                 const uint32_t s = i % S;
-                if (i >= S && !mbar_wait_abortable(&empty[s], ((i / S) - 1) & 1, abort)) break;
+                if (i >= S && !mbar_wait_abortable(&empty[s], ((i / S) - 1) & 1, abort, a.wait_ns)) break;
                 tag[s] = i;
                 mbar_arrive_expect_tx(&full[s], a.copy_bytes);
                 bulk_load(smem + (size_t)s * L.slot_bytes, a.ke + (size_t)(begin + i) * a.unit_bytes, a.copy_bytes,
@@ -630,19 +767,14 @@ __global__ void __launch_bounds__((A::kWpgWarps + 1) * 32, 1)
                 issued = i + 1;
             }
             allow_dependent_launch();
-            if (*abort) {
-                // drain: every issued copy lands before the CTA's shared memory is released
-                atomicOr(a.err, kErrTimeout);
-                const uint32_t first = issued > S ? issued - S : 0;
-                const unsigned long long t0 = globaltimer_ns();
-                for (uint32_t i = first; i < issued; i++)
-                    while (!mbar_try_wait(&full[i % S], (i / S) & 1) && globaltimer_ns() - t0 < kWaitLimitNs) {
-                    }
-            }
+            if (*abort) atomicOr(a.err, kErrTimeout);
+            // every issued copy lands before the CTA's shared memory is released
+            drain_ring(full, S, issued);
         }
         return;
     }
 
+    if (a.probe && blockIdx.x == 0 && warp == 0 && !probe_wait(a.probe, a.wait_ns)) *abort = 1;
     const uint32_t grp = warp / G.g, q = warp % G.g;
     const uint32_t rg = q / G.gc, cg = q % G.gc;
     const uint32_t r = 32 * rg + lane;
@@ -652,6 +784,8 @@ __global__ void __launch_bounds__((A::kWpgWarps + 1) * 32, 1)
     const uint32_t bar_id = 1 + grp, bar_threads = G.g * 32;
     const VT* __restrict__ u = static_cast<const VT*>(a.u);
     VO* __restrict__ v = static_cast<VO*>(a.v);
+    // the scale was written by a launch that completed before this segment's first launch
+    const int usk = load_uscale<A>(a.umax);
     unsigned char* ubuf0 = ubase + (size_t)(grp * 2) * ub;
     const uint32_t pstride = (G.gc > 1 ? G.gc - 1 : 1) * n;
     Acc* pbuf0 = pbase + (size_t)(grp * 2) * pstride;
@@ -670,7 +804,7 @@ __global__ void __launch_bounds__((A::kWpgWarps + 1) * 32, 1)
     if (gatherer && i < cnt) {
         dof_c = map_at(i);
         if (rvalid) {
-            const UT x = A::stage(load_u_hint(u, dof_c, a.bc_mode, keep));
+            const UT x = stage_s<A>(load_u_hint(u, dof_c, a.bc_mode, keep), usk);
             ubuf(0)[r] = x;
             if constexpr (A::kSym) ubuf(0)[r + n] = x;
         }
@@ -690,7 +824,8 @@ __global__ void __launch_bounds__((A::kWpgWarps + 1) * 32, 1)
         }
         const uint32_t s = i % S;
         Acc acc = A::zero();
-        if (ring_wait(&full[s], &tag[s], i, (i / S) & 1, abort)) {
+        // one verdict per warp: the block below synchronises the warp, so no lane may skip it alone
+        if (__all_sync(0xffffffffu, ring_wait(&full[s], &tag[s], i, (i / S) & 1, abort, a.wait_ns))) {
             const unsigned char* ks = smem + (size_t)s * L.slot_bytes;
             const UT* uu = ubuf(par);
             if (rvalid) {
@@ -758,7 +893,7 @@ __global__ void __launch_bounds__((A::kWpgWarps + 1) * 32, 1)
         }
         if (!gatherer && rvalid) pbuf(par)[(cg - 1) * n + r] = acc;
         if (gatherer && rvalid && i + G.ng < cnt) {
-            const UT x = A::stage(u_n);
+            const UT x = stage_s<A>(u_n, usk);
             ubuf(par ^ 1)[r] = x;
             if constexpr (A::kSym) ubuf(par ^ 1)[r + n] = x;
         }
@@ -767,7 +902,7 @@ __global__ void __launch_bounds__((A::kWpgWarps + 1) * 32, 1)
             for (uint32_t c2 = 1; c2 < G.gc; c2++) {
                 if (rvalid) A::combine(acc, pbuf(par)[(c2 - 1) * n + r]);
             }
-            if (rvalid && !*abort) st_hint(v + (dof_c & kDofMask), vold_c + A::finish(acc), keep);
+            if (rvalid && !*abort) st_hint(v + (dof_c & kDofMask), vold_c + finish_s<A>(acc, usk), keep);
             dof_c = dof_n;
             vold_c = vold_n;
             dof_n = dof_nn;
@@ -808,22 +943,30 @@ __global__ void __launch_bounds__(9 * 32, 1) afm_tpe_kernel(SegArgs a, RingLayou
     if (warp == NW) {
         if (lane == 0) {
             const uint64_t pol = l2_evict_first_policy();
+            uint32_t issued = 0;
             for (uint32_t i = 0; i < cnt; i++) {
                 const uint32_t s = i % S;
-                if (i >= S && !mbar_wait(&empty[s], ((i / S) - 1) & 1)) {
+                if (i >= S && !mbar_wait(&empty[s], ((i / S) - 1) & 1, a.wait_ns)) {
                     atomicOr(a.err, kErrTimeout);
                     break;
                 }
                 mbar_arrive_expect_tx(&full[s], a.copy_bytes);
                 bulk_load(smem + (size_t)s * L.slot_bytes, a.ke + (size_t)(begin + i) * a.unit_bytes, a.copy_bytes,
                           &full[s], pol);
+                issued = i + 1;
             }
             allow_dependent_launch();
+            drain_ring(full, S, issued);
         }
         return;
     }
     wait_prior_grid();
+    if (a.probe && blockIdx.x == 0 && warp == 0 && !probe_wait(a.probe, a.wait_ns)) {
+        if (lane == 0) atomicOr(a.err, kErrTimeout);
+        return;  // this warp's elements are left out; the producer's waits for their slots run out too
+    }
 
+    const int usk = load_uscale<A>(a.umax);
     const VT* __restrict__ u = static_cast<const VT*>(a.u);
     VT* __restrict__ v = static_cast<VT*>(a.v);
     uint32_t dof_c[NM], dof_n[NM];
@@ -864,14 +1007,14 @@ __global__ void __launch_bounds__(9 * 32, 1) afm_tpe_kernel(SegArgs a, RingLayou
         if (i + 2 * NW < cnt) load_map(i + 2 * NW, dof_nn);
 
         const uint32_t s = i % S;
-        if (!mbar_wait(&full[s], (i / S) & 1)) {
+        if (!__all_sync(0xffffffffu, mbar_wait(&full[s], (i / S) & 1, a.wait_ns))) {  // one verdict per warp
             if (lane == 0) atomicOr(a.err, kErrTimeout);
             break;
         }
         const unsigned char* ks = smem + (size_t)s * L.slot_bytes;
         UT us[NM];
 #pragma unroll
-        for (int c = 0; c < NM; c++) us[c] = A::stage(u_c[c]);
+        for (int c = 0; c < NM; c++) us[c] = stage_s<A>(u_c[c], usk);
         typename A::Acc acc[NM];
 #pragma unroll
         for (int r = 0; r < NM; r++) {
@@ -891,9 +1034,9 @@ __global__ void __launch_bounds__(9 * 32, 1) afm_tpe_kernel(SegArgs a, RingLayou
                 if (r < (int)n) {
                     const uint32_t d = dof_c[r] & kDofMask;
                     if (!DUP)
-                        v[d] = vold_c[r] + A::finish(acc[r]);
+                        v[d] = vold_c[r] + finish_s<A>(acc[r], usk);
                     else
-                        v[d] = v[d] + A::finish(acc[r]);
+                        v[d] = v[d] + finish_s<A>(acc[r], usk);
                 }
             }
         }

@@ -34,6 +34,9 @@ struct MixedSolve {
     int phase = MS_IDLE;
     int outer = 0, inner_total = 0, stall = 0, status = AFM_ERR_MAXIT;
     double bn = 0.0, tol = 0.0, rn = 0.0, best = HUGE_VAL, inner_tol = 0.0;
+    // the FP32 segment runs on sigma times the FP64 residual (sigma = 2^k with
+    // ||sigma r|| in [0.5, 1)), so that tiny or huge loads stay in FP32's range
+    double sigma = 1.0;
     bool fresh = true;
     cudaEvent_t ev = nullptr, e0 = nullptr, e1 = nullptr;
 };

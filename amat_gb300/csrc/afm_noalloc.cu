@@ -19,7 +19,6 @@
 
 #include <chrono>
 #include <cmath>
-#include <mutex>
 
 #include "afm_internal.hpp"
 #include "afm_solver.hpp"
@@ -31,24 +30,17 @@ constexpr size_t kScratchDoubles = kVecs * (size_t)AFM_NOALLOC_MAX_DOFS + afm::k
 
 static __device__ __align__(256) double g_cg_scratch[kScratchDoubles];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-double* g_scratch_ptr[kMaxDevices] = {nullptr};
-
-// Device address of g_cg_scratch on `device` (the current device). The
-// symbol's host-side name is not a device address; look it up once per
-// device with that device current.
-int scratch_for(int device, double** out) {
-    if (device < 0 || device >= kMaxDevices) return afm::set_error(AFM_ERR_INVALID_ARG, "device %d", device);
-    std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_scratch_ptr[device]) {
-        void* p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_cg_scratch);
-        if (e != cudaSuccess || !p)
-            return afm::set_error(AFM_ERR_CUDA, "cudaGetSymbolAddress(g_cg_scratch): %s", cudaGetErrorString(e));
-        g_scratch_ptr[device] = static_cast<double*>(p);
-    }
-    *out = g_scratch_ptr[device];
+// Device address of g_cg_scratch on the current device. The symbol's
+// host-side name is not a device address. The lookup is repeated on every call
+// (it allocates nothing), so a context torn down and created again
+// (cudaDeviceReset) never leaves a stale address behind; the first lookup on a
+// device loads the module that holds the array.
+int scratch_address(double** out) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_cg_scratch);
+    if (e != cudaSuccess || !p)
+        return afm::set_error(AFM_ERR_CUDA, "cudaGetSymbolAddress(g_cg_scratch): %s", cudaGetErrorString(e));
+    *out = static_cast<double*>(p);
     return AFM_SUCCESS;
 }
 
@@ -84,7 +76,7 @@ extern "C" int afm_solve_cg_device_noalloc(afm_operator* op, const double* d_b, 
     } restore{prev != op->device ? prev : -1};
 
     double* base = nullptr;
-    int s = scratch_for(op->device, &base);
+    int s = scratch_address(&base);
     if (s) return s;
     const size_t n = op->n_dofs, N = AFM_NOALLOC_MAX_DOFS;
     double* r = base;
@@ -96,6 +88,8 @@ extern "C" int afm_solve_cg_device_noalloc(afm_operator* op, const double* d_b, 
     double* part = sc + kScalarSlots;
     cudaStream_t st = op->stream;
     double* h = op->h_scalars;  // pinned, allocated by afm_create
+    // stats->seconds: host wall time of the iterations (the allocating solve reports device time from
+    // events; here each iteration's host round trip is included)
     const auto t0 = std::chrono::steady_clock::now();
 
     // the array keeps the previous call's contents: start the solver state from zero

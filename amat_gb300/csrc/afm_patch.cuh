@@ -115,7 +115,7 @@ __global__ void __launch_bounds__((G * GW + 1) * 32, 1) afm_patch_kernel(PatchAr
             for (uint32_t k = 0; k < cnt && !stop; k++) {
                 const uint32_t g = k % kPatchGroups, j = k / kPatchGroups;
                 const PatchDesc d = desc[k];
-                if (j >= 1 && !mbar_wait_abortable(&idx_empty[g], (j - 1) & 1, abort)) break;
+                if (j >= 1 && !mbar_wait_abortable(&idx_empty[g], (j - 1) & 1, abort, a.wait_ns)) break;
                 mbar_arrive_expect_tx(&idx_full[g], d.idx_bytes);
                 bulk_load(smem + L.group_offset() + g * L.group_bytes(), a.idx + d.idx_off, d.idx_bytes,
                           &idx_full[g], pol);
@@ -129,7 +129,7 @@ __global__ void __launch_bounds__((G * GW + 1) * 32, 1) afm_patch_kernel(PatchAr
                 }
                 for (uint32_t u = 0; u < d.units; u++) {
                     const uint32_t s = issued % S;
-                    if (issued >= S && !mbar_wait_abortable(&empty[s], ((issued / S) - 1) & 1, abort)) {
+                    if (issued >= S && !mbar_wait_abortable(&empty[s], ((issued / S) - 1) & 1, abort, a.wait_ns)) {
                         stop = true;
                         break;
                     }
@@ -141,24 +141,20 @@ __global__ void __launch_bounds__((G * GW + 1) * 32, 1) afm_patch_kernel(PatchAr
                 }
             }
             allow_dependent_launch();
-            if (*abort) {
-                // wait (bounded) for the copies still in flight before the CTA exits
-                atomicOr(a.err, kErrTimeout);
-                const unsigned long long t0 = globaltimer_ns();
-                const uint32_t first = issued > S ? issued - S : 0;
-                for (uint32_t i = first; i < issued; i++)
-                    while (!mbar_try_wait(&full[i % S], (i / S) & 1) && globaltimer_ns() - t0 < kWaitLimitNs) {
+            if (*abort) atomicOr(a.err, kErrTimeout);
+            // wait (bounded) for the copies still in flight before the CTA exits
+            drain_ring(full, S, issued);
+            const unsigned long long t0 = globaltimer_ns();
+            for (uint32_t g = 0; g < kPatchGroups; g++)
+                if (idx_issued[g])
+                    while (!mbar_try_wait(&idx_full[g], (idx_issued[g] - 1) & 1) &&
+                           globaltimer_ns() - t0 < kDrainLimitNs) {
                     }
-                for (uint32_t g = 0; g < kPatchGroups; g++)
-                    if (idx_issued[g])
-                        while (!mbar_try_wait(&idx_full[g], (idx_issued[g] - 1) & 1) &&
-                               globaltimer_ns() - t0 < kWaitLimitNs) {
-                        }
-            }
         }
         return;
     }
 
+    if (a.probe && blockIdx.x == 0 && warp == 0 && !probe_wait(a.probe, a.wait_ns)) *abort = 1;
     const uint32_t g = warp / kPatchGroupWarps, wg = warp % kPatchGroupWarps, t = tid % kPatchGroupThreads;
     const uint32_t bar_id = 1 + g;
     unsigned char* gbase = smem + L.group_offset() + g * L.group_bytes();
@@ -171,6 +167,8 @@ __global__ void __launch_bounds__((G * GW + 1) * 32, 1) afm_patch_kernel(PatchAr
     const VT* __restrict__ u = static_cast<const VT*>(a.u);
     VO* __restrict__ v = static_cast<VO*>(a.v);
     const uint64_t keep = l2_evict_last_policy();
+    // the scale was written by a launch that completed before this matvec's first launch
+    const int usk = load_uscale<A>(a.umax);
 
     // ring index of this group's first unit: units of the patches before it
     uint32_t base = 0;
@@ -179,7 +177,7 @@ __global__ void __launch_bounds__((G * GW + 1) * 32, 1) afm_patch_kernel(PatchAr
     for (uint32_t k = g; k < cnt; k += kPatchGroups) {
         const PatchDesc d = desc[k];
         const uint32_t j = k / kPatchGroups;
-        const bool iok = mbar_wait_abortable(&idx_full[g], j & 1, abort);
+        const bool iok = __all_sync(0xffffffffu, mbar_wait_abortable(&idx_full[g], j & 1, abort, a.wait_ns));
         const uint32_t* glob = reinterpret_cast<const uint32_t*>(gbase);
         const uint16_t* lmap = reinterpret_cast<const uint16_t*>(gbase + patch_lmap_off(d.ndof));
         const uint16_t* coff = reinterpret_cast<const uint16_t*>(gbase + patch_csr_off(d.ndof, d.units, n));
@@ -202,7 +200,7 @@ __global__ void __launch_bounds__((G * GW + 1) * 32, 1) afm_patch_kernel(PatchAr
 #pragma unroll
                 for (int q = 0; q < kBatch; q++) {
                     const uint32_t i = i0 + q * kPatchGroupThreads;
-                    if (i < d.ndof) us[i] = A::stage((a.bc_mode && (m[q] & kBcFlag)) ? VT(0) : x[q]);
+                    if (i < d.ndof) us[i] = stage_s<A>((a.bc_mode && (m[q] & kBcFlag)) ? VT(0) : x[q], usk);
                 }
             }
         named_barrier(bar_id, kPatchGroupThreads);
@@ -210,7 +208,7 @@ __global__ void __launch_bounds__((G * GW + 1) * 32, 1) afm_patch_kernel(PatchAr
         // element products: lane l of warp w takes slot (unit w + W i, lane l)
         for (uint32_t un = wg; un < d.units; un += kPatchGroupWarps) {
             const uint32_t ii = base + un, s = ii % S;
-            const bool ok = iok && ring_wait(&full[s], &tag[s], ii, (ii / S) & 1, abort);
+            const bool ok = __all_sync(0xffffffffu, iok && ring_wait(&full[s], &tag[s], ii, (ii / S) & 1, abort, a.wait_ns));
             if (ok) {
                 const unsigned char* ks = smem + (size_t)s * L.slot_bytes;
                 UT ul[NM];
@@ -248,7 +246,7 @@ __global__ void __launch_bounds__((G * GW + 1) * 32, 1) afm_patch_kernel(PatchAr
                 Acc sum = A::zero();
                 const uint32_t q1 = coff[i + 1];
                 for (uint32_t c = coff[i]; c < q1; c++) A::combine(sum, ve[slot[c]]);
-                red_add(v + (glob[i] & kDofMask), A::finish(sum));
+                red_add(v + (glob[i] & kDofMask), finish_s<A>(sum, usk));
             }
         named_barrier(bar_id, kPatchGroupThreads);
         if (t == 0) mbar_arrive(&idx_empty[g]);

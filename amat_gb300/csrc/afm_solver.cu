@@ -158,15 +158,17 @@ __global__ void __launch_bounds__(kRedThreads) k_cg_init_final(double* sc, const
 }
 
 // Reliable update of the FP32 recursion of the mixed-precision solve, pass 1:
-// r = fl32(r64) (the FP64 true residual), z = dinv r; partials of r.z, r.r,
-// z.z and r.p (p = the last direction p_k)
+// r = fl32(sigma r64) (the FP64 true residual in the new segment's scale),
+// z = dinv r; partials of r.z, r.r, z.z and r.p (p = the last direction p_k,
+// still in the previous segment's scale)
 __global__ void __launch_bounds__(kRedThreads) k_cg_reliable(const double* __restrict__ r64, float* __restrict__ r,
                                                              float* __restrict__ z, const float* __restrict__ p,
-                                                             const float* __restrict__ dinv, size_t n, double* part) {
+                                                             const float* __restrict__ dinv, size_t n, double* part,
+                                                             double sigma) {
     __shared__ double sh[kRedThreads];
     double rz = 0, rr = 0, zz = 0, rp = 0;
     for (size_t i = (size_t)blockIdx.x * kRedThreads + threadIdx.x; i < n; i += kStride) {
-        const float ri = (float)r64[i];
+        const float ri = (float)(r64[i] * sigma);
         const float zi = dinv[i] * ri;
         r[i] = ri;
         z[i] = zi;
@@ -182,8 +184,12 @@ __global__ void __launch_bounds__(kRedThreads) k_cg_reliable(const double* __res
     }
 }
 
-// pass 2 (one block): beta = r.z / r_k.z_k, gamma = r.p / r.z; S_DONE, S_ITER cleared
-__global__ void __launch_bounds__(kRedThreads) k_cg_reliable_final(double* sc, const double* part, uint32_t nb) {
+// pass 2 (one block): beta = r.z / (rho r_k.z_k), gamma = r.p / r.z; S_DONE,
+// S_ITER cleared. rho = sigma_new / sigma_old, the change of the residual's
+// scale: with r, z in the new scale and p, r_k.z_k in the old one,
+// p = z + beta (p - gamma z) is the scaled form of the unscaled update.
+__global__ void __launch_bounds__(kRedThreads) k_cg_reliable_final(double* sc, const double* part, uint32_t nb,
+                                                                   double rho) {
     __shared__ double sh[kRedThreads];
     const double rz = final_sum(part, sh, nb);
     const double rr = final_sum(part + kRedBlocks, sh, nb);
@@ -192,7 +198,7 @@ __global__ void __launch_bounds__(kRedThreads) k_cg_reliable_final(double* sc, c
     if (threadIdx.x == 0) {
         const double old = sc[S_RZOLD];
         const bool bad = (rz < 0.0 || rz != rz);
-        sc[S_BETA] = (!bad && old > 0.0) ? rz / old : 0.0;
+        sc[S_BETA] = (!bad && old > 0.0) ? rz / (old * rho) : 0.0;
         sc[S_GAMMA] = (!bad && rz > 0.0) ? rp / rz : 0.0;
         sc[S_RZ] = rz;
         sc[S_RR] = rr;
@@ -332,20 +338,109 @@ __global__ void __launch_bounds__(kRedThreads) k_axpby(double* __restrict__ y, c
         y[i] = __fma_rn(a, x[i], b * y[i]);
 }
 
-// out32 = fl32(in64)
+// out32 = fl32(scale in64) (scale a power of two: exact before the rounding)
 __global__ void __launch_bounds__(kRedThreads) k_to_f32(float* __restrict__ out, const double* __restrict__ in,
-                                                        size_t n) {
+                                                        size_t n, double scale) {
     const size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) out[i] = (float)in[i];
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) out[i] = (float)(in[i] * scale);
 }
 
-// x64 += d32, d32 = 0
-__global__ void __launch_bounds__(kRedThreads) k_add_f32(double* __restrict__ x, float* __restrict__ d, size_t n) {
+// x64 += inv d32, d32 = 0 (inv a power of two)
+__global__ void __launch_bounds__(kRedThreads) k_add_f32(double* __restrict__ x, float* __restrict__ d, size_t n,
+                                                         double inv) {
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        x[i] += (double)d[i];
+        x[i] += (double)d[i] * inv;
         d[i] = 0.0f;
     }
+}
+
+// |x| as the bits of a non-negative double: ordered like the values, with
+// NaN above infinity, so that an integer max propagates both.
+__device__ __forceinline__ unsigned long long abs_bits(double x) {
+    return (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
+}
+
+__device__ __forceinline__ unsigned long long warp_max(unsigned long long m) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long y = __shfl_down_sync(0xffffffffu, m, o);
+        m = y > m ? y : m;
+    }
+    return m;
+}
+
+// w[0] = max |u[i]| over the DoFs not masked (mask[i] != 0: a constrained DoF
+// that the product reads as zero), as double bits; vz[0 .. nv) = 0 on the way.
+// The grid's blocks leave their maxima in w[2 + block]; the last block to
+// finish (counted in the low word of w[1]) reduces them, writes w[0] and
+// resets the counter, so one launch does it all and repeats cleanly inside a
+// captured graph. The maximum is exact, hence independent of the order.
+__global__ void __launch_bounds__(kRedThreads) k_umax(const double* __restrict__ u, const uint8_t* __restrict__ mask,
+                                                      size_t n, double* __restrict__ vz, size_t nv,
+                                                      unsigned long long* __restrict__ w) {
+    __shared__ unsigned long long sh[kRedThreads / 32];
+    __shared__ bool last;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    const size_t i0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long m = 0;
+    for (size_t i = i0; i < n; i += stride) {
+        const unsigned long long b = abs_bits(u[i]);
+        if ((!mask || !mask[i]) && b > m) m = b;
+    }
+    if (vz)
+        for (size_t i = i0; i < nv; i += stride) vz[i] = 0.0;
+    m = warp_max(m);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) sh[wid] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long bm = 0;
+        for (int k = 0; k < kRedThreads / 32; k++) bm = sh[k] > bm ? sh[k] : bm;
+        w[2 + blockIdx.x] = bm;
+        __threadfence();
+        const unsigned prev = atomicAdd(reinterpret_cast<unsigned*>(w + 1), 1u);
+        last = (prev == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    unsigned long long r = 0;
+    for (uint32_t k = threadIdx.x; k < gridDim.x; k += blockDim.x) {
+        const unsigned long long b = __ldcg(w + 2 + k);
+        r = b > r ? b : r;
+    }
+    r = warp_max(r);
+    if (lane == 0) sh[wid] = r;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long bm = 0;
+        for (int k = 0; k < kRedThreads / 32; k++) bm = sh[k] > bm ? sh[k] : bm;
+        w[0] = bm;
+        *reinterpret_cast<unsigned*>(w + 1) = 0u;
+    }
+}
+
+// cm[j] = max over the unmasked rows i of |U[i ld + j]|, j < R (double bits;
+// cm zeroed before the launch). Per block in shared memory, then one global
+// atomic max per column.
+__global__ void __launch_bounds__(kRedThreads) k_umax_cols(const double* __restrict__ U, const uint8_t* __restrict__ mask,
+                                                           size_t rows, uint32_t R, uint32_t ld,
+                                                           unsigned long long* __restrict__ cm) {
+    __shared__ unsigned long long sm[kMaxUmaxCols];
+    for (uint32_t j = threadIdx.x; j < R; j += blockDim.x) sm[j] = 0;
+    __syncthreads();
+    const size_t total = rows * R, stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += stride) {
+        const size_t i = q / R;
+        const uint32_t j = (uint32_t)(q % R);
+        if (mask && mask[i]) continue;
+        const unsigned long long b = abs_bits(U[i * ld + j]);
+        if (b) atomicMax(sm + j, b);
+    }
+    __syncthreads();
+    for (uint32_t j = threadIdx.x; j < R; j += blockDim.x)
+        if (sm[j]) atomicMax(cm + j, sm[j]);
 }
 
 inline unsigned grid_for(size_t n) {
@@ -406,10 +501,10 @@ cudaError_t launch_norm2(const T* a, size_t n, double* sc, double* part, cudaStr
 }
 
 cudaError_t launch_cg_reliable(const double* r64, float* r, float* z, float* p, const float* dinv, size_t n,
-                               double* sc, double* part, cudaStream_t st) {
+                               double* sc, double* part, double sigma, double rho, cudaStream_t st) {
     const uint32_t nb = red_blocks(n);
-    k_cg_reliable<<<nb, kRedThreads, 0, st>>>(r64, r, z, p, dinv, n, part);
-    k_cg_reliable_final<<<1, kRedThreads, 0, st>>>(sc, part, nb);
+    k_cg_reliable<<<nb, kRedThreads, 0, st>>>(r64, r, z, p, dinv, n, part, sigma);
+    k_cg_reliable_final<<<1, kRedThreads, 0, st>>>(sc, part, nb, rho);
     k_cg_reliable_p<<<grid_for(n), kRedThreads, 0, st>>>(p, z, n, sc);
     return cudaGetLastError();
 }
@@ -419,13 +514,28 @@ cudaError_t launch_axpby(double* y, const double* x, double a, double b, size_t 
     return cudaGetLastError();
 }
 
-cudaError_t launch_to_f32(float* out, const double* in, size_t n, cudaStream_t st) {
-    k_to_f32<<<grid_for(n), kRedThreads, 0, st>>>(out, in, n);
+cudaError_t launch_to_f32(float* out, const double* in, size_t n, cudaStream_t st, double scale) {
+    k_to_f32<<<grid_for(n), kRedThreads, 0, st>>>(out, in, n, scale);
     return cudaGetLastError();
 }
 
-cudaError_t launch_add_f32(double* x, float* d, size_t n, cudaStream_t st) {
-    k_add_f32<<<grid_for(n), kRedThreads, 0, st>>>(x, d, n);
+cudaError_t launch_add_f32(double* x, float* d, size_t n, cudaStream_t st, double inv) {
+    k_add_f32<<<grid_for(n), kRedThreads, 0, st>>>(x, d, n, inv);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_umax(const double* u, const uint8_t* mask, size_t n, double* vz, size_t nv,
+                        unsigned long long* w, cudaStream_t st) {
+    k_umax<<<red_blocks(n > nv ? n : nv), kRedThreads, 0, st>>>(u, mask, n, vz, nv, w);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_umax_cols(const double* U, const uint8_t* mask, size_t rows, uint32_t R, uint32_t ld,
+                             unsigned long long* cm, cudaStream_t st) {
+    if (R == 0 || R > (uint32_t)kMaxUmaxCols) return cudaErrorInvalidValue;
+    cudaError_t e = cudaMemsetAsync(cm, 0, sizeof(unsigned long long) * R, st);
+    if (e != cudaSuccess) return e;
+    k_umax_cols<<<grid_for(rows * R), kRedThreads, 0, st>>>(U, mask, rows, R, ld, cm);
     return cudaGetLastError();
 }
 

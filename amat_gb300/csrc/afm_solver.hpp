@@ -57,10 +57,30 @@ cudaError_t launch_norm2(const T* a, size_t n, double* sc, double* part, cudaStr
 // p = z + beta (p - gamma z) with beta = r.z / r_k.z_k and gamma = r.p / r.z,
 // so that the new residual is orthogonal to the kept direction again;
 // sc[S_RZ], sc[S_RR], sc[S_ZZ] of the new residual; S_DONE and S_ITER cleared.
+// The recursion runs on the residual times a power of two: sigma is the new
+// segment's scale (r = fl32(sigma r64)), rho = sigma / the previous segment's.
 cudaError_t launch_cg_reliable(const double* r64, float* r, float* z, float* p, const float* dinv, size_t n,
-                               double* sc, double* part, cudaStream_t st);
+                               double* sc, double* part, double sigma, double rho, cudaStream_t st);
 cudaError_t launch_axpby(double* y, const double* x, double a, double b, size_t n, cudaStream_t st);
-cudaError_t launch_to_f32(float* out, const double* in, size_t n, cudaStream_t st);
-cudaError_t launch_add_f32(double* x, float* d, size_t n, cudaStream_t st);
+// out = fl32(scale in)
+cudaError_t launch_to_f32(float* out, const double* in, size_t n, cudaStream_t st, double scale = 1.0);
+// x += inv d, d = 0
+cudaError_t launch_add_f32(double* x, float* d, size_t n, cudaStream_t st, double inv = 1.0);
+
+// Words of the u-scale buffer of an operator (afm_operator::d_usc): [0] max|u|
+// of the last single-vector split product, [1] block counter, [2, 2 +
+// kRedBlocks) block maxima, then kMaxUmaxCols per-column maxima of a batched
+// split product.
+constexpr int kMaxUmaxCols = 256;
+constexpr int kUscWords = 2 + kRedBlocks + kMaxUmaxCols;
+constexpr int kUscColsOffset = 2 + kRedBlocks;
+// w[0] = max over the unmasked i < n of |u[i]| (double bits) and vz[0 .. nv) =
+// 0, in one launch (mask may be null; w[1] must be 0 before the first launch
+// and is left 0).
+cudaError_t launch_umax(const double* u, const uint8_t* mask, size_t n, double* vz, size_t nv,
+                        unsigned long long* w, cudaStream_t st);
+// cm[j] = max over the unmasked rows of |U(:, j)|, j < R <= kMaxUmaxCols.
+cudaError_t launch_umax_cols(const double* U, const uint8_t* mask, size_t rows, uint32_t R, uint32_t ld,
+                             unsigned long long* cm, cudaStream_t st);
 
 }  // namespace afm

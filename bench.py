@@ -141,8 +141,9 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def build_problem(w, prec, device_index):
-    """Mesh, element matrices (generated in blocks straight into the operator), operator."""
+def build_problem(w, prec, device_index, keep_ke=False):
+    """Mesh, element matrices (generated in blocks straight into the operator), operator; with keep_ke, also
+    the host copy of every element matrix (for the full-size parity check)."""
     from amat_gb300 import Maps, aMatFree
     from amat_gb300 import problems as P
     t0 = time.time()
@@ -152,15 +153,19 @@ def build_problem(w, prec, device_index):
     maps.set_map(m.n_elem, dmap, m.ndpe, m.n_dofs)
     A = aMatFree(maps, 0, device_index)
     A.set_precision(prec)
+    ke = np.empty((m.n_elem, m.ndpe, m.ndpe)) if keep_ke else None
     buf = np.empty((CHUNK, m.ndpe, m.ndpe))
     for e0 in range(0, m.n_elem, CHUNK):
         c = min(CHUNK, m.n_elem - e0)
-        m.element_matrices(e0, c, ngt=w["ngt"], out=buf[:c])
-        A.set_element_matrices(e0, buf[:c])
+        blk = ke[e0:e0 + c] if keep_ke else buf[:c]
+        m.element_matrices(e0, c, ngt=w["ngt"], out=blk)
+        A.set_element_matrices(e0, blk)
     t1 = time.time()
     A.finalize()
     t2 = time.time()
     log("setup: mesh+Ke %.1fs finalize %.1fs, %d elements, %d DoF" % (t1 - t0, t2 - t1, m.n_elem, m.n_dofs))
+    if keep_ke:
+        return m, dmap, A, ke
     return m, dmap, A
 
 
@@ -177,6 +182,14 @@ def cpu_sample(w, m, dmap, max_elems):
     n = m.ndpe
     sample_bytes = ne * (n * n * 8 + 4 * n) + 16 * m.n_dofs
     return pr, u, v, ne, sample_bytes
+
+
+def full_parity(m, dmap, ke, u, v):
+    """||v - v_ref|| / ||v_ref||, v_ref = the reference CPU loop (oracle port) over every element."""
+    import oracle
+    pr = oracle.Problem(m.n_dofs, dmap.reshape(m.n_elem, m.ndpe), ke)
+    ref, _ = pr.matvec_omp(u)
+    return float(np.linalg.norm(v - ref) / np.linalg.norm(ref))
 
 
 def time_cpu(pr, u, v, reps, seconds=0.0):
@@ -322,7 +335,11 @@ def run_ours(args, w, rank, world, local_rank):
     dev = local_rank
     torch.cuda.set_device(dev)
     prec = PREC_NAMES[args.precision]
-    m, dmap, A = build_problem(w, prec, dev)
+    keep = args.cpu_sample_elems > 0 and rank == 0
+    if keep:
+        m, dmap, A, ke_host = build_problem(w, prec, dev, keep_ke=True)
+    else:
+        (m, dmap, A), ke_host = build_problem(w, prec, dev), None
     n = m.n_dofs
     info, ms, u_host, v, clk = measure_device(A, n, args.steps, args.warmup, world, dev, rank, True)
     ms_step = ms / args.steps
@@ -382,6 +399,16 @@ def run_ours(args, w, rank, world, local_rank):
                                "kind": "port",
                                "sample": "%d of %d elements, %d matvecs (%.1f s), oracle port of matvec_ghosted_OMP"
                                          % (ne, m.n_elem, len(ts), sum(ts))}
+        # the same CPU loop once over the whole mesh, as the checker of the timed device product (outside every
+        # timed region): norm-wise relative difference of the last timed v from the reference loop's v
+        err = full_parity(m, dmap, ke_host, u_host, v.cpu().numpy())
+        out["parity_rel_err"] = err
+        out["cpu_baseline"]["parity"] = {"rel_err": err, "tolerance": 1e-12, "elements": m.n_elem,
+                                         "against": "oracle port of matvec_ghosted_OMP, whole mesh"}
+    del ke_host
+    if args.with_solves and world == 1:
+        A.close()
+        out["solves"] = default_solves(args, dev)
     return out
 
 
@@ -520,6 +547,70 @@ def build_bc_problem(w, dev):
     return m, dofs, vals, A
 
 
+def solve_compare(A, m, rhs, rtol, steps, inner_rtol, M=None, nvtx=None):
+    """FP64 Jacobi-PCG on A against the mixed-precision solve on M (default A) for the same system: one
+    short warm-up of each (graph capture), then `steps` timed solves of each (device time per solve)."""
+    M = A if M is None else M
+    A.solve(rhs, rtol=rtol, atol=0.0, maxit=8, raise_on_fail=False)
+    M.solve_mixed(rhs, rtol=rtol, atol=0.0, inner_rtol=inner_rtol, max_outer=1, max_inner=8, raise_on_fail=False)
+    t64, tmx = [], []
+    for _ in range(steps):
+        if nvtx:
+            nvtx.range_push("fp64_solve")  # ranges for profiler filters (ncu --nvtx-include)
+        x64, st = A.solve(rhs, rtol=rtol, atol=0.0, maxit=200000)
+        if nvtx:
+            nvtx.range_pop()
+            nvtx.range_push("mixed_solve")
+        xm, stm = M.solve_mixed(rhs, rtol=rtol, atol=0.0, inner_rtol=inner_rtol, raise_on_fail=False)
+        if nvtx:
+            nvtx.range_pop()
+        if stm.status != 0:
+            raise SystemExit("mixed-precision solve did not converge (status %d)" % stm.status)
+        t64.append(st.seconds)
+        tmx.append(stm.seconds)
+    s64, smx = steps / sum(t64), steps / sum(tmx)
+    log("fp64 CG: %d iterations, %.3f s; mixed: %d refinements, %d inner iterations, %.3f s" % (
+        st.iterations, t64[-1], stm.refinements, stm.iterations, tmx[-1]))
+    out = {"mixed": {"solves_per_s": smx, "inner_iterations": stm.iterations, "refinements": stm.refinements,
+                     "rel_residual": stm.rel_residual,
+                     "rel_error_vs_fp64_solution": float(np.linalg.norm(xm - x64) / np.linalg.norm(x64))},
+           "fp64": {"solves_per_s": s64, "iterations": st.iterations, "rel_residual": st.rel_residual,
+                    "dtype": "f64 (split arena)"},
+           "speedup_vs_fp64": smx / s64, "rtol": rtol, "inner_rtol": inner_rtol, "steps": steps}
+    return out, xm, x64
+
+
+def poisson_analytic_error(m, x):
+    """max |x - u| / max |u| against example03a's u = sin(2 pi x) sin(2 pi y) sin(2 pi z) / (12 pi^2)."""
+    c = m.coords
+    exact = np.sin(2 * np.pi * c[:, 0]) * np.sin(2 * np.pi * c[:, 1]) * np.sin(2 * np.pi * c[:, 2]) / (12 * np.pi ** 2)
+    return float(np.abs(x - exact).max() / np.abs(exact).max())
+
+
+def default_solves(args, dev):
+    """The solve half of the metric beside the default matvec line: config 3 (tet10 Poisson 96^3 x 6, mixed
+    precision against FP64 CG to 1e-8) and config 2 (hex20 elasticity 64^3, CG to 1e-10)."""
+    out = {}
+    w3 = WORKLOADS["tet10_poisson_96"]
+    m, dofs, vals, A = build_bc_problem(w3, dev)
+    rhs = A.apply_bc(m.load(ngt=w3["ngt"]))
+    r3, xm, _ = solve_compare(A, m, rhs, 1e-8, args.solve_steps, 0.1)
+    r3["workload"] = w3["desc"]
+    r3["n_dofs"] = m.n_dofs
+    r3["mixed"]["analytic_rel_error_max"] = poisson_analytic_error(m, xm)
+    out["config3_mixed_vs_fp64"] = r3
+    A.close()
+    w2 = WORKLOADS["hex20_elastic_64"]
+    m, dofs, vals, A = build_bc_problem(w2, dev)
+    rhs = A.apply_bc(m.load(ngt=w2["ngt"]))
+    r2, _, _ = solve_compare(A, m, rhs, 1e-10, 1, 0.3)
+    r2["workload"] = w2["desc"] + ", elastic bar: body load and end traction, clamped end"
+    r2["n_dofs"] = m.n_dofs
+    out["config2_cg_1e-10"] = r2
+    A.close()
+    return out
+
+
 def run_solve(args, w, rank, world, local_rank):
     """CG solves/s: FP64 Jacobi-PCG and mixed-precision refinement on the same system."""
     import torch
@@ -529,8 +620,6 @@ def run_solve(args, w, rank, world, local_rank):
     m, dofs, vals, A = build_bc_problem(w, dev)
     rhs = A.apply_bc(m.load(ngt=w["ngt"]))
     rtol = args.rtol
-    x64, st = A.solve(rhs, rtol=rtol, atol=0.0, maxit=100000)  # warm-up (captures the graphs)
-    log("fp64 CG: %d iterations, rel residual %.3e, %.3f s" % (st.iterations, st.rel_residual, st.seconds))
     M = A
     if args.free:
         # the mixed solve on the matrix-free operator (method 2): no element matrix on the device
@@ -543,43 +632,20 @@ def run_solve(args, w, rank, world, local_rank):
         M.set_element_kind(w["kind"], E=1.0, nu=0.3, ngt=w["ngt"])
         M.set_element_coords(0, m.coords[m.elem_nodes])
         M.finalize()
-    xm, stm = M.solve_mixed(rhs, rtol=rtol, atol=0.0, inner_rtol=args.inner_rtol, raise_on_fail=False)
-    log("mixed: status %d, %d refinements, %d inner iterations, rel residual %.3e, %.3f s" % (
-        stm.status, stm.refinements, stm.iterations, stm.rel_residual, stm.seconds))
-    if stm.status != 0:
-        raise SystemExit("mixed-precision solve did not converge")
-    t64, tmx = [], []
-    nvtx = torch.cuda.nvtx
-    for _ in range(args.steps):
-        nvtx.range_push("fp64_solve")  # ranges for profiler filters (ncu --nvtx-include)
-        x64, st = A.solve(rhs, rtol=rtol, atol=0.0, maxit=100000)
-        nvtx.range_pop()
-        t64.append(st.seconds)
-        nvtx.range_push("mixed_solve")
-        xm, stm = M.solve_mixed(rhs, rtol=rtol, atol=0.0, inner_rtol=args.inner_rtol)
-        nvtx.range_pop()
-        tmx.append(stm.seconds)
-    s64 = args.steps / sum(t64)
-    smx = args.steps / sum(tmx)
+    r, xm, _ = solve_compare(A, m, rhs, rtol, args.steps, args.inner_rtol, M, torch.cuda.nvtx)
+    smx = r["mixed"]["solves_per_s"]
+    r["mixed"]["inner_ke_bytes"] = 0 if args.free else A.info()["sym_bytes"] or A.info()["ke_bytes"] // 2
+    r["mixed"]["inner_arena"] = ("matrix-free (method 2): Ke integrated from coordinates" if args.free else
+                                 {0: "hi plane", 1: "symmetric copy, FP32",
+                                  2: "symmetric copy, FP32 + BF16 correction"}[A.info()["sym_available"]])
     out = {"metric": "CG solves/s at %g rel. residual" % rtol, "value": smx, "unit": "solves/s", "n_gpus": world,
            "steps": args.steps, "warmup": 1, "ms_per_step": 1e3 / smx, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32 inner / f64 residual", "data": "synthetic",
            "config": {"workload": w["desc"], "n_dofs": m.n_dofs, "n_elements": m.n_elem, "rtol": rtol,
                       "inner_rtol": args.inner_rtol},
-           "mixed": {"solves_per_s": smx, "inner_iterations": stm.iterations, "refinements": stm.refinements,
-                     "inner_ke_bytes": 0 if args.free else A.info()["sym_bytes"] or A.info()["ke_bytes"] // 2,
-                     "inner_arena": "matrix-free (method 2): Ke integrated from coordinates" if args.free else
-                                    {0: "hi plane", 1: "symmetric copy, FP32",
-                                     2: "symmetric copy, FP32 + BF16 correction"}[A.info()["sym_available"]],
-                     "rel_residual": stm.rel_residual,
-                     "rel_error_vs_fp64_solution": float(np.linalg.norm(xm - x64) / np.linalg.norm(x64))},
-           "fp64": {"solves_per_s": s64, "iterations": st.iterations, "rel_residual": st.rel_residual,
-                    "dtype": "f64 (split arena)"},
-           "speedup_vs_fp64": smx / s64}
+           "mixed": r["mixed"], "fp64": r["fp64"], "speedup_vs_fp64": r["speedup_vs_fp64"]}
     if P.KIND_DPN[w["kind"]] == 1:
-        c = m.coords
-        exact = np.sin(2 * np.pi * c[:, 0]) * np.sin(2 * np.pi * c[:, 1]) * np.sin(2 * np.pi * c[:, 2]) / (12 * np.pi ** 2)
-        out["analytic_rel_error_max"] = float(np.abs(xm - exact).max() / np.abs(exact).max())
+        out["analytic_rel_error_max"] = poisson_analytic_error(m, xm)
     return out if rank == 0 else None
 
 
@@ -671,7 +737,8 @@ def run_product(args, w, rank, world, local_rank):
         V = torch.empty_like(U)
         if args.tile:  # pin the lane tile (columns, rows) instead of the autotuner's choice
             ct, rt = (int(x) for x in args.tile.split(","))
-            A.set_batch_tuning(R, ct, rt, f32=f32)
+            if f32 or (ct, rt) != (0, 0):  # (0, 0), the tensor-core kernel, computes FP32 products only
+                A.set_batch_tuning(R, ct, rt, f32=f32)
         torch.cuda.synchronize()
         for _ in range(max(args.warmup, 3)):  # the first call runs the autotuner
             A.matvec_batched_device(V.data_ptr(), U.data_ptr(), R, f32=f32, stream=stream_ptr)
@@ -855,6 +922,9 @@ def main():
     ap.add_argument("--rtol", type=float, default=1e-8)
     ap.add_argument("--free", type=int, default=0, help="solve: mixed solve on the matrix-free operator (method 2)")
     ap.add_argument("--inner-rtol", type=float, default=1e-2)
+    ap.add_argument("--with-solves", type=int, default=1,
+                    help="matvec: also record the config-3 mixed/FP64 solves and the config-2 CG to 1e-10")
+    ap.add_argument("--solve-steps", type=int, default=3, help="timed solves of each kind in --with-solves")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     w = WORKLOADS[args.workload]

@@ -106,6 +106,7 @@ typedef struct afm_info {
     int sym_available;          /* format of the symmetric inner arena FP32 products use (0: none) */
     uint64_t sym_bytes;         /* device bytes of that arena once built (0: not built) */
     uint64_t csr_nnz;           /* entries of the assembled matrix (0: afm_assemble not called) */
+    uint64_t work_bytes;        /* device bytes of the solver and staging work space allocated so far */
 } afm_info;
 
 typedef struct afm_solve_stats {
@@ -180,6 +181,22 @@ int afm_set_patch_mode(afm_operator* op, int enable);
  * mixed-precision solve after a change (outside any stream capture). FP64
  * products never use it. */
 int afm_set_symmetric_inner(afm_operator* op, int format);
+/* Limit of each wait inside the operator's element kernels (no counterpart
+ * in the reference, which ends the process on a device error:
+ * include/aMatGpu.hpp:303-306). The kernels' producer and consumer warps meet
+ * on shared-memory barriers; a wait that outlasts the limit makes the launch
+ * stop early and the call report AFM_ERR_TIMEOUT, after which the operator
+ * stays usable. seconds in [1e-9, 600]; the default is 4 s. Takes effect at
+ * the next call (captured CG iterations are captured again). */
+int afm_set_wait_limit(afm_operator* op, double seconds);
+/* Test hook of that failure path (no counterpart in the reference). While
+ * enabled (1), one consumer warp of the first block of every element-kernel
+ * launch first waits for a device flag that nothing sets; its wait runs out
+ * after the wait limit, the launch stops early and the call reports
+ * AFM_ERR_TIMEOUT. Nothing faults: every wait is bounded and the operator
+ * gives correct results again once the hook is off (0). Set a short limit
+ * (milliseconds) with it. */
+int afm_set_wait_probe(afm_operator* op, int enable);
 
 /* ---- maps (par::Maps) --------------------------------------------------- */
 
@@ -308,7 +325,10 @@ int afm_matmult_bc_batched_device_f32(afm_operator* op, float* d_V, const float*
 int afm_get_batch_tuning(afm_operator* op, uint32_t nrhs, uint32_t ld, int f32, int* cols_per_thread,
                          int* rows_per_thread, float* ms);
 /* Pins the lane tile for (nrhs, ld, f32) instead of the autotuner's choice:
- * (columns, rows) one of (8, 2), (8, 4), (8, 6), (4, 4). */
+ * (columns, rows) one of (8, 2), (8, 4), (8, 6), (4, 4); or (0, 0), the
+ * tensor-core kernel (FP32 products, nrhs 32, 64 or 128, elements of 17 to 96
+ * DoFs: 3xTF32 products on tcgen05, ~2^-21 of |K||u|), which the autotuner
+ * also times when it applies. */
 int afm_set_batch_tuning(afm_operator* op, uint32_t nrhs, uint32_t ld, int f32, int cols_per_thread,
                          int rows_per_thread);
 /* Batched Jacobi-PCG: one CG per column (own scalars and stopping test
@@ -411,11 +431,14 @@ int afm_server_destroy(afm_server* s);
  * into the library (5 x AFM_NOALLOC_MAX_DOFS doubles plus 2.6k doubles of
  * partials, about 10.5 MB), which every GPU that loads the library holds until
  * the process exits. Operators with more DoFs fail with AFM_ERR_INVALID_ARG.
- * The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress); make that first call before any stream capture.
- * All calls on a device share the array and the call clears the solver state
- * it needs at its start, so calls whose work overlaps on the GPU race: run
- * them one at a time. Synchronous, like afm_solve_cg_device. */
+ * Every call looks up the array's device address (cudaGetSymbolAddress) with
+ * the operator's device current; the first lookup on a device loads the
+ * module that holds the array, so make the first call before any stream
+ * capture. All calls on a device share the array and the call clears the
+ * solver state it needs at its start, so calls whose work overlaps on the GPU
+ * race: run them one at a time. Synchronous, like afm_solve_cg_device;
+ * stats->seconds is host wall time here (each iteration's host round trip
+ * included), not device time. */
 int afm_solve_cg_device_noalloc(afm_operator* op, const double* d_b, double* d_x, double rtol, double atol,
                                 int maxit, int norm_type, afm_solve_stats* stats);
 

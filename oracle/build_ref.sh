@@ -3,13 +3,14 @@
 # oracle/_ref/libamat_ref.so (test infrastructure; never shipped or loaded by
 # the product). Only the reference's own sources are compiled, against the
 # single-rank MPI / minimal PETSc shims in oracle/shim/.
-#   REF  - reference checkout (default /root/reference)
+#   REF  - reference checkout (default: a directory named reference beside
+#          this repository's root)
 #   CXX  - C++ compiler (default g++)
 # The reference's unconditional <immintrin.h> (include/aMat.hpp:31) limits this
 # to x86 hosts; elsewhere the script exits 0 without building.
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
-REF=${REF:-/root/reference}
+REF=${REF:-$HERE/../../reference}
 CXX=${CXX:-g++}
 OUT="$HERE/_ref"
 if [ ! -d "$REF/include" ]; then echo "build_ref: no reference tree at $REF, skipped"; exit 0; fi

@@ -1,8 +1,9 @@
 """Writes the golden fixtures of tests/golden/ from the reference aMat itself.
 
 Run in a checkout where the reference tree is available (AMAT_REFERENCE,
-default /root/reference): it builds oracle/_ref/libamat_ref.so from the
-reference sources in place (oracle/build_ref.sh) and records, for small seeded
+default: a directory named reference beside the repository's root): it
+builds oracle/_ref/libamat_ref.so from the reference sources in place
+(oracle/build_ref.sh) and records, for small seeded
 problems, the reference's own outputs:
   - aMatFree (method 1) matvec, MatMult_mf, MatGetDiagonal_mf, apply_bc rhs
     (identity and penalty), for blocks_dim 1 and 2;

@@ -46,12 +46,38 @@ def solve(A, fn, b, rtol=1e-10):
 
 
 def test_noalloc_cg_matches_allocating_cg(gpu):
+    """On a fresh operator the allocation-free solve runs first: the device's free memory is the same
+    before and after it and the operator has allocated no work space; then it agrees with the allocating
+    solve on the same operator, on two calls in a row (the shared array keeps the previous call's
+    contents)."""
+    import torch
+    # set-up: the first call on the device loads the module that holds the array (a one-time reservation)
+    m0, A0 = poisson_operator(4)
+    solve(A0, "afm_solve_cg_device_noalloc", A0.apply_bc(np.ones(m0.n_dofs)))
     m, A = poisson_operator(12)
+    _, B = poisson_operator(12)  # the same system: its host calls make the loads, so A stays untouched
     rng = np.random.default_rng(0)
-    for _ in range(2):  # two calls in a row: the shared array keeps the previous call's contents
-        b = A.apply_bc(rng.normal(size=m.n_dofs))
-        x_ref, st_ref = solve(A, "afm_solve_cg_device", b)
+    bs = [B.apply_bc(rng.normal(size=m.n_dofs)) for _ in range(2)]
+    assert A.info()["work_bytes"] == 0
+    db = torch.tensor(bs[0], dtype=torch.float64, device="cuda")
+    dx = torch.zeros_like(db)
+    torch.cuda.synchronize()
+    lib = libafm()
+    st = AfmSolveStats()
+    free0 = torch.cuda.mem_get_info()[0]
+    s = lib.afm_solve_cg_device_noalloc(A._h, C.c_void_p(db.data_ptr()), C.c_void_p(dx.data_ptr()), 1e-10, 0.0,
+                                        5000, 0, C.byref(st))
+    torch.cuda.synchronize()
+    free1 = torch.cuda.mem_get_info()[0]
+    assert s == 0, lib.afm_last_error().decode()
+    assert free1 == free0
+    assert A.info()["work_bytes"] == 0
+    first = dx.cpu().numpy()
+    for k, b in enumerate(bs):
         x, st = solve(A, "afm_solve_cg_device_noalloc", b)
+        if k == 0:
+            assert np.array_equal(x, first)
+        x_ref, st_ref = solve(A, "afm_solve_cg_device", b)
         assert st.status == 0 and st.iterations == st_ref.iterations
         assert rel(x, x_ref) < FP64_RTOL
         assert abs(st.rel_residual - st_ref.rel_residual) <= 1e-12
