@@ -45,11 +45,19 @@ def _ptr(a):
 
 
 class Maps:
-    """par::Maps for one rank: element -> DoF map and boundary conditions."""
+    """par::Maps: element -> DoF map and boundary conditions.
+
+    With comm = a torch.distributed process group of more than one rank, the
+    map is partitioned (one GPU per rank): set_map builds the scatter map of
+    Maps::buildScatterMap (amat_gb300.partition.ScatterMap) and the operator
+    works over the rank-local numbering [pre-ghosts | owned | post-ghosts].
+    """
 
     def __init__(self, comm=None):
         self._map = None
         self._bdr = None
+        self._comm = comm
+        self.scatter = None
 
     def set_map(self, n_elements_on_rank, element_to_rank_map, dofs_per_element, n_all_dofs_on_rank,
                 rank_to_global_map=None, owned_global_dof_range_begin=0, owned_global_dof_range_end=None,
@@ -75,16 +83,44 @@ class Maps:
             if np.all(dpe == dpe[0]):
                 offsets, n_uniform = None, int(dpe[0])
         l2g = None if rank_to_global_map is None else np.ascontiguousarray(rank_to_global_map, dtype=np.uint64)
+        if self._partitioned():
+            from .partition import ScatterMap
+            gdofs = m.astype(np.int64) if l2g is None else l2g[m].astype(np.int64)
+            begin = int(owned_global_dof_range_begin)
+            self.scatter = ScatterMap(self._comm, gdofs, end - begin + 1, begin, offsets, n_uniform)
+            if self.scatter.n_all != int(n_all_dofs_on_rank) or self.scatter.n_global != n_global:
+                raise ValueError("n_all_dofs_on_rank %d / n_global_dofs %d disagree with the scatter map (%d, %d)"
+                                 % (n_all_dofs_on_rank, n_global, self.scatter.n_all, self.scatter.n_global))
+            # the rank's operator: a single-rank map over the local numbering
+            m, l2g, n_all = self.scatter.local_map, None, self.scatter.n_all
+            self._map = dict(n_elem=int(n_elements_on_rank), offsets=offsets, n_uniform=n_uniform, map=m,
+                             n_all=n_all, l2g=None, begin=0, end=n_all - 1, n_global=n_all)
+            return
         self._map = dict(n_elem=int(n_elements_on_rank), offsets=offsets, n_uniform=n_uniform, map=m,
                          n_all=int(n_all_dofs_on_rank), l2g=l2g, begin=int(owned_global_dof_range_begin), end=end,
                          n_global=n_global)
+
+    def _partitioned(self):
+        if self._comm is None:
+            return False
+        import torch.distributed as dist
+        return dist.get_world_size(self._comm) > 1
 
     def set_bdr_map(self, constrained_dofs, prescribed_values, num_constraints=None):
         """Maps::set_bdr_map (include/maps.hpp:829-880)."""
         c = np.ascontiguousarray(constrained_dofs, dtype=np.uint64).reshape(-1)
         v = np.ascontiguousarray(prescribed_values, dtype=np.float64).reshape(-1)
         n = len(c) if num_constraints is None else int(num_constraints)
-        self._bdr = (c[:n].copy(), v[:n].copy())
+        c, v = c[:n].copy(), v[:n].copy()
+        if self.scatter is not None:
+            # global ids -> this rank's local ids; constraints on DoFs this rank does not hold are dropped
+            l2g = self.scatter.local2global
+            order = np.argsort(l2g)
+            pos = np.searchsorted(l2g[order], c.astype(np.int64))
+            pos = np.minimum(pos, len(l2g) - 1)
+            hit = l2g[order][pos] == c.astype(np.int64)
+            c, v = order[pos[hit]].astype(np.uint64), v[hit]
+        self._bdr = (c, v)
 
     @property
     def n_dofs(self):
@@ -111,6 +147,13 @@ class aMatFree:
             c, v = maps._bdr
             check(lib.afm_set_bdr_map(h, _ptr(c), _ptr(v), len(c)), "afm_set_bdr_map")
         self.n_dofs = mp["n_global"]
+        self._part = None
+        if maps.scatter is not None:
+            from .partition import PartitionedProduct
+            self._part = PartitionedProduct(maps.scatter, self._local_matvec)
+            self._bc_local = np.zeros(self.n_dofs, dtype=bool)
+            if maps._bdr is not None:
+                self._bc_local[maps._bdr[0].astype(np.int64)] = True
 
     def close(self):
         if getattr(self, "_h", None):
@@ -130,9 +173,11 @@ class aMatFree:
     def set_precision(self, p):
         check(self._lib.afm_set_precision(self._h, int(p)), "afm_set_precision")
 
-    def set_patch_mode(self, enable):
-        """Small elements as shared-memory patches (1, default) or one launch per colour (0)."""
-        check(self._lib.afm_set_patch_mode(self._h, int(bool(enable))), "afm_set_patch_mode")
+    def set_patch_mode(self, mode):
+        """Small elements as shared-memory patches, in one launch plus a combine pass when the patch colours
+        are small and one launch per colour otherwise (1, default), always per colour (2), always in one
+        launch (3); or no patches, one launch per element colour (0)."""
+        check(self._lib.afm_set_patch_mode(self._h, int(mode)), "afm_set_patch_mode")
 
     def set_symmetric_inner(self, fmt):
         """Inner format of FP32 products: 1 (default) symmetric copy in FP32, 2 symmetric copy in FP32 + BF16
@@ -178,16 +223,36 @@ class aMatFree:
         check(self._lib.afm_finalize(self._h), "afm_finalize")
 
     # ---- operator --------------------------------------------------------
+    def _local_matvec(self, v, u):
+        check(self._lib.afm_matvec(self._h, _ptr(v), _ptr(np.ascontiguousarray(u, dtype=np.float64)), 1),
+              "afm_matvec")
+
     def matvec(self, v, u, isGhosted=True):
-        """aMatFree::matvec(v, u, isGhosted): v = K u on host arrays."""
-        u = np.ascontiguousarray(u, dtype=np.float64)
+        """aMatFree::matvec(v, u, isGhosted): v = K u on host arrays. Partitioned maps: u, v are the rank's
+        ghosted local vectors (isGhosted) or its owned entries; u's ghosts are received from their owners
+        and v's ghost rows sent to theirs (matvec_ghosted, include/aMatFree.hpp:1682-1775)."""
         assert v.dtype == np.float64 and v.flags.c_contiguous
+        if self._part is not None:
+            u = np.array(u, dtype=np.float64, copy=True)
+            return self._part.matvec(v, u, isGhosted)
+        u = np.ascontiguousarray(u, dtype=np.float64)
         check(self._lib.afm_matvec(self._h, _ptr(v), _ptr(u), int(bool(isGhosted))), "afm_matvec")
         return v
 
     def matmult_bc(self, v, u):
-        """MatMult_mf (include/aMatFree.hpp:3894-3941)."""
+        """MatMult_mf (include/aMatFree.hpp:3894-3941). Partitioned maps: ghosted local vectors; a
+        constrained row keeps its owner's v_c = u_c (the ghost copies send nothing for it)."""
         u = np.ascontiguousarray(u, dtype=np.float64)
+        if self._part is not None:
+            s = self._part.smap
+            u = u.copy()
+            s.ghost_receive(u)
+            check(self._lib.afm_matmult_bc(self._h, _ptr(v), _ptr(u)), "afm_matmult_bc")
+            ghost_bc = self._bc_local.copy()
+            ghost_bc[s.n_pre:s.n_pre + s.n_owned] = False
+            v[ghost_bc] = 0.0
+            s.ghost_send(v)
+            return v
         check(self._lib.afm_matmult_bc(self._h, _ptr(v), _ptr(u)), "afm_matmult_bc")
         return v
 
@@ -207,6 +272,23 @@ class aMatFree:
         """MatGetDiagonal_mf with apply_bc_diagonal (include/aMatFree.hpp:3945-3975, 4310-4338)."""
         d = np.empty(self.n_dofs, dtype=np.float64)
         check(self._lib.afm_get_diagonal(self._h, _ptr(d)), "afm_get_diagonal")
+        if self._part is not None:
+            # element sums of every rank on the owned rows (mat_get_diagonal_ghosted's ghost_send), then
+            # the constrained rows set wherever any rank has an element on them (apply_bc_diagonal inserts
+            # the value from every rank that holds such an element)
+            s = self._part.smap
+            in_elem = np.zeros(s.n_all, dtype=bool)
+            in_elem[s.local_map.astype(np.int64)] = True
+            d[self._bc_local] = 0.0
+            s.ghost_send(d)
+            flag = (self._bc_local & in_elem).astype(np.float64)
+            s.ghost_send(flag)
+            own = np.zeros(s.n_all, dtype=bool)
+            own[s.n_pre:s.n_pre + s.n_owned] = True
+            set_rows = own & self._bc_local & (flag > 0)
+            if self.bc_method != BC_METH.BC_IMATRIX:
+                raise NotImplementedError("partitioned diagonal with the penalty method")
+            d[set_rows] = 1.0
         return d
 
     def apply_bc(self, rhs):

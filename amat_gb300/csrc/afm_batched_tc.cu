@@ -26,6 +26,9 @@
 // per SM overlap each other's gathers, MMAs and updates.
 //
 // Every wait is bounded; TMEM is always released before the CTA exits.
+#include <mutex>
+#include <vector>
+
 #include "afm_matvec.cuh"
 
 namespace afm {
@@ -100,13 +103,14 @@ struct TcGeom {
 };
 
 template <int NT>
-__global__ void __launch_bounds__(kTcThreads) afm_batched_tc_kernel(BatchArgs a, TcGeom G, uint32_t n_rt) {
+__global__ void __launch_bounds__(kTcThreads, (NT != 0 && NT <= 32) ? 4 : 1) afm_batched_tc_kernel(BatchArgs a, TcGeom G, uint32_t n_rt) {
     const uint32_t n = NT ? NT : n_rt;
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char* sA = smem;                           // hi plane, then lo plane
     unsigned char* sB = smem + 2 * G.a_bytes;           // hi plane, then lo plane
-    uint32_t* mp = reinterpret_cast<uint32_t*>(sB + 2 * G.b_bytes);  // E x n map entries
-    uint64_t* bar = reinterpret_cast<uint64_t*>(mp + ((G.E * n + 1) & ~1u));
+    const uint32_t mapw = (G.E * n + 1) & ~1u;
+    uint32_t* mp0 = reinterpret_cast<uint32_t*>(sB + 2 * G.b_bytes);  // 2 x (E x n) map entries (double buffer)
+    uint64_t* bar = reinterpret_cast<uint64_t*>(mp0 + 2 * mapw);
     uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 1);
     const uint32_t t = threadIdx.x, warp = t >> 5, lane = t & 31;
     const uint32_t kc = G.Kp / 4;
@@ -134,22 +138,34 @@ __global__ void __launch_bounds__(kTcThreads) afm_batched_tc_kernel(BatchArgs a,
     const uint32_t idesc = tc_idesc(128, G.N);
     bool failed = false;
     uint32_t phase = 0;
-    for (uint32_t grp = blockIdx.x; grp < groups && !failed; grp += gridDim.x, phase ^= 1u) {
+    // map entry i (< E n <= 256) of the group starting at element e0 (0 past the segment's end)
+    auto map_entry = [&](uint32_t e0, uint32_t i) -> uint32_t {
+        const uint32_t e = e0 + i / n;
+        return (i < G.E * n && e < a.count) ? __ldg(a.map + (size_t)e * n + i % n) : 0u;
+    };
+    if (blockIdx.x < groups) {
+        const uint32_t e0 = blockIdx.x * G.E;
+        if (t < mapw) mp0[t] = map_entry(e0, t);
+        if (t + kTcThreads < mapw) mp0[t + kTcThreads] = map_entry(e0, t + kTcThreads);
+    }
+    __syncthreads();
+    // A is gathered KA columns at a time, every load of a batch in flight before any is used
+    constexpr uint32_t KA = (NT != 0 && NT <= 32) ? ((NT + 7) / 8) * 8 : 8;
+    for (uint32_t grp = blockIdx.x, it = 0; grp < groups && !failed; grp += gridDim.x, phase ^= 1u, it++) {
         const uint32_t e0 = grp * G.E;
-        // maps of the group's elements (0 past the segment's end)
-        for (uint32_t i = t; i < G.E * n; i += kTcThreads) {
-            const uint32_t e = e0 + i / n;
-            mp[i] = e < a.count ? __ldg(a.map + (size_t)e * n + i % n) : 0u;
-        }
-        __syncthreads();
-        // A: this thread's row m, every column c (lanes read consecutive j of one U row); eight loads in
-        // flight before any is used, then 16-byte stores of (hi, lo) into the core-matrix rows
+        uint32_t* mp = mp0 + (it & 1u) * mapw;
+        uint32_t* mp_next = mp0 + ((it + 1u) & 1u) * mapw;
+        const uint32_t e_next = (grp + gridDim.x) * G.E;
+        uint32_t nm0 = 0, nm1 = 0;
+        bool next_loaded = false;
+        // A: this thread's row m, every column c (lanes read consecutive j of one U row), then 16-byte
+        // stores of (hi, lo) into the core-matrix rows
         {
             const bool valid = e0 + em < a.count;
-            for (uint32_t c0 = 0; c0 < G.Kp; c0 += 8) {
-                float x[8];
+            for (uint32_t c0 = 0; c0 < G.Kp; c0 += KA) {
+                float x[KA];
 #pragma unroll
-                for (int q = 0; q < 8; q++) {
+                for (uint32_t q = 0; q < KA; q++) {
                     const uint32_t c = c0 + q;
                     x[q] = 0.0f;
                     if (valid && c < n) {
@@ -161,8 +177,16 @@ __global__ void __launch_bounds__(kTcThreads) afm_batched_tc_kernel(BatchArgs a,
                             x[q] = __ldg(U + (size_t)row * a.ld + j);
                     }
                 }
+                if (!next_loaded) {
+                    // the next group's map, in flight with this batch (stored after the conversion)
+                    next_loaded = true;
+                    if (grp + gridDim.x < groups) {
+                        nm0 = map_entry(e_next, t);
+                        nm1 = map_entry(e_next, t + kTcThreads);
+                    }
+                }
 #pragma unroll
-                for (int h4 = 0; h4 < 2; h4++) {
+                for (uint32_t h4 = 0; h4 < KA / 4; h4++) {
                     float4 hi, lo;
                     hi.x = tf32_hi(x[4 * h4]), hi.y = tf32_hi(x[4 * h4 + 1]);
                     hi.z = tf32_hi(x[4 * h4 + 2]), hi.w = tf32_hi(x[4 * h4 + 3]);
@@ -205,6 +229,9 @@ __global__ void __launch_bounds__(kTcThreads) afm_batched_tc_kernel(BatchArgs a,
                 }
             }
         }
+        // the next group's map into the other buffer (the epilogue below reads this group's)
+        if (t < mapw) mp_next[t] = nm0;
+        if (t + kTcThreads < mapw) mp_next[t + kTcThreads] = nm1;
         // generic-proxy stores -> async-proxy reads of the tensor cores
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -289,6 +316,37 @@ void* tc_kernel_for(uint32_t n) {
     }
 }
 
+// Once per kernel and device: the largest dynamic shared memory, the whole
+// carveout for shared memory, and the kernel's registers per thread (host
+// calls kept out of every launch).
+cudaError_t tc_configure(void* fn, int* regs) {
+    struct Entry {
+        void* fn;
+        int device, regs;
+    };
+    static std::mutex mu;
+    static std::vector<Entry> cache;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(mu);
+    for (const Entry& c : cache)
+        if (c.fn == fn && c.device == dev) {
+            *regs = c.regs;
+            return cudaSuccess;
+        }
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBudget);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    if (e != cudaSuccess) return e;
+    cudaFuncAttributes fa;
+    e = cudaFuncGetAttributes(&fa, fn);
+    if (e != cudaSuccess) return e;
+    *regs = fa.numRegs > 0 ? fa.numRegs : 255;
+    cache.push_back({fn, dev, *regs});
+    return cudaSuccess;
+}
+
 bool tc_geom(uint32_t n, uint32_t nrhs, TcGeom* G) {
     if (nrhs != 32 && nrhs != 64 && nrhs != 128) return false;
     if (n <= kTpeMaxN || n > kMaxN) return false;
@@ -304,7 +362,8 @@ bool tc_geom(uint32_t n, uint32_t nrhs, TcGeom* G) {
     G->a_bytes = 128 * G->Kp * 4;
     G->b_bytes = G->N * G->Kp * 4;
     const uint32_t map_words = (G->E * n + 1) & ~1u;
-    G->smem = 2 * G->a_bytes + 2 * G->b_bytes + 4 * map_words + 16;
+    if (G->E * n > 2 * kTcThreads) return false;  // each thread loads at most two map entries
+    G->smem = 2 * G->a_bytes + 2 * G->b_bytes + 8 * map_words + 16;
     G->smem = (G->smem + 127) & ~127u;
     return G->smem <= kSmemBudget;
 }
@@ -323,15 +382,17 @@ cudaError_t launch_batched_tc(const Segment& s, const BatchArgs& a, int sm_count
     TcGeom G;
     if (s.regime != REG_WPE || !tc_geom(s.n, a.nrhs, &G)) return cudaErrorInvalidValue;
     void* fn = tc_kernel_for(s.n);
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G.smem);
+    // resident CTAs per SM from registers, shared memory (the whole carveout) and TMEM: the co-resident
+    // CTAs must fit the SM's 512 TMEM columns, or an allocation would wait for another CTA to finish
+    int regs = 0;
+    cudaError_t e = tc_configure(fn, &regs);
     if (e != cudaSuccess) return e;
-    // the co-resident CTAs must fit the SM's 512 TMEM columns, or an allocation would wait for
-    // another CTA to finish
-    int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)fn, kTcThreads, G.smem);
-    if (e != cudaSuccess) return e;
+    int per_sm = 65536 / (regs * kTcThreads);
+    const int by_smem = (int)((227u * 1024u) / (G.smem + 1024u));  // 1 KB reserved per CTA
     const int by_tmem = (int)(512 / G.cols);  // every resident CTA holds its TMEM columns
+    if (per_sm > by_smem) per_sm = by_smem;
     if (per_sm > by_tmem) per_sm = by_tmem;
+    if (per_sm > 8) per_sm = 8;
     if (per_sm < 1) return cudaErrorInvalidConfiguration;
     const uint32_t groups = (s.count + G.E - 1) / G.E;
     const uint32_t cap = (uint32_t)(sm_count * per_sm);

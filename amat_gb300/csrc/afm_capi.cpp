@@ -216,6 +216,10 @@ void free_device(afm_operator* op) {
     dfree(op, op->d_work32);
     dfree(op, op->d_patch_desc);
     dfree(op, op->d_patch_idx);
+    dfree(op, op->d_pv);
+    dfree(op, op->d_shared_dof);
+    dfree(op, op->d_shared_off);
+    dfree(op, op->d_shared_idx);
     dfree(op, op->d_sym);
     dfree(op, op->d_vx);
     dfree(op, op->d_csr_rp);
@@ -331,7 +335,10 @@ void layout_element(const afm_operator* op, const Segment& s, uint32_t e, uint64
 // patches need more than 64 colours or do not fit the shared memory.
 bool build_patch_plan(afm_operator* op, uint32_t n, int prec, std::vector<PatchDesc>& desc,
                       std::vector<unsigned char>& idx) {
-    const uint32_t P = 128;
+    // patch size: 128 elements, or down to 32 on meshes too small to give every SM several patches
+    uint32_t P = 128;
+    const uint64_t slots = 4ull * (uint64_t)std::max(op->sm_count, 1);
+    while (P > 32 && (uint64_t)op->n_elem < slots * P) P /= 2;
     const uint32_t NE = op->n_elem, ND = op->n_dofs;
     const uint32_t* off = op->offsets.data();
     const uint32_t* map = op->map.data();
@@ -440,9 +447,11 @@ bool build_patch_plan(afm_operator* op, uint32_t n, int prec, std::vector<PatchD
     G = PatchPlanGeom{};
     G.n = n;
     uint64_t units = 0, ib = 0;
+    uint64_t pv = 0;
     for (PatchDesc& d : desc) {
         d.unit0 = (uint32_t)units;
-        d.pad_ = 0;
+        d.pv_off = (uint32_t)pv;
+        pv += d.ndof;
         d.ke_off = units * s.unit_bytes;
         d.idx_off = ib;
         units += d.units;
@@ -452,11 +461,22 @@ bool build_patch_plan(afm_operator* op, uint32_t n, int prec, std::vector<PatchD
         G.max_idx = std::max(G.max_idx, d.idx_bytes);
     }
     if (patch_smem_bytes(prec, G, (uint32_t)s.unit_bytes) == 0) return false;
+    if (pv > 0xffffffffull || ND > kPatchDofMask) return false;
     s.units = (uint32_t)units;
     s.count = (uint32_t)(units * kTpeWidth);
     s.ke_offset = 0;
     s.map_offset = 0;
 
+    // DoFs that more than one patch lists: their patch sums are combined in a
+    // second pass (one-launch mode); the others are written straight to v
+    std::vector<uint32_t> npatch(ND, 0);
+    {
+        std::vector<uint32_t> ld;
+        for (uint32_t x = 0; x < np; x++) {
+            local_dofs(order[x], ld);
+            for (uint32_t g : ld) npatch[g]++;
+        }
+    }
     // element slots and index blocks
     std::vector<uint8_t> is_bc(ND, 0);
     for (uint32_t d : op->bc_unique) is_bc[d] = 1;
@@ -477,7 +497,8 @@ bool build_patch_plan(afm_operator* op, uint32_t n, int prec, std::vector<PatchD
             uint16_t* lmap = reinterpret_cast<uint16_t*>(blk + patch_lmap_off(d.ndof));
             uint16_t* coff = reinterpret_cast<uint16_t*>(blk + patch_csr_off(d.ndof, d.units, n));
             uint16_t* slot = reinterpret_cast<uint16_t*>(blk + patch_slot_off(d.ndof, d.units, n));
-            for (uint32_t k = 0; k < d.ndof; k++) glob[k] = ld[k] | (is_bc[ld[k]] ? kBcFlag : 0u);
+            for (uint32_t k = 0; k < d.ndof; k++)
+                glob[k] = ld[k] | (is_bc[ld[k]] ? kBcFlag : 0u) | (npatch[ld[k]] > 1 ? kSharedFlag : 0u);
             auto loc = [&](uint32_t g) {
                 return (uint32_t)(std::lower_bound(ld.begin(), ld.end(), g) - ld.begin());
             };
@@ -500,6 +521,31 @@ bool build_patch_plan(afm_operator* op, uint32_t n, int prec, std::vector<PatchD
             }
         }
     }
+    // combine lists: per shared DoF (ascending), its entries pv_off + local index in patch order, which
+    // is colour order, so the sums are added in the order of the one-launch-per-colour mode
+    op->pv_count = pv;
+    op->shared_dof.clear();
+    op->shared_off.assign(1, 0);
+    op->shared_idx.clear();
+    {
+        std::vector<uint32_t> first((size_t)ND + 1, 0);
+        for (uint32_t g = 0; g < ND; g++)
+            if (npatch[g] > 1) {
+                op->shared_dof.push_back(g);
+                first[g + 1] = npatch[g];
+            }
+        for (uint32_t g = 0; g < ND; g++) first[g + 1] += first[g];
+        op->shared_idx.assign(first[ND], 0);
+        std::vector<uint32_t> fill(first.begin(), first.end() - 1);
+        std::vector<uint32_t> ld;
+        for (uint32_t x = 0; x < np; x++) {
+            local_dofs(order[x], ld);
+            for (uint32_t k = 0; k < (uint32_t)ld.size(); k++)
+                if (npatch[ld[k]] > 1) op->shared_idx[fill[ld[k]]++] = desc[x].pv_off + k;
+        }
+        for (uint32_t g : op->shared_dof) op->shared_off.push_back(first[g + 1]);
+    }
+    op->n_shared = (uint32_t)op->shared_dof.size();
     op->segs.assign(1, s);
     op->n_patches = np;
     return true;
@@ -771,10 +817,14 @@ int enqueue_matvec(afm_operator* op, void* d_v, const void* d_u, int bc_mode, cu
     bool first = true;
     if (op->use_patches) {
         const Segment& s = op->segs[0];
-        for (size_t c = 0; c + 1 < op->patch_color_first.size(); c++) {
+        // one launch over every patch plus the combine pass, or one launch per patch colour
+        const bool one = op->patch_one_launch;
+        const size_t launches = one ? 1 : op->patch_color_first.size() - 1;
+        for (size_t c = 0; c < launches; c++) {
             PatchArgs a;
-            a.desc = op->d_patch_desc + op->patch_color_first[c];
-            a.count = op->patch_color_first[c + 1] - op->patch_color_first[c];
+            a.desc = op->d_patch_desc + (one ? 0 : op->patch_color_first[c]);
+            a.count = one ? op->n_patches : op->patch_color_first[c + 1] - op->patch_color_first[c];
+            a.pv = one ? (void*)op->d_pv : nullptr;
             a.ke = sym ? op->d_sym : op->d_ke;
             a.idx = op->d_patch_idx;
             a.u = d_u;
@@ -791,6 +841,9 @@ int enqueue_matvec(afm_operator* op, void* d_v, const void* d_u, int bc_mode, cu
             AFM_CUDA(launch_patches(kprec, op->patch_geom, a, op->sm_count, !first, st));
             first = false;
         }
+        if (one)
+            AFM_CUDA(launch_patch_combine((f32 && !symx) ? 4 : 8, d_v, op->d_pv, op->d_shared_dof,
+                                          op->d_shared_off, op->d_shared_idx, op->n_shared, st));
         if (symx) AFM_CUDA(launch_to_f32(d_v32, op->d_vx, op->n_dofs, st));
         return AFM_SUCCESS;
     }
@@ -920,6 +973,7 @@ int batch_tuning(afm_operator* op, void* d_V, const void* d_U, uint32_t nrhs, ui
             g_last_error.clear();
             continue;
         }
+            enqueue_matvec_batched(op, d_V, d_U, nrhs, ld, 0, st, f32, c.first, c.second);  // a second warm-up
         cudaEventRecord(e0, st);
         for (int r = 0; r < 3; r++) enqueue_matvec_batched(op, d_V, d_U, nrhs, ld, 0, st, f32, c.first, c.second);
         cudaEventRecord(e1, st);
@@ -1541,9 +1595,10 @@ int afm_set_precision(afm_operator* op, int p) {
     return ok();
 }
 
-int afm_set_patch_mode(afm_operator* op, int enable) {
+int afm_set_patch_mode(afm_operator* op, int mode) {
     AFM_CHECK_OP(op);
-    op->patch_mode = enable ? 1 : 0;
+    if (mode < 0 || mode > 3) return fail(AFM_ERR_INVALID_ARG, "patch mode %d (0 to 3)", mode);
+    op->patch_mode = mode;
     op->finalized = false;
     return ok();
 }
@@ -1986,6 +2041,26 @@ int afm_finalize(afm_operator* op) {
         AFM_CUDA(cudaMemcpyAsync(op->d_bc_idx, bci.data(), sizeof(uint32_t) * op->n_bc, cudaMemcpyHostToDevice,
                                  op->stream));
         AFM_CUDA(cudaMemcpyAsync(op->d_bc_val, op->values.data(), sizeof(double) * op->n_bc,
+                                 cudaMemcpyHostToDevice, op->stream));
+    }
+    // one launch for every patch colour when the colours are small (a launch per colour would leave
+    // most SMs idle between colours), else one launch per colour
+    op->patch_one_launch = false;
+    if (op->use_patches) {
+        const size_t ncol = std::max<size_t>(op->patch_color_first.size() - 1, 1);
+        const bool small = op->n_patches / ncol < 16ull * (uint64_t)std::max(op->sm_count, 1);
+        op->patch_one_launch = op->patch_mode == 3 || (op->patch_mode == 1 && small);
+    }
+    if (op->patch_one_launch) {
+        AFM_CUDA(dalloc(op, &op->d_pv, sizeof(double) * std::max<size_t>(op->pv_count, 1)));
+        AFM_CUDA(dalloc(op, &op->d_shared_dof, sizeof(uint32_t) * std::max<size_t>(op->shared_dof.size(), 1)));
+        AFM_CUDA(dalloc(op, &op->d_shared_off, sizeof(uint32_t) * op->shared_off.size()));
+        AFM_CUDA(dalloc(op, &op->d_shared_idx, sizeof(uint32_t) * std::max<size_t>(op->shared_idx.size(), 1)));
+        AFM_CUDA(cudaMemcpyAsync(op->d_shared_dof, op->shared_dof.data(), sizeof(uint32_t) * op->shared_dof.size(),
+                                 cudaMemcpyHostToDevice, op->stream));
+        AFM_CUDA(cudaMemcpyAsync(op->d_shared_off, op->shared_off.data(), sizeof(uint32_t) * op->shared_off.size(),
+                                 cudaMemcpyHostToDevice, op->stream));
+        AFM_CUDA(cudaMemcpyAsync(op->d_shared_idx, op->shared_idx.data(), sizeof(uint32_t) * op->shared_idx.size(),
                                  cudaMemcpyHostToDevice, op->stream));
     }
     if (op->use_patches) {
@@ -2537,6 +2612,9 @@ int afm_patch_plan_host_matvec(uint32_t n_elem, uint32_t n_dofs, const uint32_t*
         if (seen[e] != 1) return fail(AFM_ERR_INTERNAL, "element %u in %u slots", e, seen[e]);
     std::fill(v, v + n_dofs, 0.0);
     std::vector<uint32_t> stamp(n_dofs, UINT32_MAX);
+    std::vector<uint32_t> listed(n_dofs, 0);
+    std::vector<uint8_t> shared(n_dofs, 0);
+    for (uint32_t g : op.shared_dof) shared[g] = 1;
     std::vector<double> us, ve;
     const size_t ncol = op.patch_color_first.size() - 1;
     for (size_t c = 0; c < ncol; c++) {
@@ -2554,15 +2632,15 @@ int afm_patch_plan_host_matvec(uint32_t n_elem, uint32_t n_dofs, const uint32_t*
             const uint32_t cap = d.units * 32;
             // patches of one colour share no DoF
             for (uint32_t k = 0; k < d.ndof; k++) {
-                const uint32_t g = glob[k] & kDofMask;
-                if (g >= n_dofs || (k && g <= (glob[k - 1] & kDofMask)))
+                const uint32_t g = glob[k] & kPatchDofMask;
+                if (g >= n_dofs || (k && g <= (glob[k - 1] & kPatchDofMask)))
                     return fail(AFM_ERR_INTERNAL, "patch %u DoF list", x);
                 if (stamp[g] == c) return fail(AFM_ERR_INTERNAL, "colour %zu: DoF %u in two patches", c, g);
                 stamp[g] = (uint32_t)c;
             }
             if (coff[0] != 0 || coff[d.ndof] != d.elems * n) return fail(AFM_ERR_INTERNAL, "patch %u offsets", x);
             us.assign(d.ndof, 0.0);
-            for (uint32_t k = 0; k < d.ndof; k++) us[k] = u[glob[k] & kDofMask];
+            for (uint32_t k = 0; k < d.ndof; k++) us[k] = u[glob[k] & kPatchDofMask];
             ve.assign((size_t)n * cap, -1.0);
             const uint64_t slot0 = d.ke_off / s.unit_bytes * kTpeWidth;
             for (uint32_t un = 0; un < d.units; un++)
@@ -2576,7 +2654,7 @@ int afm_patch_plan_host_matvec(uint32_t n_elem, uint32_t n_dofs, const uint32_t*
                             const uint32_t l = lmap[((size_t)un * n + cc) * 32 + lane];
                             if (l >= d.ndof) return fail(AFM_ERR_INTERNAL, "patch %u local index", x);
                             if (e != kNoElement) {
-                                if ((glob[l] & kDofMask) != map[offsets[e] + cc])
+                                if ((glob[l] & kPatchDofMask) != map[offsets[e] + cc])
                                     return fail(AFM_ERR_INTERNAL, "patch %u element %u column %u", x, e, cc);
                                 acc += ke[(size_t)e * n * n + (size_t)r * n + cc] * us[l];
                             }
@@ -2591,8 +2669,33 @@ int afm_patch_plan_host_matvec(uint32_t n_elem, uint32_t n_dofs, const uint32_t*
                         return fail(AFM_ERR_INTERNAL, "patch %u contribution slot", x);
                     sum += ve[slot[q]];
                 }
-                v[glob[k] & kDofMask] += sum;
+                v[glob[k] & kPatchDofMask] += sum;
+                listed[glob[k] & kPatchDofMask]++;
+                if (((glob[k] & kSharedFlag) != 0) != (shared[glob[k] & kPatchDofMask] != 0))
+                    return fail(AFM_ERR_INTERNAL, "patch %u: shared flag of DoF %u", x, glob[k] & kPatchDofMask);
             }
+        }
+    }
+    // shared flags and combine lists: a DoF is shared iff several patches list it, and its list holds
+    // one entry per listing patch, in patch order, inside the combine buffer
+    for (uint32_t g = 0; g < n_dofs; g++)
+        if ((listed[g] > 1) != (shared[g] != 0)) return fail(AFM_ERR_INTERNAL, "DoF %u shared flag", g);
+    if (op.shared_off.size() != op.shared_dof.size() + 1 || op.shared_off.back() != op.shared_idx.size())
+        return fail(AFM_ERR_INTERNAL, "combine list offsets");
+    for (size_t i = 0; i < op.shared_dof.size(); i++) {
+        const uint32_t g = op.shared_dof[i];
+        if (op.shared_off[i + 1] - op.shared_off[i] != listed[g]) return fail(AFM_ERR_INTERNAL, "DoF %u list", g);
+        for (uint32_t k = op.shared_off[i]; k < op.shared_off[i + 1]; k++) {
+            if (op.shared_idx[k] >= op.pv_count || (k > op.shared_off[i] && op.shared_idx[k] <= op.shared_idx[k - 1]))
+                return fail(AFM_ERR_INTERNAL, "DoF %u list entry %u", g, k);
+            // the entry is the local index of g in the patch whose range holds it
+            const uint32_t e = op.shared_idx[k];
+            const auto it = std::upper_bound(desc.begin(), desc.end(), e,
+                                             [](uint32_t val, const PatchDesc& d) { return val < d.pv_off; });
+            const size_t x = (size_t)(it - desc.begin()) - 1;
+            const uint32_t* glob = reinterpret_cast<const uint32_t*>(idx.data() + desc[x].idx_off);
+            if (e - desc[x].pv_off >= desc[x].ndof || (glob[e - desc[x].pv_off] & kPatchDofMask) != g)
+                return fail(AFM_ERR_INTERNAL, "DoF %u list entry %u points elsewhere", g, k);
         }
     }
     if (n_patches) *n_patches = op.n_patches;
@@ -2629,7 +2732,7 @@ int afm_get_info(afm_operator* op, afm_info* info) {
                                   16 * (uint64_t)op->n_dofs;
         launches += (uint32_t)op->free_color_first.size() - 1;
     } else if (op->use_patches) {
-        launches += (uint32_t)op->patch_color_first.size() - 1;
+        launches += op->patch_one_launch ? 1u + (op->n_shared ? 1u : 0u) : (uint32_t)op->patch_color_first.size() - 1;
     } else {
         for (const Segment& s : op->segs)
             if (s.units) launches++;

@@ -24,6 +24,10 @@ constexpr uint32_t kTpeWidth = 32;
 constexpr uint32_t kMaxN = 96;           // largest element supported (3 rows per lane)
 constexpr uint32_t kBcFlag = 0x80000000u;  // map bit: DoF is constrained
 constexpr uint32_t kDofMask = 0x7fffffffu;
+// Patch index blocks also flag DoFs that more than one patch lists (their sums
+// go through the combine pass), so their DoF ids keep 30 bits.
+constexpr uint32_t kSharedFlag = 0x40000000u;
+constexpr uint32_t kPatchDofMask = 0x3fffffffu;
 
 // Device error flags (bit set in err[0]); err[1..6] record the first failed
 // bounds check (kind, block, thread and three values); kErrWords ints in all.
@@ -120,7 +124,7 @@ struct PatchDesc {
     uint32_t idx_bytes;  // size of the index block (16-byte multiple)
     uint32_t elems;      // elements (the rest of the slots are empty)
     uint32_t unit0;      // first unit of the patch, in units of any arena
-    uint32_t pad_;
+    uint32_t pv_off;     // first entry of the patch's local DoF sums in the combine buffer
 };
 
 // Arguments of one patch-colour launch.
@@ -136,6 +140,8 @@ struct PatchArgs {
     uint32_t plane;           // entries per plane (split arena)
     int bc_mode;
     int* err;
+    void* pv;                 // one launch for every colour: sums of shared DoFs go here (VO), others to v;
+                              // null: one launch per colour, every sum added to v
     const unsigned long long* umax;  // split arithmetic: max|u| (double bits)
     unsigned long long wait_ns;  // limit of each pipeline wait
     const int* probe;         // test hook: a flag nothing sets, or null (afm_set_wait_probe)
@@ -151,6 +157,11 @@ struct PatchPlanGeom {
 
 cudaError_t launch_patches(int prec, const PatchPlanGeom& pg, const PatchArgs& a, int sm_count, bool pdl,
                            cudaStream_t stream);
+// The combine pass of one-launch patches: v[dof[i]] = sum over k in
+// [off[i], off[i+1]) of pv[idx[k]], in order (vo_bytes 8: double, 4: float).
+// Launched with programmatic dependence on the patch launch.
+cudaError_t launch_patch_combine(int vo_bytes, void* v, const void* pv, const uint32_t* dof, const uint32_t* off,
+                                 const uint32_t* idx, uint32_t nb, cudaStream_t st);
 // Shared memory of a patch launch (0 if it does not fit).
 size_t patch_smem_bytes(int prec, const PatchPlanGeom& pg, uint32_t copy_bytes);
 
@@ -211,7 +222,10 @@ struct afm_operator {
     std::vector<uint32_t> offsets;  // n_elem + 1
     std::vector<uint32_t> map;      // global DoF ids
     bool dup_in_element = false;    // some element lists a DoF twice
-    int patch_mode = 1;             // 1: small elements run as patches when eligible; 0: colour segments
+    int patch_mode = 1;             // small elements: patches, 1 one launch + combine pass when the patch colours
+                                    // are small, else one launch per colour; 2 always per colour; 3 always one
+                                    // launch; 0 colour segments
+    bool patch_one_launch = false;  // the choice made at finalize
 
     // boundary conditions
     std::vector<uint64_t> constrained;
@@ -301,6 +315,15 @@ struct afm_operator {
     afm::PatchDesc* d_patch_desc = nullptr;
     unsigned char* d_patch_idx = nullptr;
     size_t patch_idx_bytes = 0;
+    // one-launch patches: local sums of shared DoFs (pv_count entries of 8 bytes) and, per shared DoF,
+    // the list of its entries in patch order
+    size_t pv_count = 0;
+    uint32_t n_shared = 0;
+    std::vector<uint32_t> shared_dof, shared_off, shared_idx;  // host copies (finalize)
+    double* d_pv = nullptr;
+    uint32_t* d_shared_dof = nullptr;
+    uint32_t* d_shared_off = nullptr;
+    uint32_t* d_shared_idx = nullptr;
 
     // batched (multi right-hand side) state
     double* d_bwork = nullptr;

@@ -1,10 +1,15 @@
 // Patch kernel for small elements (n <= kPatchMaxN): v += sum over the patches
-// of one patch colour of P_p^T (sum over the patch's elements of P_e^T Ke P_e) P_p u.
+// of one patch colour of P_p^T (sum over the patch's elements of P_e^T Ke P_e) P_p u;
+// or, in one launch over every patch, the same sums written out: straight to
+// v for a DoF that only this patch lists, to the patch's slice of a combine
+// buffer for a shared DoF (kSharedFlag), which a second pass adds up in patch
+// order (the colour order of the per-colour launches, hence the same bits).
 //
 // A patch is a compact group of up to 128 elements, grown breadth first over
 // shared DoFs when the operator is finalised. Patches of one
 // colour share no DoF. Per patch an index block is stored:
-//   glob[ndof]           sorted global DoF ids (kBcFlag on constrained DoFs)
+//   glob[ndof]           sorted global DoF ids (kBcFlag on constrained DoFs,
+//                        kSharedFlag on DoFs that other patches list too)
 //   lmap[units][n][32]   uint16 local DoF index of column c of element slot
 //   csr_off[ndof + 1]    uint16: contributions of local DoF d are
 //   slot[...]            slot[csr_off[d] .. csr_off[d+1]), each r * cap + e
@@ -166,6 +171,7 @@ __global__ void __launch_bounds__((G * GW + 1) * 32, 1) afm_patch_kernel(PatchAr
     Acc* ve = reinterpret_cast<Acc*>(gbase + L.idx_bytes + L.us_bytes);
     const VT* __restrict__ u = static_cast<const VT*>(a.u);
     VO* __restrict__ v = static_cast<VO*>(a.v);
+    VO* __restrict__ pv = static_cast<VO*>(a.pv);
     const uint64_t keep = l2_evict_last_policy();
     // the scale was written by a launch that completed before this matvec's first launch
     const int usk = load_uscale<A>(a.umax);
@@ -195,7 +201,7 @@ __global__ void __launch_bounds__((G * GW + 1) * 32, 1) afm_patch_kernel(PatchAr
                 for (int q = 0; q < kBatch; q++) {
                     const uint32_t i = i0 + q * kPatchGroupThreads;
                     m[q] = i < d.ndof ? glob[i] : 0u;
-                    x[q] = i < d.ndof ? ld_nc_hint(u + (m[q] & kDofMask), keep) : VT(0);
+                    x[q] = i < d.ndof ? ld_nc_hint(u + (m[q] & kPatchDofMask), keep) : VT(0);
                 }
 #pragma unroll
                 for (int q = 0; q < kBatch; q++) {
@@ -246,7 +252,14 @@ __global__ void __launch_bounds__((G * GW + 1) * 32, 1) afm_patch_kernel(PatchAr
                 Acc sum = A::zero();
                 const uint32_t q1 = coff[i + 1];
                 for (uint32_t c = coff[i]; c < q1; c++) A::combine(sum, ve[slot[c]]);
-                red_add(v + (glob[i] & kDofMask), finish_s<A>(sum, usk));
+                const VO val = finish_s<A>(sum, usk);
+                const uint32_t g = glob[i];
+                if (pv == nullptr)
+                    red_add(v + (g & kPatchDofMask), val);
+                else if (g & kSharedFlag)
+                    pv[d.pv_off + i] = val;  // added to v by the combine pass, in patch order
+                else
+                    v[g & kPatchDofMask] = val;  // the only patch that lists this DoF
             }
         named_barrier(bar_id, kPatchGroupThreads);
         if (t == 0) mbar_arrive(&idx_empty[g]);

@@ -5,7 +5,8 @@
 // host) and load. Requests wait in a FIFO queue and are admitted while the
 // server's HBM budget, the device's free memory and the slot limit allow.
 // Admission finalises the operator on a worker thread (colouring, patch plan,
-// upload of Ke and maps), so the polling thread never blocks on host work.
+// upload of Ke and maps), so the polling thread never blocks on host work, and
+// then drops the operator's host copy of the element matrices.
 // An admitted request keeps all of its state on the device: Ke, maps, b, x
 // and the Krylov vectors of its mixed-precision solve (afm_mixed.hpp). The
 // server's progress thread keeps taking the next step of each request whose
@@ -163,7 +164,14 @@ int admit(afm_server* s) {
         const int dev = s->device;
         r->fin = std::async(std::launch::async, [op, dev]() {
             cudaSetDevice(dev);
-            return afm_finalize(op);
+            const int st = afm_finalize(op);
+            // the device arena holds the element matrices now; the server never finalizes again, so the
+            // host copy goes (large requests would otherwise hold gigabytes of host memory until they end)
+            if (st == AFM_SUCCESS) {
+                std::vector<double>().swap(op->ke);
+                op->ke_dirty = true;
+            }
+            return st;
         });
         s->active.push_back(r);
         finalizing++;

@@ -13,6 +13,7 @@
 #include <stdint.h>
 
 #include "afm_solver.hpp"
+#include "afm_internal.hpp"
 
 namespace afm {
 
@@ -443,6 +444,25 @@ __global__ void __launch_bounds__(kRedThreads) k_umax_cols(const double* __restr
         if (sm[j]) atomicMax(cm + j, sm[j]);
 }
 
+// Combine pass of one-launch patches: v[dof[i]] = the entries of shared DoF
+// i in the combine buffer, summed in patch order (the first entry, then each
+// next one added), one thread per shared DoF. Waits for the patch launch
+// (programmatic dependence) before reading.
+template <typename VO>
+__global__ void __launch_bounds__(kRedThreads) k_patch_combine(VO* __restrict__ v, const VO* __restrict__ pv,
+                                                               const uint32_t* __restrict__ dof,
+                                                               const uint32_t* __restrict__ off,
+                                                               const uint32_t* __restrict__ idx, uint32_t nb) {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nb; i += stride) {
+        const uint32_t k0 = off[i], k1 = off[i + 1];
+        VO s = pv[idx[k0]];
+        for (uint32_t k = k0 + 1; k < k1; k++) s += pv[idx[k]];
+        v[dof[i]] = s;
+    }
+}
+
 inline unsigned grid_for(size_t n) {
     size_t g = (n + kRedThreads - 1) / kRedThreads;
     if (g > 4096) g = 4096;
@@ -522,6 +542,25 @@ cudaError_t launch_to_f32(float* out, const double* in, size_t n, cudaStream_t s
 cudaError_t launch_add_f32(double* x, float* d, size_t n, cudaStream_t st, double inv) {
     k_add_f32<<<grid_for(n), kRedThreads, 0, st>>>(x, d, n, inv);
     return cudaGetLastError();
+}
+
+cudaError_t launch_patch_combine(int vo_bytes, void* v, const void* pv, const uint32_t* dof, const uint32_t* off,
+                                 const uint32_t* idx, uint32_t nb, cudaStream_t st) {
+    if (nb == 0) return cudaSuccess;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid_for(nb));
+    cfg.blockDim = dim3(kRedThreads);
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    if (vo_bytes == 8)
+        return cudaLaunchKernelEx(&cfg, k_patch_combine<double>, static_cast<double*>(v),
+                                  static_cast<const double*>(pv), dof, off, idx, nb);
+    return cudaLaunchKernelEx(&cfg, k_patch_combine<float>, static_cast<float*>(v), static_cast<const float*>(pv),
+                              dof, off, idx, nb);
 }
 
 cudaError_t launch_umax(const double* u, const uint8_t* mask, size_t n, double* vz, size_t nv,

@@ -749,6 +749,7 @@ def run_product(args, w, rank, world, local_rank):
             A.matvec_batched_device(V.data_ptr(), U.data_ptr(), R, f32=f32, stream=stream_ptr)
         e1.record(stream)
         torch.cuda.synchronize()
+        A.synchronize()  # reports any device-side error of the timed products
         ms = e0.elapsed_time(e1) / args.steps
         ke_bytes = info["ke_bytes"] // 2 if f32 else info["ke_bytes"]
         vec_bytes = 3 * m.n_dofs * R * (4 if f32 else 8)

@@ -155,14 +155,21 @@ int afm_set_element_kind(afm_operator* op, int kind, double E, double nu, uint32
 int afm_set_element_coords(afm_operator* op, uint32_t first, uint32_t count, const double* xe);
 /* Arithmetic of the stored Ke; call before afm_finalize. Default AUTO. */
 int afm_set_precision(afm_operator* op, int precision);
-/* Execution of small elements (no counterpart in the reference). enable = 1
- * (default): when every element has the same size n <= 12 and lists no DoF
- * twice, the matvec runs over patches, compact groups of up to 128 elements
- * whose vector entries are staged in shared memory; patches of one colour
- * share no DoF. enable = 0: one launch per element colour, as for larger
- * elements. Both are deterministic and agree within rounding. Takes effect at
- * the next afm_finalize. */
-int afm_set_patch_mode(afm_operator* op, int enable);
+/* Execution of small elements (no counterpart in the reference). When every
+ * element has the same size n <= 12 and lists no DoF twice, the matvec can
+ * run over patches, compact groups of 32 to 128 elements whose vector entries
+ * are staged in shared memory. Patches run either in one launch over every
+ * patch, which writes each DoF sum straight to v when one patch lists the DoF
+ * and to a combine buffer otherwise, followed by a pass that adds the buffered
+ * sums in patch order; or in one launch per patch colour (patches of one
+ * colour share no DoF), each adding its sums to v. Both add every DoF's sums
+ * in the same order, so they give the same bits. mode = 1 (default): one
+ * launch when a patch colour holds fewer than 16 patches per SM, else one
+ * per colour; 2: always one per colour; 3: always one launch; 0: no patches,
+ * one launch per element colour, as for larger elements. All modes are
+ * deterministic and agree within rounding. Takes effect at the next
+ * afm_finalize. */
+int afm_set_patch_mode(afm_operator* op, int mode);
 /* FP32 products of an FP64_SPLIT operator (no counterpart in the reference),
  * which the mixed-precision solves use: when every Ke is symmetric (to 1e-6
  * of its largest diagonal entry; the copy holds the symmetric part) and the

@@ -287,21 +287,26 @@ def _mesh_operator(kind, shape, jitter, prec, patch, bc=True):
 ])
 def test_patch_path_against_oracle(gpu, kind, shape, jitter, prec):
     """Small elements as shared-memory patches: v = K u and MatMult_mf against
-    the oracle, the same products through one launch per colour, and two
-    calls in a row bit for bit."""
+    the oracle; one launch over every patch plus the combine pass (mode 3)
+    gives the same bits as one launch per patch colour (mode 2); element
+    colours (mode 0) agree within rounding; two calls in a row bit for bit."""
     import torch
-    m, ke, dofs, vals, A = _mesh_operator(kind, shape, jitter, prec, 1)
+    m, ke, dofs, vals, A = _mesh_operator(kind, shape, jitter, prec, 3)
     info = A.info()
-    assert info["n_patches"] > 0 and info["n_launches"] == info["n_patch_colors"] + 1
+    assert info["n_patches"] > 0 and info["n_launches"] <= 3
+    _, _, _, _, C = _mesh_operator(kind, shape, jitter, prec, 2)
+    assert C.info()["n_launches"] == C.info()["n_patch_colors"] + 1
     _, _, _, _, B = _mesh_operator(kind, shape, jitter, prec, 0)
     assert B.info()["n_patches"] == 0
     pr = oracle.Problem(m.n_dofs, m.dof_map(), ke, dofs, vals)
     u = np.random.default_rng(3).uniform(-1, 1, m.n_dofs)
-    v, w = np.empty(m.n_dofs), np.empty(m.n_dofs)
+    v, w, x = np.empty(m.n_dofs), np.empty(m.n_dofs), np.empty(m.n_dofs)
     A.matvec(v, u, True)
     B.matvec(w, u, True)
+    C.matvec(x, u, True)
     vo = pr.matvec(u)
     assert rel(v, vo) < FP64_RTOL and rel(w, vo) < FP64_RTOL
+    assert np.array_equal(v, x)
     A.matmult_bc(v, u)
     assert rel(v, pr.matmult_bc(u)) < FP64_RTOL
     du = torch.tensor(u, device="cuda")

@@ -72,6 +72,42 @@ def test_results_alone_and_in_the_mix(gpu):
     srv.close()
 
 
+def test_arrivals_while_others_run(gpu):
+    """Continuous batching: requests submitted while an earlier one is mid-solve are admitted and started
+    before it finishes, run beside it, and every result, the long one's included, equals the one computed
+    alone, bit for bit."""
+    long_case = (P.HEX20_ELASTIC, 12, 7)
+    cases = CASES[:4]
+    srv = Server(0)
+    alone = {}
+    for case in [long_case] + cases:
+        A, b, _ = request(*case)
+        rid = srv.submit(A, b, rtol=RTOL)
+        alone[case] = drain(srv, [rid])[rid][0]
+    pending = [(case, request(*case)) for case in cases]  # built before, submitted while the long one runs
+    A, b, _ = request(*long_case)
+    first = srv.submit(A, b, rtol=RTOL)
+    t0 = time.time()
+    while True:  # until the long request runs (admitted and its solve started)
+        q, a = srv.poll()
+        if q == 0 and a == 1 and time.time() - t0 > 0.02:
+            break
+        assert time.time() - t0 < 60
+    assert srv.take(first) is None, "the long request finished before the others arrived"
+    ids = {}
+    for case, (A, b, _) in pending:
+        ids[srv.submit(A, b, rtol=RTOL)] = case
+        srv.poll()
+    res = drain(srv, [first] + list(ids))
+    t_done_first = res[first][2][3]
+    assert np.array_equal(res[first][0], alone[long_case])
+    for rid, case in ids.items():
+        x, st, t = res[rid]
+        assert np.array_equal(x, alone[case])
+        assert t[2] < t_done_first  # started while the long one was still running
+    srv.close()
+
+
 def test_admission_waits_for_memory(gpu):
     """A budget below any two requests admits one at a time; arrivals wait in
     the queue and every one finishes with the same result as alone."""
