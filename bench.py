@@ -911,9 +911,9 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU time the baseline sample is timed for")
     ap.add_argument("--mode", default="matvec", choices=["matvec", "solve", "batched", "product", "serve",
                                                          "assembled", "free"])
-    ap.add_argument("--rates", default="20,100,500", help="serve: arrival rates (requests/s)")
-    ap.add_argument("--requests", type=int, default=160, help="serve: requests per rate")
-    ap.add_argument("--edge-max", type=int, default=32, help="serve: largest mesh edge")
+    ap.add_argument("--rates", default="10,20,50,100,200,500", help="serve: arrival rates (requests/s)")
+    ap.add_argument("--requests", type=int, default=48, help="serve: requests per rate")
+    ap.add_argument("--edge-max", type=int, default=96, help="serve: largest mesh edge")
     ap.add_argument("--serve-inner", type=float, default=0.3, help="serve: FP32 reduction between FP64 updates")
     ap.add_argument("--nrhs", type=int, default=64)
     ap.add_argument("--single-cols", type=int, default=2, help="columns solved one by one for the FP64 comparison")
