@@ -102,10 +102,11 @@ def build_reference():
     """Compiles the reference CPU path in place (x86 container only)."""
     script = os.path.join(ORACLE_DIR, "build_ref.sh")
     out = os.path.join(ORACLE_DIR, "_ref", "libamat_ref.so")
+    out_simd = os.path.join(ORACLE_DIR, "_ref", "libamat_ref_simd.so")
     ref = os.environ.get("AMAT_REFERENCE", os.path.join(os.path.dirname(ROOT), "reference"))
     if not os.path.isdir(os.path.join(ref, "include")):
         return None
-    if os.path.exists(out):
+    if os.path.exists(out) and os.path.exists(out_simd):
         return out
     subprocess.run(["sh", script], check=True, env=dict(os.environ, REF=ref))
     return out if os.path.exists(out) else None

@@ -13,6 +13,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_LIB = os.path.join(HERE, "_build", "liboracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libamat_ref.so")
+REF_SIMD_LIB = os.path.join(HERE, "_ref", "libamat_ref_simd.so")  # the reference's VECTORIZED_OPENMP build
 
 P = C.c_void_p
 U32 = C.c_uint32
@@ -22,6 +23,7 @@ D = C.c_double
 _ORACLE_SIGS = {
     "oracle_matvec": (None, [U32, U32, P, P, P, P, P]),
     "oracle_matvec_omp": (I, [U32, U32, P, P, P, P, P, P]),
+    "oracle_matvec_omp_cfg": (I, [U32, U32, P, P, P, P, P, P, I, I]),
     "oracle_coloring": (U32, [U32, U32, P, P, P]),
     "oracle_trace": (D, [U32, P, P]),
     "oracle_get_diagonal": (None, [U32, U32, P, P, P, P, U32, I, P]),
@@ -71,9 +73,10 @@ def lib():
     return _bind(ORACLE_LIB, _ORACLE_SIGS)
 
 
-def ref():
-    """The reference compiled in place, or None where it was not built."""
-    return _bind(REF_LIB, _REF_SIGS) if os.path.exists(REF_LIB) else None
+def ref(simd=False):
+    """The reference compiled in place (simd: its VECTORIZED_OPENMP build), or None where it was not built."""
+    path = REF_SIMD_LIB if simd else REF_LIB
+    return _bind(path, _REF_SIGS) if os.path.exists(path) else None
 
 
 def _p(a):
@@ -118,6 +121,25 @@ class Problem:
         v = np.empty(self.n_dofs) if v is None else v
         t = lib().oracle_matvec_omp(self.n_elem, self.n_dofs, _p(self.offsets), _p(self.map), _p(self.ke), None,
                                     _p(u), _p(v))
+        return v, t
+
+    def matvec_omp_cfg(self, u, v=None, threads=0, simd=False):
+        """The OpenMP loop with a thread cap and, with simd, the reference's VECTORIZED_OPENMP element product
+        (column-major Ke, column-by-column axpy under omp simd). Returns (v, threads used)."""
+        u = _f64(u)
+        v = np.empty(self.n_dofs) if v is None else v
+        cm = None
+        if simd:
+            if getattr(self, "_ke_cm", None) is None:
+                parts, k = [], 0
+                for e in range(self.n_elem):
+                    n = int(self.offsets[e + 1] - self.offsets[e])
+                    parts.append(self.ke[k:k + n * n].reshape(n, n).T.reshape(-1))
+                    k += n * n
+                self._ke_cm = np.ascontiguousarray(np.concatenate(parts))
+            cm = self._ke_cm
+        t = lib().oracle_matvec_omp_cfg(self.n_elem, self.n_dofs, _p(self.offsets), _p(self.map), _p(self.ke),
+                                        _p(cm), _p(u), _p(v), int(threads), int(bool(simd)))
         return v, t
 
     def coloring(self):

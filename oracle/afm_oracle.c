@@ -104,6 +104,57 @@ int oracle_matvec_omp(uint32_t n_elem, uint32_t n_dofs, const uint32_t* offsets,
     return threads;
 }
 
+/* The same loop with a thread count (nthreads > 0: at most that many; 0:
+ * the default) and, with simd = 1, the element product of the reference's
+ * VECTORIZED_OPENMP build (include/aMatFree.hpp:1965-1973): the element
+ * matrix stored column-major (the transposed copy that build keeps,
+ * 931-937), v_e accumulated column by column, v_e += u_c * Ke(:, c), with the
+ * row loop under omp simd. ke_cm holds every element matrix column-major
+ * (null unless simd). Returns the threads used. */
+int oracle_matvec_omp_cfg(uint32_t n_elem, uint32_t n_dofs, const uint32_t* offsets, const uint32_t* map,
+                          const double* ke, const double* ke_cm, const double* u, double* v, int nthreads, int simd) {
+    uint64_t* kofs = ke_offsets(n_elem, offsets);
+    int threads = 1;
+    for (uint32_t i = 0; i < n_dofs; i++) v[i] = 0.0;
+#ifdef _OPENMP
+    const int nt = nthreads > 0 ? nthreads : omp_get_max_threads();
+#pragma omp parallel num_threads(nt)
+#endif
+    {
+        double ue[128], ve[128]; /* n <= 128 asserted by the caller */
+#ifdef _OPENMP
+#pragma omp single
+        threads = omp_get_num_threads();
+#endif
+#pragma omp for schedule(static)
+        for (int64_t e = 0; e < (int64_t)n_elem; e++) {
+            const uint32_t n = offsets[e + 1] - offsets[e];
+            const uint32_t* emap = map + offsets[e];
+            if (simd) {
+                const double* kc = ke_cm + kofs[e];
+                for (uint32_t r = 0; r < n; r++) {
+                    ue[r] = u[emap[r]];
+                    ve[r] = 0.0;
+                }
+                for (uint32_t c = 0; c < n; c++) {
+                    const double alpha = ue[c];
+                    const double* x = kc + (size_t)c * n;
+#pragma omp simd
+                    for (uint32_t r = 0; r < n; r++) ve[r] += alpha * x[r];
+                }
+            } else {
+                element_product(n, emap, ke + kofs[e], u, ue, ve);
+            }
+            for (uint32_t r = 0; r < n; r++) {
+#pragma omp atomic
+                v[emap[r]] += ve[r];
+            }
+        }
+    }
+    free(kofs);
+    return threads;
+}
+
 /* Greedy first-fit colouring of the element conflict graph, elements visited
  * in index order: restates meshGraph::mesh2Graph (include/meshGraph.hpp:132-155:
  * two elements are adjacent when they share a DoF) and greedyColoring (59-109:

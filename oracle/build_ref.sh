@@ -21,3 +21,8 @@ $CXX $FLAGS -c "$REF/examples/src/ke_matrix.cpp" -o "$OUT/ke_matrix.o"
 $CXX $FLAGS -c "$HERE/ref_harness.cpp" -o "$OUT/ref_harness.o"
 $CXX -shared -fopenmp "$OUT/ref_harness.o" "$OUT/ke_matrix.o" -o "$OUT/libamat_ref.so"
 echo "build_ref: $OUT/libamat_ref.so"
+# the reference's VECTORIZED_OPENMP build (column-major element matrices, omp simd element product)
+$CXX $FLAGS -DVECTORIZED_OPENMP -c "$REF/examples/src/ke_matrix.cpp" -o "$OUT/ke_matrix_simd.o"
+$CXX $FLAGS -DVECTORIZED_OPENMP -c "$HERE/ref_harness.cpp" -o "$OUT/ref_harness_simd.o"
+$CXX -shared -fopenmp "$OUT/ref_harness_simd.o" "$OUT/ke_matrix_simd.o" -o "$OUT/libamat_ref_simd.so"
+echo "build_ref: $OUT/libamat_ref_simd.so"

@@ -37,6 +37,38 @@ def test_oracle_matvec_matches_reference(name):
 
 
 @pytest.mark.parametrize("name", golden_names())
+def test_oracle_cpu_baseline_variants_match_reference(name):
+    """Both element products the CPU baseline times (the reference's row-major GEMV and its
+    VECTORIZED_OPENMP column-by-column form), on one thread and on every thread."""
+    g = load(name)
+    p = problem(g)
+    for simd in (False, True):
+        for threads in (1, 0):
+            v, used = p.matvec_omp_cfg(g["u"], threads=threads, simd=simd)
+            assert used >= 1 and (threads == 0 or used == threads)
+            assert rel(v, g["matvec"]) < FP64_RTOL
+
+
+def test_reference_vectorized_build_agrees():
+    """The reference's own VECTORIZED_OPENMP build (compiled in place where the reference tree is
+    available) gives the product of its default build."""
+    import ctypes as C
+    R = oracle.ref(simd=True)
+    if R is None:
+        pytest.skip("reference not compiled on this machine")
+    for name in ("hex20_elastic_2", "mixed_random", "hex8_poisson_4"):
+        g = load(name)
+        p = problem(g)
+        h = R.ref_afm_create(p.n_elem, p.n_dofs, C.c_void_p(p.offsets.ctypes.data), C.c_void_p(p.map.ctypes.data),
+                             C.c_void_p(p.ke.ctypes.data), 1, None, None, 0, 0)
+        u = np.ascontiguousarray(g["u"], dtype=np.float64)
+        v = np.empty(p.n_dofs)
+        R.ref_afm_matvec(h, C.c_void_p(v.ctypes.data), C.c_void_p(u.ctypes.data))
+        R.ref_afm_destroy(h)
+        assert rel(v, g["matvec"]) < FP64_RTOL
+
+
+@pytest.mark.parametrize("name", golden_names())
 def test_oracle_bc_matches_reference(name):
     g = load(name)
     p = problem(g)
