@@ -967,13 +967,13 @@ int batch_tuning(afm_operator* op, void* d_V, const void* d_U, uint32_t nrhs, ui
     float best = 1e30f;
     int btr = 4, bng = 2;
     for (auto c : cand) {
-        if (nrhs % (uint32_t)c.first) continue;
+        if (c.first != 0 && nrhs % (uint32_t)c.first) continue;  // a lane tile must divide the columns
         int s = enqueue_matvec_batched(op, d_V, d_U, nrhs, ld, 0, st, f32, c.first, c.second);  // warm-up
         if (s) {
             g_last_error.clear();
             continue;
         }
-            enqueue_matvec_batched(op, d_V, d_U, nrhs, ld, 0, st, f32, c.first, c.second);  // a second warm-up
+        enqueue_matvec_batched(op, d_V, d_U, nrhs, ld, 0, st, f32, c.first, c.second);  // a second warm-up
         cudaEventRecord(e0, st);
         for (int r = 0; r < 3; r++) enqueue_matvec_batched(op, d_V, d_U, nrhs, ld, 0, st, f32, c.first, c.second);
         cudaEventRecord(e1, st);

@@ -197,7 +197,7 @@ int start(afm_server* s, Request* r) {
     r->ms.atol = 0.0;
     r->ms.inner_rtol = r->inner_rtol;
     r->ms.max_outer = 200;
-    r->ms.max_inner = 1000000;
+    r->ms.max_inner = 20000;  // FP32 iterations per segment before the next FP64 update
     r->t_start = now_s();
     return afm::mixed_begin(r->ms);
 }

@@ -632,7 +632,11 @@ def run_solve(args, w, rank, world, local_rank):
     dev = local_rank
     torch.cuda.set_device(dev)
     m, dofs, vals, A = build_bc_problem(w, dev)
-    rhs = A.apply_bc(m.load(ngt=w["ngt"]))
+    if args.load == "random":  # N(0,1) per DoF, the prescribed values on constrained DoFs (the serving mix)
+        rhs = np.random.default_rng(w["seed"]).normal(size=m.n_dofs)
+        rhs[dofs.astype(np.int64)] = vals
+    else:
+        rhs = A.apply_bc(m.load(ngt=w["ngt"]))
     rtol = args.rtol
     M = A
     if args.free:
@@ -656,7 +660,7 @@ def run_solve(args, w, rank, world, local_rank):
            "steps": args.steps, "warmup": 1, "ms_per_step": 1e3 / smx, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32 inner / f64 residual", "data": "synthetic",
            "config": {"workload": w["desc"], "n_dofs": m.n_dofs, "n_elements": m.n_elem, "rtol": rtol,
-                      "inner_rtol": args.inner_rtol},
+                      "inner_rtol": args.inner_rtol, "load": args.load},
            "mixed": r["mixed"], "fp64": r["fp64"], "speedup_vs_fp64": r["speedup_vs_fp64"]}
     if P.KIND_DPN[w["kind"]] == 1:
         out["analytic_rel_error_max"] = poisson_analytic_error(m, xm)
@@ -832,6 +836,8 @@ def run_serve(args, w, rank, world, local_rank):
         x, st = r["A"].solve(r["b"], rtol=args.rtol, atol=0.0, maxit=1000000)
         its += st.iterations
         t_dev += st.seconds
+        log("  plain: %s edge %d, %d DoF: %d FP64 iterations, %.2f s" % (r["kind"], r["edge"], r["n_dofs"],
+                                                                       st.iterations, st.seconds))
         r["A"].close()
     t_plain = time.perf_counter() - t0
     plain = {"solves_per_s": len(reqs) / t_plain, "total_s": t_plain, "finalize_s": t_fin, "solve_device_s": t_dev,
@@ -843,8 +849,12 @@ def run_serve(args, w, rank, world, local_rank):
     t0 = time.perf_counter()
     for r in reqs:
         rid = srv.submit(r["A"], r["b"], rtol=args.rtol, inner_rtol=args.serve_inner)
-        while srv.take(rid) is None:
+        while (res := srv.take(rid)) is None:
             time.sleep(0.0002)
+        _, st, tt = res
+        log("  alone: %s edge %d, %d DoF: %.2f s (solve %.2f s), %d inner iterations, %d updates, status %d" % (
+            r["kind"], r["edge"], r["n_dofs"], tt[3] - tt[0], st.seconds, st.iterations, st.refinements,
+            st.status))
     t_alone = time.perf_counter() - t0
     srv.close()
     alone = {"solves_per_s": len(reqs) / t_alone, "total_s": t_alone}
@@ -937,6 +947,8 @@ def main():
     ap.add_argument("--rtol", type=float, default=1e-8)
     ap.add_argument("--free", type=int, default=0, help="solve: mixed solve on the matrix-free operator (method 2)")
     ap.add_argument("--inner-rtol", type=float, default=1e-2)
+    ap.add_argument("--load", default="example", choices=["example", "random"],
+                    help="solve: the example's load, or N(0,1) per DoF as in the serving mix")
     ap.add_argument("--with-solves", type=int, default=1,
                     help="matvec: also record the config-3 mixed/FP64 solves and the config-2 CG to 1e-10")
     ap.add_argument("--solve-steps", type=int, default=3, help="timed solves of each kind in --with-solves")
