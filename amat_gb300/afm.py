@@ -343,10 +343,12 @@ class aMatFree:
         check(self._lib.afm_set_batch_tuning(self._h, int(nrhs), int(ld), int(bool(f32)), int(cols_per_thread),
                                              int(rows_per_thread)), "afm_set_batch_tuning")
 
-    def batch_tuning(self, nrhs, ld=None, f32=False):
+    def batch_tuning(self, nrhs, ld=None, f32=False, solve=False):
+        """(columns, rows, ms) the autotuner chose; solve=True: the FP32 products of the batched mixed solve."""
         ld = nrhs if ld is None else ld
         tr, ng, ms = C.c_int(), C.c_int(), C.c_float()
-        check(self._lib.afm_get_batch_tuning(self._h, int(nrhs), int(ld), int(bool(f32)), C.byref(tr), C.byref(ng),
+        sel = 2 if solve else int(bool(f32))
+        check(self._lib.afm_get_batch_tuning(self._h, int(nrhs), int(ld), sel, C.byref(tr), C.byref(ng),
                                              C.byref(ms)), "afm_get_batch_tuning")
         return tr.value, ng.value, ms.value
 

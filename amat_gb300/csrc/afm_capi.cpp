@@ -948,10 +948,15 @@ bool batched_tc_all(afm_operator* op, uint32_t nrhs) {
 // The project's autotuner: the first batched call for (nrhs, ld, arithmetic)
 // times every (columns per thread tile, element groups per CTA) candidate on
 // the caller's data, three runs each, and keeps the fastest for the operator.
+// allow_tc = false leaves the tensor-core kernel out: the mixed block CG's
+// FP32 recursion takes the CUDA-core kernels, whose products are IEEE FP32
+// (the 3xTF32 products drop the lo x lo term and accumulate in the tensor
+// pipe; on hex20 elasticity they raised the inner iterations by 58% and cost
+// more time than the faster product saved). Its choice is kept under its own key.
 int batch_tuning(afm_operator* op, void* d_V, const void* d_U, uint32_t nrhs, uint32_t ld, bool f32, cudaStream_t st,
-                 int* tr, int* ng) {
+                 int* tr, int* ng, bool allow_tc = true) {
     const int kprec = f32 ? AFM_PREC_FP32 : op->precision;
-    const uint64_t key = ((uint64_t)nrhs << 40) | ((uint64_t)ld << 8) | (uint64_t)kprec;
+    const uint64_t key = ((uint64_t)nrhs << 40) | ((uint64_t)ld << 8) | (uint64_t)kprec | (allow_tc ? 0u : 0x80u);
     for (const auto& t : op->batch_tune)
         if (t.key == key) {
             *tr = t.tr;
@@ -960,7 +965,7 @@ int batch_tuning(afm_operator* op, void* d_V, const void* d_U, uint32_t nrhs, ui
         }
     // (columns, rows) of the lane tile; (0, 0): the tensor-core kernel (FP32 products)
     std::vector<std::pair<int, int>> cand = {{8, 6}, {8, 4}, {8, 2}, {4, 4}};
-    if (f32 && batched_tc_all(op, nrhs)) cand.insert(cand.begin(), {0, 0});
+    if (f32 && allow_tc && batched_tc_all(op, nrhs)) cand.insert(cand.begin(), {0, 0});
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -2383,8 +2388,10 @@ int afm_matmult_bc_batched_device_f32(afm_operator* op, float* d_V, const float*
 int afm_get_batch_tuning(afm_operator* op, uint32_t nrhs, uint32_t ld, int f32, int* cols_per_thread,
                          int* rows_per_thread, float* ms) {
     AFM_CHECK_OP(op);
+    if (f32 < 0 || f32 > 2) return fail(AFM_ERR_INVALID_ARG, "f32 %d: 0, 1 or 2", f32);
     const int kprec = f32 ? AFM_PREC_FP32 : op->precision;
-    const uint64_t key = ((uint64_t)nrhs << 40) | ((uint64_t)ld << 8) | (uint64_t)kprec;
+    const uint64_t key =
+        ((uint64_t)nrhs << 40) | ((uint64_t)ld << 8) | (uint64_t)kprec | (f32 == 2 ? 0x80u : 0u);
     for (const auto& t : op->batch_tune)
         if (t.key == key) {
             if (cols_per_thread) *cols_per_thread = t.tr;
@@ -2504,7 +2511,7 @@ int afm_solve_cg_batched_mixed_device(afm_operator* op, const double* d_B, doubl
     s = batch_tuning(op, q64, d_X, nrhs, nrhs, false, st, &tr64, &ng64);
     if (s) return s;
     AFM_CUDA(launch_to_f32(b32, d_B, N, st));
-    s = batch_tuning(op, V.q, b32, nrhs, nrhs, true, st, &tr32, &ng32);
+    s = batch_tuning(op, V.q, b32, nrhs, nrhs, true, st, &tr32, &ng32, false);
     if (s) return s;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);

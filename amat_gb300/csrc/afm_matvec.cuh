@@ -688,12 +688,16 @@ struct GroupGeom {
 
 __host__ __device__ inline uint32_t wpg_ubuf_bytes(uint32_t n, uint32_t ut) { return (n * ut + 15) / 16 * 16; }
 
-// Column groups of the warp-group kernel for gr row groups: four warps per
-// element when the products are expensive (8-byte staged u: FP64 and split
-// arithmetic), two for FP32, whose element takes little time to multiply and
-// whose throughput comes from having more elements in flight per SM.
+// Column groups of the warp-group kernel for gr row groups. Elements of two
+// row groups (33..64 DoFs) with 8-byte staged u (FP64 and split arithmetic)
+// take two column groups, so four warps share one element's long products;
+// elements of one row group (<= 32 DoFs) take one warp each: splitting their
+// short rows across warps only adds the cross-warp sum, while more elements in
+// flight per SM hide the gathers (hex8 elasticity, n = 24: 0.31 -> 0.19 ms at
+// 48^3). FP32 takes two column groups for one row group for the same reason
+// in reverse: its products are cheap and its gathers half as wide.
 __host__ __device__ constexpr uint32_t wpg_gc(uint32_t gr, uint32_t ut_bytes) {
-    return gr >= 3 ? 1u : (ut_bytes == 4 ? (gr >= 2 ? 1u : 2u) : 4u / gr);
+    return gr >= 3 ? 1u : (ut_bytes == 4 ? (gr >= 2 ? 1u : 2u) : (gr >= 2 ? 2u : 1u));
 }
 
 // Terms [T0, T1) of row r of a symmetric element in the wrapped-diagonal

@@ -328,14 +328,17 @@ int afm_matmult_bc_batched_device(afm_operator* op, double* d_V, const double* d
 int afm_matmult_bc_batched_device_f32(afm_operator* op, float* d_V, const float* d_U, uint32_t nrhs, uint32_t ld,
                                       void* stream);
 /* The autotuner's choice for (nrhs, ld, f32): columns and rows of the lane
- * tile, and the time of one product in ms. */
+ * tile, and the time of one product in ms. f32 = 0: FP64 (or split) products;
+ * 1: FP32 products; 2: the FP32 products of the batched mixed solve. */
 int afm_get_batch_tuning(afm_operator* op, uint32_t nrhs, uint32_t ld, int f32, int* cols_per_thread,
                          int* rows_per_thread, float* ms);
 /* Pins the lane tile for (nrhs, ld, f32) instead of the autotuner's choice:
  * (columns, rows) one of (8, 2), (8, 4), (8, 6), (4, 4); or (0, 0), the
  * tensor-core kernel (FP32 products, nrhs 32, 64 or 128, elements of 17 to 96
  * DoFs: 3xTF32 products on tcgen05, ~2^-21 of |K||u|), which the autotuner
- * also times when it applies. */
+ * also times when it applies. The batched mixed solve's FP32 recursion tunes
+ * among the CUDA-core tiles only (IEEE FP32 products) and keeps its choice
+ * apart from these. */
 int afm_set_batch_tuning(afm_operator* op, uint32_t nrhs, uint32_t ld, int f32, int cols_per_thread,
                          int rows_per_thread);
 /* Batched Jacobi-PCG: one CG per column (own scalars and stopping test

@@ -89,3 +89,26 @@ def test_tc_agrees_with_cuda_core_kernel(gpu):
         A.synchronize()
         out.append(dV.double().cpu().numpy())
     assert rel(out[0], out[1]) < 2e-6
+
+
+def test_mixed_block_solve_keeps_cuda_core_products(gpu):
+    """The batched mixed solve tunes its FP32 recursion among the CUDA-core tiles only, under its own
+    key: pinning the plain FP32 product to the tensor cores leaves the solve's choice alone."""
+    import torch
+    m, ke, dofs, vals, A = operator(P.HEX8_ELASTIC, 6, True)
+    nrhs = 64
+    A.set_batch_tuning(nrhs, 0, 0, f32=True)
+    B = np.random.default_rng(4).normal(size=(m.n_dofs, nrhs))
+    B[dofs.astype(np.int64), :] = 0.0
+    dB = torch.tensor(B, device="cuda")
+    dX = torch.zeros_like(dB)
+    torch.cuda.synchronize()
+    st = A.solve_batched_device(dB.data_ptr(), dX.data_ptr(), nrhs, rtol=1e-8, mixed=True, inner_rtol=1e-3)
+    assert st.status == 0 and st.rel_residual <= 1e-8
+    assert A.batch_tuning(nrhs, solve=True)[:2] != (0, 0)
+    assert A.batch_tuning(nrhs, f32=True)[:2] == (0, 0)
+    X = dX.cpu().numpy()
+    pr = oracle.Problem(m.n_dofs, m.dof_map(), ke, dofs, np.zeros(len(dofs)))
+    for j in (0, 40):
+        r = B[:, j] - pr.matmult_bc(X[:, j])
+        assert np.linalg.norm(r) <= 1.01e-8 * np.linalg.norm(B[:, j])
