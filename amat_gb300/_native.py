@@ -39,6 +39,13 @@ class AfmSolveStats(C.Structure):
     ]
 
 
+class AfmServerInfo(C.Structure):
+    _fields_ = [
+        ("lane_launches", C.c_uint64), ("lane_solve_launches", C.c_uint64), ("lane_max_batch", C.c_uint32),
+        ("reserved", C.c_uint32), ("lane_requests", C.c_uint64), ("stream_requests", C.c_uint64),
+    ]
+
+
 class AfmMesh(C.Structure):
     _fields_ = [
         ("n_nodes", C.c_uint32), ("n_elem", C.c_uint32), ("nodes_per_elem", C.c_uint32),
@@ -91,6 +98,9 @@ AFM_SIGNATURES = {
     "afm_server_poll": (I, [P, P, P]),
     "afm_server_take": (I, [P, U64, P, P, P, P]),
     "afm_server_destroy": (I, [P]),
+    "afm_server_set_lane": (I, [P, U64, U32]),
+    "afm_get_solve_trace": (I, [P, U32, P, P, P]),
+    "afm_server_get_info": (I, [P, P]),
     "afm_patch_plan_host_matvec": (I, [U32, U32, P, P, P, P, P, P, P]),
     "afm_set_map": (I, [P, U32, P, U32, P, U32, P, U64, U64, U64]),
     "afm_set_bdr_map": (I, [P, P, P, U32]),

@@ -326,6 +326,17 @@ class aMatFree:
             check(s, "afm_solve_cg_mixed")
         return x, st
 
+    def solve_trace(self):
+        """The last mixed-precision solve: [(inner iterations so far, ||b - A x|| / ||b||)] at each FP64
+        residual."""
+        n = C.c_uint32()
+        check(self._lib.afm_get_solve_trace(self._h, 0, None, None, C.byref(n)), "afm_get_solve_trace")
+        it = np.zeros(n.value, dtype=np.int32)
+        res = np.zeros(n.value)
+        check(self._lib.afm_get_solve_trace(self._h, n.value, _ptr(it), _ptr(res), C.byref(n)),
+              "afm_get_solve_trace")
+        return list(zip(it.tolist(), res.tolist()))
+
     def matmult_bc_device_f32(self, v_ptr, u_ptr, stream=None):
         check(self._lib.afm_matmult_bc_device_f32(self._h, C.c_void_p(v_ptr), C.c_void_p(u_ptr),
                                                   C.c_void_p(stream) if stream else None), "afm_matmult_bc_device_f32")

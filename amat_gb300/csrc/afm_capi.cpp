@@ -1372,8 +1372,10 @@ int mixed_begin(MixedSolve& m) {
     if (s) return s;
     s = ensure_work32(op, 7);
     if (s) return s;
-    s = ensure_sym(op, op->stream);  // once per operator, before the timed solve
-    if (s) return s;
+    if (!m.lane) {
+        s = ensure_sym(op, op->stream);  // once per operator, before the timed solve
+        if (s) return s;
+    }
     AFM_CUDA(cudaEventCreateWithFlags(&m.ev, cudaEventDisableTiming));
     AFM_CUDA(cudaEventCreate(&m.e0));
     AFM_CUDA(cudaEventCreate(&m.e1));
@@ -1389,6 +1391,29 @@ int mixed_begin(MixedSolve& m) {
 }
 
 bool mixed_ready(const MixedSolve& m) { return m.ev && cudaEventQuery(m.ev) == cudaSuccess; }
+
+int mixed_lane_record(MixedSolve& m, cudaStream_t lane_stream) {
+    AFM_CUDA(cudaMemcpyAsync(m.op->h_scalars, m.op->d_scalars, sizeof(double) * kScalarSlots,
+                             cudaMemcpyDeviceToHost, lane_stream));
+    AFM_CUDA(cudaEventRecord(m.ev, lane_stream));
+    m.phase = MS_LANEITER;
+    return AFM_SUCCESS;
+}
+
+void mixed_lane_job(const MixedSolve& m, LaneJob& J) {
+    afm_operator* op = m.op;
+    const MixedVectors W = mixed_vectors(op);
+    J.x = W.V.x;
+    J.r = W.V.r;
+    J.z = W.V.z;
+    J.p = W.V.p;
+    J.q = W.V.q;
+    J.dinv = W.V.dinv;
+    J.bcmask = op->d_bcmask;
+    J.sc = op->d_scalars;
+    J.err = op->d_err;
+    J.n_dofs = op->n_dofs;
+}
 
 int mixed_advance(MixedSolve& m) {
     afm_operator* op = m.op;
@@ -1406,6 +1431,8 @@ int mixed_advance(MixedSolve& m) {
             return mixed_residual(m);
         case MS_RESID: {
             m.rn = std::sqrt(h[S_PQ]);
+            m.trace_iters.push_back(m.inner_total);
+            m.trace_res.push_back(m.bn > 0 ? m.rn / m.bn : m.rn);
             if (std::isnan(m.rn)) return mixed_finish(m, AFM_ERR_BREAKDOWN);
             if (m.rn <= m.tol) return mixed_finish(m, AFM_SUCCESS);
             if (!ir_progress(m.rn, &m.best, &m.stall) || m.outer >= m.max_outer)
@@ -1438,6 +1465,11 @@ int mixed_advance(MixedSolve& m) {
             h[S_NORM] = 0.0;
             AFM_CUDA(cudaMemcpyAsync(sc + S_DONE, h + S_DONE, sizeof(double) * (S_NORM - S_DONE + 1),
                                      cudaMemcpyHostToDevice, st));
+            if (m.lane) {  // the iterations join the next lane launch
+                AFM_CUDA(cudaEventRecord(m.ev, st));
+                m.phase = MS_LANE;
+                return AFM_SUCCESS;
+            }
             int s = ensure_cg_graph<float>(op, op->cg32, W.V);
             if (s) return s;
             AFM_CUDA(cudaGraphLaunch(op->cg32.exec, st));
@@ -1445,6 +1477,14 @@ int mixed_advance(MixedSolve& m) {
             m.phase = MS_ITER;
             return AFM_SUCCESS;
         }
+        case MS_LANEITER:
+            // the solve's stream continues after the lane launch
+            AFM_CUDA(cudaStreamWaitEvent(st, m.ev, 0));
+            if (h[S_DONE] == 0.0) {
+                m.phase = MS_LANE;
+                return AFM_SUCCESS;
+            }
+            [[fallthrough]];
         case MS_ITER: {
             if (h[S_DONE] == 0.0) {
                 AFM_CUDA(cudaGraphLaunch(op->cg32.exec, st));
@@ -1472,6 +1512,10 @@ int mixed_end(MixedSolve& m, afm_solve_stats* stats) {
     if (m.e0) cudaEventDestroy(m.e0);
     if (m.e1) cudaEventDestroy(m.e1);
     m.ev = m.e0 = m.e1 = nullptr;
+    if (m.op) {
+        m.op->trace_iters = m.trace_iters;
+        m.op->trace_res = m.trace_res;
+    }
     if (s) return s;
     if (m.phase != MS_DONE) return fail(AFM_ERR_STATE, "mixed solve not finished");
     if (stats) {
@@ -2338,6 +2382,18 @@ int afm_solve_cg_mixed_device(afm_operator* op, const double* d_b, double* d_x, 
     }
     const int st = mixed_end(m, stats);
     return s != AFM_SUCCESS ? s : st;
+}
+
+int afm_get_solve_trace(afm_operator* op, uint32_t cap, int* inner_iterations, double* rel_residual, uint32_t* n) {
+    AFM_CHECK_OP(op);
+    if (!n || (cap && (!inner_iterations || !rel_residual))) return fail(AFM_ERR_INVALID_ARG, "null argument");
+    *n = (uint32_t)op->trace_iters.size();
+    const uint32_t k = std::min<uint32_t>(cap, *n);
+    for (uint32_t i = 0; i < k; i++) {
+        inner_iterations[i] = op->trace_iters[i];
+        rel_residual[i] = op->trace_res[i];
+    }
+    return ok();
 }
 
 int afm_solve_cg_mixed(afm_operator* op, const double* b, double* x, double rtol, double atol, int max_outer,

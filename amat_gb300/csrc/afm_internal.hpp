@@ -199,6 +199,41 @@ cudaError_t launch_segment(const Segment& s, int prec, const SegArgs& a, int sm_
 // Dynamic shared memory the launch of segment s uses (for reporting).
 size_t segment_smem_bytes(const Segment& s, int prec);
 
+// ---- serving lane (afm_lane.cu) ---------------------------------------------
+// One launch advances the FP32 CG recursion of many served solves at once:
+// every request is one thread-block cluster of kLaneCtas CTAs that runs whole
+// CG iterations (colour-ordered FP32 products on the hi plane of the split
+// arena, dot products, vector updates) with cluster barriers between phases.
+constexpr uint32_t kLaneCtas = 8;
+constexpr uint32_t kLaneThreads = 512;
+
+// One colour-size segment of a request, as the lane reads it.
+struct LaneSeg {
+    const float* ke;        // hi plane of the segment's first unit
+    const uint32_t* map;    // the segment's map (kBcFlag on constrained DoFs)
+    uint64_t unit_floats;   // floats from one unit to the next
+    uint32_t n, regime, units, count;
+    uint32_t sync_after;    // 1: the last segment of its colour (a cluster barrier follows)
+    uint32_t pad;
+};
+
+// One request's FP32 recursion: the vectors of its solve (float, n_dofs) and
+// its solver scalars on the device.
+struct LaneJob {
+    float *x, *r, *z, *p, *q;
+    const float* dinv;
+    const uint8_t* bcmask;  // 1 on constrained DoFs (q = p there), or null
+    const LaneSeg* segs;
+    double* sc;
+    int* err;
+    uint32_t n_dofs, n_segs;
+};
+
+// Runs at most iters CG iterations of each of the n_jobs requests (a request
+// whose S_DONE is set does nothing), then writes every request's scalars to
+// its sc.
+cudaError_t launch_lane(const LaneJob* d_jobs, uint32_t n_jobs, uint32_t iters, cudaStream_t st);
+
 // Records the calling thread's last error message (returned by
 // afm_last_error) and returns status.
 int set_error(int status, const char* fmt, ...);
@@ -260,6 +295,8 @@ struct afm_operator {
     bool wait_probe = false;         // afm_set_wait_probe
     unsigned long long* d_usc = nullptr;  // u-scale words of the split products (kUscWords, afm_solver.hpp)
     uint8_t* d_bcmask = nullptr;     // 1 per constrained DoF (null without constraints)
+    std::vector<int> trace_iters;    // the last mixed solve: inner iterations at each FP64 residual
+    std::vector<double> trace_res;   // ... and that residual over ||b||
     double* d_work = nullptr;        // host-API staging and solver vectors
     size_t work_elems = 0;
     double* d_scalars = nullptr;     // solver scalars / reduction partials

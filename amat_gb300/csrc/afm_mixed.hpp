@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <vector>
 
 #include "afm_internal.hpp"
 
@@ -21,7 +22,9 @@ enum MixedPhase : int {
     MS_RESID,     // FP64 true residual in flight
     MS_SEGSTART,  // start of an FP32 segment (init or reliable update) in flight
     MS_ITER,      // a captured batch of FP32 iterations in flight
-    MS_DONE
+    MS_DONE,
+    MS_LANE,      // serving lane: FP32 iterations wait for the next lane launch (afm_lane.cu)
+    MS_LANEITER   // serving lane: a lane launch with this solve's iterations in flight
 };
 
 struct MixedSolve {
@@ -38,16 +41,28 @@ struct MixedSolve {
     // ||sigma r|| in [0.5, 1)), so that tiny or huge loads stay in FP32's range
     double sigma = 1.0;
     bool fresh = true;
+    // the FP32 iterations run in the serving lane: the owner of the solve
+    // launches them (launch_lane) for every solve in MS_LANE, records ev on the
+    // lane's stream and sets MS_LANEITER; no symmetric inner arena is built
+    bool lane = false;
     cudaEvent_t ev = nullptr, e0 = nullptr, e1 = nullptr;
+    // each FP64 residual of the solve: inner iterations so far and ||r|| / ||b||
+    std::vector<int> trace_iters;
+    std::vector<double> trace_res;
 };
 
 // Checks the arguments, allocates the work vectors and enqueues the set-up.
 int mixed_begin(MixedSolve& m);
 // True when the work enqueued by the last step has completed.
 bool mixed_ready(const MixedSolve& m);
-// Takes the next step (call only when mixed_ready): reads the scalars of the
-// finished work and enqueues the next, or moves to MS_DONE.
+// Takes the next step (call only when mixed_ready and not in MS_LANE): reads
+// the scalars of the finished work and enqueues the next, or moves to MS_DONE.
 int mixed_advance(MixedSolve& m);
+// The FP32 vectors, scalars and error flags of the solve, as a lane job (the
+// caller fills segs and n_segs). After the launch, the caller copies the
+// device scalars to the host mirror (mixed_lane_record) on the lane's stream.
+void mixed_lane_job(const MixedSolve& m, LaneJob& J);
+int mixed_lane_record(MixedSolve& m, cudaStream_t lane_stream);
 // Fills stats (device time between begin and done), releases the events and
 // returns the solve's status.
 int mixed_end(MixedSolve& m, afm_solve_stats* stats);

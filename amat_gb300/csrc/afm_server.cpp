@@ -17,9 +17,17 @@
 // batching). A finished request copies x back asynchronously, releases its
 // device memory at once, and waits for afm_server_take.
 //
+// Small requests (FP32 element matrices up to lane_max_bytes) run their FP32
+// iterations in the serving lane instead (afm_lane.cu): whenever no lane
+// launch is in flight, the progress thread gathers every solve waiting for
+// FP32 iterations into one launch, one thread-block cluster per solve, that
+// runs up to lane_iters iterations of each of them. Requests admitted while a
+// launch runs join the next one, so the lane batches the matvecs of all active
+// small solves without waiting for any of them to finish.
+//
 // Each request's arithmetic is independent of the others (own operator, own
-// vectors, deterministic kernels), so its result is the same alone and in
-// any mix, bit for bit.
+// vectors, deterministic kernels, a lane cluster per request), so its result
+// is the same alone and in any mix, bit for bit.
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string.h>
@@ -53,6 +61,9 @@ struct Request {
     std::vector<double> x;   // result on the host
     cudaEvent_t copied = nullptr;
     afm::MixedSolve ms;
+    bool lane_candidate = false;         // small enough for the serving lane (decided at admission)
+    afm::LaneSeg* d_lane_segs = nullptr; // the lane's view of the operator's segments
+    uint32_t lane_nsegs = 0;
     afm_solve_stats stats{};
     int status = AFM_SUCCESS;
     std::string message;
@@ -78,6 +89,22 @@ uint64_t estimate_bytes(const afm_operator* op) {
     return (ke + vec) * 11 / 10 + (1u << 20);
 }
 
+// Bytes of FP32 element matrices the lane streams per product (hi plane).
+uint64_t lane_bytes(const afm_operator* op) {
+    uint64_t b = 0;
+    for (uint32_t e = 0; e < op->n_elem; e++) {
+        const uint64_t n = op->offsets[e + 1] - op->offsets[e];
+        b += n * n * 4;
+    }
+    return b;
+}
+
+// Lane defaults: requests whose FP32 element matrices are at most 8 MB (a
+// cluster of kLaneCtas SMs streams them in tens of microseconds, below the
+// launch overheads of a per-request iteration), 32 iterations per launch.
+constexpr uint64_t kLaneMaxBytes = 8ull << 20;
+constexpr uint32_t kLaneIters = 32;
+
 }  // namespace
 
 struct afm_server {
@@ -101,6 +128,16 @@ struct afm_server {
     std::thread progress;
     std::mutex state_mu;
     std::atomic<bool> running{false};
+    // serving lane: one launch in flight at most, its job table in pinned
+    // memory (rewritten only once the launch that read it has finished)
+    uint64_t lane_max_bytes = kLaneMaxBytes;
+    uint32_t lane_iters = kLaneIters;
+    cudaStream_t lane_stream = nullptr;
+    cudaEvent_t lane_done = nullptr;
+    bool lane_busy = false;
+    afm::LaneJob* h_jobs = nullptr;
+    afm::LaneJob* d_jobs = nullptr;
+    afm_server_info info{};
 };
 
 namespace {
@@ -108,6 +145,8 @@ namespace {
 void release_device(afm_server* s, Request* r) {
     if (r->d_bx && r->op) cudaFreeAsync(r->d_bx, r->op->stream);
     r->d_bx = nullptr;
+    if (r->d_lane_segs && r->op) cudaFreeAsync(r->d_lane_segs, r->op->stream);
+    r->d_lane_segs = nullptr;
     if (r->copied) cudaEventDestroy(r->copied);
     r->copied = nullptr;
     if (r->op) {
@@ -161,6 +200,9 @@ int admit(afm_server* s) {
         r->state = RQ_ADMITTING;
         r->t_admit = now_s();
         afm_operator* op = r->op;
+        // lane requests run colour segments (the lane reads their units), never patches
+        r->lane_candidate = s->lane_max_bytes > 0 && op->matfree_type != 2 && lane_bytes(op) <= s->lane_max_bytes;
+        if (r->lane_candidate) afm_set_patch_mode(op, 0);
         const int dev = s->device;
         r->fin = std::async(std::launch::async, [op, dev]() {
             cudaSetDevice(dev);
@@ -180,10 +222,49 @@ int admit(afm_server* s) {
     return admitted;
 }
 
+// The lane's segment table of a finalised operator (FP64_SPLIT arena in
+// colour segments), uploaded on the operator's stream.
+int build_lane_segs(Request* r) {
+    afm_operator* op = r->op;
+    std::vector<afm::LaneSeg> segs;
+    std::vector<uint32_t> colors;
+    for (const afm::Segment& g : op->segs) {
+        if (g.units == 0) continue;
+        afm::LaneSeg L{};
+        L.ke = reinterpret_cast<const float*>(op->d_ke + g.ke_offset);  // hi plane first in every unit
+        L.map = op->d_map + g.map_offset;
+        L.unit_floats = g.unit_bytes / 4;
+        L.n = g.n;
+        L.regime = (uint32_t)g.regime;
+        L.units = g.units;
+        L.count = g.count;
+        segs.push_back(L);
+        colors.push_back(g.color);
+    }
+    // segments are colour-sorted: a cluster barrier after the last segment of each colour
+    for (size_t k = 0; k < segs.size(); k++)
+        segs[k].sync_after = (k + 1 == segs.size() || colors[k + 1] != colors[k]) ? 1u : 0u;
+    r->lane_nsegs = (uint32_t)segs.size();
+    if (segs.empty()) return AFM_SUCCESS;
+    if (cudaMallocAsync((void**)&r->d_lane_segs, sizeof(afm::LaneSeg) * segs.size(), op->stream) != cudaSuccess)
+        return AFM_ERR_OOM;
+    if (cudaMemcpyAsync(r->d_lane_segs, segs.data(), sizeof(afm::LaneSeg) * segs.size(), cudaMemcpyHostToDevice,
+                        op->stream) != cudaSuccess ||
+        cudaStreamSynchronize(op->stream) != cudaSuccess)  // segs is a local vector
+        return AFM_ERR_CUDA;
+    return AFM_SUCCESS;
+}
+
 int start(afm_server* s, Request* r) {
     (void)s;
     afm_operator* op = r->op;
     const size_t n = op->n_dofs;
+    const bool lane = r->lane_candidate && op->precision == AFM_PREC_FP64_SPLIT && !op->use_patches &&
+                      op->matfree_type != 2;
+    if (lane) {
+        const int st = build_lane_segs(r);
+        if (st != AFM_SUCCESS) return st;
+    }
     if (cudaMallocAsync((void**)&r->d_bx, 2 * n * sizeof(double), op->stream) != cudaSuccess) return AFM_ERR_OOM;
     if (cudaEventCreateWithFlags(&r->copied, cudaEventDisableTiming) != cudaSuccess) return AFM_ERR_CUDA;
     if (cudaMemcpyAsync(r->d_bx, r->b.data(), n * sizeof(double), cudaMemcpyHostToDevice, op->stream) != cudaSuccess ||
@@ -198,8 +279,60 @@ int start(afm_server* s, Request* r) {
     r->ms.inner_rtol = r->inner_rtol;
     r->ms.max_outer = 200;
     r->ms.max_inner = 20000;  // FP32 iterations per segment before the next FP64 update
+    r->ms.lane = lane;
     r->t_start = now_s();
+    if (lane) s->info.lane_requests++;
+    else s->info.stream_requests++;
     return afm::mixed_begin(r->ms);
+}
+
+// Launches the FP32 iterations of every solve waiting for the lane (at most
+// one launch in flight). Returns the number of solves launched.
+int launch_lane_batch(afm_server* s) {
+    if (s->lane_busy) {
+        if (cudaEventQuery(s->lane_done) != cudaSuccess) return 0;
+        s->lane_busy = false;
+    }
+    std::vector<Request*> batch;
+    for (Request* r : s->active)
+        if (r->state == RQ_RUNNING && r->ms.phase == afm::MS_LANE && afm::mixed_ready(r->ms) &&
+            batch.size() < s->max_active)
+            batch.push_back(r);
+    if (batch.empty()) return 0;
+    for (size_t i = 0; i < batch.size(); i++) {
+        Request* r = batch[i];
+        afm::LaneJob& J = s->h_jobs[i];
+        afm::mixed_lane_job(r->ms, J);
+        J.segs = r->d_lane_segs;
+        J.n_segs = r->lane_nsegs;
+        cudaStreamWaitEvent(s->lane_stream, r->ms.ev, 0);
+    }
+    cudaError_t e = cudaMemcpyAsync(s->d_jobs, s->h_jobs, sizeof(afm::LaneJob) * batch.size(),
+                                    cudaMemcpyHostToDevice, s->lane_stream);
+    if (e == cudaSuccess) e = afm::launch_lane(s->d_jobs, (uint32_t)batch.size(), s->lane_iters, s->lane_stream);
+    int st = e == cudaSuccess ? AFM_SUCCESS : AFM_ERR_CUDA;
+    for (Request* r : batch) {  // scalars to each solve's host mirror, then its event
+        if (st == AFM_SUCCESS) st = afm::mixed_lane_record(r->ms, s->lane_stream);
+        r->ms.phase = afm::MS_LANEITER;
+    }
+    if (st == AFM_SUCCESS) e = cudaEventRecord(s->lane_done, s->lane_stream);
+    if (st != AFM_SUCCESS || e != cudaSuccess) {
+        if (e == cudaSuccess) e = cudaGetLastError();
+        for (Request* r : batch) {
+            afm::mixed_end(r->ms, nullptr);
+            finish(s, r, AFM_ERR_CUDA, cudaGetErrorString(e));
+        }
+        std::vector<Request*> still;
+        for (Request* r : s->active)
+            if (r->state != RQ_DONE) still.push_back(r);
+        s->active.swap(still);
+        return (int)batch.size();
+    }
+    s->lane_busy = true;
+    s->info.lane_launches++;
+    s->info.lane_solve_launches += batch.size();
+    s->info.lane_max_batch = std::max<uint32_t>(s->info.lane_max_batch, (uint32_t)batch.size());
+    return (int)batch.size();
 }
 
 }  // namespace
@@ -232,7 +365,8 @@ int step(afm_server* s) {
         }
         if (r->state == RQ_RUNNING) {
             int st = AFM_SUCCESS;
-            while (st == AFM_SUCCESS && r->ms.phase != afm::MS_DONE && afm::mixed_ready(r->ms)) {
+            while (st == AFM_SUCCESS && r->ms.phase != afm::MS_DONE && r->ms.phase != afm::MS_LANE &&
+                   afm::mixed_ready(r->ms)) {
                 st = afm::mixed_advance(r->ms);
                 changes++;
             }
@@ -258,6 +392,7 @@ int step(afm_server* s) {
         still.push_back(r);
     }
     s->active.swap(still);
+    changes += launch_lane_batch(s);
     changes += admit(s);
     return changes;
 }
@@ -293,6 +428,17 @@ int afm_server_create(afm_server** out, int device, uint64_t hbm_budget_bytes, u
     s->budget = hbm_budget_bytes ? hbm_budget_bytes : (uint64_t)(free_b * 0.85);
     s->reserve = std::min<uint64_t>(total_b / 50, 2ull << 30);
     s->max_active = max_active ? max_active : 64;
+    if (cudaStreamCreateWithFlags(&s->lane_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&s->lane_done, cudaEventDisableTiming) != cudaSuccess ||
+        cudaMallocHost((void**)&s->h_jobs, sizeof(afm::LaneJob) * s->max_active) != cudaSuccess ||
+        cudaMalloc((void**)&s->d_jobs, sizeof(afm::LaneJob) * s->max_active) != cudaSuccess) {
+        if (s->d_jobs) cudaFree(s->d_jobs);
+        if (s->h_jobs) cudaFreeHost(s->h_jobs);
+        if (s->lane_done) cudaEventDestroy(s->lane_done);
+        if (s->lane_stream) cudaStreamDestroy(s->lane_stream);
+        delete s;
+        return afm::set_error(AFM_ERR_CUDA, "serving lane resources");
+    }
     s->reaper = std::thread(reap, s);
     s->running = true;
     s->progress = std::thread(run_progress, s);
@@ -375,8 +521,29 @@ int afm_server_destroy(afm_server* s) {
         s->cv.notify_one();
     }
     s->reaper.join();
+    cudaFree(s->d_jobs);
+    cudaFreeHost(s->h_jobs);
+    cudaEventDestroy(s->lane_done);
+    cudaStreamDestroy(s->lane_stream);
     delete s;
     return AFM_SUCCESS;
+}
+
+int afm_server_set_lane(afm_server* s, uint64_t max_ke_bytes, uint32_t iters_per_launch) {
+    if (!s) return afm::set_error(AFM_ERR_INVALID_ARG, "null server");
+    if (iters_per_launch == 0 || iters_per_launch > 4096)
+        return afm::set_error(AFM_ERR_INVALID_ARG, "iters_per_launch %u (1 to 4096)", iters_per_launch);
+    std::lock_guard<std::mutex> lk(s->state_mu);
+    s->lane_max_bytes = max_ke_bytes;
+    s->lane_iters = iters_per_launch;
+    return afm::set_error(AFM_SUCCESS, "");
+}
+
+int afm_server_get_info(afm_server* s, afm_server_info* info) {
+    if (!s || !info) return afm::set_error(AFM_ERR_INVALID_ARG, "null argument");
+    std::lock_guard<std::mutex> lk(s->state_mu);
+    *info = s->info;
+    return afm::set_error(AFM_SUCCESS, "");
 }
 
 }  // extern "C"

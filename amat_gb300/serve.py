@@ -1,11 +1,13 @@
 """Serving loop for many CG solves on different operators (afm_server_* in
 include/afm.h): FIFO admission by HBM budget, device-resident state, every
-admitted request advanced on its own stream by the server's progress thread."""
+admitted request advanced by the server's progress thread, on its own stream or,
+for small requests, in the serving lane (one launch for the FP32 iterations of
+all of them)."""
 import ctypes as C
 
 import numpy as np
 
-from ._native import AfmSolveStats, check, libafm
+from ._native import AfmServerInfo, AfmSolveStats, check, libafm
 
 
 class Server:
@@ -29,6 +31,18 @@ class Server:
         A._h = None  # owned by the server now
         self._n[rid.value] = len(bb)
         return rid.value
+
+    def set_lane(self, max_ke_bytes=8 << 20, iters_per_launch=32):
+        """Requests whose FP32 element matrices take at most max_ke_bytes run their FP32 iterations in the
+        serving lane (0: off), at most iters_per_launch iterations per launch."""
+        check(self._lib.afm_server_set_lane(self._h, int(max_ke_bytes), int(iters_per_launch)),
+              "afm_server_set_lane")
+
+    def info(self):
+        """Counters of the serving lane: launches, requests carried, largest batch, requests per path."""
+        i = AfmServerInfo()
+        check(self._lib.afm_server_get_info(self._h, C.byref(i)), "afm_server_get_info")
+        return {k: getattr(i, k) for k, _ in AfmServerInfo._fields_ if k != "reserved"}
 
     def poll(self):
         """One more round of progress without blocking; returns (queued, admitted)."""

@@ -683,6 +683,8 @@ def run_solve(args, w, rank, world, local_rank):
         M.finalize()
     r, xm, _ = solve_compare(A, m, rhs, rtol, args.steps, args.inner_rtol, M, torch.cuda.nvtx)
     smx = r["mixed"]["solves_per_s"]
+    # inner iterations so far and ||b - A x|| / ||b|| at each FP64 residual of the last mixed solve
+    r["mixed"]["trace"] = [[i, float("%.3e" % v)] for i, v in M.solve_trace()]
     r["mixed"]["inner_ke_bytes"] = 0 if args.free else A.info()["sym_bytes"] or A.info()["ke_bytes"] // 2
     r["mixed"]["inner_arena"] = ("matrix-free (method 2): Ke integrated from coordinates" if args.free else
                                  {0: "hi plane", 1: "symmetric copy, FP32",
@@ -846,6 +848,13 @@ def serve_requests(args, seed):
     return reqs
 
 
+def new_server(dev, args):
+    from amat_gb300.serve import Server
+    srv = Server(dev)
+    srv.set_lane(int(args.lane_mb * 2 ** 20), 32)
+    return srv
+
+
 def run_serve(args, w, rank, world, local_rank):
     """Served CG solves: Poisson arrivals at each rate, admission by HBM, mixed-precision solves to rtol,
     p50/p99 latency (arrival to result) beside solves/s; against the plain path (finalize + FP64 CG, one
@@ -876,7 +885,7 @@ def run_serve(args, w, rank, world, local_rank):
     log("plain: %d solves in %.2f s" % (len(reqs), t_plain))
     # the same requests one at a time through the server (mixed precision, no overlap)
     reqs = serve_requests(args, seed)
-    srv = Server(dev)
+    srv = new_server(dev, args)
     t0 = time.perf_counter()
     for r in reqs:
         rid = srv.submit(r["A"], r["b"], rtol=args.rtol, inner_rtol=args.serve_inner)
@@ -896,7 +905,7 @@ def run_serve(args, w, rank, world, local_rank):
         for rate in rates:
             reqs = serve_requests(args, seed)
             arr = np.cumsum(np.random.default_rng(seed + int(rate)).exponential(1.0 / rate, len(reqs)))
-            srv = Server(dev)
+            srv = new_server(dev, args)
             ids, lat, res, brk = {}, [], [], []
             k = 0
             t0 = time.monotonic()
@@ -921,6 +930,7 @@ def run_serve(args, w, rank, world, local_rank):
                 if not got:  # the server's progress thread does the work; wait a little
                     nxt = arr[k] - (time.monotonic() - t0) if k < len(reqs) else 0.0005
                     time.sleep(max(0.0, min(nxt, 0.0005)))
+            lane = srv.info()
             srv.close()
             span = last - (t0 + arr[0])
             lat = np.array(lat)
@@ -930,7 +940,8 @@ def run_serve(args, w, rank, world, local_rank):
                           "median_ms": {"queued": 1e3 * float(np.median(brk[:, 0])),
                                         "finalize": 1e3 * float(np.median(brk[:, 1])),
                                         "solve_wall": 1e3 * float(np.median(brk[:, 2])),
-                                        "solve_device": 1e3 * float(np.median(brk[:, 3]))}})
+                                        "solve_device": 1e3 * float(np.median(brk[:, 3]))},
+                          "lane": lane})
             log("rate %g: %.2f solves/s, p50 %.1f ms, p99 %.1f ms" % (rate, lines[-1]["solves_per_s"],
                                                                      lines[-1]["p50_ms"], lines[-1]["p99_ms"]))
     best = max(lines, key=lambda d: d["solves_per_s"])
@@ -943,7 +954,8 @@ def run_serve(args, w, rank, world, local_rank):
                                   "jitter 0.1h, loads N(0,1)" % (args.requests, [k[1] for k in SERVE_KINDS],
                                                                   args.edge_max),
                       "n_dofs_range": [int(min(sizes)), int(max(sizes))], "rtol": args.rtol,
-                      "inner_rtol": args.serve_inner, "admission": "FIFO by HBM budget (85% of free), 64 slots"},
+                      "inner_rtol": args.serve_inner, "admission": "FIFO by HBM budget (85% of free), 64 slots",
+                      "lane_mb": args.lane_mb},
            "rates": lines, "p50_ms": best["p50_ms"], "p99_ms": best["p99_ms"], "plain_fp64_sequential": plain,
            "served_one_at_a_time": alone,
            "speedup_vs_plain": best["solves_per_s"] / plain["solves_per_s"]}
@@ -970,6 +982,8 @@ def main():
     ap.add_argument("--requests", type=int, default=48, help="serve: requests per rate")
     ap.add_argument("--edge-max", type=int, default=96, help="serve: largest mesh edge")
     ap.add_argument("--serve-inner", type=float, default=0.3, help="serve: FP32 reduction between FP64 updates")
+    ap.add_argument("--lane-mb", type=float, default=8.0,
+                    help="serve: requests with at most this many MB of FP32 element matrices share lane launches")
     ap.add_argument("--nrhs", type=int, default=64)
     ap.add_argument("--single-cols", type=int, default=2, help="columns solved one by one for the FP64 comparison")
     ap.add_argument("--batched-fp64", type=int, default=0, help="also time the FP64 batched block CG")

@@ -286,6 +286,10 @@ int afm_solve_cg(afm_operator* op, const double* b, double* x, double rtol, doub
 int afm_solve_cg_device(afm_operator* op, const double* d_b, double* d_x, double rtol, double atol, int maxit,
                         int norm_type, afm_solve_stats* stats);
 
+/* The last mixed-precision solve of the operator (afm_solve_cg_mixed*): at
+ * each FP64 residual, the inner iterations done so far and ||b - A x|| / ||b||.
+ * *n = the count; up to cap entries are written. */
+int afm_get_solve_trace(afm_operator* op, uint32_t cap, int* inner_iterations, double* rel_residual, uint32_t* n);
 /* Mixed-precision solve of the same system (no counterpart in the
  * reference): Jacobi-PCG whose recursion runs in FP32 (the FP32 products of
  * afm_matvec_device_f32: the symmetric FP32 copy of the element matrices at
@@ -407,7 +411,8 @@ int afm_get_assembled_csr(afm_operator* op, uint64_t* nnz, uint64_t* row_ptr, ui
  * taking the next step of every request whose previous step has finished on
  * the GPU, so progress never waits for the caller. Each request runs on its
  * own stream, so the work of all running requests overlaps on the device, and
- * requests arriving meanwhile join as slots and memory free up. A request's
+ * requests arriving meanwhile join as slots and memory free up; the FP32
+ * iterations of small requests share one launch (afm_server_set_lane). A request's
  * result does not depend on the others: it is the same, bit for bit, alone
  * and in any mix. The calls below are thread-safe. */
 typedef struct afm_server afm_server;
@@ -427,6 +432,22 @@ int afm_server_poll(afm_server* s, uint32_t* n_queued, uint32_t* n_active);
 int afm_server_take(afm_server* s, uint64_t id, int* finished, double* x, afm_solve_stats* stats, double* times);
 /* Waits for running work and releases everything. */
 int afm_server_destroy(afm_server* s);
+/* Serving lane: requests whose FP32 element matrices take at most
+ * max_ke_bytes (n^2 x 4 bytes per element; 8 MB by default, 0 turns the lane
+ * off) run their FP32 iterations in one launch shared by all such requests
+ * (one thread-block cluster per request, at most iters_per_launch iterations,
+ * 32 by default, per launch); larger requests run on their own streams. Takes
+ * effect for requests admitted afterwards. */
+int afm_server_set_lane(afm_server* s, uint64_t max_ke_bytes, uint32_t iters_per_launch);
+typedef struct {
+    uint64_t lane_launches;       /* serving-lane launches */
+    uint64_t lane_solve_launches; /* requests carried, summed over those launches */
+    uint32_t lane_max_batch;      /* most requests carried by one launch */
+    uint32_t reserved;
+    uint64_t lane_requests;       /* requests whose FP32 iterations ran in the lane */
+    uint64_t stream_requests;     /* requests whose FP32 iterations ran on their own streams */
+} afm_server_info;
+int afm_server_get_info(afm_server* s, afm_server_info* info);
 
 /* Largest operator (DoFs) afm_solve_cg_device_noalloc accepts. */
 #define AFM_NOALLOC_MAX_DOFS 262144u

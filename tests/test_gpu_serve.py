@@ -69,6 +69,7 @@ def test_results_alone_and_in_the_mix(gpu):
     res = drain(srv, ids)
     for x0, rid in zip(alone, ids):
         assert np.array_equal(res[rid][0], x0)
+    assert srv.info()["lane_max_batch"] >= 2  # the mix shared serving-lane launches
     srv.close()
 
 
@@ -105,6 +106,8 @@ def test_arrivals_while_others_run(gpu):
         x, st, t = res[rid]
         assert np.array_equal(x, alone[case])
         assert t[2] < t_done_first  # started while the long one was still running
+    info = srv.info()  # the long request on its own stream, the small ones in the lane
+    assert info["stream_requests"] >= 2 and info["lane_requests"] >= 2 * len(cases)
     srv.close()
 
 
@@ -159,4 +162,54 @@ def test_failed_request_is_reported(gpu):
     assert isinstance(done[bad], AfmError) and done[bad].name == "ERR_STATE"
     x = done[good][0]
     assert np.linalg.norm(b2 - pr2.matmult_bc(x)) <= 1.01 * RTOL * np.linalg.norm(b2)
+    srv.close()
+
+
+def _solve_all(srv, cases):
+    reqs = [request(*c) for c in cases]
+    ids = [srv.submit(A, b, rtol=RTOL) for A, b, _ in reqs]
+    res = drain(srv, ids)
+    return [(res[i], pr, b) for i, (_, b, pr) in zip(ids, reqs)]
+
+
+def test_lane_batches_the_small_requests(gpu):
+    """The serving lane: every request of CASES is small enough for it, so their FP32 iterations run in
+    shared launches (one cluster per request); launches carry several requests at once, every result meets
+    its FP64-checked tolerance, and the number of iterations per launch does not change a single bit."""
+    out = {}
+    for iters in (8, 32):
+        srv = Server(0)
+        srv.set_lane(8 << 20, iters)
+        out[iters] = _solve_all(srv, CASES)
+        info = srv.info()
+        srv.close()
+        assert info["lane_requests"] == len(CASES) and info["stream_requests"] == 0
+        assert info["lane_max_batch"] >= 2
+        assert info["lane_solve_launches"] > info["lane_launches"]
+        for (x, st, _), pr, b in out[iters]:
+            assert st.status == 0 and st.rel_residual <= RTOL
+            assert np.linalg.norm(b - pr.matmult_bc(x)) <= 1.01 * RTOL * np.linalg.norm(b)
+    for a, b in zip(out[8], out[32]):
+        assert np.array_equal(a[0][0], b[0][0])
+
+
+def test_lane_off_runs_every_request_on_its_stream(gpu):
+    srv = Server(0)
+    srv.set_lane(0, 32)
+    res = _solve_all(srv, CASES[:3])
+    info = srv.info()
+    srv.close()
+    assert info["lane_requests"] == 0 and info["stream_requests"] == 3 and info["lane_launches"] == 0
+    for (x, st, _), pr, b in res:
+        assert st.status == 0
+        assert np.linalg.norm(b - pr.matmult_bc(x)) <= 1.01 * RTOL * np.linalg.norm(b)
+
+
+def test_lane_arguments(gpu):
+    from amat_gb300 import AfmError
+    srv = Server(0)
+    for bad in (0, 5000):
+        with pytest.raises(AfmError) as e:
+            srv.set_lane(1 << 20, bad)
+        assert e.value.name == "ERR_INVALID_ARG"
     srv.close()
