@@ -110,6 +110,7 @@ AFM_SIGNATURES = {
     "afm_matvec": (I, [P, P, P, I]),
     "afm_matvec_device": (I, [P, P, P, P]),
     "afm_matvec_device_f32": (I, [P, P, P, P]),
+    "afm_matvec_inner_device": (I, [P, P, P, P]),
     "afm_matmult_bc": (I, [P, P, P]),
     "afm_matmult_bc_device": (I, [P, P, P, P]),
     "afm_get_diagonal": (I, [P, P]),

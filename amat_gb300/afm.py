@@ -264,6 +264,12 @@ class aMatFree:
         check(self._lib.afm_matvec_device_f32(self._h, C.c_void_p(v_ptr), C.c_void_p(u_ptr),
                                               C.c_void_p(stream) if stream else None), "afm_matvec_device_f32")
 
+    def matvec_inner_device(self, v_ptr, u_ptr, stream=None):
+        """v = K u on double device vectors with the double-float products of the corrected symmetric arena
+        (symmetric inner format 3)."""
+        check(self._lib.afm_matvec_inner_device(self._h, C.c_void_p(v_ptr), C.c_void_p(u_ptr),
+                                                C.c_void_p(stream) if stream else None), "afm_matvec_inner_device")
+
     def matmult_bc_device(self, v_ptr, u_ptr, stream=None):
         check(self._lib.afm_matmult_bc_device(self._h, C.c_void_p(v_ptr), C.c_void_p(u_ptr),
                                               C.c_void_p(stream) if stream else None), "afm_matmult_bc_device")

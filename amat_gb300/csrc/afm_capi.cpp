@@ -63,6 +63,13 @@ cudaError_t launch_patches_f32symx(const PatchPlanGeom& pg, const PatchArgs& a, 
 cudaError_t configure_kernels_f32symx();
 size_t patch_smem_f32symx(const PatchPlanGeom& pg, uint32_t copy_bytes);
 size_t segment_smem_f32symx(const Segment& s);
+cudaError_t launch_segment_splitsymx(const Segment& s, const SegArgs& a, int sm_count, bool dup, bool pdl,
+                                     cudaStream_t st);
+cudaError_t launch_patches_splitsymx(const PatchPlanGeom& pg, const PatchArgs& a, int sm_count, bool pdl,
+                                     cudaStream_t st);
+cudaError_t configure_kernels_splitsymx();
+size_t patch_smem_splitsymx(const PatchPlanGeom& pg, uint32_t copy_bytes);
+size_t segment_smem_splitsymx(const Segment& s);
 size_t patch_smem_f32sym(const PatchPlanGeom& pg, uint32_t copy_bytes);
 size_t segment_smem_f32sym(const Segment& s);
 size_t patch_smem_fp64(const PatchPlanGeom& pg, uint32_t copy_bytes);
@@ -76,6 +83,7 @@ cudaError_t launch_patches(int prec, const PatchPlanGeom& pg, const PatchArgs& a
         case AFM_PREC_FP64_SPLIT: return launch_patches_split(pg, a, sm_count, pdl, stream);
         case kPrecF32Sym: return launch_patches_f32sym(pg, a, sm_count, pdl, stream);
         case kPrecF32SymX: return launch_patches_f32symx(pg, a, sm_count, pdl, stream);
+        case kPrecSplitSymX: return launch_patches_splitsymx(pg, a, sm_count, pdl, stream);
         default: return launch_patches_fp32(pg, a, sm_count, pdl, stream);
     }
 }
@@ -86,6 +94,7 @@ size_t patch_smem_bytes(int prec, const PatchPlanGeom& pg, uint32_t copy_bytes) 
         case AFM_PREC_FP64_SPLIT: return patch_smem_split(pg, copy_bytes);
         case kPrecF32Sym: return patch_smem_f32sym(pg, copy_bytes);
         case kPrecF32SymX: return patch_smem_f32symx(pg, copy_bytes);
+        case kPrecSplitSymX: return patch_smem_splitsymx(pg, copy_bytes);
         default: return patch_smem_fp32(pg, copy_bytes);
     }
 }
@@ -101,6 +110,7 @@ cudaError_t launch_segment(const Segment& s, int prec, const SegArgs& a, int sm_
         case AFM_PREC_FP64_SPLIT: return launch_segment_split(s, a, sm_count, dup, pdl, stream);
         case kPrecF32Sym: return launch_segment_f32sym(s, a, sm_count, dup, pdl, stream);
         case kPrecF32SymX: return launch_segment_f32symx(s, a, sm_count, dup, pdl, stream);
+        case kPrecSplitSymX: return launch_segment_splitsymx(s, a, sm_count, dup, pdl, stream);
         default: return launch_segment_fp32(s, a, sm_count, dup, pdl, stream);
     }
 }
@@ -111,6 +121,7 @@ size_t segment_smem_bytes(const Segment& s, int prec) {
         case AFM_PREC_FP64_SPLIT: return segment_smem_split(s);
         case kPrecF32Sym: return segment_smem_f32sym(s);
         case kPrecF32SymX: return segment_smem_f32symx(s);
+        case kPrecSplitSymX: return segment_smem_splitsymx(s);
         default: return segment_smem_fp32(s);
     }
 }
@@ -198,6 +209,7 @@ void drop_graph(afm_operator::CgGraph& g);
 void free_device(afm_operator* op) {
     drop_graph(op->cg64);
     drop_graph(op->cg32);
+    drop_graph(op->cg64i);
     drop_graph(op->bcg64);
     drop_graph(op->bcg32);
     op->batch_tune.clear();
@@ -214,6 +226,7 @@ void free_device(afm_operator* op) {
     dfree(op, op->d_bcmask);
     dfree(op, op->d_work);
     dfree(op, op->d_work32);
+    dfree(op, op->d_work64i);
     dfree(op, op->d_patch_desc);
     dfree(op, op->d_patch_idx);
     dfree(op, op->d_pv);
@@ -232,6 +245,7 @@ void free_device(afm_operator* op) {
     dfree(op, op->d_free_ref32);
     op->work_elems = 0;
     op->work32_elems = 0;
+    op->work64i_elems = 0;
 }
 
 // Greedy first-fit colouring in element order (include/meshGraph.hpp:59-109)
@@ -651,11 +665,18 @@ void layout_sym(afm_operator* op, int mode) {
 // none, they read the hi plane).
 int sym_format(const afm_operator* op) { return op->sym_ok ? op->sym_mode : 0; }
 
+// The arena the format needs: format 3 (FP64 inner vectors) reads the
+// corrected arena of format 2.
+int sym_arena(const afm_operator* op) {
+    const int f = sym_format(op);
+    return f == 3 ? 2 : f;
+}
+
 // Builds the symmetric inner arena in the operator's format on its stream
 // (once per format); work enqueued afterwards on `st` is ordered after it.
 // Call outside stream capture.
 int ensure_sym(afm_operator* op, cudaStream_t st) {
-    const int fmt = sym_format(op);
+    const int fmt = sym_arena(op);
     if (!fmt) return AFM_SUCCESS;
     if (op->d_sym && op->sym_built == fmt) return AFM_SUCCESS;
     dfree(op, op->d_sym);
@@ -748,6 +769,16 @@ int ensure_work(afm_operator* op, size_t vectors) {
     return AFM_SUCCESS;
 }
 
+int ensure_work64i(afm_operator* op, size_t vectors) {
+    const size_t need = vectors * (size_t)std::max<uint32_t>(op->n_dofs, 1);
+    if (op->work64i_elems >= need) return AFM_SUCCESS;
+    dfree(op, op->d_work64i);
+    op->work64i_elems = 0;
+    AFM_CUDA(dalloc(op, &op->d_work64i, need * sizeof(double)));
+    op->work64i_elems = need;
+    return AFM_SUCCESS;
+}
+
 int ensure_work32(afm_operator* op, size_t vectors) {
     const size_t need = vectors * (size_t)std::max<uint32_t>(op->n_dofs, 1);
     if (op->work32_elems >= need) return AFM_SUCCESS;
@@ -794,26 +825,31 @@ int enqueue_free(afm_operator* op, void* d_v, const void* d_u, int bc_mode, cuda
     return AFM_SUCCESS;
 }
 
-int enqueue_matvec(afm_operator* op, void* d_v, const void* d_u, int bc_mode, cudaStream_t st, bool f32 = false) {
+int enqueue_matvec(afm_operator* op, void* d_v, const void* d_u, int bc_mode, cudaStream_t st, bool f32 = false,
+                   bool inner64 = false) {
     if (op->matfree_type == 2) return enqueue_free(op, d_v, d_u, bc_mode, st, f32);
     // f32: FP32 product on float vectors, from the symmetric inner arena once
     // built, else from an FP32 arena or the hi plane of a split arena (half of
-    // each unit is copied)
-    const bool sym = f32 && op->d_sym != nullptr;
+    // each unit is copied). inner64: FP64 vectors, double-float products from
+    // the corrected symmetric arena (it must be built).
+    const bool sym = (f32 || inner64) && op->d_sym != nullptr;
     const bool symx = sym && op->sym_built == 2;
-    const int kprec = sym ? (symx ? kPrecF32SymX : kPrecF32Sym) : f32 ? AFM_PREC_FP32 : op->precision;
+    if (inner64 && !symx) return fail(AFM_ERR_STATE, "FP64 inner product without the corrected symmetric arena");
+    const int kprec = inner64 ? kPrecSplitSymX
+                              : sym ? (symx ? kPrecF32SymX : kPrecF32Sym) : f32 ? AFM_PREC_FP32 : op->precision;
     const size_t vbytes = (size_t)op->n_dofs * (f32 || kprec == AFM_PREC_FP32 ? 4 : 8);
-    // the corrected format sums into an FP64 vector, rounded to FP32 at the end
+    // the corrected format's FP32 products sum into an FP64 vector, rounded to FP32 at the end
+    const bool via_vx = symx && !inner64;
     float* const d_v32 = static_cast<float*>(d_v);
-    if (symx) d_v = op->d_vx;
+    if (via_vx) d_v = op->d_vx;
     // split arithmetic: max|u| for the launches' power-of-two u scale (and v = 0) in one launch, before
     // the first element launch, which waits for it in full; other arithmetic: v = 0
-    const bool scaled = kprec == AFM_PREC_FP64_SPLIT;
+    const bool scaled = kprec == AFM_PREC_FP64_SPLIT || kprec == kPrecSplitSymX;
     if (scaled)
         AFM_CUDA(launch_umax(static_cast<const double*>(d_u), bc_mode ? op->d_bcmask : nullptr, op->n_dofs,
                              static_cast<double*>(d_v), op->n_dofs, op->d_usc, st));
     else
-        AFM_CUDA(cudaMemsetAsync(d_v, 0, symx ? (size_t)op->n_dofs * 8 : vbytes, st));
+        AFM_CUDA(cudaMemsetAsync(d_v, 0, via_vx ? (size_t)op->n_dofs * 8 : vbytes, st));
     bool first = true;
     if (op->use_patches) {
         const Segment& s = op->segs[0];
@@ -844,7 +880,7 @@ int enqueue_matvec(afm_operator* op, void* d_v, const void* d_u, int bc_mode, cu
         if (one)
             AFM_CUDA(launch_patch_combine((f32 && !symx) ? 4 : 8, d_v, op->d_pv, op->d_shared_dof,
                                           op->d_shared_off, op->d_shared_idx, op->n_shared, st));
-        if (symx) AFM_CUDA(launch_to_f32(d_v32, op->d_vx, op->n_dofs, st));
+        if (via_vx) AFM_CUDA(launch_to_f32(d_v32, op->d_vx, op->n_dofs, st));
         return AFM_SUCCESS;
     }
     for (const Segment& s : op->segs) {
@@ -869,7 +905,7 @@ int enqueue_matvec(afm_operator* op, void* d_v, const void* d_u, int bc_mode, cu
         AFM_CUDA(launch_segment(s, kprec, a, op->sm_count, op->dup_in_element, !first, st));
         first = false;
     }
-    if (symx) AFM_CUDA(launch_to_f32(d_v32, op->d_vx, op->n_dofs, st));
+    if (via_vx) AFM_CUDA(launch_to_f32(d_v32, op->d_vx, op->n_dofs, st));
     return AFM_SUCCESS;
 }
 
@@ -1179,6 +1215,19 @@ int cg_step<float>(afm_operator* op, const CgVectors<float>& V, cudaStream_t st)
     return AFM_SUCCESS;
 }
 
+// One iteration of the FP64-vector inner recursion (symmetric inner format
+// 3): the double-float product of the corrected symmetric arena.
+int cg_step_inner64(afm_operator* op, const CgVectors<double>& V, cudaStream_t st) {
+    int s = enqueue_matvec(op, V.q, V.p, 1, st, false, true);
+    if (s) return s;
+    AFM_CUDA(launch_set_constrained(V.q, V.p, op->d_bc_idx, op->n_bc, st));
+    double* sc = op->d_scalars;
+    double* part = sc + kScalarSlots;
+    AFM_CUDA(launch_cg_alpha(V.p, V.q, op->n_dofs, sc, part, st));
+    AFM_CUDA(launch_cg_update(V.x, V.r, V.z, V.p, V.q, V.dinv, op->n_dofs, sc, part, st));
+    return AFM_SUCCESS;
+}
+
 void drop_graph(afm_operator::CgGraph& g) {
     if (g.exec) cudaGraphExecDestroy(g.exec);
     g = afm_operator::CgGraph();
@@ -1195,7 +1244,7 @@ void drop_graph(afm_operator::CgGraph& g) {
 // graph ends with a copy of the scalars to the pinned host mirror. The stream
 // must be idle.
 template <typename T>
-int ensure_cg_graph(afm_operator* op, afm_operator::CgGraph& gc, const CgVectors<T>& V) {
+int ensure_cg_graph(afm_operator* op, afm_operator::CgGraph& gc, const CgVectors<T>& V, bool inner64 = false) {
     cudaStream_t st = op->stream;
     double* h = op->h_scalars;
     const int batch = op->n_dofs > (1u << 20) ? 4 : 8;
@@ -1207,7 +1256,12 @@ int ensure_cg_graph(afm_operator* op, afm_operator::CgGraph& gc, const CgVectors
     AFM_CUDA(cudaStreamSynchronize(st));
     AFM_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     int s = AFM_SUCCESS;
-    for (int i = 0; i < batch && s == AFM_SUCCESS; i++) s = cg_step<T>(op, V, st);
+    for (int i = 0; i < batch && s == AFM_SUCCESS; i++) {
+        if constexpr (std::is_same<T, double>::value)
+            s = inner64 ? cg_step_inner64(op, V, st) : cg_step<T>(op, V, st);
+        else
+            s = cg_step<T>(op, V, st);
+    }
     if (s == AFM_SUCCESS &&
         cudaMemcpyAsync(h, op->d_scalars, sizeof(double) * kScalarSlots, cudaMemcpyDeviceToHost, st) != cudaSuccess)
         s = fail(AFM_ERR_CUDA, "capture: scalar copy");
@@ -1311,13 +1365,19 @@ struct MixedVectors {
     double *r64, *q64;
     float* b32;
     CgVectors<float> V;
+    double* b64;         // format 3: the inner right-hand side and vectors in FP64
+    CgVectors<double> D;
 };
 
 MixedVectors mixed_vectors(afm_operator* op) {
     const size_t n = op->n_dofs;
     float* b32 = op->d_work32;
-    return MixedVectors{op->d_work + 2 * n, op->d_work + 5 * n, b32,
-                        CgVectors<float>{b32 + n, b32 + 2 * n, b32 + 3 * n, b32 + 4 * n, b32 + 6 * n, b32 + 5 * n}};
+    double* b64 = op->d_work64i;
+    MixedVectors W{op->d_work + 2 * n, op->d_work + 5 * n, b32,
+                   CgVectors<float>{b32 + n, b32 + 2 * n, b32 + 3 * n, b32 + 4 * n, b32 + 6 * n, b32 + 5 * n},
+                   b64, CgVectors<double>{}};
+    if (b64) W.D = CgVectors<double>{b64 + n, b64 + 2 * n, b64 + 3 * n, b64 + 4 * n, b64 + 6 * n, b64 + 5 * n};
+    return W;
 }
 
 int mixed_record(MixedSolve& m) {
@@ -1353,7 +1413,11 @@ int mixed_finish(MixedSolve& m, int status) {
 int mixed_segment_end(MixedSolve& m, int iters, int seg_status) {
     m.inner_total += iters;
     m.fresh = (seg_status == AFM_ERR_BREAKDOWN);
-    AFM_CUDA(launch_add_f32(m.d_x, mixed_vectors(m.op).V.x, m.op->n_dofs, m.op->stream, 1.0 / m.sigma));
+    const MixedVectors W = mixed_vectors(m.op);
+    if (m.inner64)
+        AFM_CUDA(launch_add_f32(m.d_x, W.D.x, m.op->n_dofs, m.op->stream, 1.0 / m.sigma));
+    else
+        AFM_CUDA(launch_add_f32(m.d_x, W.V.x, m.op->n_dofs, m.op->stream, 1.0 / m.sigma));
     m.outer++;
     return mixed_residual(m);
 }
@@ -1370,12 +1434,14 @@ int mixed_begin(MixedSolve& m) {
     DeviceGuard g(op->device);
     int s = ensure_work(op, 8);
     if (s) return s;
-    s = ensure_work32(op, 7);
+    m.inner64 = !m.lane && op->matfree_type != 2 && sym_format(op) == 3;
+    s = m.inner64 ? ensure_work64i(op, 7) : ensure_work32(op, 7);
     if (s) return s;
     if (!m.lane) {
         s = ensure_sym(op, op->stream);  // once per operator, before the timed solve
         if (s) return s;
     }
+    if (m.inner64 && op->sym_built != 2) return fail(AFM_ERR_STATE, "symmetric inner format 3 needs symmetric Ke");
     AFM_CUDA(cudaEventCreateWithFlags(&m.ev, cudaEventDisableTiming));
     AFM_CUDA(cudaEventCreate(&m.e0));
     AFM_CUDA(cudaEventCreate(&m.e1));
@@ -1383,8 +1449,13 @@ int mixed_begin(MixedSolve& m) {
     const size_t n = op->n_dofs;
     cudaStream_t st = op->stream;
     AFM_CUDA(cudaEventRecord(m.e0, st));
-    AFM_CUDA(launch_invert(W.V.dinv, op->d_diag, n, st));
-    AFM_CUDA(cudaMemsetAsync(W.V.x, 0, n * sizeof(float), st));
+    if (m.inner64) {
+        AFM_CUDA(launch_invert(W.D.dinv, op->d_diag, n, st));
+        AFM_CUDA(cudaMemsetAsync(W.D.x, 0, n * sizeof(double), st));
+    } else {
+        AFM_CUDA(launch_invert(W.V.dinv, op->d_diag, n, st));
+        AFM_CUDA(cudaMemsetAsync(W.V.x, 0, n * sizeof(float), st));
+    }
     AFM_CUDA(launch_norm2(m.d_b, n, op->d_scalars, op->d_scalars + kScalarSlots, st));
     m.phase = MS_NORMB;
     return mixed_record(m);
@@ -1439,13 +1510,21 @@ int mixed_advance(MixedSolve& m) {
                 return mixed_finish(m, AFM_ERR_MAXIT);
             // the segment's scale: a power of two that brings ||r|| into [0.5, 1) (exact)
             const double sigma = residual_scale(m.rn);
-            if (m.fresh) {
+            if (m.fresh && m.inner64) {
+                // FP64-vector Jacobi-PCG on A d = sigma r from d = 0
+                AFM_CUDA(launch_to_f32(W.b64, W.r64, n, st, sigma));
+                AFM_CUDA(cudaMemsetAsync(W.D.q, 0, n * sizeof(double), st));
+                AFM_CUDA(launch_cg_init(W.b64, W.D.q, W.D.dinv, W.D.r, W.D.z, W.D.p, n, sc, part, st));
+            } else if (m.fresh) {
                 // FP32 Jacobi-PCG on A d = sigma r from d = 0
                 AFM_CUDA(launch_to_f32(W.b32, W.r64, n, st, sigma));
                 AFM_CUDA(cudaMemsetAsync(W.V.q, 0, n * sizeof(float), st));
                 AFM_CUDA(launch_cg_init(W.b32, W.V.q, W.V.dinv, W.V.r, W.V.z, W.V.p, n, sc, part, st));
-            } else {
+            } else if (m.inner64) {
                 // reliable update: the recursion continues from the true residual
+                AFM_CUDA(launch_cg_reliable(W.r64, W.D.r, W.D.z, W.D.p, W.D.dinv, n, sc, part, sigma,
+                                            sigma / m.sigma, st));
+            } else {
                 AFM_CUDA(launch_cg_reliable(W.r64, W.V.r, W.V.z, W.V.p, W.V.dinv, n, sc, part, sigma,
                                             sigma / m.sigma, st));
             }
@@ -1470,9 +1549,10 @@ int mixed_advance(MixedSolve& m) {
                 m.phase = MS_LANE;
                 return AFM_SUCCESS;
             }
-            int s = ensure_cg_graph<float>(op, op->cg32, W.V);
+            int s = m.inner64 ? ensure_cg_graph<double>(op, op->cg64i, W.D, true)
+                              : ensure_cg_graph<float>(op, op->cg32, W.V);
             if (s) return s;
-            AFM_CUDA(cudaGraphLaunch(op->cg32.exec, st));
+            AFM_CUDA(cudaGraphLaunch(m.inner64 ? op->cg64i.exec : op->cg32.exec, st));
             AFM_CUDA(cudaEventRecord(m.ev, st));
             m.phase = MS_ITER;
             return AFM_SUCCESS;
@@ -1487,7 +1567,7 @@ int mixed_advance(MixedSolve& m) {
             [[fallthrough]];
         case MS_ITER: {
             if (h[S_DONE] == 0.0) {
-                AFM_CUDA(cudaGraphLaunch(op->cg32.exec, st));
+                AFM_CUDA(cudaGraphLaunch(m.inner64 ? op->cg64i.exec : op->cg32.exec, st));
                 AFM_CUDA(cudaEventRecord(m.ev, st));
                 return AFM_SUCCESS;
             }
@@ -1586,7 +1666,7 @@ int afm_create(afm_operator** out, int bc_method, int device) {
     // kernels' shared-memory limits, before any launch or graph capture
     if (configure_kernels_fp64() != cudaSuccess || configure_kernels_split() != cudaSuccess ||
         configure_kernels_fp32() != cudaSuccess || configure_kernels_f32sym() != cudaSuccess ||
-        configure_kernels_f32symx() != cudaSuccess)
+        configure_kernels_f32symx() != cudaSuccess || configure_kernels_splitsymx() != cudaSuccess)
         return fail(AFM_ERR_CUDA, "kernel configuration failed on device %d", device);
     auto* op = new afm_operator();
     op->device = device;
@@ -1675,9 +1755,9 @@ int afm_set_wait_probe(afm_operator* op, int enable) {
 
 int afm_set_symmetric_inner(afm_operator* op, int format) {
     AFM_CHECK_OP(op);
-    if (format < 0 || format > 2) return fail(AFM_ERR_INVALID_ARG, "symmetric inner format %d (0, 1 or 2)", format);
+    if (format < 0 || format > 3) return fail(AFM_ERR_INVALID_ARG, "symmetric inner format %d (0 to 3)", format);
     op->sym_mode = format;
-    if (op->d_sym && op->sym_built != sym_format(op)) {
+    if (op->d_sym && op->sym_built != sym_arena(op)) {
         DeviceGuard g(op->device);
         dfree(op, op->d_sym);
         dfree(op, op->d_vx);
@@ -2165,6 +2245,20 @@ int afm_matvec_device_f32(afm_operator* op, float* d_v, const float* d_u, void* 
     int s = ensure_sym(op, st);
     if (s) return s;
     s = enqueue_matvec(op, d_v, d_u, 0, st, true);
+    return s == AFM_SUCCESS ? ok() : s;
+}
+
+int afm_matvec_inner_device(afm_operator* op, double* d_v, const double* d_u, void* stream) {
+    AFM_CHECK_OP(op);
+    if (!op->finalized) return fail(AFM_ERR_STATE, "matvec before finalize");
+    if (op->precision != AFM_PREC_FP64_SPLIT || op->matfree_type == 2 || sym_format(op) != 3)
+        return fail(AFM_ERR_STATE, "the FP64 inner product needs an FP64_SPLIT operator in symmetric inner format 3");
+    if (!d_v || !d_u || (void*)d_v == (const void*)d_u) return fail(AFM_ERR_INVALID_ARG, "bad vectors");
+    DeviceGuard g(op->device);
+    cudaStream_t st = pick_stream(op, stream);
+    int s = ensure_sym(op, st);
+    if (s) return s;
+    s = enqueue_matvec(op, d_v, d_u, 0, st, false, true);
     return s == AFM_SUCCESS ? ok() : s;
 }
 
@@ -2809,6 +2903,7 @@ int afm_get_info(afm_operator* op, afm_info* info) {
     info->sym_bytes = op->d_sym ? op->sym_bytes : 0;
     info->csr_nnz = op->csr_nnz;
     info->work_bytes = op->work_elems * sizeof(double) + op->work32_elems * sizeof(float) +
+                       op->work64i_elems * sizeof(double) +
                        op->bwork_elems * sizeof(double) + op->bsc_elems * sizeof(double);
     info->device = op->device;
     return ok();

@@ -184,6 +184,8 @@ cudaError_t launch_free(int kind, bool f32, const FreeArgs& a, int sm_count, cud
 constexpr int kPrecF32Sym = 16;
 // ... and from the symmetric inner arena with its BF16 correction plane.
 constexpr int kPrecF32SymX = 17;
+// FP64 vectors, double-float products from that corrected arena (ArithSplitSymX).
+constexpr int kPrecSplitSymX = 18;
 
 // Fills segment s's part of the symmetric inner arena from its split-arena
 // units (afm_mv_f32sym.cu).
@@ -303,6 +305,8 @@ struct afm_operator {
     double* h_scalars = nullptr;     // pinned mirror
     float* d_work32 = nullptr;       // mixed-precision inner vectors
     size_t work32_elems = 0;
+    double* d_work64i = nullptr;     // inner vectors of the FP64-vector mixed solve (symmetric inner format 3)
+    size_t work64i_elems = 0;
 
     // captured CG iteration graphs (FP64 and FP32 inner), keyed by buffers
     struct CgGraph {
@@ -311,7 +315,7 @@ struct afm_operator {
         int batch = 0;
         uint64_t gen = 0;
     };
-    CgGraph cg64, cg32, bcg64, bcg32;
+    CgGraph cg64, cg32, cg64i, bcg64, bcg32;
     uint64_t generation = 0;  // bumped whenever device buffers are released
 
     // symmetric inner arena: FP32 element matrices with each symmetric pair of

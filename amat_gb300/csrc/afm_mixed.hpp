@@ -45,6 +45,9 @@ struct MixedSolve {
     // launches them (launch_lane) for every solve in MS_LANE, records ev on the
     // lane's stream and sets MS_LANEITER; no symmetric inner arena is built
     bool lane = false;
+    // symmetric inner format 3: the inner recursion in FP64 vectors with the
+    // double-float products of the corrected symmetric arena (set by mixed_begin)
+    bool inner64 = false;
     cudaEvent_t ev = nullptr, e0 = nullptr, e1 = nullptr;
     // each FP64 residual of the solve: inner iterations so far and ||r|| / ||b||
     std::vector<int> trace_iters;

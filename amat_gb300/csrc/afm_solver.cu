@@ -162,15 +162,16 @@ __global__ void __launch_bounds__(kRedThreads) k_cg_init_final(double* sc, const
 // r = fl32(sigma r64) (the FP64 true residual in the new segment's scale),
 // z = dinv r; partials of r.z, r.r, z.z and r.p (p = the last direction p_k,
 // still in the previous segment's scale)
-__global__ void __launch_bounds__(kRedThreads) k_cg_reliable(const double* __restrict__ r64, float* __restrict__ r,
-                                                             float* __restrict__ z, const float* __restrict__ p,
-                                                             const float* __restrict__ dinv, size_t n, double* part,
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads) k_cg_reliable(const double* __restrict__ r64, T* __restrict__ r,
+                                                             T* __restrict__ z, const T* __restrict__ p,
+                                                             const T* __restrict__ dinv, size_t n, double* part,
                                                              double sigma) {
     __shared__ double sh[kRedThreads];
     double rz = 0, rr = 0, zz = 0, rp = 0;
     for (size_t i = (size_t)blockIdx.x * kRedThreads + threadIdx.x; i < n; i += kStride) {
-        const float ri = (float)(r64[i] * sigma);
-        const float zi = dinv[i] * ri;
+        const T ri = (T)(r64[i] * sigma);
+        const T zi = dinv[i] * ri;
         r[i] = ri;
         z[i] = zi;
         rz = __fma_rn((double)ri, (double)zi, rz);
@@ -211,13 +212,17 @@ __global__ void __launch_bounds__(kRedThreads) k_cg_reliable_final(double* sc, c
 }
 
 // pass 3: p = z + beta (p - gamma z)
-__global__ void __launch_bounds__(kRedThreads) k_cg_reliable_p(float* __restrict__ p, const float* __restrict__ z,
+__device__ __forceinline__ float fma_rn(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fma_rn(double a, double b, double c) { return __fma_rn(a, b, c); }
+
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads) k_cg_reliable_p(T* __restrict__ p, const T* __restrict__ z,
                                                                size_t n, const double* sc) {
-    const float beta = (float)sc[S_BETA];
-    const float c = (float)(1.0 - sc[S_BETA] * sc[S_GAMMA]);
+    const T beta = (T)sc[S_BETA];
+    const T c = (T)(1.0 - sc[S_BETA] * sc[S_GAMMA]);
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
-        p[i] = __fmaf_rn(beta, p[i], c * z[i]);
+        p[i] = fma_rn(beta, p[i], c * z[i]);
 }
 
 // alpha = rz / (p.q); flag on p.q <= 0 or NaN
@@ -339,20 +344,22 @@ __global__ void __launch_bounds__(kRedThreads) k_axpby(double* __restrict__ y, c
         y[i] = __fma_rn(a, x[i], b * y[i]);
 }
 
-// out32 = fl32(scale in64) (scale a power of two: exact before the rounding)
-__global__ void __launch_bounds__(kRedThreads) k_to_f32(float* __restrict__ out, const double* __restrict__ in,
+// out = (T)(scale in64) (scale a power of two: exact before the rounding)
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads) k_to_f32(T* __restrict__ out, const double* __restrict__ in,
                                                         size_t n, double scale) {
     const size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) out[i] = (float)(in[i] * scale);
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) out[i] = (T)(in[i] * scale);
 }
 
-// x64 += inv d32, d32 = 0 (inv a power of two)
-__global__ void __launch_bounds__(kRedThreads) k_add_f32(double* __restrict__ x, float* __restrict__ d, size_t n,
+// x64 += inv d, d = 0 (inv a power of two)
+template <typename T>
+__global__ void __launch_bounds__(kRedThreads) k_add_f32(double* __restrict__ x, T* __restrict__ d, size_t n,
                                                          double inv) {
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
         x[i] += (double)d[i] * inv;
-        d[i] = 0.0f;
+        d[i] = (T)0;
     }
 }
 
@@ -520,14 +527,19 @@ cudaError_t launch_norm2(const T* a, size_t n, double* sc, double* part, cudaStr
     return cudaGetLastError();
 }
 
-cudaError_t launch_cg_reliable(const double* r64, float* r, float* z, float* p, const float* dinv, size_t n,
-                               double* sc, double* part, double sigma, double rho, cudaStream_t st) {
+template <typename T>
+cudaError_t launch_cg_reliable(const double* r64, T* r, T* z, T* p, const T* dinv, size_t n, double* sc,
+                               double* part, double sigma, double rho, cudaStream_t st) {
     const uint32_t nb = red_blocks(n);
-    k_cg_reliable<<<nb, kRedThreads, 0, st>>>(r64, r, z, p, dinv, n, part, sigma);
+    k_cg_reliable<T><<<nb, kRedThreads, 0, st>>>(r64, r, z, p, dinv, n, part, sigma);
     k_cg_reliable_final<<<1, kRedThreads, 0, st>>>(sc, part, nb, rho);
-    k_cg_reliable_p<<<grid_for(n), kRedThreads, 0, st>>>(p, z, n, sc);
+    k_cg_reliable_p<T><<<grid_for(n), kRedThreads, 0, st>>>(p, z, n, sc);
     return cudaGetLastError();
 }
+template cudaError_t launch_cg_reliable<float>(const double*, float*, float*, float*, const float*, size_t, double*,
+                                               double*, double, double, cudaStream_t);
+template cudaError_t launch_cg_reliable<double>(const double*, double*, double*, double*, const double*, size_t,
+                                                double*, double*, double, double, cudaStream_t);
 
 cudaError_t launch_axpby(double* y, const double* x, double a, double b, size_t n, cudaStream_t st) {
     k_axpby<<<grid_for(n), kRedThreads, 0, st>>>(y, x, a, b, n);
@@ -535,12 +547,22 @@ cudaError_t launch_axpby(double* y, const double* x, double a, double b, size_t 
 }
 
 cudaError_t launch_to_f32(float* out, const double* in, size_t n, cudaStream_t st, double scale) {
-    k_to_f32<<<grid_for(n), kRedThreads, 0, st>>>(out, in, n, scale);
+    k_to_f32<float><<<grid_for(n), kRedThreads, 0, st>>>(out, in, n, scale);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_to_f32(double* out, const double* in, size_t n, cudaStream_t st, double scale) {
+    k_to_f32<double><<<grid_for(n), kRedThreads, 0, st>>>(out, in, n, scale);
     return cudaGetLastError();
 }
 
 cudaError_t launch_add_f32(double* x, float* d, size_t n, cudaStream_t st, double inv) {
-    k_add_f32<<<grid_for(n), kRedThreads, 0, st>>>(x, d, n, inv);
+    k_add_f32<float><<<grid_for(n), kRedThreads, 0, st>>>(x, d, n, inv);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_add_f32(double* x, double* d, size_t n, cudaStream_t st, double inv) {
+    k_add_f32<double><<<grid_for(n), kRedThreads, 0, st>>>(x, d, n, inv);
     return cudaGetLastError();
 }
 

@@ -59,13 +59,18 @@ cudaError_t launch_norm2(const T* a, size_t n, double* sc, double* part, cudaStr
 // sc[S_RZ], sc[S_RR], sc[S_ZZ] of the new residual; S_DONE and S_ITER cleared.
 // The recursion runs on the residual times a power of two: sigma is the new
 // segment's scale (r = fl32(sigma r64)), rho = sigma / the previous segment's.
-cudaError_t launch_cg_reliable(const double* r64, float* r, float* z, float* p, const float* dinv, size_t n,
-                               double* sc, double* part, double sigma, double rho, cudaStream_t st);
+// T = float (the FP32 recursion) or double (the FP64-vector recursion of
+// symmetric inner format 3).
+template <typename T>
+cudaError_t launch_cg_reliable(const double* r64, T* r, T* z, T* p, const T* dinv, size_t n, double* sc,
+                               double* part, double sigma, double rho, cudaStream_t st);
 cudaError_t launch_axpby(double* y, const double* x, double a, double b, size_t n, cudaStream_t st);
-// out = fl32(scale in)
+// out = fl32(scale in), or scale in for a double out
 cudaError_t launch_to_f32(float* out, const double* in, size_t n, cudaStream_t st, double scale = 1.0);
+cudaError_t launch_to_f32(double* out, const double* in, size_t n, cudaStream_t st, double scale = 1.0);
 // x += inv d, d = 0
 cudaError_t launch_add_f32(double* x, float* d, size_t n, cudaStream_t st, double inv = 1.0);
+cudaError_t launch_add_f32(double* x, double* d, size_t n, cudaStream_t st, double inv = 1.0);
 
 // Words of the u-scale buffer of an operator (afm_operator::d_usc): [0] max|u|
 // of the last single-vector split product, [1] block counter, [2, 2 +

@@ -688,7 +688,9 @@ def run_solve(args, w, rank, world, local_rank):
     r["mixed"]["inner_ke_bytes"] = 0 if args.free else A.info()["sym_bytes"] or A.info()["ke_bytes"] // 2
     r["mixed"]["inner_arena"] = ("matrix-free (method 2): Ke integrated from coordinates" if args.free else
                                  {0: "hi plane", 1: "symmetric copy, FP32",
-                                  2: "symmetric copy, FP32 + BF16 correction"}[A.info()["sym_available"]])
+                                  2: "symmetric copy, FP32 + BF16 correction",
+                                  3: "symmetric copy, FP32 + BF16 correction; FP64 inner vectors"}[
+                                     A.info()["sym_available"]])
     out = {"metric": "CG solves/s at %g rel. residual" % rtol, "value": smx, "unit": "solves/s", "n_gpus": world,
            "steps": args.steps, "warmup": 1, "ms_per_step": 1e3 / smx, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32 inner / f64 residual", "data": "synthetic",
@@ -992,8 +994,9 @@ def main():
     ap.add_argument("--rtol", type=float, default=1e-8)
     ap.add_argument("--free", type=int, default=0, help="solve: mixed solve on the matrix-free operator (method 2)")
     ap.add_argument("--inner-rtol", type=float, default=1e-2)
-    ap.add_argument("--sym-format", type=int, default=1, choices=[0, 1, 2],
-                    help="solve: FP32 inner arena (1 symmetric FP32, 2 with BF16 correction, 0 hi plane)")
+    ap.add_argument("--sym-format", type=int, default=1, choices=[0, 1, 2, 3],
+                    help="solve: inner arena (1 symmetric FP32, 2 with BF16 correction, 0 hi plane; 3 the arena "
+                         "of 2 with FP64 inner vectors)")
     ap.add_argument("--load", default="example", choices=["example", "random"],
                     help="solve: the example's load, or N(0,1) per DoF as in the serving mix")
     ap.add_argument("--with-solves", type=int, default=1,

@@ -183,7 +183,11 @@ int afm_set_patch_mode(afm_operator* op, int mode);
  * perturbs the product by ~2^-24 |K| |u|, which costs the inner CG of
  * ill-conditioned systems (elasticity under rough loads) up to ~1.9x the
  * iterations of FP64 CG; format 2 brings that to ~1.1-1.2x, at a higher cost
- * per product. format = 0: FP32 products read the hi plane. The copy is
+ * per product. format = 3: the arena of format 2, and the mixed-precision
+ * solve's inner recursion in FP64 vectors with double-float products from it
+ * (about 40% of the split arena's bytes per product, no FP32 rounding of the
+ * vectors), for large ill-conditioned systems whose FP32 recursion stalls.
+ * format = 0: FP32 products read the hi plane. The copy is
  * built on the device from the split arena by the first FP32 product or
  * mixed-precision solve after a change (outside any stream capture). FP64
  * products never use it. */
@@ -255,6 +259,11 @@ int afm_matvec_device(afm_operator* op, double* d_v, const double* d_u, void* st
  * or its hi plane (the FP32-rounded Ke); or, for the matrix-free operator,
  * by the element kernels in FP32. */
 int afm_matvec_device_f32(afm_operator* op, float* d_v, const float* d_u, void* stream);
+/* The inner product of symmetric inner format 3 on double device vectors:
+ * double-float products from the corrected symmetric arena (K to about
+ * 2^-32), what the FP64-vector mixed solve iterates on. FP64_SPLIT operators
+ * with symmetric element matrices, after afm_set_symmetric_inner(op, 3). */
+int afm_matvec_inner_device(afm_operator* op, double* d_v, const double* d_u, void* stream);
 
 /* aMatFree::MatMult_mf (include/aMatFree.hpp:3894-3941): u_c taken as zero
  * in the product, then v_c = u_c. Host arrays. */
