@@ -351,16 +351,25 @@ def measure_inner_f32(A, m, steps, warmup):
     v = torch.empty_like(u)
     base = 4 * m.n_elem * m.ndpe + 8 * m.n_dofs  # map entries, u read, v written
     out = {}
-    names = {2: "symmetric_copy_bf16_correction", 1: "symmetric_copy", 0: "hi_plane"}
-    for sym in (2, 1, 0):
+    names = {3: "symmetric_copy_bf16_correction_fp64_vectors", 2: "symmetric_copy_bf16_correction",
+             1: "symmetric_copy", 0: "hi_plane"}
+    u64 = u.double()
+    v64 = torch.empty_like(u64)
+    for sym in (3, 2, 1, 0):
         A.set_symmetric_inner(sym)
+
+        def product():
+            if sym == 3:  # FP64 vectors, double-float products (the inner product of format 3)
+                A.matvec_inner_device(v64.data_ptr(), u64.data_ptr(), stream_ptr)
+            else:
+                A.matvec_device_f32(v.data_ptr(), u.data_ptr(), stream_ptr)
         for _ in range(warmup):
-            A.matvec_device_f32(v.data_ptr(), u.data_ptr(), stream_ptr)
+            product()
         torch.cuda.synchronize()
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         ev0.record(stream)
         for _ in range(steps):
-            A.matvec_device_f32(v.data_ptr(), u.data_ptr(), stream_ptr)
+            product()
         ev1.record(stream)
         torch.cuda.synchronize()
         ms = ev0.elapsed_time(ev1) / steps
@@ -368,8 +377,9 @@ def measure_inner_f32(A, m, steps, warmup):
         ke = info["sym_bytes"] if sym else info["ke_bytes"] // 2
         if sym and not ke:
             continue  # no symmetric copy for this operator
+        vec = base + 8 * m.n_dofs if sym == 3 else base  # FP64 u and v
         out[names[sym]] = {
-            "ms": ms, "ke_bytes": ke, "streamed_gbs": (ke + base) / (ms * 1e-3) / 1e9}
+            "ms": ms, "ke_bytes": ke, "streamed_gbs": (ke + vec) / (ms * 1e-3) / 1e9}
     A.set_symmetric_inner(1)
     return out
 
