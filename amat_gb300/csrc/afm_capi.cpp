@@ -665,11 +665,11 @@ void layout_sym(afm_operator* op, int mode) {
 // none, they read the hi plane).
 int sym_format(const afm_operator* op) { return op->sym_ok ? op->sym_mode : 0; }
 
-// The arena the format needs: format 3 (FP64 inner vectors) reads the
+// The arena the format needs: formats 3 and 4 (FP64 inner vectors) read the
 // corrected arena of format 2.
 int sym_arena(const afm_operator* op) {
     const int f = sym_format(op);
-    return f == 3 ? 2 : f;
+    return f >= 3 ? 2 : f;
 }
 
 // Builds the symmetric inner arena in the operator's format on its stream
@@ -830,12 +830,21 @@ int enqueue_matvec(afm_operator* op, void* d_v, const void* d_u, int bc_mode, cu
     if (op->matfree_type == 2) return enqueue_free(op, d_v, d_u, bc_mode, st, f32);
     // f32: FP32 product on float vectors, from the symmetric inner arena once
     // built, else from an FP32 arena or the hi plane of a split arena (half of
-    // each unit is copied). inner64: FP64 vectors, double-float products from
-    // the corrected symmetric arena (it must be built).
+    // each unit is copied). inner64: FP64 vectors on the corrected symmetric
+    // arena (it must be built): format 3, double-float products of the FP64 u;
+    // format 4, the products of format 2 on u rounded to FP32, summed into v
+    // in FP64.
     const bool sym = (f32 || inner64) && op->d_sym != nullptr;
     const bool symx = sym && op->sym_built == 2;
     if (inner64 && !symx) return fail(AFM_ERR_STATE, "FP64 inner product without the corrected symmetric arena");
-    const int kprec = inner64 ? kPrecSplitSymX
+    const bool inner_f32u = inner64 && sym_format(op) == 4;
+    if (inner_f32u) {
+        if (op->work64i_elems < 8ull * op->n_dofs) return fail(AFM_ERR_STATE, "format 4 product without its buffer");
+        float* u32 = reinterpret_cast<float*>(op->d_work64i + 7ull * op->n_dofs);
+        AFM_CUDA(launch_to_f32(u32, static_cast<const double*>(d_u), op->n_dofs, st));
+        d_u = u32;
+    }
+    const int kprec = inner64 ? (inner_f32u ? kPrecF32SymX : kPrecSplitSymX)
                               : sym ? (symx ? kPrecF32SymX : kPrecF32Sym) : f32 ? AFM_PREC_FP32 : op->precision;
     const size_t vbytes = (size_t)op->n_dofs * (f32 || kprec == AFM_PREC_FP32 ? 4 : 8);
     // the corrected format's FP32 products sum into an FP64 vector, rounded to FP32 at the end
@@ -1434,8 +1443,8 @@ int mixed_begin(MixedSolve& m) {
     DeviceGuard g(op->device);
     int s = ensure_work(op, 8);
     if (s) return s;
-    m.inner64 = !m.lane && op->matfree_type != 2 && sym_format(op) == 3;
-    s = m.inner64 ? ensure_work64i(op, 7) : ensure_work32(op, 7);
+    m.inner64 = !m.lane && op->matfree_type != 2 && (sym_format(op) == 3 || sym_format(op) == 4);
+    s = m.inner64 ? ensure_work64i(op, 8) : ensure_work32(op, 7);
     if (s) return s;
     if (!m.lane) {
         s = ensure_sym(op, op->stream);  // once per operator, before the timed solve
@@ -1755,7 +1764,7 @@ int afm_set_wait_probe(afm_operator* op, int enable) {
 
 int afm_set_symmetric_inner(afm_operator* op, int format) {
     AFM_CHECK_OP(op);
-    if (format < 0 || format > 3) return fail(AFM_ERR_INVALID_ARG, "symmetric inner format %d (0 to 3)", format);
+    if (format < 0 || format > 4) return fail(AFM_ERR_INVALID_ARG, "symmetric inner format %d (0 to 4)", format);
     op->sym_mode = format;
     if (op->d_sym && op->sym_built != sym_arena(op)) {
         DeviceGuard g(op->device);
@@ -2251,12 +2260,14 @@ int afm_matvec_device_f32(afm_operator* op, float* d_v, const float* d_u, void* 
 int afm_matvec_inner_device(afm_operator* op, double* d_v, const double* d_u, void* stream) {
     AFM_CHECK_OP(op);
     if (!op->finalized) return fail(AFM_ERR_STATE, "matvec before finalize");
-    if (op->precision != AFM_PREC_FP64_SPLIT || op->matfree_type == 2 || sym_format(op) != 3)
-        return fail(AFM_ERR_STATE, "the FP64 inner product needs an FP64_SPLIT operator in symmetric inner format 3");
+    if (op->precision != AFM_PREC_FP64_SPLIT || op->matfree_type == 2 || sym_format(op) < 3)
+        return fail(AFM_ERR_STATE, "the FP64 inner product needs an FP64_SPLIT operator in symmetric inner format 3 or 4");
     if (!d_v || !d_u || (void*)d_v == (const void*)d_u) return fail(AFM_ERR_INVALID_ARG, "bad vectors");
     DeviceGuard g(op->device);
     cudaStream_t st = pick_stream(op, stream);
     int s = ensure_sym(op, st);
+    if (s) return s;
+    s = ensure_work64i(op, 8);
     if (s) return s;
     s = enqueue_matvec(op, d_v, d_u, 0, st, false, true);
     return s == AFM_SUCCESS ? ok() : s;

@@ -351,15 +351,16 @@ def measure_inner_f32(A, m, steps, warmup):
     v = torch.empty_like(u)
     base = 4 * m.n_elem * m.ndpe + 8 * m.n_dofs  # map entries, u read, v written
     out = {}
-    names = {3: "symmetric_copy_bf16_correction_fp64_vectors", 2: "symmetric_copy_bf16_correction",
+    names = {4: "symmetric_copy_bf16_correction_fp64_vectors_fp32_u",
+             3: "symmetric_copy_bf16_correction_fp64_vectors", 2: "symmetric_copy_bf16_correction",
              1: "symmetric_copy", 0: "hi_plane"}
     u64 = u.double()
     v64 = torch.empty_like(u64)
-    for sym in (3, 2, 1, 0):
+    for sym in (4, 3, 2, 1, 0):
         A.set_symmetric_inner(sym)
 
         def product():
-            if sym == 3:  # FP64 vectors, double-float products (the inner product of format 3)
+            if sym >= 3:  # FP64 vectors (the inner products of formats 3 and 4)
                 A.matvec_inner_device(v64.data_ptr(), u64.data_ptr(), stream_ptr)
             else:
                 A.matvec_device_f32(v.data_ptr(), u.data_ptr(), stream_ptr)
@@ -377,7 +378,7 @@ def measure_inner_f32(A, m, steps, warmup):
         ke = info["sym_bytes"] if sym else info["ke_bytes"] // 2
         if sym and not ke:
             continue  # no symmetric copy for this operator
-        vec = base + 8 * m.n_dofs if sym == 3 else base  # FP64 u and v
+        vec = base + 8 * m.n_dofs if sym >= 3 else base  # FP64 u and v
         out[names[sym]] = {
             "ms": ms, "ke_bytes": ke, "streamed_gbs": (ke + vec) / (ms * 1e-3) / 1e9}
     A.set_symmetric_inner(1)
@@ -699,7 +700,8 @@ def run_solve(args, w, rank, world, local_rank):
     r["mixed"]["inner_arena"] = ("matrix-free (method 2): Ke integrated from coordinates" if args.free else
                                  {0: "hi plane", 1: "symmetric copy, FP32",
                                   2: "symmetric copy, FP32 + BF16 correction",
-                                  3: "symmetric copy, FP32 + BF16 correction; FP64 inner vectors"}[
+                                  3: "symmetric copy, FP32 + BF16 correction; FP64 inner vectors",
+                                  4: "symmetric copy, FP32 + BF16 correction; FP64 inner vectors, FP32 u"}[
                                      A.info()["sym_available"]])
     out = {"metric": "CG solves/s at %g rel. residual" % rtol, "value": smx, "unit": "solves/s", "n_gpus": world,
            "steps": args.steps, "warmup": 1, "ms_per_step": 1e3 / smx, "higher_is_better": True, "scaling": "weak",
@@ -864,6 +866,7 @@ def new_server(dev, args):
     from amat_gb300.serve import Server
     srv = Server(dev)
     srv.set_lane(int(args.lane_mb * 2 ** 20), 32)
+    srv.set_inner_format(args.serve_format)
     return srv
 
 
@@ -967,7 +970,7 @@ def run_serve(args, w, rank, world, local_rank):
                                                                   args.edge_max),
                       "n_dofs_range": [int(min(sizes)), int(max(sizes))], "rtol": args.rtol,
                       "inner_rtol": args.serve_inner, "admission": "FIFO by HBM budget (85% of free), 64 slots",
-                      "lane_mb": args.lane_mb},
+                      "lane_mb": args.lane_mb, "inner_format": args.serve_format},
            "rates": lines, "p50_ms": best["p50_ms"], "p99_ms": best["p99_ms"], "plain_fp64_sequential": plain,
            "served_one_at_a_time": alone,
            "speedup_vs_plain": best["solves_per_s"] / plain["solves_per_s"]}
@@ -994,6 +997,8 @@ def main():
     ap.add_argument("--requests", type=int, default=48, help="serve: requests per rate")
     ap.add_argument("--edge-max", type=int, default=96, help="serve: largest mesh edge")
     ap.add_argument("--serve-inner", type=float, default=0.3, help="serve: FP32 reduction between FP64 updates")
+    ap.add_argument("--serve-format", type=int, default=3, choices=[0, 1, 2, 3],
+                    help="serve: symmetric inner format of the requests on their own streams")
     ap.add_argument("--lane-mb", type=float, default=8.0,
                     help="serve: requests with at most this many MB of FP32 element matrices share lane launches")
     ap.add_argument("--nrhs", type=int, default=64)
@@ -1004,7 +1009,7 @@ def main():
     ap.add_argument("--rtol", type=float, default=1e-8)
     ap.add_argument("--free", type=int, default=0, help="solve: mixed solve on the matrix-free operator (method 2)")
     ap.add_argument("--inner-rtol", type=float, default=1e-2)
-    ap.add_argument("--sym-format", type=int, default=1, choices=[0, 1, 2, 3],
+    ap.add_argument("--sym-format", type=int, default=1, choices=[0, 1, 2, 3, 4],
                     help="solve: inner arena (1 symmetric FP32, 2 with BF16 correction, 0 hi plane; 3 the arena "
                          "of 2 with FP64 inner vectors)")
     ap.add_argument("--load", default="example", choices=["example", "random"],

@@ -187,6 +187,8 @@ int afm_set_patch_mode(afm_operator* op, int mode);
  * solve's inner recursion in FP64 vectors with double-float products from it
  * (about 40% of the split arena's bytes per product, no FP32 rounding of the
  * vectors), for large ill-conditioned systems whose FP32 recursion stalls.
+ * format = 4: as 3, but the products are those of format 2 on u rounded to
+ * FP32 (summed into v in FP64): cheaper products, u perturbed by 2^-24.
  * format = 0: FP32 products read the hi plane. The copy is
  * built on the device from the split arena by the first FP32 product or
  * mixed-precision solve after a change (outside any stream capture). FP64
@@ -259,10 +261,11 @@ int afm_matvec_device(afm_operator* op, double* d_v, const double* d_u, void* st
  * or its hi plane (the FP32-rounded Ke); or, for the matrix-free operator,
  * by the element kernels in FP32. */
 int afm_matvec_device_f32(afm_operator* op, float* d_v, const float* d_u, void* stream);
-/* The inner product of symmetric inner format 3 on double device vectors:
- * double-float products from the corrected symmetric arena (K to about
- * 2^-32), what the FP64-vector mixed solve iterates on. FP64_SPLIT operators
- * with symmetric element matrices, after afm_set_symmetric_inner(op, 3). */
+/* The inner product of symmetric inner format 3 or 4 on double device
+ * vectors (what the FP64-vector mixed solve iterates on): from the corrected
+ * symmetric arena (K to about 2^-32), double-float products of u (3) or of u
+ * rounded to FP32 (4). FP64_SPLIT operators with symmetric element matrices,
+ * after afm_set_symmetric_inner(op, 3 or 4). */
 int afm_matvec_inner_device(afm_operator* op, double* d_v, const double* d_u, void* stream);
 
 /* aMatFree::MatMult_mf (include/aMatFree.hpp:3894-3941): u_c taken as zero
@@ -448,6 +451,11 @@ int afm_server_destroy(afm_server* s);
  * 32 by default, per launch); larger requests run on their own streams. Takes
  * effect for requests admitted afterwards. */
 int afm_server_set_lane(afm_server* s, uint64_t max_ke_bytes, uint32_t iters_per_launch);
+/* Symmetric inner format (afm_set_symmetric_inner) of the requests that run
+ * on their own streams: 3 by default (FP64 inner vectors on the corrected
+ * symmetric arena), 0 to 2 as afm_set_symmetric_inner. Takes effect for
+ * requests started afterwards. */
+int afm_server_set_inner_format(afm_server* s, int format);
 typedef struct {
     uint64_t lane_launches;       /* serving-lane launches */
     uint64_t lane_solve_launches; /* requests carried, summed over those launches */

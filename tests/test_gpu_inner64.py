@@ -1,6 +1,7 @@
-"""Symmetric inner format 3: the mixed-precision solve's inner recursion in FP64
-vectors on double-float products from the corrected symmetric arena (each
-symmetric pair of Ke entries once, as FP32 + BF16: K to about 2^-32). The
+"""Symmetric inner formats 3 and 4: the mixed-precision solve's inner recursion
+in FP64 vectors on products from the corrected symmetric arena (each symmetric
+pair of Ke entries once, as FP32 + BF16: K to about 2^-32), of the FP64 u as a
+double-float pair (3) or of u rounded to FP32 (4). The
 product against the oracle for every kernel that reads the arena (warp-group
 elements, patches), its exact power-of-two scaling, and the solve checked in
 FP64 against the oracle's MatMult_mf."""
@@ -33,11 +34,12 @@ def operator(kind, n, bc=False, seed=3, fmt=3):
     return m, ke, dofs, vals, A
 
 
+@pytest.mark.parametrize("fmt", [3, 4])
 @pytest.mark.parametrize("kind,n", [(P.HEX20_ELASTIC, 5), (P.HEX8_ELASTIC, 8), (P.TET10_ELASTIC, 4),
                                     (P.HEX8_POISSON, 10), (P.TET10_POISSON, 6)])
-def test_inner_product_matches_oracle(gpu, kind, n):
+def test_inner_product_matches_oracle(gpu, kind, n, fmt):
     import torch
-    m, ke, _, _, A = operator(kind, n)
+    m, ke, _, _, A = operator(kind, n, fmt=fmt)
     u = np.random.default_rng(n).uniform(-1, 1, m.n_dofs)
     du = torch.tensor(u, device="cuda")
     dv = torch.full_like(du, float("nan"))
@@ -45,7 +47,10 @@ def test_inner_product_matches_oracle(gpu, kind, n):
     A.synchronize()
     v = dv.cpu().numpy()
     ref = oracle.Problem(m.n_dofs, m.dof_map(), ke).matvec(u)
-    assert rel(v, ref) < INNER_RTOL
+    # format 4 rounds u to FP32 (2^-24 of each entry)
+    assert rel(v, ref) < (INNER_RTOL if fmt == 3 else 1e-6)
+    if fmt == 4:
+        return
     # u scaled by powers of two far from 1: the product scales exactly
     for k in (-600, 600):
         du2 = du * 2.0 ** k
@@ -64,12 +69,13 @@ def test_inner_product_needs_format_3(gpu):
     assert e.value.name == "ERR_STATE"
 
 
+@pytest.mark.parametrize("fmt", [3, 4])
 @pytest.mark.parametrize("kind,n", [(P.HEX20_ELASTIC, 8), (P.HEX8_ELASTIC, 12)])
-def test_format3_mixed_solve(gpu, kind, n):
+def test_fp64_vector_mixed_solve(gpu, kind, n, fmt):
     """The FP64-vector inner recursion converges to the FP64-checked tolerance in about the FP64 CG's
     iteration count (random loads on the elastic bar with its six point constraints)."""
     rtol = 1e-8
-    m, ke, dofs, vals, A = operator(kind, n, bc=True)
+    m, ke, dofs, vals, A = operator(kind, n, bc=True, fmt=fmt)
     b = np.random.default_rng(7).normal(size=m.n_dofs)
     b[dofs.astype(np.int64)] = vals
     _, s64 = A.solve(b, rtol=rtol, atol=0.0, maxit=100000)
