@@ -54,6 +54,8 @@ WORKLOADS = {
                              desc="tet10 Poisson 64^3 x 6 (1.57M tets), 10x10 Ke"),
     "tet10_elastic_64": dict(kind=4, n=64, ngt=2, jitter=0.15, seed=2,
                              desc="tet10 elasticity 64^3 x 6 (1.57M tets), 30x30 Ke, E=1, nu=0.3"),
+    "tet10_elastic_96": dict(kind=4, n=96, ngt=2, jitter=0.15, seed=2,
+                             desc="tet10 elasticity 96^3 x 6 (5.3M tets), 30x30 Ke, E=1, nu=0.3"),
     "hex8_poisson_96": dict(kind=0, n=96, ngt=2, jitter=0.1, seed=0,
                             desc="hex8 Poisson 96^3, 8x8 FP64 Ke, 2x2x2 Gauss, jitter 0.1h"),
 }
