@@ -24,7 +24,7 @@ ORACLE_LIB = os.path.join(ORACLE_DIR, "_build", "liboracle.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fopenmp", "--expt-relaxed-constexpr"] + ARCH
-CU_SOURCES = ["afm_mv_fp64.cu", "afm_mv_split.cu", "afm_mv_fp32.cu", "afm_mv_f32sym.cu", "afm_mv_f32symx.cu", "afm_mv_splitsymx.cu",
+CU_SOURCES = ["afm_mv_fp64.cu", "afm_mv_split.cu", "afm_mv_fp32.cu", "afm_mv_f32sym.cu", "afm_mv_f32symx.cu", "afm_mv_splitsymx.cu", "afm_mv_f32symc.cu",
               "afm_solver.cu",
               "afm_batched_solver.cu", "afm_batched_tc.cu", "afm_lane.cu", "afm_noalloc.cu", "afm_spmv.cu", "afm_free.cu", "afm_capi.cpp", "afm_server.cpp",
               "afm_assembled.cpp"]

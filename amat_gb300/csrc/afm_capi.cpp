@@ -68,6 +68,13 @@ cudaError_t launch_segment_splitsymx(const Segment& s, const SegArgs& a, int sm_
 cudaError_t launch_patches_splitsymx(const PatchPlanGeom& pg, const PatchArgs& a, int sm_count, bool pdl,
                                      cudaStream_t st);
 cudaError_t configure_kernels_splitsymx();
+cudaError_t launch_segment_f32symc(const Segment& s, const SegArgs& a, int sm_count, bool dup, bool pdl,
+                                   cudaStream_t st);
+cudaError_t launch_patches_f32symc(const PatchPlanGeom& pg, const PatchArgs& a, int sm_count, bool pdl,
+                                   cudaStream_t st);
+cudaError_t configure_kernels_f32symc();
+size_t patch_smem_f32symc(const PatchPlanGeom& pg, uint32_t copy_bytes);
+size_t segment_smem_f32symc(const Segment& s);
 size_t patch_smem_splitsymx(const PatchPlanGeom& pg, uint32_t copy_bytes);
 size_t segment_smem_splitsymx(const Segment& s);
 size_t patch_smem_f32sym(const PatchPlanGeom& pg, uint32_t copy_bytes);
@@ -84,6 +91,7 @@ cudaError_t launch_patches(int prec, const PatchPlanGeom& pg, const PatchArgs& a
         case kPrecF32Sym: return launch_patches_f32sym(pg, a, sm_count, pdl, stream);
         case kPrecF32SymX: return launch_patches_f32symx(pg, a, sm_count, pdl, stream);
         case kPrecSplitSymX: return launch_patches_splitsymx(pg, a, sm_count, pdl, stream);
+        case kPrecF32SymC: return launch_patches_f32symc(pg, a, sm_count, pdl, stream);
         default: return launch_patches_fp32(pg, a, sm_count, pdl, stream);
     }
 }
@@ -95,6 +103,7 @@ size_t patch_smem_bytes(int prec, const PatchPlanGeom& pg, uint32_t copy_bytes) 
         case kPrecF32Sym: return patch_smem_f32sym(pg, copy_bytes);
         case kPrecF32SymX: return patch_smem_f32symx(pg, copy_bytes);
         case kPrecSplitSymX: return patch_smem_splitsymx(pg, copy_bytes);
+        case kPrecF32SymC: return patch_smem_f32symc(pg, copy_bytes);
         default: return patch_smem_fp32(pg, copy_bytes);
     }
 }
@@ -111,6 +120,7 @@ cudaError_t launch_segment(const Segment& s, int prec, const SegArgs& a, int sm_
         case kPrecF32Sym: return launch_segment_f32sym(s, a, sm_count, dup, pdl, stream);
         case kPrecF32SymX: return launch_segment_f32symx(s, a, sm_count, dup, pdl, stream);
         case kPrecSplitSymX: return launch_segment_splitsymx(s, a, sm_count, dup, pdl, stream);
+        case kPrecF32SymC: return launch_segment_f32symc(s, a, sm_count, dup, pdl, stream);
         default: return launch_segment_fp32(s, a, sm_count, dup, pdl, stream);
     }
 }
@@ -122,6 +132,7 @@ size_t segment_smem_bytes(const Segment& s, int prec) {
         case kPrecF32Sym: return segment_smem_f32sym(s);
         case kPrecF32SymX: return segment_smem_f32symx(s);
         case kPrecSplitSymX: return segment_smem_splitsymx(s);
+        case kPrecF32SymC: return segment_smem_f32symc(s);
         default: return segment_smem_fp32(s);
     }
 }
@@ -665,7 +676,7 @@ void layout_sym(afm_operator* op, int mode) {
 // none, they read the hi plane).
 int sym_format(const afm_operator* op) { return op->sym_ok ? op->sym_mode : 0; }
 
-// The arena the format needs: formats 3 and 4 (FP64 inner vectors) read the
+// The arena the format needs: formats 3 to 5 (FP64 inner vectors) read the
 // corrected arena of format 2.
 int sym_arena(const afm_operator* op) {
     const int f = sym_format(op);
@@ -833,18 +844,18 @@ int enqueue_matvec(afm_operator* op, void* d_v, const void* d_u, int bc_mode, cu
     // each unit is copied). inner64: FP64 vectors on the corrected symmetric
     // arena (it must be built): format 3, double-float products of the FP64 u;
     // format 4, the products of format 2 on u rounded to FP32, summed into v
-    // in FP64.
+    // in FP64; format 5, as 4 with the element rows summed in plain FP32.
     const bool sym = (f32 || inner64) && op->d_sym != nullptr;
     const bool symx = sym && op->sym_built == 2;
     if (inner64 && !symx) return fail(AFM_ERR_STATE, "FP64 inner product without the corrected symmetric arena");
-    const bool inner_f32u = inner64 && sym_format(op) == 4;
+    const bool inner_f32u = inner64 && sym_format(op) >= 4;
     if (inner_f32u) {
         if (op->work64i_elems < 8ull * op->n_dofs) return fail(AFM_ERR_STATE, "format 4 product without its buffer");
         float* u32 = reinterpret_cast<float*>(op->d_work64i + 7ull * op->n_dofs);
         AFM_CUDA(launch_to_f32(u32, static_cast<const double*>(d_u), op->n_dofs, st));
         d_u = u32;
     }
-    const int kprec = inner64 ? (inner_f32u ? kPrecF32SymX : kPrecSplitSymX)
+    const int kprec = inner64 ? (inner_f32u ? (sym_format(op) == 5 ? kPrecF32SymC : kPrecF32SymX) : kPrecSplitSymX)
                               : sym ? (symx ? kPrecF32SymX : kPrecF32Sym) : f32 ? AFM_PREC_FP32 : op->precision;
     const size_t vbytes = (size_t)op->n_dofs * (f32 || kprec == AFM_PREC_FP32 ? 4 : 8);
     // the corrected format's FP32 products sum into an FP64 vector, rounded to FP32 at the end
@@ -1443,7 +1454,7 @@ int mixed_begin(MixedSolve& m) {
     DeviceGuard g(op->device);
     int s = ensure_work(op, 8);
     if (s) return s;
-    m.inner64 = !m.lane && op->matfree_type != 2 && (sym_format(op) == 3 || sym_format(op) == 4);
+    m.inner64 = !m.lane && op->matfree_type != 2 && sym_format(op) >= 3;
     s = m.inner64 ? ensure_work64i(op, 8) : ensure_work32(op, 7);
     if (s) return s;
     if (!m.lane) {
@@ -1675,7 +1686,8 @@ int afm_create(afm_operator** out, int bc_method, int device) {
     // kernels' shared-memory limits, before any launch or graph capture
     if (configure_kernels_fp64() != cudaSuccess || configure_kernels_split() != cudaSuccess ||
         configure_kernels_fp32() != cudaSuccess || configure_kernels_f32sym() != cudaSuccess ||
-        configure_kernels_f32symx() != cudaSuccess || configure_kernels_splitsymx() != cudaSuccess)
+        configure_kernels_f32symx() != cudaSuccess || configure_kernels_splitsymx() != cudaSuccess ||
+        configure_kernels_f32symc() != cudaSuccess)
         return fail(AFM_ERR_CUDA, "kernel configuration failed on device %d", device);
     auto* op = new afm_operator();
     op->device = device;
@@ -1764,7 +1776,7 @@ int afm_set_wait_probe(afm_operator* op, int enable) {
 
 int afm_set_symmetric_inner(afm_operator* op, int format) {
     AFM_CHECK_OP(op);
-    if (format < 0 || format > 4) return fail(AFM_ERR_INVALID_ARG, "symmetric inner format %d (0 to 4)", format);
+    if (format < 0 || format > 5) return fail(AFM_ERR_INVALID_ARG, "symmetric inner format %d (0 to 5)", format);
     op->sym_mode = format;
     if (op->d_sym && op->sym_built != sym_arena(op)) {
         DeviceGuard g(op->device);
@@ -2261,7 +2273,7 @@ int afm_matvec_inner_device(afm_operator* op, double* d_v, const double* d_u, vo
     AFM_CHECK_OP(op);
     if (!op->finalized) return fail(AFM_ERR_STATE, "matvec before finalize");
     if (op->precision != AFM_PREC_FP64_SPLIT || op->matfree_type == 2 || sym_format(op) < 3)
-        return fail(AFM_ERR_STATE, "the FP64 inner product needs an FP64_SPLIT operator in symmetric inner format 3 or 4");
+        return fail(AFM_ERR_STATE, "the FP64 inner product needs an FP64_SPLIT operator in symmetric inner format 3 to 5");
     if (!d_v || !d_u || (void*)d_v == (const void*)d_u) return fail(AFM_ERR_INVALID_ARG, "bad vectors");
     DeviceGuard g(op->device);
     cudaStream_t st = pick_stream(op, stream);

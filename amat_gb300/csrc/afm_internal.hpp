@@ -186,6 +186,8 @@ constexpr int kPrecF32Sym = 16;
 constexpr int kPrecF32SymX = 17;
 // FP64 vectors, double-float products from that corrected arena (ArithSplitSymX).
 constexpr int kPrecSplitSymX = 18;
+// The corrected arena on FP32 u with FP32 row sums and FP64 v (ArithF32SymC).
+constexpr int kPrecF32SymC = 19;
 
 // Fills segment s's part of the symmetric inner arena from its split-arena
 // units (afm_mv_f32sym.cu).

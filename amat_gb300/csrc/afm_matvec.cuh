@@ -329,6 +329,31 @@ struct ArithF32SymX {
     }
 };
 
+// Products from the corrected symmetric arena on u rounded to FP32, each
+// element row summed in plain FP32 ((hi + lo) u as two FMAs) and the rows
+// summed into v in FP64: the inner product of symmetric inner format 5. Ke
+// keeps its 2^-32 representation; the row sums are rounded to FP32, which
+// perturbs the product far less than rounding Ke (emulated on hex20 12^3:
+// FP32 Ke alone +50% CG iterations, FP32 sums on top of it +10%).
+struct ArithF32SymC {
+    static constexpr bool kSym = true;
+    static constexpr bool kScaled = false;
+    static constexpr uint32_t kWpgWarps = 24;
+    using KT = float2;  // (hi, lo)
+    using UT = float;
+    using VT = float;
+    using VO = double;
+    struct Acc { float s; };
+    static __device__ __forceinline__ KT kload(const unsigned char* slot, size_t i, uint32_t plane) {
+        return ArithF32SymX::kload(slot, i, plane);
+    }
+    static __device__ __forceinline__ Acc zero() { return {0.0f}; }
+    static __device__ __forceinline__ UT stage(VT x) { return x; }
+    static __device__ __forceinline__ void fma(Acc& a, KT k, UT u) { a.s = __fmaf_rn(k.x, u, __fmaf_rn(k.y, u, a.s)); }
+    static __device__ __forceinline__ VO finish(const Acc& a) { return (double)a.s; }
+    static __device__ __forceinline__ void combine(Acc& a, const Acc& b) { a.s += b.s; }
+};
+
 // FP64 products from the corrected symmetric arena (the arena of ArithF32SymX:
 // K to about 2^-32, each pair of entries once): u and v are FP64 vectors, u is
 // staged as a scaled float pair like the split arithmetic, and each product

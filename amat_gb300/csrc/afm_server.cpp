@@ -106,11 +106,12 @@ constexpr uint64_t kLaneMaxBytes = 8ull << 20;
 constexpr uint32_t kLaneIters = 32;
 
 // Requests on their own streams iterate in FP64 vectors on the corrected
-// symmetric arena (format 3): the FP32 recursion stalls on the large elastic
+// symmetric arena (format 4): the FP32 recursion stalls on the large elastic
 // requests of a serving mix (hex20 elasticity 64^3 under a random load: 100,053
-// FP32 iterations against 6,209 for FP64 CG; 6,384 in format 3), and costs
-// Poisson requests, which converge in few iterations either way, little.
-constexpr int kStreamInnerFormat = 3;
+// FP32 iterations against 6,209 for FP64 CG; 6,385 in format 4, whose product
+// takes 0.71 ms against 1.36 ms for the split product), and costs Poisson
+// requests, which converge in few iterations either way, little.
+constexpr int kStreamInnerFormat = 4;
 
 }  // namespace
 
@@ -551,7 +552,7 @@ int afm_server_set_lane(afm_server* s, uint64_t max_ke_bytes, uint32_t iters_per
 
 int afm_server_set_inner_format(afm_server* s, int format) {
     if (!s) return afm::set_error(AFM_ERR_INVALID_ARG, "null server");
-    if (format < 0 || format > 3) return afm::set_error(AFM_ERR_INVALID_ARG, "inner format %d (0 to 3)", format);
+    if (format < 0 || format > 5) return afm::set_error(AFM_ERR_INVALID_ARG, "inner format %d (0 to 5)", format);
     std::lock_guard<std::mutex> lk(s->state_mu);
     s->inner_format = format;
     return afm::set_error(AFM_SUCCESS, "");

@@ -38,9 +38,9 @@ class Server:
         check(self._lib.afm_server_set_lane(self._h, int(max_ke_bytes), int(iters_per_launch)),
               "afm_server_set_lane")
 
-    def set_inner_format(self, fmt=3):
-        """Symmetric inner format of the requests on their own streams (3: FP64 inner vectors on the corrected
-        symmetric arena; 0 to 2 as aMatFree.set_symmetric_inner)."""
+    def set_inner_format(self, fmt=4):
+        """Symmetric inner format of the requests on their own streams (4: FP64 inner vectors on the corrected
+        symmetric arena; 0 to 5 as aMatFree.set_symmetric_inner)."""
         check(self._lib.afm_server_set_inner_format(self._h, int(fmt)), "afm_server_set_inner_format")
 
     def info(self):

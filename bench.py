@@ -353,12 +353,13 @@ def measure_inner_f32(A, m, steps, warmup):
     v = torch.empty_like(u)
     base = 4 * m.n_elem * m.ndpe + 8 * m.n_dofs  # map entries, u read, v written
     out = {}
-    names = {4: "symmetric_copy_bf16_correction_fp64_vectors_fp32_u",
+    names = {5: "symmetric_copy_bf16_correction_fp64_vectors_fp32_u_fp32_rows",
+             4: "symmetric_copy_bf16_correction_fp64_vectors_fp32_u",
              3: "symmetric_copy_bf16_correction_fp64_vectors", 2: "symmetric_copy_bf16_correction",
              1: "symmetric_copy", 0: "hi_plane"}
     u64 = u.double()
     v64 = torch.empty_like(u64)
-    for sym in (4, 3, 2, 1, 0):
+    for sym in (5, 4, 3, 2, 1, 0):
         A.set_symmetric_inner(sym)
 
         def product():
@@ -660,7 +661,11 @@ def default_solves(args, dev):
     w2 = WORKLOADS["hex20_elastic_64"]
     m, dofs, vals, A = build_bc_problem(w2, dev)
     rhs = A.apply_bc(m.load(ngt=w2["ngt"]))
+    # the mixed solve of this ill-conditioned system iterates in FP64 vectors (symmetric inner format 4): its
+    # FP32 recursion stalls
+    A.set_symmetric_inner(4)
     r2, _, _ = solve_compare(A, m, rhs, 1e-10, 1, 0.3)
+    r2["mixed"]["inner_format"] = 4
     r2["workload"] = w2["desc"] + ", elastic bar: body load and end traction, clamped end"
     r2["n_dofs"] = m.n_dofs
     out["config2_cg_1e-10"] = r2
@@ -703,7 +708,9 @@ def run_solve(args, w, rank, world, local_rank):
                                  {0: "hi plane", 1: "symmetric copy, FP32",
                                   2: "symmetric copy, FP32 + BF16 correction",
                                   3: "symmetric copy, FP32 + BF16 correction; FP64 inner vectors",
-                                  4: "symmetric copy, FP32 + BF16 correction; FP64 inner vectors, FP32 u"}[
+                                  4: "symmetric copy, FP32 + BF16 correction; FP64 inner vectors, FP32 u",
+                                  5: "symmetric copy, FP32 + BF16 correction; FP64 inner vectors, FP32 u, "
+                                     "FP32 row sums"}[
                                      A.info()["sym_available"]])
     out = {"metric": "CG solves/s at %g rel. residual" % rtol, "value": smx, "unit": "solves/s", "n_gpus": world,
            "steps": args.steps, "warmup": 1, "ms_per_step": 1e3 / smx, "higher_is_better": True, "scaling": "weak",
@@ -999,7 +1006,7 @@ def main():
     ap.add_argument("--requests", type=int, default=48, help="serve: requests per rate")
     ap.add_argument("--edge-max", type=int, default=96, help="serve: largest mesh edge")
     ap.add_argument("--serve-inner", type=float, default=0.3, help="serve: FP32 reduction between FP64 updates")
-    ap.add_argument("--serve-format", type=int, default=3, choices=[0, 1, 2, 3],
+    ap.add_argument("--serve-format", type=int, default=4, choices=[0, 1, 2, 3, 4, 5],
                     help="serve: symmetric inner format of the requests on their own streams")
     ap.add_argument("--lane-mb", type=float, default=8.0,
                     help="serve: requests with at most this many MB of FP32 element matrices share lane launches")
@@ -1011,7 +1018,7 @@ def main():
     ap.add_argument("--rtol", type=float, default=1e-8)
     ap.add_argument("--free", type=int, default=0, help="solve: mixed solve on the matrix-free operator (method 2)")
     ap.add_argument("--inner-rtol", type=float, default=1e-2)
-    ap.add_argument("--sym-format", type=int, default=1, choices=[0, 1, 2, 3, 4],
+    ap.add_argument("--sym-format", type=int, default=1, choices=[0, 1, 2, 3, 4, 5],
                     help="solve: inner arena (1 symmetric FP32, 2 with BF16 correction, 0 hi plane; 3 the arena "
                          "of 2 with FP64 inner vectors)")
     ap.add_argument("--load", default="example", choices=["example", "random"],

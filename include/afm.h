@@ -189,6 +189,8 @@ int afm_set_patch_mode(afm_operator* op, int mode);
  * vectors), for large ill-conditioned systems whose FP32 recursion stalls.
  * format = 4: as 3, but the products are those of format 2 on u rounded to
  * FP32 (summed into v in FP64): cheaper products, u perturbed by 2^-24.
+ * format = 5: as 4 with each element row summed in plain FP32 ((hi + lo) u as
+ * two FMAs; the rows summed into v in FP64): the cheapest FP64-vector product.
  * format = 0: FP32 products read the hi plane. The copy is
  * built on the device from the split arena by the first FP32 product or
  * mixed-precision solve after a change (outside any stream capture). FP64
@@ -261,11 +263,11 @@ int afm_matvec_device(afm_operator* op, double* d_v, const double* d_u, void* st
  * or its hi plane (the FP32-rounded Ke); or, for the matrix-free operator,
  * by the element kernels in FP32. */
 int afm_matvec_device_f32(afm_operator* op, float* d_v, const float* d_u, void* stream);
-/* The inner product of symmetric inner format 3 or 4 on double device
+/* The inner product of symmetric inner formats 3 to 5 on double device
  * vectors (what the FP64-vector mixed solve iterates on): from the corrected
  * symmetric arena (K to about 2^-32), double-float products of u (3) or of u
- * rounded to FP32 (4). FP64_SPLIT operators with symmetric element matrices,
- * after afm_set_symmetric_inner(op, 3 or 4). */
+ * rounded to FP32 (4), or FP32 row sums of u rounded to FP32 (5). FP64_SPLIT
+ * operators with symmetric element matrices, after afm_set_symmetric_inner. */
 int afm_matvec_inner_device(afm_operator* op, double* d_v, const double* d_u, void* stream);
 
 /* aMatFree::MatMult_mf (include/aMatFree.hpp:3894-3941): u_c taken as zero
@@ -452,8 +454,8 @@ int afm_server_destroy(afm_server* s);
  * effect for requests admitted afterwards. */
 int afm_server_set_lane(afm_server* s, uint64_t max_ke_bytes, uint32_t iters_per_launch);
 /* Symmetric inner format (afm_set_symmetric_inner) of the requests that run
- * on their own streams: 3 by default (FP64 inner vectors on the corrected
- * symmetric arena), 0 to 2 as afm_set_symmetric_inner. Takes effect for
+ * on their own streams: 4 by default (FP64 inner vectors on the corrected
+ * symmetric arena), 0 to 5 as afm_set_symmetric_inner. Takes effect for
  * requests started afterwards. */
 int afm_server_set_inner_format(afm_server* s, int format);
 typedef struct {
