@@ -1635,6 +1635,23 @@ int mixed_end(MixedSolve& m, afm_solve_stats* stats) {
 
 }  // namespace afm
 
+int afm::set_stream_priority(afm_operator* op, int priority) {
+    AFM_CHECK_OP(op);
+    DeviceGuard g(op->device);
+    cudaStream_t st = nullptr;
+    AFM_CUDA(cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, priority));
+    if (cudaStreamSynchronize(op->stream) != cudaSuccess) {
+        cudaStreamDestroy(st);
+        return fail(AFM_ERR_CUDA, "stream priority: %s", cudaGetErrorString(cudaGetLastError()));
+    }
+    cudaStreamDestroy(op->stream);
+    op->stream = st;
+    drop_graph(op->cg64);  // no captured iteration keeps the old stream's work order
+    drop_graph(op->cg32);
+    drop_graph(op->cg64i);
+    return ok();
+}
+
 extern "C" {
 
 const char* afm_last_error(void) { return g_last_error.c_str(); }

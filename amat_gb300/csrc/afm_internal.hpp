@@ -238,6 +238,11 @@ struct LaneJob {
 // its sc.
 cudaError_t launch_lane(const LaneJob* d_jobs, uint32_t n_jobs, uint32_t iters, cudaStream_t st);
 
+// Replaces the operator's stream by one of the given priority (lower numbers
+// run first, cudaDeviceGetStreamPriorityRange), after the old stream's work
+// has finished. Call before any solve has captured work on the stream.
+int set_stream_priority(afm_operator* op, int priority);
+
 // Records the calling thread's last error message (returned by
 // afm_last_error) and returns status.
 int set_error(int status, const char* fmt, ...);

@@ -142,6 +142,10 @@ struct afm_server {
     uint32_t lane_iters = kLaneIters;
     // symmetric inner format of the requests that run on their own streams
     int inner_format = kStreamInnerFormat;
+    // stream priorities (lower numbers first): the lane and small requests
+    // ahead of large ones, so that a small request's launches do not queue
+    // behind the many launches a large request has in flight
+    int prio_low = 0, prio_high = 0;
     cudaStream_t lane_stream = nullptr;
     cudaEvent_t lane_done = nullptr;
     bool lane_busy = false;
@@ -266,11 +270,17 @@ int build_lane_segs(Request* r) {
 }
 
 int start(afm_server* s, Request* r) {
-    (void)s;
     afm_operator* op = r->op;
     const size_t n = op->n_dofs;
     const bool lane = r->lane_candidate && op->precision == AFM_PREC_FP64_SPLIT && !op->use_patches &&
                       op->matfree_type != 2;
+    // priority by size: one level per factor 8 of element-matrix bytes above 8 MB
+    if (s->prio_high < s->prio_low) {
+        int level = 0;
+        for (uint64_t b = lane_bytes(op); b > (8ull << 20) && level < s->prio_low - s->prio_high; b >>= 3) level++;
+        const int st = afm::set_stream_priority(op, s->prio_high + level);
+        if (st != AFM_SUCCESS) return st;
+    }
     if (lane) {
         const int st = build_lane_segs(r);
         if (st != AFM_SUCCESS) return st;
@@ -439,7 +449,8 @@ int afm_server_create(afm_server** out, int device, uint64_t hbm_budget_bytes, u
     s->budget = hbm_budget_bytes ? hbm_budget_bytes : (uint64_t)(free_b * 0.85);
     s->reserve = std::min<uint64_t>(total_b / 50, 2ull << 30);
     s->max_active = max_active ? max_active : 64;
-    if (cudaStreamCreateWithFlags(&s->lane_stream, cudaStreamNonBlocking) != cudaSuccess ||
+    cudaDeviceGetStreamPriorityRange(&s->prio_low, &s->prio_high);
+    if (cudaStreamCreateWithPriority(&s->lane_stream, cudaStreamNonBlocking, s->prio_high) != cudaSuccess ||
         cudaEventCreateWithFlags(&s->lane_done, cudaEventDisableTiming) != cudaSuccess ||
         cudaMallocHost((void**)&s->h_jobs, sizeof(afm::LaneJob) * s->max_active) != cudaSuccess ||
         cudaMalloc((void**)&s->d_jobs, sizeof(afm::LaneJob) * s->max_active) != cudaSuccess) {
