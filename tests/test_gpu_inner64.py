@@ -83,7 +83,8 @@ def test_fp64_vector_mixed_solve(gpu, kind, n, fmt):
     assert st.status == 0 and st.rel_residual <= rtol
     pr = oracle.Problem(m.n_dofs, m.dof_map(), ke, dofs, vals)
     assert np.linalg.norm(b - pr.matmult_bc(x)) <= 1.01 * rtol * np.linalg.norm(b)
-    assert st.iterations <= 1.3 * s64.iterations + 20, (st.iterations, s64.iterations)
+    # format 5 rounds each element row's sum to FP32: a cheaper product, more iterations
+    assert st.iterations <= (1.3 if fmt != 5 else 1.6) * s64.iterations + 20, (st.iterations, s64.iterations)
     tr = A.solve_trace()
     assert len(tr) == st.refinements + 1 and tr[-1][1] <= rtol
     assert all(a[0] <= b_[0] for a, b_ in zip(tr, tr[1:]))
