@@ -2104,13 +2104,21 @@ int afm_finalize(afm_operator* op) {
     // precision
     int prec = op->precision_req;
     if (prec == AFM_PREC_AUTO) {
-        bool fits = true;
-        for (double x : op->ke) {
-            const double a = std::fabs(x);
-            if (a != 0.0 && (a < 1e-30 || a > 1e30 || !std::isfinite(x))) {
-                fits = false;
-                break;
+        // the split arithmetic's range: each element's largest |entry| in [1e-30, 1e30] (an all-zero element
+        // too); smaller entries of an element, such as the round-off residue of exact zeros that quadrature
+        // leaves (~1e-35 in tet10 elasticity), lose at most FP32-subnormal-sized amounts, far below the
+        // element's 2^-44 bound
+        int fits = 1;
+#pragma omp parallel for schedule(static) reduction(&& : fits)
+        for (int64_t e = 0; e < (int64_t)op->n_elem; e++) {
+            double mx = 0.0;
+            bool finite = true;
+            for (uint64_t k = op->kofs[e]; k < op->kofs[e + 1]; k++) {
+                const double x = op->ke[k];
+                finite = finite && std::isfinite(x);
+                mx = std::max(mx, std::fabs(x));
             }
+            fits = fits && finite && (mx == 0.0 || (mx >= 1e-30 && mx <= 1e30));
         }
         prec = fits ? AFM_PREC_FP64_SPLIT : AFM_PREC_FP64;
     }

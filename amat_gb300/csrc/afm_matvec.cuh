@@ -396,8 +396,10 @@ struct ArithSplitSymX {
 // entries would fall into FP32 subnormals and lose their low bits. So every
 // launch scales u by 2^k with k = -eu, max|u| = f 2^eu (f in [0.5, 1)), over
 // the DoFs the product reads: the largest scaled entry lies in [0.5, 1), and
-// with max|Ke| in [1e-30, 1e30] (checked at finalize) every product of a
-// scaled u entry and a Ke entry stays within FP32's normal range. The element
+// with each element's max|Ke| in [1e-30, 1e30] (checked at finalize) the
+// products of a scaled u entry and the element's leading entries stay within
+// FP32's normal range (smaller entries may reach FP32 subnormals, whose
+// absolute rounding, below 2^-149, is far under the element's error bound). The element
 // sums are scaled back by 2^-k in FP64. Both steps only move exponents, so
 // they are exact, and they run on the integer pipe (GB300 issues FP64 at 1/64
 // of the FP32 rate): the staged pair (hi, lo) of 2^k x is cut from the bits of

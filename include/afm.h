@@ -65,12 +65,13 @@ typedef enum afm_bc_method { AFM_BC_IMATRIX = 0, AFM_BC_PENALTY = 1 } afm_bc_met
  *                       taking the same 8 bytes per entry; the product runs
  *                       in double-float arithmetic (error-free TwoProduct and
  *                       TwoSum, Ogita, Rump & Oishi 2005) with FP64 gather and
- *                       scatter. About 2^-48 relative per entry; for Ke
- *                       entries whose magnitude lies within 1e-30..1e30.
+ *                       scatter. About 2^-48 relative per entry; for
+ *                       element matrices whose largest |entry| lies within
+ *                       1e-30..1e30 (smaller entries of the element are fine).
  *  AFM_PREC_FP32        Ke stored as float, FP32 multiply and accumulate, on
  *                       float vectors (afm_matvec_device_f32).
- * AFM_PREC_AUTO picks FP64_SPLIT when every Ke entry is in its range, FP64
- * otherwise. */
+ * AFM_PREC_AUTO picks FP64_SPLIT when every element matrix is in its range,
+ * FP64 otherwise. */
 typedef enum afm_precision {
     AFM_PREC_FP64 = 0,
     AFM_PREC_FP64_SPLIT = 1,

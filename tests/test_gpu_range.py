@@ -208,3 +208,24 @@ def test_solves_scale_exactly_with_the_load(gpu, k):
     assert (t1.iterations, t1.refinements) == (t2.iterations, t2.refinements)
     assert np.array_equal(y2, y1 * f)
     assert rel(y2 / f, x1) < 1e-7
+
+
+def test_split_accepts_tiny_entries_beside_large_ones(gpu):
+    """Quadrature leaves the exact zeros of an element matrix as ~1e-35 round-off (tet10 elasticity): the
+    split range is judged per element (its largest entry), so AUTO keeps the split arithmetic and the
+    product stays within the FP64 bar."""
+    m = P.Mesh(P.TET10_ELASTIC, 3, jitter=0.15, seed=2)
+    ke = m.element_matrices(ngt=2)
+    ke[0, 0, 5] = ke[0, 5, 0] = 3e-40  # a double below FP32's normal range, beside O(0.1) entries
+    ke[1, 2, 7] = 1e-36
+    A = _operator(m, ke, PRECISION.AUTO)
+    assert A.info()["precision"] == PRECISION.FP64_SPLIT
+    pr = oracle.Problem(m.n_dofs, m.dof_map(), ke)
+    u = np.random.default_rng(4).uniform(-1, 1, m.n_dofs)
+    v = np.empty(m.n_dofs)
+    A.matvec(v, u, True)
+    assert rel(v, pr.matvec(u)) < FP64_RTOL
+    # an element whose largest entry is below 1e-30 keeps the operator in FP64
+    ke2 = ke.copy()
+    ke2[3] *= 1e-35
+    assert _operator(m, ke2, PRECISION.AUTO).info()["precision"] == PRECISION.FP64
