@@ -2,8 +2,9 @@
 // include/afm.h; no counterpart in the reference).
 //
 // A request carries its own operator (maps and element matrices set on the
-// host) and load. Requests wait in a FIFO queue and are admitted while the
-// server's HBM budget, the device's free memory and the slot limit allow.
+// host) and load. Requests wait in a queue and are admitted, smallest first
+// (a request that has waited 2 s goes first), while the server's HBM budget,
+// the device's free memory and the slot limit allow.
 // Admission finalises the operator on a worker thread (colouring, patch plan,
 // upload of Ke and maps), so the polling thread never blocks on host work, and
 // then drops the operator's host copy of the element matrices.
@@ -55,6 +56,7 @@ struct Request {
     std::vector<double> b;
     double rtol = 1e-8, inner_rtol = 0.1;
     uint64_t est_bytes = 0;
+    uint64_t lane_bytes = 0;  // FP32 element-matrix bytes (lane eligibility, stream priority)
     int state = RQ_QUEUED;
     std::future<int> fin;
     double* d_bx = nullptr;  // b then x on the device
@@ -78,14 +80,15 @@ double now_s() {
 // Device bytes a request holds once admitted: element matrices (8 bytes per
 // entry in every arena but FP32, plus the symmetric inner copy of at most 6
 // bytes per stored pair), maps or patch index blocks, diagonal, the solver's
-// FP64 and FP32 work vectors, b and x; 10% and 1 MB of slack.
+// FP64 and FP32 work vectors (and the FP64 inner vectors of formats 3 to 5),
+// b and x; 10% and 1 MB of slack.
 uint64_t estimate_bytes(const afm_operator* op) {
     uint64_t ke = 0;
     for (uint32_t e = 0; e < op->n_elem; e++) {
         const uint64_t n = op->offsets[e + 1] - op->offsets[e];
         ke += n * n * 8 + 8 * n + 6 * n * (n / 2 + 1);
     }
-    const uint64_t vec = (uint64_t)op->n_dofs * (8 * 8 + 7 * 4 + 3 * 8);
+    const uint64_t vec = (uint64_t)op->n_dofs * (8 * 8 + 7 * 4 + 8 * 8 + 3 * 8);
     return (ke + vec) * 11 / 10 + (1u << 20);
 }
 
@@ -195,27 +198,48 @@ void finish(afm_server* s, Request* r, int status, const char* msg) {
 }
 
 // At most this many operators are finalised at once: each finalize runs
-// OpenMP loops over all host cores, and more in parallel only contend.
+// OpenMP loops over all host cores, and more in parallel only contend. Small
+// requests (the lane's) may use kExtraSmallFinalizing more slots, so that
+// they do not wait behind the seconds-long finalizes of large meshes.
 constexpr int kMaxFinalizing = 4;
+constexpr int kExtraSmallFinalizing = 2;
+// Admission order: shortest first (estimated device bytes), which keeps small
+// requests' latency independent of the large ones' finalize and solve time;
+// a request that has waited kAgingSeconds goes first (oldest first), so large
+// requests are never held back for long.
+constexpr double kAgingSeconds = 2.0;
 
-// admission: FIFO while the budget, free device memory and slots allow
+// Index in the queue of the next request to admit.
+size_t next_in_queue(const afm_server* s, double now) {
+    if (now - s->queue.front()->t_submit > kAgingSeconds) return 0;
+    size_t best = 0;
+    for (size_t i = 1; i < s->queue.size(); i++)
+        if (s->queue[i]->est_bytes < s->queue[best]->est_bytes) best = i;
+    return best;
+}
+
+// admission while the budget, free device memory and slots allow
 int admit(afm_server* s) {
     int admitted = 0;
     int finalizing = 0;
     for (const Request* r : s->active) finalizing += (r->state == RQ_ADMITTING);
-    while (!s->queue.empty() && s->active.size() < s->max_active && finalizing < kMaxFinalizing) {
-        Request* r = s->queue.front();
+    while (!s->queue.empty() && s->active.size() < s->max_active &&
+           finalizing < kMaxFinalizing + kExtraSmallFinalizing) {
+        const size_t k = next_in_queue(s, now_s());
+        Request* r = s->queue[k];
+        const bool small = s->lane_max_bytes > 0 && r->op->matfree_type != 2 && r->lane_bytes <= s->lane_max_bytes;
+        if (!small && finalizing >= kMaxFinalizing) break;
         size_t free_b = 0, total_b = 0;
         if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) break;
         const bool fits = s->in_use + r->est_bytes <= s->budget && r->est_bytes + s->reserve <= free_b;
         if (!fits && !s->active.empty()) break;  // wait for memory to free up
-        s->queue.pop_front();
+        s->queue.erase(s->queue.begin() + (std::ptrdiff_t)k);
         s->in_use += r->est_bytes;
         r->state = RQ_ADMITTING;
         r->t_admit = now_s();
         afm_operator* op = r->op;
         // lane requests run colour segments (the lane reads their units), never patches
-        r->lane_candidate = s->lane_max_bytes > 0 && op->matfree_type != 2 && lane_bytes(op) <= s->lane_max_bytes;
+        r->lane_candidate = small;
         if (r->lane_candidate) afm_set_patch_mode(op, 0);
         const int dev = s->device;
         r->fin = std::async(std::launch::async, [op, dev]() {
@@ -277,7 +301,7 @@ int start(afm_server* s, Request* r) {
     // priority by size: one level per factor 8 of element-matrix bytes above 8 MB
     if (s->prio_high < s->prio_low) {
         int level = 0;
-        for (uint64_t b = lane_bytes(op); b > (8ull << 20) && level < s->prio_low - s->prio_high; b >>= 3) level++;
+        for (uint64_t b = r->lane_bytes; b > (8ull << 20) && level < s->prio_low - s->prio_high; b >>= 3) level++;
         const int st = afm::set_stream_priority(op, s->prio_high + level);
         if (st != AFM_SUCCESS) return st;
     }
@@ -482,6 +506,7 @@ int afm_server_submit(afm_server* s, afm_operator* op, const double* b, double r
     r->rtol = rtol;
     r->inner_rtol = inner_rtol;
     r->est_bytes = estimate_bytes(op);
+    r->lane_bytes = lane_bytes(op);
     r->t_submit = now_s();
     s->queue.push_back(r);
     s->all[r->id] = r;

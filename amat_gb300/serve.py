@@ -1,5 +1,5 @@
 """Serving loop for many CG solves on different operators (afm_server_* in
-include/afm.h): FIFO admission by HBM budget, device-resident state, every
+include/afm.h): admission by HBM budget (smallest first, with aging), device-resident state, every
 admitted request advanced by the server's progress thread, on its own stream or,
 for small requests, in the serving lane (one launch for the FP32 iterations of
 all of them)."""

@@ -417,9 +417,10 @@ int afm_get_assembled_csr(afm_operator* op, uint64_t* nnz, uint64_t* row_ptr, ui
 /* ---- serving: many CG solves on different operators ----------------------
  * No counterpart in the reference. A request is an operator whose maps and
  * element matrices are set on the host (finalize not needed) and a load b
- * (host, n_dofs, boundary conditions applied). Requests wait in a FIFO queue
- * and are admitted while the HBM budget, the device's free memory and the
- * slot limit allow; admission finalises the operator on a worker thread. An
+ * (host, n_dofs, boundary conditions applied). Requests wait in a queue and
+ * are admitted smallest first (a request waiting 2 s goes first) while the HBM
+ * budget, the device's free memory and the slot limit allow; admission
+ * finalises the operator on a worker thread. An
  * admitted request keeps Ke, maps, b, x and its Krylov vectors on the device
  * and is solved by the mixed-precision solve (afm_solve_cg_mixed, to rtol,
  * FP64-checked). A progress thread of the server's own keeps admitting and
