@@ -755,13 +755,12 @@ __host__ __device__ inline uint32_t wpg_ubuf_bytes(uint32_t n, uint32_t ut) { re
 // Column groups of the warp-group kernel for gr row groups. Elements of two
 // row groups (33..64 DoFs) with 8-byte staged u (FP64 and split arithmetic)
 // take two column groups, so four warps share one element's long products;
-// elements of one row group (<= 32 DoFs) take one warp each: splitting their
-// short rows across warps only adds the cross-warp sum, while more elements in
-// flight per SM hide the gathers (hex8 elasticity, n = 24: 0.31 -> 0.19 ms at
-// 48^3). FP32 takes two column groups for one row group for the same reason
-// in reverse: its products are cheap and its gathers half as wide.
+// every other element takes one warp per row group: for short rows, splitting
+// them across warps only adds the cross-warp sum, while more elements in
+// flight per SM hide the gathers (hex8 elasticity, n = 24, at 48^3: split
+// product 0.31 -> 0.19 ms, FP32 products 0.19-0.22 -> 0.18-0.20 ms).
 __host__ __device__ constexpr uint32_t wpg_gc(uint32_t gr, uint32_t ut_bytes) {
-    return gr >= 3 ? 1u : (ut_bytes == 4 ? (gr >= 2 ? 1u : 2u) : (gr >= 2 ? 2u : 1u));
+    return gr == 2 && ut_bytes == 8 ? 2u : 1u;
 }
 
 // Terms [T0, T1) of row r of a symmetric element in the wrapped-diagonal
