@@ -547,6 +547,9 @@ __device__ __forceinline__ VT load_u_hint(const VT* u, uint32_t m, int bc_mode, 
 // last loaded with; see ring_wait).
 struct RingLayout {
     uint32_t slot_bytes, stages, warps, ubuf_bytes, extra_bytes;
+    // warp-group kernel: consecutive element units per ring slot, copied by
+    // one bulk copy (1 for the other kernels)
+    uint32_t chunk = 1;
     __host__ __device__ uint32_t bars_offset() const { return slot_bytes * stages; }
     __host__ __device__ uint32_t tags_offset() const { return bars_offset() + 16 * stages + 16; }
     __host__ __device__ uint32_t ubuf_offset() const { return tags_offset() + ((4 * stages + 15) & ~15u); }
@@ -785,6 +788,15 @@ __device__ __forceinline__ void sym_terms(typename A::Acc& acc, const unsigned c
     }
 }
 
+// Synchronises an element group: a one-warp group with __syncwarp, a larger
+// one with its named barrier (ids 1..15).
+__device__ __forceinline__ void group_sync(uint32_t id, uint32_t threads) {
+    if (threads == 32)
+        __syncwarp();
+    else
+        named_barrier(id, threads);
+}
+
 template <int NT, typename A>
 __global__ void __launch_bounds__((A::kWpgWarps + 1) * 32, 1)
     afm_wpg_kernel(SegArgs a, RingLayout L, GroupGeom G, uint32_t n_rt) {
@@ -820,18 +832,25 @@ __global__ void __launch_bounds__((A::kWpgWarps + 1) * 32, 1)
     }
     __syncthreads();
 
+    // ring slots hold chunks of E consecutive elements (one bulk copy each: the
+    // copies of small element units are issue-bound one by one); chunk c goes
+    // to group c % ng, which takes its elements in order
+    const uint32_t E = L.chunk;
+    const uint32_t nch = (cnt + E - 1) / E;
     if (warp == G.ng * G.g) {  // producer
         if (lane == 0) {
             const uint64_t pol = l2_evict_first_policy();
             uint32_t issued = 0;
-            for (uint32_t i = 0; i < cnt; i++) {
-                const uint32_t s = i % S;
-                if (i >= S && !mbar_wait_abortable(&empty[s], ((i / S) - 1) & 1, abort, a.wait_ns)) break;
-                tag[s] = i;
-                mbar_arrive_expect_tx(&full[s], a.copy_bytes);
-                bulk_load(smem + (size_t)s * L.slot_bytes, a.ke + (size_t)(begin + i) * a.unit_bytes, a.copy_bytes,
-                          &full[s], pol);
-                issued = i + 1;
+            for (uint32_t c = 0; c < nch; c++) {
+                const uint32_t s = c % S;
+                if (c >= S && !mbar_wait_abortable(&empty[s], ((c / S) - 1) & 1, abort, a.wait_ns)) break;
+                const uint32_t e0 = c * E, ne = min(E, cnt - e0);
+                tag[s] = c;
+                // E > 1 only for whole units (copy_bytes == unit_bytes), so the chunk is contiguous
+                mbar_arrive_expect_tx(&full[s], ne * a.copy_bytes);
+                bulk_load(smem + (size_t)s * L.slot_bytes, a.ke + (size_t)(begin + e0) * a.unit_bytes,
+                          ne * a.copy_bytes, &full[s], pol);
+                issued = c + 1;
             }
             allow_dependent_launch();
             if (*abort) atomicOr(a.err, kErrTimeout);
@@ -867,7 +886,9 @@ __global__ void __launch_bounds__((A::kWpgWarps + 1) * 32, 1)
         return rvalid ? ld_nc_hint(a.map + (size_t)(begin + i) * n + r, stream_pol) : 0u;
     };
 
-    uint32_t i = grp;
+    // the group's k-th element (CTA-relative), increasing in k
+    auto elem = [&](uint32_t k) { return (grp + (k / E) * G.ng) * E + k % E; };
+    uint32_t i = elem(0);
     if (gatherer && i < cnt) {
         dof_c = map_at(i);
         if (rvalid) {
@@ -875,25 +896,28 @@ __global__ void __launch_bounds__((A::kWpgWarps + 1) * 32, 1)
             ubuf(0)[r] = x;
             if constexpr (A::kSym) ubuf(0)[r + n] = x;
         }
-        if (i + G.ng < cnt) dof_n = map_at(i + G.ng);
+        if (elem(1) < cnt) dof_n = map_at(elem(1));
     }
     wait_prior_grid();
     if (gatherer && i < cnt && rvalid) vold_c = ld_hint(v + (dof_c & kDofMask), keep);
-    named_barrier(bar_id, bar_threads);
-    for (uint32_t k = 0; i < cnt; i += G.ng, k++) {
+    group_sync(bar_id, bar_threads);
+    bool ok = false;  // the current chunk's slot has landed (one verdict per warp and chunk)
+    for (uint32_t k = 0; i < cnt; k++) {
         const uint32_t par = k & 1;
+        const uint32_t inext = elem(k + 1), jc = k % E, ch = i / E;
         if (gatherer && rvalid) {
-            if (i + G.ng < cnt) {
+            if (inext < cnt) {
                 u_n = load_u_hint(u, dof_n, a.bc_mode, keep);
                 vold_n = ld_hint(v + (dof_n & kDofMask), keep);
             }
-            if (i + 2 * G.ng < cnt) dof_nn = map_at(i + 2 * G.ng);
+            if (elem(k + 2) < cnt) dof_nn = map_at(elem(k + 2));
         }
-        const uint32_t s = i % S;
+        const uint32_t s = ch % S;
         Acc acc = A::zero();
         // one verdict per warp: the block below synchronises the warp, so no lane may skip it alone
-        if (__all_sync(0xffffffffu, ring_wait(&full[s], &tag[s], i, (i / S) & 1, abort, a.wait_ns))) {
-            const unsigned char* ks = smem + (size_t)s * L.slot_bytes;
+        if (jc == 0) ok = __all_sync(0xffffffffu, ring_wait(&full[s], &tag[s], ch, (ch / S) & 1, abort, a.wait_ns));
+        if (ok) {
+            const unsigned char* ks = smem + (size_t)s * L.slot_bytes + (size_t)jc * a.unit_bytes;
             const UT* uu = ubuf(par);
             if (rvalid) {
                 if constexpr (A::kSym && NT != 0) {
@@ -956,15 +980,16 @@ __global__ void __launch_bounds__((A::kWpgWarps + 1) * 32, 1)
                 }
             }
             __syncwarp();
-            if (lane == 0) mbar_arrive(&empty[s]);
+            // the chunk's last element (a CTA's last chunk may be short) releases the slot
+            if (lane == 0 && (jc + 1 == E || i + 1 == cnt)) mbar_arrive(&empty[s]);
         }
         if (!gatherer && rvalid) pbuf(par)[(cg - 1) * n + r] = acc;
-        if (gatherer && rvalid && i + G.ng < cnt) {
+        if (gatherer && rvalid && inext < cnt) {
             const UT x = stage_s<A>(u_n, usk);
             ubuf(par ^ 1)[r] = x;
             if constexpr (A::kSym) ubuf(par ^ 1)[r + n] = x;
         }
-        named_barrier(bar_id, bar_threads);
+        group_sync(bar_id, bar_threads);
         if (gatherer) {
             for (uint32_t c2 = 1; c2 < G.gc; c2++) {
                 if (rvalid) A::combine(acc, pbuf(par)[(c2 - 1) * n + r]);
@@ -974,6 +999,7 @@ __global__ void __launch_bounds__((A::kWpgWarps + 1) * 32, 1)
             vold_c = vold_n;
             dof_n = dof_nn;
         }
+        i = inext;
     }
     if (lane == 0 && *abort) atomicOr(a.err, kErrTimeout);
 }

@@ -61,13 +61,24 @@ static uint32_t stages_for(uint32_t slot_bytes, uint32_t extra) {
     return st > kMaxStages ? kMaxStages : st;
 }
 
-// Ring layout and (for the warp-group kernel) group geometry of a segment.
-static RingLayout ring_layout(const Segment& s, uint64_t copy_bytes, bool dup, GroupGeom* geom) {
+// Warp-group kernel: ring slots hold up to kMaxChunk consecutive element
+// units, about kChunkBytes per bulk copy. One copy per small unit (a few KB)
+// is issue-bound: every kernel on units of 1-8 KB moved ~0.6-0.7 G elements/s
+// whatever its bytes per element (hex8 elasticity, tet10 elasticity, FP32 and
+// split), against ~0.2 G/s of 28.8 KB hex20 units at the HBM roof.
+constexpr uint32_t kMaxChunk = 8;
+constexpr uint32_t kChunkBytes = 16384;
+
+// Ring layout and (for the warp-group kernel) group geometry of a segment;
+// unit_bytes: the stride between units (chunks need whole units copied).
+static RingLayout ring_layout(const Segment& s, uint64_t copy_bytes, uint64_t unit_bytes, bool dup,
+                              GroupGeom* geom) {
     RingLayout L;
     const size_t ut = sizeof(typename ARITH::UT), acc = sizeof(typename ARITH::Acc);
     L.slot_bytes = (uint32_t)((copy_bytes + kSlotAlign - 1) / kSlotAlign * kSlotAlign);
     L.ubuf_bytes = 0;
     L.extra_bytes = 0;
+    L.chunk = 1;
     if (s.regime == REG_WPE && !dup) {
         GroupGeom G;
         G.gr = (s.n + 31) / 32;
@@ -75,11 +86,22 @@ static RingLayout ring_layout(const Segment& s, uint64_t copy_bytes, bool dup, G
         G.g = G.gr * G.gc;
         const uint32_t ub = wpg_ubuf_bytes(ARITH::kSym ? 2 * s.n : s.n, (uint32_t)ut);  // u staged twice (symmetric)
         const uint32_t pstride = (G.gc > 1 ? G.gc - 1 : 1) * s.n;
-        // element groups: up to ARITH::kWpgWarps consumer warps, at most 15 groups (one named barrier each)
-        for (G.ng = std::min<uint32_t>(ARITH::kWpgWarps / G.g, 15u); G.ng >= 1; G.ng--) {
-            L.extra_bytes = G.ng * 2 * ub + G.ng * 2 * pstride * (uint32_t)acc;
-            L.stages = stages_for(L.slot_bytes, L.extra_bytes);
-            if (L.stages >= G.ng + 2 || G.ng == 1) break;
+        // groups of one warp synchronise with __syncwarp; larger groups take one named barrier each (15 ids)
+        const uint32_t ng_max = G.g == 1 ? ARITH::kWpgWarps : std::min<uint32_t>(ARITH::kWpgWarps / G.g, 15u);
+        const uint32_t emax = copy_bytes == unit_bytes
+                                  ? std::max<uint32_t>(1u, std::min<uint32_t>(kMaxChunk, (uint32_t)(kChunkBytes / copy_bytes)))
+                                  : 1u;
+        // the largest chunk that keeps every element group (up to ARITH::kWpgWarps consumer warps) and
+        // stages >= groups + 2; with single units, fewer groups if needed
+        for (uint32_t E = emax; E >= 1; E--) {
+            L.chunk = E;
+            L.slot_bytes = (uint32_t)((E * copy_bytes + kSlotAlign - 1) / kSlotAlign * kSlotAlign);
+            for (G.ng = ng_max; G.ng >= 1; G.ng--) {
+                L.extra_bytes = G.ng * 2 * ub + G.ng * 2 * pstride * (uint32_t)acc;
+                L.stages = stages_for(L.slot_bytes, L.extra_bytes);
+                if (L.stages >= G.ng + 2 || G.ng == 1) break;
+            }
+            if (G.ng == ng_max && L.stages >= G.ng + 2) break;
         }
         L.warps = G.ng * G.g;
         L.ubuf_bytes = ub;
@@ -102,7 +124,7 @@ static RingLayout ring_layout(const Segment& s, uint64_t copy_bytes, bool dup, G
 cudaError_t LAUNCH_FN(const Segment& s, const SegArgs& a, int sm_count, bool dup, bool pdl, cudaStream_t stream) {
     if (s.units == 0) return cudaSuccess;
     GroupGeom G{1, 1, 1, 1};
-    const RingLayout L = ring_layout(s, a.copy_bytes, dup, &G);
+    const RingLayout L = ring_layout(s, a.copy_bytes, a.unit_bytes, dup, &G);
     if (L.stages < 2) return cudaErrorInvalidConfiguration;
     void* fn = pick_kernel(s.regime, s.n, dup);
     if (!fn) return cudaErrorInvalidValue;
@@ -275,7 +297,7 @@ size_t PATCH_SMEM_FN(const PatchPlanGeom& pg, uint32_t copy_bytes) {
     return L.stages >= 2 ? L.total() : 0;
 }
 
-size_t SMEM_FN(const Segment& s) { return ring_layout(s, s.unit_bytes, false, nullptr).total(); }
+size_t SMEM_FN(const Segment& s) { return ring_layout(s, s.unit_bytes, s.unit_bytes, false, nullptr).total(); }
 
 // Raises the dynamic shared-memory limit of every kernel instance on the
 // current device; called once per device before any launch or capture.
