@@ -797,7 +797,9 @@ __device__ __forceinline__ void group_sync(uint32_t id, uint32_t threads) {
         named_barrier(id, threads);
 }
 
-template <int NT, typename A>
+// CH: ring slots may hold several element units (L.chunk); without it the
+// chunk is the constant 1 and the walk folds to one element per slot.
+template <int NT, typename A, bool CH>
 __global__ void __launch_bounds__((A::kWpgWarps + 1) * 32, 1)
     afm_wpg_kernel(SegArgs a, RingLayout L, GroupGeom G, uint32_t n_rt) {
     using KT = typename A::KT;
@@ -835,7 +837,7 @@ __global__ void __launch_bounds__((A::kWpgWarps + 1) * 32, 1)
     // ring slots hold chunks of E consecutive elements (one bulk copy each: the
     // copies of small element units are issue-bound one by one); chunk c goes
     // to group c % ng, which takes its elements in order
-    const uint32_t E = L.chunk;
+    const uint32_t E = CH ? L.chunk : 1u;
     const uint32_t nch = (cnt + E - 1) / E;
     if (warp == G.ng * G.g) {  // producer
         if (lane == 0) {
@@ -886,9 +888,18 @@ __global__ void __launch_bounds__((A::kWpgWarps + 1) * 32, 1)
         return rvalid ? ld_nc_hint(a.map + (size_t)(begin + i) * n + r, stream_pol) : 0u;
     };
 
-    // the group's k-th element (CTA-relative), increasing in k
-    auto elem = [&](uint32_t k) { return (grp + (k / E) * G.ng) * E + k % E; };
-    uint32_t i = elem(0);
+    // The group's elements in order: element ch E + jc of chunk ch, the chunks
+    // grp, grp + ng, ...; positions advance by increments (no division in
+    // the loop but the slot of a new chunk).
+    auto advance = [&](uint32_t& c, uint32_t& j) {
+        if (++j == E) {
+            j = 0;
+            c += G.ng;
+        }
+    };
+    uint32_t ch = grp, jc = 0, chn = grp, jn = 0;
+    advance(chn, jn);
+    uint32_t i = ch * E, inext = chn * E + jn;
     if (gatherer && i < cnt) {
         dof_c = map_at(i);
         if (rvalid) {
@@ -896,26 +907,31 @@ __global__ void __launch_bounds__((A::kWpgWarps + 1) * 32, 1)
             ubuf(0)[r] = x;
             if constexpr (A::kSym) ubuf(0)[r + n] = x;
         }
-        if (elem(1) < cnt) dof_n = map_at(elem(1));
+        if (inext < cnt) dof_n = map_at(inext);
     }
     wait_prior_grid();
     if (gatherer && i < cnt && rvalid) vold_c = ld_hint(v + (dof_c & kDofMask), keep);
     group_sync(bar_id, bar_threads);
     bool ok = false;  // the current chunk's slot has landed (one verdict per warp and chunk)
+    uint32_t s = 0;   // the current chunk's ring slot
     for (uint32_t k = 0; i < cnt; k++) {
         const uint32_t par = k & 1;
-        const uint32_t inext = elem(k + 1), jc = k % E, ch = i / E;
+        uint32_t chnn = chn, jnn = jn;
+        advance(chnn, jnn);
+        const uint32_t inn = chnn * E + jnn;
         if (gatherer && rvalid) {
             if (inext < cnt) {
                 u_n = load_u_hint(u, dof_n, a.bc_mode, keep);
                 vold_n = ld_hint(v + (dof_n & kDofMask), keep);
             }
-            if (elem(k + 2) < cnt) dof_nn = map_at(elem(k + 2));
+            if (inn < cnt) dof_nn = map_at(inn);
         }
-        const uint32_t s = ch % S;
         Acc acc = A::zero();
-        // one verdict per warp: the block below synchronises the warp, so no lane may skip it alone
-        if (jc == 0) ok = __all_sync(0xffffffffu, ring_wait(&full[s], &tag[s], ch, (ch / S) & 1, abort, a.wait_ns));
+        // one verdict per warp and chunk: the block below synchronises the warp, so no lane may skip it alone
+        if (jc == 0) {
+            s = ch % S;
+            ok = __all_sync(0xffffffffu, ring_wait(&full[s], &tag[s], ch, (ch / S) & 1, abort, a.wait_ns));
+        }
         if (ok) {
             const unsigned char* ks = smem + (size_t)s * L.slot_bytes + (size_t)jc * a.unit_bytes;
             const UT* uu = ubuf(par);
@@ -999,7 +1015,12 @@ __global__ void __launch_bounds__((A::kWpgWarps + 1) * 32, 1)
             vold_c = vold_n;
             dof_n = dof_nn;
         }
+        ch = chn;
+        jc = jn;
         i = inext;
+        chn = chnn;
+        jn = jnn;
+        inext = inn;
     }
     if (lane == 0 && *abort) atomicOr(a.err, kErrTimeout);
 }

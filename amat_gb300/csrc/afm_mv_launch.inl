@@ -13,7 +13,7 @@ namespace {
 
 // Element sizes with a compile-time specialisation; any other n <= 16 (TPE)
 // or <= kMaxN (WPE) runs the run-time-n instance (template argument 0).
-template <int NT, bool WPE, bool DUP>
+template <int NT, bool WPE, bool DUP, bool CH = false>
 void* kernel_ptr() {
     if constexpr (ARITH::kSym && (!WPE || DUP)) {
         return nullptr;  // the symmetric arena has element units for the warp-group kernel only
@@ -21,13 +21,15 @@ void* kernel_ptr() {
         if constexpr (DUP)
             return (void*)afm_wpe_kernel<NT, ARITH, true>;
         else
-            return (void*)afm_wpg_kernel<NT, ARITH>;
+            return (void*)afm_wpg_kernel<NT, ARITH, CH>;
     } else {
         return (void*)afm_tpe_kernel<NT, ARITH, DUP>;
     }
 }
 
-void* pick_kernel(int regime, uint32_t n, bool dup) {
+// chunked: warp-group launches whose ring slots hold several units (small
+// elements; hex20's units fill a slot alone and keep the single-unit kernel)
+void* pick_kernel(int regime, uint32_t n, bool dup, bool chunked = false) {
     if (regime == REG_TPE) {
         if (dup) return kernel_ptr<0, false, true>();
         switch (n) {
@@ -38,6 +40,14 @@ void* pick_kernel(int regime, uint32_t n, bool dup) {
         }
     }
     if (dup) return kernel_ptr<0, true, true>();
+    if (chunked) {
+        switch (n) {
+            case 20: return kernel_ptr<20, true, false, true>();
+            case 24: return kernel_ptr<24, true, false, true>();
+            case 30: return kernel_ptr<30, true, false, true>();
+            default: return kernel_ptr<0, true, false, true>();
+        }
+    }
     switch (n) {
         case 20: return kernel_ptr<20, true, false>();
         case 24: return kernel_ptr<24, true, false>();
@@ -126,7 +136,7 @@ cudaError_t LAUNCH_FN(const Segment& s, const SegArgs& a, int sm_count, bool dup
     GroupGeom G{1, 1, 1, 1};
     const RingLayout L = ring_layout(s, a.copy_bytes, a.unit_bytes, dup, &G);
     if (L.stages < 2) return cudaErrorInvalidConfiguration;
-    void* fn = pick_kernel(s.regime, s.n, dup);
+    void* fn = pick_kernel(s.regime, s.n, dup, L.chunk > 1);
     if (!fn) return cudaErrorInvalidValue;
     const uint32_t smem = L.total();
     // at least 4 elements (2 thread-per-element units) per CTA: a small segment occupies few SMs
@@ -304,13 +314,14 @@ size_t SMEM_FN(const Segment& s) { return ring_layout(s, s.unit_bytes, s.unit_by
 cudaError_t CONFIG_FN() {
     for (int reg = 0; reg < 2; reg++)
         for (uint32_t nn : {4u, 8u, 10u, 20u, 24u, 30u, 60u, 0u})
-            for (int d = 0; d < 2; d++) {
-                void* f = pick_kernel(reg, nn == 0 ? 7u : nn, d != 0);
-                if (!f) continue;
-                cudaError_t e =
-                    cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kSmemBudget + 1024));
-                if (e != cudaSuccess) return e;
-            }
+            for (int d = 0; d < 2; d++)
+                for (int ch = 0; ch < 2; ch++) {
+                    void* f = pick_kernel(reg, nn == 0 ? 7u : nn, d != 0, ch != 0);
+                    if (!f) continue;
+                    cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                         (int)(kSmemBudget + 1024));
+                    if (e != cudaSuccess) return e;
+                }
     for (uint32_t nn : {4u, 8u, 10u, 0u})
         for (uint32_t gg : {2u, 4u, 8u}) {
             cudaError_t e = cudaFuncSetAttribute(pick_patch_kernel(nn, gg),
