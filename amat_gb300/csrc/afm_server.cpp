@@ -2,9 +2,9 @@
 // include/afm.h; no counterpart in the reference).
 //
 // A request carries its own operator (maps and element matrices set on the
-// host) and load. Requests wait in a queue and are admitted, smallest first
-// (a request that has waited 2 s goes first), while the server's HBM budget,
-// the device's free memory and the slot limit allow.
+// host) and load. Requests wait in a queue and are admitted (lane-sized ones
+// first, the rest in arrival order) while the server's HBM budget, the
+// device's free memory and the slot limit allow.
 // Admission finalises the operator on a worker thread (colouring, patch plan,
 // upload of Ke and maps), so the polling thread never blocks on host work, and
 // then drops the operator's host copy of the element matrices.
@@ -108,13 +108,16 @@ uint64_t lane_bytes(const afm_operator* op) {
 constexpr uint64_t kLaneMaxBytes = 8ull << 20;
 constexpr uint32_t kLaneIters = 32;
 
-// Requests on their own streams iterate in FP64 vectors on the corrected
-// symmetric arena (format 4): the FP32 recursion stalls on the large elastic
-// requests of a serving mix (hex20 elasticity 64^3 under a random load: 100,053
-// FP32 iterations against 6,209 for FP64 CG; 6,385 in format 4, whose product
-// takes 0.71 ms against 1.36 ms for the split product), and costs Poisson
-// requests, which converge in few iterations either way, little.
+// Requests on their own streams with at least kFp64InnerDofs DoFs iterate in
+// FP64 vectors on the corrected symmetric arena (format 4): the FP32
+// recursion stalls on the large elastic requests of a serving mix (hex20
+// elasticity 64^3, 3.3M DoF, under a random load: 100,053 FP32 iterations
+// against 6,209 for FP64 CG; 6,385 in format 4, whose product takes 0.71 ms
+// against 1.36 ms for the split product). Smaller ones keep the cheaper FP32
+// recursion (format 1), which converges like format 4 up to ~0.5M DoF (hex20
+// 32^3: 1.32x against 1.38x over FP64 CG; hex8 elasticity 48^3: 1.29x and 1.28x).
 constexpr int kStreamInnerFormat = 4;
+constexpr uint32_t kFp64InnerDofs = 1u << 20;
 
 }  // namespace
 
@@ -203,19 +206,21 @@ void finish(afm_server* s, Request* r, int status, const char* msg) {
 // they do not wait behind the seconds-long finalizes of large meshes.
 constexpr int kMaxFinalizing = 4;
 constexpr int kExtraSmallFinalizing = 2;
-// Admission order: shortest first (estimated device bytes), which keeps small
-// requests' latency independent of the large ones' finalize and solve time;
-// a request that has waited kAgingSeconds goes first (oldest first), so large
-// requests are never held back for long.
-constexpr double kAgingSeconds = 2.0;
+// Admission order: lane-sized requests first (oldest first), then the rest
+// in arrival order. Small requests then never wait behind the seconds-long
+// finalizes of large meshes, while large requests still start in arrival
+// order and overlap the rest of the mix (shortest-first throughout held
+// them back until the end of a burst, where they ran with little overlap:
+// 18.7 against 20.2 solves/s on the edge-8..32 mix).
+bool is_small(const afm_server* s, const Request* r) {
+    return s->lane_max_bytes > 0 && r->op->matfree_type != 2 && r->lane_bytes <= s->lane_max_bytes;
+}
 
 // Index in the queue of the next request to admit.
-size_t next_in_queue(const afm_server* s, double now) {
-    if (now - s->queue.front()->t_submit > kAgingSeconds) return 0;
-    size_t best = 0;
-    for (size_t i = 1; i < s->queue.size(); i++)
-        if (s->queue[i]->est_bytes < s->queue[best]->est_bytes) best = i;
-    return best;
+size_t next_in_queue(const afm_server* s) {
+    for (size_t i = 0; i < s->queue.size(); i++)
+        if (is_small(s, s->queue[i])) return i;
+    return 0;
 }
 
 // admission while the budget, free device memory and slots allow
@@ -225,9 +230,9 @@ int admit(afm_server* s) {
     for (const Request* r : s->active) finalizing += (r->state == RQ_ADMITTING);
     while (!s->queue.empty() && s->active.size() < s->max_active &&
            finalizing < kMaxFinalizing + kExtraSmallFinalizing) {
-        const size_t k = next_in_queue(s, now_s());
+        const size_t k = next_in_queue(s);
         Request* r = s->queue[k];
-        const bool small = s->lane_max_bytes > 0 && r->op->matfree_type != 2 && r->lane_bytes <= s->lane_max_bytes;
+        const bool small = is_small(s, r);
         if (!small && finalizing >= kMaxFinalizing) break;
         size_t free_b = 0, total_b = 0;
         if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) break;
@@ -324,7 +329,7 @@ int start(afm_server* s, Request* r) {
     r->ms.max_outer = 200;
     r->ms.max_inner = 20000;  // FP32 iterations per segment before the next FP64 update
     r->ms.lane = lane;
-    if (!lane) afm_set_symmetric_inner(op, s->inner_format);
+    if (!lane) afm_set_symmetric_inner(op, op->n_dofs >= kFp64InnerDofs ? s->inner_format : 1);
     r->t_start = now_s();
     if (lane) s->info.lane_requests++;
     else s->info.stream_requests++;

@@ -1,5 +1,5 @@
 """Serving loop for many CG solves on different operators (afm_server_* in
-include/afm.h): admission by HBM budget (smallest first, with aging), device-resident state, every
+include/afm.h): admission by HBM budget (lane-sized requests first), device-resident state, every
 admitted request advanced by the server's progress thread, on its own stream or,
 for small requests, in the serving lane (one launch for the FP32 iterations of
 all of them)."""
@@ -39,8 +39,8 @@ class Server:
               "afm_server_set_lane")
 
     def set_inner_format(self, fmt=4):
-        """Symmetric inner format of the requests on their own streams (4: FP64 inner vectors on the corrected
-        symmetric arena; 0 to 5 as aMatFree.set_symmetric_inner)."""
+        """Symmetric inner format of the requests with 2^20 DoFs or more on their own streams (4: FP64 inner
+        vectors on the corrected symmetric arena; 0 to 5 as aMatFree.set_symmetric_inner); smaller ones use 1."""
         check(self._lib.afm_server_set_inner_format(self._h, int(fmt)), "afm_server_set_inner_format")
 
     def info(self):

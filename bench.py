@@ -978,7 +978,7 @@ def run_serve(args, w, rank, world, local_rank):
                                   "jitter 0.1h, loads N(0,1)" % (args.requests, [k[1] for k in SERVE_KINDS],
                                                                   args.edge_max),
                       "n_dofs_range": [int(min(sizes)), int(max(sizes))], "rtol": args.rtol,
-                      "inner_rtol": args.serve_inner, "admission": "smallest first (2 s aging) by HBM budget (85% of free), 64 slots",
+                      "inner_rtol": args.serve_inner, "admission": "lane-sized first, then arrival order, by HBM budget (85% of free), 64 slots",
                       "lane_mb": args.lane_mb, "inner_format": args.serve_format},
            "rates": lines, "p50_ms": best["p50_ms"], "p99_ms": best["p99_ms"], "plain_fp64_sequential": plain,
            "served_one_at_a_time": alone,

@@ -418,9 +418,9 @@ int afm_get_assembled_csr(afm_operator* op, uint64_t* nnz, uint64_t* row_ptr, ui
  * No counterpart in the reference. A request is an operator whose maps and
  * element matrices are set on the host (finalize not needed) and a load b
  * (host, n_dofs, boundary conditions applied). Requests wait in a queue and
- * are admitted smallest first (a request waiting 2 s goes first) while the HBM
- * budget, the device's free memory and the slot limit allow; admission
- * finalises the operator on a worker thread. An
+ * are admitted (requests small enough for the serving lane first, the rest in
+ * arrival order) while the HBM budget, the device's free memory and the slot
+ * limit allow; admission finalises the operator on a worker thread. An
  * admitted request keeps Ke, maps, b, x and its Krylov vectors on the device
  * and is solved by the mixed-precision solve (afm_solve_cg_mixed, to rtol,
  * FP64-checked). A progress thread of the server's own keeps admitting and
@@ -455,10 +455,10 @@ int afm_server_destroy(afm_server* s);
  * 32 by default, per launch); larger requests run on their own streams. Takes
  * effect for requests admitted afterwards. */
 int afm_server_set_lane(afm_server* s, uint64_t max_ke_bytes, uint32_t iters_per_launch);
-/* Symmetric inner format (afm_set_symmetric_inner) of the requests that run
- * on their own streams: 4 by default (FP64 inner vectors on the corrected
- * symmetric arena), 0 to 5 as afm_set_symmetric_inner. Takes effect for
- * requests started afterwards. */
+/* Symmetric inner format (afm_set_symmetric_inner) of the requests with at
+ * least 2^20 DoFs that run on their own streams: 4 by default (FP64 inner
+ * vectors on the corrected symmetric arena), 0 to 5 as afm_set_symmetric_inner;
+ * smaller ones use format 1. Takes effect for requests started afterwards. */
 int afm_server_set_inner_format(afm_server* s, int format);
 typedef struct {
     uint64_t lane_launches;       /* serving-lane launches */
