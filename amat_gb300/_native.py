@@ -102,6 +102,7 @@ AFM_SIGNATURES = {
     "afm_get_solve_trace": (I, [P, U32, P, P, P]),
     "afm_server_get_info": (I, [P, P]),
     "afm_server_set_inner_format": (I, [P, I]),
+    "afm_server_set_priorities": (I, [P, I]),
     "afm_patch_plan_host_matvec": (I, [U32, U32, P, P, P, P, P, P, P]),
     "afm_set_map": (I, [P, U32, P, U32, P, U32, P, U64, U64, U64]),
     "afm_set_bdr_map": (I, [P, P, P, U32]),

@@ -152,6 +152,7 @@ struct afm_server {
     // ahead of large ones, so that a small request's launches do not queue
     // behind the many launches a large request has in flight
     int prio_low = 0, prio_high = 0;
+    bool priorities = true;
     cudaStream_t lane_stream = nullptr;
     cudaEvent_t lane_done = nullptr;
     bool lane_busy = false;
@@ -304,7 +305,7 @@ int start(afm_server* s, Request* r) {
     const bool lane = r->lane_candidate && op->precision == AFM_PREC_FP64_SPLIT && !op->use_patches &&
                       op->matfree_type != 2;
     // priority by size: one level per factor 8 of element-matrix bytes above 8 MB
-    if (s->prio_high < s->prio_low) {
+    if (s->priorities && s->prio_high < s->prio_low) {
         int level = 0;
         for (uint64_t b = r->lane_bytes; b > (8ull << 20) && level < s->prio_low - s->prio_high; b >>= 3) level++;
         const int st = afm::set_stream_priority(op, s->prio_high + level);
@@ -588,6 +589,13 @@ int afm_server_set_lane(afm_server* s, uint64_t max_ke_bytes, uint32_t iters_per
     std::lock_guard<std::mutex> lk(s->state_mu);
     s->lane_max_bytes = max_ke_bytes;
     s->lane_iters = iters_per_launch;
+    return afm::set_error(AFM_SUCCESS, "");
+}
+
+int afm_server_set_priorities(afm_server* s, int enable) {
+    if (!s || (enable != 0 && enable != 1)) return afm::set_error(AFM_ERR_INVALID_ARG, "server or enable %d", enable);
+    std::lock_guard<std::mutex> lk(s->state_mu);
+    s->priorities = enable == 1;
     return afm::set_error(AFM_SUCCESS, "");
 }
 

@@ -43,6 +43,10 @@ class Server:
         vectors on the corrected symmetric arena; 0 to 5 as aMatFree.set_symmetric_inner); smaller ones use 1."""
         check(self._lib.afm_server_set_inner_format(self._h, int(fmt)), "afm_server_set_inner_format")
 
+    def set_priorities(self, enable=True):
+        """Stream priority by request size (the lane and small requests first), or none."""
+        check(self._lib.afm_server_set_priorities(self._h, int(bool(enable))), "afm_server_set_priorities")
+
     def info(self):
         """Counters of the serving lane: launches, requests carried, largest batch, requests per path."""
         i = AfmServerInfo()

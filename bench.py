@@ -876,6 +876,7 @@ def new_server(dev, args):
     srv = Server(dev)
     srv.set_lane(int(args.lane_mb * 2 ** 20), 32)
     srv.set_inner_format(args.serve_format)
+    srv.set_priorities(bool(args.serve_prio))
     return srv
 
 
@@ -979,7 +980,7 @@ def run_serve(args, w, rank, world, local_rank):
                                                                   args.edge_max),
                       "n_dofs_range": [int(min(sizes)), int(max(sizes))], "rtol": args.rtol,
                       "inner_rtol": args.serve_inner, "admission": "lane-sized first, then arrival order, by HBM budget (85% of free), 64 slots",
-                      "lane_mb": args.lane_mb, "inner_format": args.serve_format},
+                      "lane_mb": args.lane_mb, "inner_format": args.serve_format, "priorities": args.serve_prio},
            "rates": lines, "p50_ms": best["p50_ms"], "p99_ms": best["p99_ms"], "plain_fp64_sequential": plain,
            "served_one_at_a_time": alone,
            "speedup_vs_plain": best["solves_per_s"] / plain["solves_per_s"]}
@@ -1008,6 +1009,8 @@ def main():
     ap.add_argument("--serve-inner", type=float, default=0.3, help="serve: FP32 reduction between FP64 updates")
     ap.add_argument("--serve-format", type=int, default=4, choices=[0, 1, 2, 3, 4, 5],
                     help="serve: symmetric inner format of the requests on their own streams")
+    ap.add_argument("--serve-prio", type=int, default=1, choices=[0, 1],
+                    help="serve: stream priorities by request size")
     ap.add_argument("--lane-mb", type=float, default=8.0,
                     help="serve: requests with at most this many MB of FP32 element matrices share lane launches")
     ap.add_argument("--nrhs", type=int, default=64)

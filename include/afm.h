@@ -455,6 +455,10 @@ int afm_server_destroy(afm_server* s);
  * 32 by default, per launch); larger requests run on their own streams. Takes
  * effect for requests admitted afterwards. */
 int afm_server_set_lane(afm_server* s, uint64_t max_ke_bytes, uint32_t iters_per_launch);
+/* 1 (default): each request's stream gets a priority by its size (the lane
+ * and small requests first); 0: every request at the default priority. Takes
+ * effect for requests started afterwards. */
+int afm_server_set_priorities(afm_server* s, int enable);
 /* Symmetric inner format (afm_set_symmetric_inner) of the requests with at
  * least 2^20 DoFs that run on their own streams: 4 by default (FP64 inner
  * vectors on the corrected symmetric arena), 0 to 5 as afm_set_symmetric_inner;
