@@ -125,7 +125,7 @@ __global__ void __cluster_dims__(kLaneCtas, 1, 1) __launch_bounds__(kLaneThreads
     for (uint32_t k = 0; k < iters && done == 0.0; k++) {
         // q = A p, row by row over the DoF-to-element pairs
         for (uint32_t d = gt; d < n; d += kClusterThreads) {
-            float acc4[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+            float acc = 0.0f;
             const uint32_t k1 = min(J.rowptr[d + 1], J.n_pairs);
             for (uint32_t kk = J.rowptr[d]; kk < k1; kk++) {
                 const uint32_t pr = J.pairs[kk];
@@ -142,26 +142,19 @@ __global__ void __cluster_dims__(kLaneCtas, 1, 1) __launch_bounds__(kLaneThreads
                 }
                 const float* __restrict__ K = J.ke32 + koff + (size_t)rr * ne;
                 const uint32_t* __restrict__ M = J.emap + moff;
-                // four independent chains of columns c = 4j + t: four gathers in flight per thread
-                for (uint32_t c0 = 0; c0 < ne; c0 += 4) {
-#pragma unroll
-                    for (uint32_t t = 0; t < 4; t++) {
-                        const uint32_t c = c0 + t;
-                        if (c < ne) {
-                            const uint32_t m = M[c];
-                            const uint32_t g = m & kDofMask;
-                            float uc = 0.0f;
-                            if (g < n) {
-                                if (!(m & kBcFlag)) uc = p[g];
-                            } else {
-                                bounds_error(J.err, g, n);
-                            }
-                            acc4[t] = fmaf(K[c], uc, acc4[t]);
-                        }
+                for (uint32_t c = 0; c < ne; c++) {
+                    const uint32_t m = M[c];
+                    const uint32_t g = m & kDofMask;
+                    float uc = 0.0f;
+                    if (g < n) {
+                        if (!(m & kBcFlag)) uc = p[g];
+                    } else {
+                        bounds_error(J.err, g, n);
                     }
+                    acc = fmaf(K[c], uc, acc);
                 }
             }
-            q[d] = (acc4[0] + acc4[1]) + (acc4[2] + acc4[3]);
+            q[d] = acc;
         }
         cl.sync();
         // p.q with q = p on constrained rows
