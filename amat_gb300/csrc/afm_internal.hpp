@@ -206,33 +206,31 @@ size_t segment_smem_bytes(const Segment& s, int prec);
 // ---- serving lane (afm_lane.cu) ---------------------------------------------
 // One launch advances the FP32 CG recursion of many served solves at once:
 // every request is one thread-block cluster of kLaneCtas CTAs that runs whole
-// CG iterations (FP32 products, dot products, vector updates) with cluster
-// barriers between phases. The product sums whole rows: each DoF's row is the
-// sum over its elements (in element order) of the element row times u_e, read
-// through a DoF-to-element adjacency, so it needs no colour phases and no
-// atomics and its result does not depend on timing.
+// CG iterations (colour-ordered FP32 products on the hi plane of the split
+// arena, dot products, vector updates) with cluster barriers between phases.
 constexpr uint32_t kLaneCtas = 8;
 constexpr uint32_t kLaneThreads = 512;
-constexpr uint32_t kLaneRowBits = 7;  // a pair packs element << 7 | local row (n <= 96)
 
-// One request's FP32 recursion: the vectors of its solve (float, n_dofs), its
-// solver scalars on the device, and its lane copy of the operator: element
-// matrices in FP32 row-major (element e at einfo[3e] floats, n = einfo[3e+2]),
-// element maps (at einfo[3e+1], kBcFlag on constrained DoFs), and for every
-// DoF d the pairs rowptr[d] .. rowptr[d+1] of (element, local row).
+// One colour-size segment of a request, as the lane reads it.
+struct LaneSeg {
+    const float* ke;        // hi plane of the segment's first unit
+    const uint32_t* map;    // the segment's map (kBcFlag on constrained DoFs)
+    uint64_t unit_floats;   // floats from one unit to the next
+    uint32_t n, regime, units, count;
+    uint32_t sync_after;    // 1: the last segment of its colour (a cluster barrier follows)
+    uint32_t pad;
+};
+
+// One request's FP32 recursion: the vectors of its solve (float, n_dofs) and
+// its solver scalars on the device.
 struct LaneJob {
     float *x, *r, *z, *p, *q;
     const float* dinv;
     const uint8_t* bcmask;  // 1 on constrained DoFs (q = p there), or null
-    const float* ke32;
-    const uint32_t* emap;
-    const uint32_t* einfo;
-    const uint32_t* rowptr;
-    const uint32_t* pairs;
+    const LaneSeg* segs;
     double* sc;
     int* err;
-    uint32_t n_dofs, n_elem;
-    uint32_t n_ke, n_map, n_pairs;  // lengths of ke32, emap and pairs (bounds checks)
+    uint32_t n_dofs, n_segs;
 };
 
 // Runs at most iters CG iterations of each of the n_jobs requests (a request

@@ -1,25 +1,21 @@
 // Serving lane: one launch runs the FP32 Jacobi-PCG iterations of many served
 // solves. Each request is one thread-block cluster of kLaneCtas CTAs; the
-// cluster runs whole iterations on its own (q = A p, p.q, the x, r, z updates
-// with r.z, r.r, z.z, then p), separated by hardware cluster barriers, with
-// the partial sums of every dot product exchanged through distributed shared
-// memory. A launch of n requests replaces n x iters x (colours + 5) launches
-// of the per-request path, whose small requests are bound by launch latency.
-//
-// The product sums rows: thread t of the cluster owns DoFs t, t + T, ... and
-// forms q_d = sum over the pairs (e, r) of d, in element order, of row r of
-// Ke times u_e (constrained columns read as zero; constrained rows q = p, the
-// MatMult_mf form). Every row is written once by its owner, so the product
-// needs no colour phases (a colour-by-colour product spent most of its time
-// at the barriers between the few elements of each colour) and no atomics.
+// cluster runs whole iterations on its own (q = A p colour by colour, p.q, the
+// x, r, z updates with r.z, r.r, z.z, then p), separated by hardware cluster
+// barriers, with the partial sums of every dot product exchanged through
+// distributed shared memory. A launch of n requests replaces n x iters x
+// (colours + 5) launches of the per-request path, whose small requests are
+// bound by launch latency.
 //
 // The iteration is the one of cg_step<float> (afm_capi.cpp) and the solver
 // kernels (afm_solver.cu): alpha = r.z / p.q, x += alpha p, r -= alpha q,
 // z = D^-1 r, beta = r.z_new / r.z, p = z + beta p, with the same stopping
-// rules on S_TOL / S_MAXIT and breakdown flags. Every sum runs in a fixed
-// order that depends only on the request (its size and the cluster shape),
-// never on the other requests of the launch or on timing, so a request's
-// result is the same alone and in any mix, bit for bit.
+// rules on S_TOL / S_MAXIT and breakdown flags; the products read the hi
+// plane of the split arena (FP32 Ke) with constrained columns as zero and
+// constrained rows q = p (MatMult_mf form). Every sum runs in a fixed order
+// that depends only on the request (its size and the cluster shape), never on
+// the other requests of the launch or on timing, so a request's result is the
+// same alone and in any mix, bit for bit.
 //
 // No thread waits on a flag: the only waits are the cluster barriers, which
 // every thread of the cluster reaches the same number of times (the loop
@@ -39,6 +35,7 @@ namespace {
 
 constexpr uint32_t kLaneWarps = kLaneThreads / 32;
 constexpr uint32_t kClusterThreads = kLaneCtas * kLaneThreads;
+constexpr uint32_t kClusterWarps = kLaneCtas * kLaneWarps;
 
 // Compensated FP32 dot accumulator (Dot2 of Ogita, Rump & Oishi, 2005), the
 // arithmetic of the per-request path's FP32 dot products.
@@ -64,6 +61,89 @@ __device__ __forceinline__ void bounds_error(int* err, uint32_t d, uint32_t n) {
         err[4] = (int)d;
         err[5] = (int)n;
         err[6] = 0;
+    }
+}
+
+// One element of a warp-per-element segment (column-major Ke, entry (r, c)
+// at c n + r): lane l holds rows l, l + 32, l + 64 and the same entries of u.
+template <int NR>
+__device__ __forceinline__ void wpe_element(const float* __restrict__ ke, const uint32_t* __restrict__ map,
+                                            uint32_t n, const float* __restrict__ p, float* __restrict__ q,
+                                            uint32_t n_dofs, int* err) {
+    const uint32_t lane = threadIdx.x & 31;
+    float u[NR], acc[NR];
+    uint32_t d[NR];
+#pragma unroll
+    for (int k = 0; k < NR; k++) {
+        const uint32_t i = lane + 32 * k;
+        u[k] = 0.0f;
+        acc[k] = 0.0f;
+        d[k] = 0xffffffffu;
+        if (i < n) {
+            const uint32_t m = map[i];
+            const uint32_t g = m & kDofMask;
+            if (g < n_dofs) {
+                d[k] = g;
+                u[k] = (m & kBcFlag) ? 0.0f : p[g];
+            } else {
+                bounds_error(err, g, n_dofs);
+            }
+        }
+    }
+#pragma unroll
+    for (int kb = 0; kb < NR; kb++) {
+        const uint32_t c1 = min(n, 32u * (kb + 1));
+#pragma unroll 4
+        for (uint32_t c = 32u * kb; c < c1; c++) {
+            const float uc = __shfl_sync(0xffffffffu, u[kb], c & 31);
+            const float* col = ke + (size_t)c * n;
+#pragma unroll
+            for (int k = 0; k < NR; k++) {
+                const uint32_t r = lane + 32 * k;
+                if (r < n) acc[k] = fmaf(col[r], uc, acc[k]);
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < NR; k++)
+        if (d[k] != 0xffffffffu) q[d[k]] += acc[k];
+}
+
+// One element slot of a thread-per-element unit (entry (r, c) of slot l at
+// (r n + c) 32 + l, map entry i of slot l at i 32 + l).
+__device__ __forceinline__ void tpe_slot(const float* __restrict__ ke, const uint32_t* __restrict__ map, uint32_t n,
+                                         const float* __restrict__ p, float* __restrict__ q, uint32_t n_dofs,
+                                         int* err) {
+    const uint32_t l = threadIdx.x & 31;
+    float u[kTpeMaxN];
+    uint32_t d[kTpeMaxN];
+    bool ok = true;
+#pragma unroll
+    for (uint32_t i = 0; i < kTpeMaxN; i++) {
+        u[i] = 0.0f;
+        d[i] = 0;
+        if (i < n) {
+            const uint32_t m = map[i * kTpeWidth + l];
+            const uint32_t g = m & kDofMask;
+            if (g < n_dofs) {
+                d[i] = g;
+                u[i] = (m & kBcFlag) ? 0.0f : p[g];
+            } else {
+                bounds_error(err, g, n_dofs);
+                ok = false;
+            }
+        }
+    }
+    if (!ok) return;
+#pragma unroll
+    for (uint32_t r = 0; r < kTpeMaxN; r++) {
+        if (r >= n) break;
+        float acc = 0.0f;
+        const float* row = ke + (size_t)r * n * kTpeWidth + l;
+#pragma unroll
+        for (uint32_t c = 0; c < kTpeMaxN; c++)
+            if (c < n) acc = fmaf(row[(size_t)c * kTpeWidth], u[c], acc);
+        q[d[r]] += acc;
     }
 }
 
@@ -108,6 +188,7 @@ __global__ void __cluster_dims__(kLaneCtas, 1, 1) __launch_bounds__(kLaneThreads
     const LaneJob J = jobs[blockIdx.x / kLaneCtas];
     const uint32_t rank = cl.block_rank();
     const uint32_t gt = rank * kLaneThreads + threadIdx.x;
+    const uint32_t gw = rank * kLaneWarps + (threadIdx.x >> 5);
     const uint32_t n = J.n_dofs;
     float* __restrict__ x = J.x;
     float* __restrict__ r = J.r;
@@ -122,41 +203,34 @@ __global__ void __cluster_dims__(kLaneCtas, 1, 1) __launch_bounds__(kLaneThreads
     double rzold = sc[S_RZOLD], it = sc[S_ITER], flag = sc[S_FLAG], done = sc[S_DONE];
     const double tol = sc[S_TOL], maxit = sc[S_MAXIT], norm = sc[S_NORM];
 
+    for (uint32_t i = gt; i < n; i += kClusterThreads) q[i] = 0.0f;
+    cl.sync();
+
     for (uint32_t k = 0; k < iters && done == 0.0; k++) {
-        // q = A p, row by row over the DoF-to-element pairs
-        for (uint32_t d = gt; d < n; d += kClusterThreads) {
-            float acc = 0.0f;
-            const uint32_t k1 = min(J.rowptr[d + 1], J.n_pairs);
-            for (uint32_t kk = J.rowptr[d]; kk < k1; kk++) {
-                const uint32_t pr = J.pairs[kk];
-                const uint32_t e = pr >> kLaneRowBits, rr = pr & ((1u << kLaneRowBits) - 1);
-                if (e >= J.n_elem) {
-                    bounds_error(J.err, e, J.n_elem);
-                    continue;
+        // q = A p, colour by colour (elements of a colour share no DoF)
+        for (uint32_t s = 0; s < J.n_segs; s++) {
+            const LaneSeg S = J.segs[s];
+            if (S.regime == REG_WPE) {
+                for (uint32_t e = gw; e < S.count; e += kClusterWarps) {
+                    const float* ke = S.ke + (size_t)e * S.unit_floats;
+                    const uint32_t* mp = S.map + (size_t)e * S.n;
+                    if (S.n <= 32)
+                        wpe_element<1>(ke, mp, S.n, p, q, n, J.err);
+                    else if (S.n <= 64)
+                        wpe_element<2>(ke, mp, S.n, p, q, n, J.err);
+                    else
+                        wpe_element<3>(ke, mp, S.n, p, q, n, J.err);
                 }
-                const uint32_t koff = J.einfo[3 * e], moff = J.einfo[3 * e + 1], ne = J.einfo[3 * e + 2];
-                if (rr >= ne || ne > kMaxN || (uint64_t)koff + (uint64_t)(rr + 1) * ne > J.n_ke ||
-                    (uint64_t)moff + ne > J.n_map) {
-                    bounds_error(J.err, e, rr);
-                    continue;
-                }
-                const float* __restrict__ K = J.ke32 + koff + (size_t)rr * ne;
-                const uint32_t* __restrict__ M = J.emap + moff;
-                for (uint32_t c = 0; c < ne; c++) {
-                    const uint32_t m = M[c];
-                    const uint32_t g = m & kDofMask;
-                    float uc = 0.0f;
-                    if (g < n) {
-                        if (!(m & kBcFlag)) uc = p[g];
-                    } else {
-                        bounds_error(J.err, g, n);
-                    }
-                    acc = fmaf(K[c], uc, acc);
+            } else {
+                for (uint32_t u = gw; u < S.units; u += kClusterWarps) {
+                    const uint32_t slot = u * kTpeWidth + (threadIdx.x & 31);
+                    if (slot < S.count)
+                        tpe_slot(S.ke + (size_t)u * S.unit_floats, S.map + (size_t)u * S.n * kTpeWidth, S.n, p, q,
+                                 n, J.err);
                 }
             }
-            q[d] = acc;
+            if (S.sync_after) cl.sync();
         }
-        cl.sync();
         // p.q with q = p on constrained rows
         {
             Dot2 a;
@@ -179,7 +253,7 @@ __global__ void __cluster_dims__(kLaneCtas, 1, 1) __launch_bounds__(kLaneThreads
             pq = pq_new;
             alpha = rz / pq_new;
         }
-        // x += alpha p, r -= alpha q, z = D^-1 r
+        // x += alpha p, r -= alpha q, z = D^-1 r; q cleared for the next product
         {
             const float al = (float)alpha;
             Dot2 a_rz, a_rr, a_zz;
@@ -191,6 +265,7 @@ __global__ void __cluster_dims__(kLaneCtas, 1, 1) __launch_bounds__(kLaneThreads
                 const float zi = dinv[i] * ri;
                 r[i] = ri;
                 z[i] = zi;
+                q[i] = 0.0f;
                 a_rz.add(ri, zi);
                 a_rr.add(ri, ri);
                 a_zz.add(zi, zi);

@@ -44,7 +44,6 @@ struct MixedSolve {
     // the FP32 iterations run in the serving lane: the owner of the solve
     // launches them (launch_lane) for every solve in MS_LANE, records ev on the
     // lane's stream and sets MS_LANEITER; no symmetric inner arena is built
-    // (the lane multiplies with its own FP32 copy of the element matrices)
     bool lane = false;
     // symmetric inner format 3: the inner recursion in FP64 vectors with the
     // double-float products of the corrected symmetric arena (set by mixed_begin)
@@ -63,8 +62,8 @@ bool mixed_ready(const MixedSolve& m);
 // the scalars of the finished work and enqueues the next, or moves to MS_DONE.
 int mixed_advance(MixedSolve& m);
 // The FP32 vectors, scalars and error flags of the solve, as a lane job (the
-// caller fills the operator's lane copy). After the launch, the caller copies
-// the device scalars to the host mirror (mixed_lane_record) on the lane's stream.
+// caller fills segs and n_segs). After the launch, the caller copies the
+// device scalars to the host mirror (mixed_lane_record) on the lane's stream.
 void mixed_lane_job(const MixedSolve& m, LaneJob& J);
 int mixed_lane_record(MixedSolve& m, cudaStream_t lane_stream);
 // Fills stats (device time between begin and done), releases the events and

@@ -63,14 +63,9 @@ struct Request {
     std::vector<double> x;   // result on the host
     cudaEvent_t copied = nullptr;
     afm::MixedSolve ms;
-    bool lane_candidate = false;  // small enough for the serving lane (decided at admission)
-    // the lane's copy of the operator (built on the finalize worker from the
-    // host element matrices, uploaded when the solve starts): FP32 row-major
-    // Ke, element maps, element info, DoF row pointers and (element, row) pairs
-    std::vector<float> lane_ke;
-    std::vector<uint32_t> lane_map, lane_info, lane_rowptr, lane_pairs;
-    unsigned char* d_lane = nullptr;
-    afm::LaneJob lane_job{};
+    bool lane_candidate = false;         // small enough for the serving lane (decided at admission)
+    afm::LaneSeg* d_lane_segs = nullptr; // the lane's view of the operator's segments
+    uint32_t lane_nsegs = 0;
     afm_solve_stats stats{};
     int status = AFM_SUCCESS;
     std::string message;
@@ -171,8 +166,8 @@ namespace {
 void release_device(afm_server* s, Request* r) {
     if (r->d_bx && r->op) cudaFreeAsync(r->d_bx, r->op->stream);
     r->d_bx = nullptr;
-    if (r->d_lane && r->op) cudaFreeAsync(r->d_lane, r->op->stream);
-    r->d_lane = nullptr;
+    if (r->d_lane_segs && r->op) cudaFreeAsync(r->d_lane_segs, r->op->stream);
+    r->d_lane_segs = nullptr;
     if (r->copied) cudaEventDestroy(r->copied);
     r->copied = nullptr;
     if (r->op) {
@@ -229,8 +224,6 @@ size_t next_in_queue(const afm_server* s) {
     return 0;
 }
 
-void build_lane_host(Request* r);
-
 // admission while the budget, free device memory and slots allow
 int admit(afm_server* s) {
     int admitted = 0;
@@ -251,12 +244,13 @@ int admit(afm_server* s) {
         r->state = RQ_ADMITTING;
         r->t_admit = now_s();
         afm_operator* op = r->op;
+        // lane requests run colour segments (the lane reads their units), never patches
         r->lane_candidate = small;
+        if (r->lane_candidate) afm_set_patch_mode(op, 0);
         const int dev = s->device;
-        r->fin = std::async(std::launch::async, [op, dev, r]() {
+        r->fin = std::async(std::launch::async, [op, dev]() {
             cudaSetDevice(dev);
             const int st = afm_finalize(op);
-            if (st == AFM_SUCCESS && r->lane_candidate) build_lane_host(r);
             // the device arena holds the element matrices now; the server never finalizes again, so the
             // host copy goes (large requests would otherwise hold gigabytes of host memory until they end)
             if (st == AFM_SUCCESS) {
@@ -272,87 +266,44 @@ int admit(afm_server* s) {
     return admitted;
 }
 
-// The lane's copy of a finalised operator, built from its host element
-// matrices (row-major, the reference layout) on the finalize worker.
-void build_lane_host(Request* r) {
-    const afm_operator* op = r->op;
-    const uint32_t ne = op->n_elem, nd = op->n_dofs;
-    std::vector<uint8_t> is_bc(nd, 0);
-    for (uint32_t d : op->bc_unique) is_bc[d] = 1;
-    r->lane_info.resize(3ull * ne);
-    r->lane_rowptr.assign((size_t)nd + 1, 0);
-    uint64_t kf = 0, mf = 0;
-    for (uint32_t e = 0; e < ne; e++) {
-        const uint32_t n = op->offsets[e + 1] - op->offsets[e];
-        r->lane_info[3ull * e] = (uint32_t)kf;
-        r->lane_info[3ull * e + 1] = (uint32_t)mf;
-        r->lane_info[3ull * e + 2] = n;
-        kf += (uint64_t)n * n;
-        mf += n;
-        for (uint32_t i = 0; i < n; i++) r->lane_rowptr[op->map[op->offsets[e] + i] + 1]++;
-    }
-    r->lane_ke.resize(kf);
-    r->lane_map.resize(mf);
-    for (uint32_t e = 0; e < ne; e++) {
-        const uint32_t n = op->offsets[e + 1] - op->offsets[e];
-        const double* k = op->ke.data() + op->kofs[e];
-        float* kd = r->lane_ke.data() + r->lane_info[3ull * e];
-        for (uint64_t i = 0; i < (uint64_t)n * n; i++) kd[i] = (float)k[i];
-        for (uint32_t i = 0; i < n; i++) {
-            const uint32_t d = op->map[op->offsets[e] + i];
-            r->lane_map[r->lane_info[3ull * e + 1] + i] = d | (is_bc[d] ? afm::kBcFlag : 0u);
-        }
-    }
-    for (uint32_t d = 0; d < nd; d++) r->lane_rowptr[d + 1] += r->lane_rowptr[d];
-    r->lane_pairs.resize(r->lane_rowptr[nd]);
-    std::vector<uint32_t> fill(r->lane_rowptr.begin(), r->lane_rowptr.end() - 1);
-    for (uint32_t e = 0; e < ne; e++)  // element order: each row sums its elements in that order
-        for (uint32_t i = 0; i < op->offsets[e + 1] - op->offsets[e]; i++)
-            r->lane_pairs[fill[op->map[op->offsets[e] + i]]++] = (e << afm::kLaneRowBits) | i;
-}
-
-// Uploads the lane copy (one allocation on the operator's stream) and fills
-// the request's lane job; the host copy is released.
-int upload_lane(Request* r) {
+// The lane's segment table of a finalised operator (FP64_SPLIT arena in
+// colour segments), uploaded on the operator's stream.
+int build_lane_segs(Request* r) {
     afm_operator* op = r->op;
-    const size_t b_ke = r->lane_ke.size() * 4, b_map = r->lane_map.size() * 4, b_info = r->lane_info.size() * 4,
-                 b_row = r->lane_rowptr.size() * 4, b_pair = r->lane_pairs.size() * 4;
-    auto up = [](size_t b) { return (b + 255) / 256 * 256; };
-    const size_t total = up(b_ke) + up(b_map) + up(b_info) + up(b_row) + up(b_pair);
-    if (cudaMallocAsync((void**)&r->d_lane, total, op->stream) != cudaSuccess) return AFM_ERR_OOM;
-    unsigned char* at = r->d_lane;
-    auto put = [&](const void* src, size_t b) {
-        unsigned char* dst = at;
-        at += up(b);
-        return b == 0 || cudaMemcpyAsync(dst, src, b, cudaMemcpyHostToDevice, op->stream) == cudaSuccess ? dst
-                                                                                                         : nullptr;
-    };
-    afm::LaneJob& J = r->lane_job;
-    J.ke32 = reinterpret_cast<const float*>(put(r->lane_ke.data(), b_ke));
-    J.emap = reinterpret_cast<const uint32_t*>(put(r->lane_map.data(), b_map));
-    J.einfo = reinterpret_cast<const uint32_t*>(put(r->lane_info.data(), b_info));
-    J.rowptr = reinterpret_cast<const uint32_t*>(put(r->lane_rowptr.data(), b_row));
-    J.pairs = reinterpret_cast<const uint32_t*>(put(r->lane_pairs.data(), b_pair));
-    J.n_elem = op->n_elem;
-    J.n_ke = (uint32_t)r->lane_ke.size();
-    J.n_map = (uint32_t)r->lane_map.size();
-    J.n_pairs = (uint32_t)r->lane_pairs.size();
-    // pageable sources: the copies must finish before the vectors are released
-    if (!J.ke32 || !J.emap || !J.einfo || !J.rowptr || !J.pairs || cudaStreamSynchronize(op->stream) != cudaSuccess)
+    std::vector<afm::LaneSeg> segs;
+    std::vector<uint32_t> colors;
+    for (const afm::Segment& g : op->segs) {
+        if (g.units == 0) continue;
+        afm::LaneSeg L{};
+        L.ke = reinterpret_cast<const float*>(op->d_ke + g.ke_offset);  // hi plane first in every unit
+        L.map = op->d_map + g.map_offset;
+        L.unit_floats = g.unit_bytes / 4;
+        L.n = g.n;
+        L.regime = (uint32_t)g.regime;
+        L.units = g.units;
+        L.count = g.count;
+        segs.push_back(L);
+        colors.push_back(g.color);
+    }
+    // segments are colour-sorted: a cluster barrier after the last segment of each colour
+    for (size_t k = 0; k < segs.size(); k++)
+        segs[k].sync_after = (k + 1 == segs.size() || colors[k + 1] != colors[k]) ? 1u : 0u;
+    r->lane_nsegs = (uint32_t)segs.size();
+    if (segs.empty()) return AFM_SUCCESS;
+    if (cudaMallocAsync((void**)&r->d_lane_segs, sizeof(afm::LaneSeg) * segs.size(), op->stream) != cudaSuccess)
+        return AFM_ERR_OOM;
+    if (cudaMemcpyAsync(r->d_lane_segs, segs.data(), sizeof(afm::LaneSeg) * segs.size(), cudaMemcpyHostToDevice,
+                        op->stream) != cudaSuccess ||
+        cudaStreamSynchronize(op->stream) != cudaSuccess)  // segs is a local vector
         return AFM_ERR_CUDA;
-    std::vector<float>().swap(r->lane_ke);
-    std::vector<uint32_t>().swap(r->lane_map);
-    std::vector<uint32_t>().swap(r->lane_info);
-    std::vector<uint32_t>().swap(r->lane_rowptr);
-    std::vector<uint32_t>().swap(r->lane_pairs);
     return AFM_SUCCESS;
 }
 
 int start(afm_server* s, Request* r) {
     afm_operator* op = r->op;
     const size_t n = op->n_dofs;
-    const bool lane = r->lane_candidate && op->precision == AFM_PREC_FP64_SPLIT && op->matfree_type != 2 &&
-                      !r->lane_rowptr.empty();
+    const bool lane = r->lane_candidate && op->precision == AFM_PREC_FP64_SPLIT && !op->use_patches &&
+                      op->matfree_type != 2;
     // priority by size: one level per factor 8 of element-matrix bytes above 8 MB
     if (s->priorities && s->prio_high < s->prio_low) {
         int level = 0;
@@ -361,7 +312,7 @@ int start(afm_server* s, Request* r) {
         if (st != AFM_SUCCESS) return st;
     }
     if (lane) {
-        const int st = upload_lane(r);
+        const int st = build_lane_segs(r);
         if (st != AFM_SUCCESS) return st;
     }
     if (cudaMallocAsync((void**)&r->d_bx, 2 * n * sizeof(double), op->stream) != cudaSuccess) return AFM_ERR_OOM;
@@ -402,8 +353,9 @@ int launch_lane_batch(afm_server* s) {
     for (size_t i = 0; i < batch.size(); i++) {
         Request* r = batch[i];
         afm::LaneJob& J = s->h_jobs[i];
-        J = r->lane_job;  // the operator's lane copy
-        afm::mixed_lane_job(r->ms, J);  // the solve's vectors, scalars and error flags
+        afm::mixed_lane_job(r->ms, J);
+        J.segs = r->d_lane_segs;
+        J.n_segs = r->lane_nsegs;
         cudaStreamWaitEvent(s->lane_stream, r->ms.ev, 0);
     }
     cudaError_t e = cudaMemcpyAsync(s->d_jobs, s->h_jobs, sizeof(afm::LaneJob) * batch.size(),
