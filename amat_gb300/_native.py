@@ -100,6 +100,7 @@ AFM_SIGNATURES = {
     "afm_server_destroy": (I, [P]),
     "afm_server_set_lane": (I, [P, U64, U32]),
     "afm_get_solve_trace": (I, [P, U32, P, P, P]),
+    "afm_debug_segment_geometry": (I, [I, U32, P]),
     "afm_server_get_info": (I, [P, P]),
     "afm_server_set_inner_format": (I, [P, I]),
     "afm_server_set_priorities": (I, [P, I]),

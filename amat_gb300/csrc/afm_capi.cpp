@@ -83,6 +83,14 @@ size_t patch_smem_fp64(const PatchPlanGeom& pg, uint32_t copy_bytes);
 size_t patch_smem_split(const PatchPlanGeom& pg, uint32_t copy_bytes);
 size_t patch_smem_fp32(const PatchPlanGeom& pg, uint32_t copy_bytes);
 
+void segment_smem_fp64_geom(const Segment& s, uint64_t copy_bytes, uint64_t unit_bytes, uint32_t* out);
+void segment_smem_split_geom(const Segment& s, uint64_t copy_bytes, uint64_t unit_bytes, uint32_t* out);
+void segment_smem_fp32_geom(const Segment& s, uint64_t copy_bytes, uint64_t unit_bytes, uint32_t* out);
+void segment_smem_f32sym_geom(const Segment& s, uint64_t copy_bytes, uint64_t unit_bytes, uint32_t* out);
+void segment_smem_f32symx_geom(const Segment& s, uint64_t copy_bytes, uint64_t unit_bytes, uint32_t* out);
+void segment_smem_splitsymx_geom(const Segment& s, uint64_t copy_bytes, uint64_t unit_bytes, uint32_t* out);
+void segment_smem_f32symc_geom(const Segment& s, uint64_t copy_bytes, uint64_t unit_bytes, uint32_t* out);
+
 cudaError_t launch_patches(int prec, const PatchPlanGeom& pg, const PatchArgs& a, int sm_count, bool pdl,
                            cudaStream_t stream) {
     switch (prec) {
@@ -2524,6 +2532,31 @@ int afm_solve_cg_mixed_device(afm_operator* op, const double* d_b, double* d_x, 
     }
     const int st = mixed_end(m, stats);
     return s != AFM_SUCCESS ? s : st;
+}
+
+int afm_debug_segment_geometry(int kind, uint32_t n, uint32_t* out) {
+    if (!out || n <= kTpeMaxN || n > kMaxN || kind < 0 || kind > 6)
+        return fail(AFM_ERR_INVALID_ARG, "kind %d (0..6), n %u (%u..%u)", kind, n, kTpeMaxN + 1, kMaxN);
+    // the unit sizes of build_segments and layout_sym for one element of n DoFs
+    const uint64_t plane = (uint64_t)(n * n + 3) / 4 * 4;
+    const uint64_t S = (uint64_t)(n / 2 + 1) * n, P = (S + 3) / 4 * 4;
+    uint64_t unit = 0, copy = 0;
+    Segment s;
+    s.n = n;
+    s.regime = REG_WPE;
+    s.units = s.count = 1u << 20;
+    switch (kind) {
+        case 0: unit = copy = round16((uint64_t)n * n * 8); segment_smem_fp64_geom(s, copy, unit, out); break;
+        case 1: unit = copy = 2 * plane * 4; segment_smem_split_geom(s, copy, unit, out); break;
+        case 2: unit = 2 * plane * 4; copy = plane * 4; segment_smem_fp32_geom(s, copy, unit, out); break;
+        case 3: unit = copy = round16(S * 4); segment_smem_f32sym_geom(s, copy, unit, out); break;
+        case 4: unit = copy = round16(P * 4 + S * 2); segment_smem_f32symx_geom(s, copy, unit, out); break;
+        case 5: unit = copy = round16(P * 4 + S * 2); segment_smem_splitsymx_geom(s, copy, unit, out); break;
+        default: unit = copy = round16(P * 4 + S * 2); segment_smem_f32symc_geom(s, copy, unit, out); break;
+    }
+    out[6] = (uint32_t)unit;
+    out[7] = (uint32_t)copy;
+    return ok();
 }
 
 int afm_get_solve_trace(afm_operator* op, uint32_t cap, int* inner_iterations, double* rel_residual, uint32_t* n) {

@@ -309,6 +309,22 @@ size_t PATCH_SMEM_FN(const PatchPlanGeom& pg, uint32_t copy_bytes) {
 
 size_t SMEM_FN(const Segment& s) { return ring_layout(s, s.unit_bytes, s.unit_bytes, false, nullptr).total(); }
 
+#define AFM_CAT2(a, b) a##b
+#define AFM_CAT(a, b) AFM_CAT2(a, b)
+// Launch geometry of a warp-group segment (host checks): out = chunk,
+// stages, consumer warps, element groups, column groups, dynamic shared
+// memory bytes.
+void AFM_CAT(SMEM_FN, _geom)(const Segment& s, uint64_t copy_bytes, uint64_t unit_bytes, uint32_t* out) {
+    GroupGeom G{1, 1, 1, 1};
+    const RingLayout L = ring_layout(s, copy_bytes, unit_bytes, false, &G);
+    out[0] = L.chunk;
+    out[1] = L.stages;
+    out[2] = L.warps;
+    out[3] = G.ng;
+    out[4] = G.gc;
+    out[5] = L.total();
+}
+
 // Raises the dynamic shared-memory limit of every kernel instance on the
 // current device; called once per device before any launch or capture.
 cudaError_t CONFIG_FN() {

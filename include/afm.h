@@ -301,6 +301,14 @@ int afm_solve_cg(afm_operator* op, const double* b, double* x, double rtol, doub
 int afm_solve_cg_device(afm_operator* op, const double* d_b, double* d_x, double rtol, double atol, int maxit,
                         int norm_type, afm_solve_stats* stats);
 
+/* Diagnostic, host only: the launch geometry the warp-group kernel takes for
+ * elements of n DoFs (16 < n <= 96) in arithmetic `kind` (0 FP64, 1 split,
+ * 2 FP32 from the split arena's hi plane, 3 symmetric FP32 copy, 4 corrected
+ * copy with FP32 u, 5 corrected copy with double-float u, 6 corrected copy with
+ * FP32 row sums): out[0..7] = element units per ring slot, ring stages,
+ * consumer warps, element groups, column groups, dynamic shared memory bytes,
+ * unit bytes, bytes copied per unit. */
+int afm_debug_segment_geometry(int kind, uint32_t n, uint32_t* out);
 /* The last mixed-precision solve of the operator (afm_solve_cg_mixed*): at
  * each FP64 residual, the inner iterations done so far and ||b - A x|| / ||b||.
  * *n = the count; up to cap entries are written. */
