@@ -85,6 +85,7 @@ AFM_SIGNATURES = {
     "afm_set_precision": (I, [P, I]),
     "afm_set_patch_mode": (I, [P, I]),
     "afm_set_symmetric_inner": (I, [P, I]),
+    "afm_set_fused_colours": (I, [P, I]),
     "afm_set_wait_limit": (I, [P, D]),
     "afm_set_wait_probe": (I, [P, I]),
     "afm_set_element_kind": (I, [P, I, D, D, U32]),

@@ -184,6 +184,10 @@ class aMatFree:
         correction with FP64 sums, 0 the hi plane."""
         check(self._lib.afm_set_symmetric_inner(self._h, int(fmt)), "afm_set_symmetric_inner")
 
+    def set_fused_colours(self, enable):
+        """Every colour of a split product in one cooperative launch (default) or one launch per colour."""
+        check(self._lib.afm_set_fused_colours(self._h, int(bool(enable))), "afm_set_fused_colours")
+
     def set_wait_limit(self, seconds):
         """Limit of each wait inside the element kernels (4 s by default); past it a call reports ERR_TIMEOUT."""
         check(self._lib.afm_set_wait_limit(self._h, float(seconds)), "afm_set_wait_limit")

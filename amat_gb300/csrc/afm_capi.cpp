@@ -41,6 +41,8 @@ cudaError_t launch_batched_fp64(const Segment& s, const BatchArgs& a, int sm_cou
                                 cudaStream_t st);
 cudaError_t launch_batched_split(const Segment& s, const BatchArgs& a, int sm_count, int tr, int ng, bool pdl,
                                  cudaStream_t st);
+cudaError_t launch_fused_split(const Segment* segs, uint32_t ncol, const SegArgs& a, unsigned* gbar, int sm_count,
+                               cudaStream_t st);
 bool batched_tc_supported(uint32_t n, uint32_t nrhs);
 cudaError_t launch_batched_tc(const Segment& s, const BatchArgs& a, int sm_count, bool pdl, cudaStream_t stream);
 cudaError_t launch_batched_fp32(const Segment& s, const BatchArgs& a, int sm_count, int tr, int ng, bool pdl,
@@ -243,6 +245,8 @@ void free_device(afm_operator* op) {
     dfree(op, op->d_bc_idx);
     dfree(op, op->d_bc_val);
     dfree(op, op->d_bcmask);
+    dfree(op, op->d_gbar);
+    op->fused_ok = false;
     dfree(op, op->d_work);
     dfree(op, op->d_work32);
     dfree(op, op->d_work64i);
@@ -909,6 +913,31 @@ int enqueue_matvec(afm_operator* op, void* d_v, const void* d_u, int bc_mode, cu
             AFM_CUDA(launch_patch_combine((f32 && !symx) ? 4 : 8, d_v, op->d_pv, op->d_shared_dof,
                                           op->d_shared_off, op->d_shared_idx, op->n_shared, st));
         if (via_vx) AFM_CUDA(launch_to_f32(d_v32, op->d_vx, op->n_dofs, st));
+        return AFM_SUCCESS;
+    }
+    // split products of a plan with one element size: every colour in one cooperative launch (outside
+    // stream capture: captured solve iterations keep the colour launches)
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (op->fused && op->fused_ok && kprec == AFM_PREC_FP64_SPLIT && !sym && !f32 &&
+        cudaStreamIsCapturing(st, &cap) == cudaSuccess && cap == cudaStreamCaptureStatusNone) {
+        const Segment& s0 = op->segs[0];
+        SegArgs a;
+        a.ke = op->d_ke;
+        a.map = op->d_map;
+        a.u = d_u;
+        a.v = d_v;
+        a.units = s0.units;
+        a.count = s0.count;
+        a.unit_bytes = s0.unit_bytes;
+        a.copy_bytes = (uint32_t)s0.unit_bytes;
+        a.plane = s0.plane;
+        a.bc_mode = bc_mode;
+        a.err = op->d_err;
+        a.umax = op->d_usc;
+        a.wait_ns = op->wait_ns;
+        a.probe = op->wait_probe ? op->d_err + (kErrWords - 1) : nullptr;
+        AFM_CUDA(cudaMemsetAsync(op->d_gbar, 0, sizeof(unsigned) * op->segs.size(), st));
+        AFM_CUDA(launch_fused_split(op->segs.data(), (uint32_t)op->segs.size(), a, op->d_gbar, op->sm_count, st));
         return AFM_SUCCESS;
     }
     for (const Segment& s : op->segs) {
@@ -1799,6 +1828,13 @@ int afm_set_wait_probe(afm_operator* op, int enable) {
     return ok();
 }
 
+int afm_set_fused_colours(afm_operator* op, int enable) {
+    AFM_CHECK_OP(op);
+    if (enable != 0 && enable != 1) return fail(AFM_ERR_INVALID_ARG, "fused colours %d (0 or 1)", enable);
+    op->fused = enable == 1;
+    return ok();
+}
+
 int afm_set_symmetric_inner(afm_operator* op, int format) {
     AFM_CHECK_OP(op);
     if (format < 0 || format > 5) return fail(AFM_ERR_INVALID_ARG, "symmetric inner format %d (0 to 5)", format);
@@ -2225,6 +2261,20 @@ int afm_finalize(afm_operator* op) {
                                  op->stream));
         AFM_CUDA(cudaMemcpyAsync(op->d_bc_val, op->values.data(), sizeof(double) * op->n_bc,
                                  cudaMemcpyHostToDevice, op->stream));
+    }
+    // every colour of a split product in one cooperative launch: a segment plan whose elements share one size
+    // in the warp-group regime (each colour launch of its own pays the ramp of its copies and the tail of its
+    // last elements, with the next launch unable to overlap: one CTA fills an SM's shared memory)
+    op->fused_ok = false;
+    if (!op->use_patches && !op->dup_in_element && prec == AFM_PREC_FP64_SPLIT && !op->segs.empty() &&
+        op->segs.size() <= kMaxFusedColours) {
+        bool same = true;
+        for (const Segment& g : op->segs)
+            same = same && g.regime == REG_WPE && g.n == op->segs[0].n && g.units > 0;
+        if (same) {
+            AFM_CUDA(dalloc(op, &op->d_gbar, sizeof(unsigned) * kMaxFusedColours));
+            op->fused_ok = true;
+        }
     }
     // one launch for every patch colour when the colours are small (a launch per colour would leave
     // most SMs idle between colours), else one launch per colour

@@ -52,6 +52,9 @@ struct Segment {
     uint32_t sym_plane = 0;      // entries of a unit's FP32 plane before its BF16 correction plane (0: none)
 };
 
+// Colours of one fused (cooperative) launch of the warp-group kernel, at most.
+constexpr uint32_t kMaxFusedColours = 48;
+
 // Arguments of one segment launch.
 struct SegArgs {
     const unsigned char* ke;  // arena + segment offset
@@ -304,6 +307,10 @@ struct afm_operator {
     bool wait_probe = false;         // afm_set_wait_probe
     unsigned long long* d_usc = nullptr;  // u-scale words of the split products (kUscWords, afm_solver.hpp)
     uint8_t* d_bcmask = nullptr;     // 1 per constrained DoF (null without constraints)
+    // one cooperative launch for every colour of a split product (segment plans of one element size)
+    bool fused_ok = false;           // the plan allows it (decided at finalize)
+    bool fused = true;               // afm_set_fused_colours
+    unsigned* d_gbar = nullptr;      // grid-barrier counters of the fused launch
     std::vector<int> trace_iters;    // the last mixed solve: inner iterations at each FP64 residual
     std::vector<double> trace_res;   // ... and that residual over ||b||
     double* d_work = nullptr;        // host-API staging and solver vectors

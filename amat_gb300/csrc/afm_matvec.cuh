@@ -797,11 +797,67 @@ __device__ __forceinline__ void group_sync(uint32_t id, uint32_t threads) {
         named_barrier(id, threads);
 }
 
+// Colours of one fused launch (afm_wpg_fused_kernel): per colour the offset
+// of its first unit in the arena (bytes) and in the map (entries), its units
+// and elements; gbar[c - 1] counts the CTAs that finished colour c - 1.
+struct ColourTable {
+    uint32_t ncol;
+    unsigned* gbar;
+    uint64_t ke_off[kMaxFusedColours];
+    uint64_t map_off[kMaxFusedColours];
+    uint32_t units[kMaxFusedColours];
+};
+
+// ld.global.cg: an L2 load that bypasses L1, for v in a fused launch, whose
+// earlier colours other CTAs have written since this SM may have cached it.
+__device__ __forceinline__ double ld_cg_hint(const double* p, uint64_t pol) {
+    double x;
+    asm volatile("ld.global.cg.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(x) : "l"(p), "l"(pol) : "memory");
+    return x;
+}
+__device__ __forceinline__ float ld_cg_hint(const float* p, uint64_t pol) {
+    float x;
+    asm volatile("ld.global.cg.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(x) : "l"(p), "l"(pol) : "memory");
+    return x;
+}
+
+__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
+    unsigned x;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(x) : "l"(p) : "memory");
+    return x;
+}
+
+// Grid barrier of a cooperative launch (all CTAs resident), between two
+// colours: the CTA's consumer warps meet on named barrier 15, thread 0
+// publishes the CTA's writes and counts it in, then waits (bounded by limit;
+// on expiry it sets *abort) until every CTA has arrived.
+__device__ __forceinline__ void grid_barrier(unsigned* ctr, uint32_t threads, volatile int* abort,
+                                             unsigned long long limit) {
+    named_barrier(15, threads);
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(ctr, 1u);
+        const unsigned long long t0 = globaltimer_ns();
+        while (ld_acquire_gpu(ctr) < gridDim.x) {
+            if (*abort || globaltimer_ns() - t0 > limit) {
+                *abort = 1;
+                break;
+            }
+            __nanosleep(64);
+        }
+        __threadfence();
+    }
+    named_barrier(15, threads);
+}
+
 // CH: ring slots may hold several element units (L.chunk); without it the
 // chunk is the constant 1 and the walk folds to one element per slot.
-template <int NT, typename A, bool CH>
-__global__ void __launch_bounds__((A::kWpgWarps + 1) * 32, 1)
-    afm_wpg_kernel(SegArgs a, RingLayout L, GroupGeom G, uint32_t n_rt) {
+// FU: the colours of T in one cooperative launch, a grid barrier between
+// them (every colour's CTA split as a colour launch of its own would have);
+// without it one segment, a.units units from a.ke and a.map.
+template <int NT, typename A, bool CH, bool FU>
+__device__ __forceinline__ void wpg_run(const SegArgs& a, const RingLayout& L, const GroupGeom& G, uint32_t n_rt,
+                                        const ColourTable* T) {
     using KT = typename A::KT;
     using UT = typename A::UT;
     using VT = typename A::VT;
@@ -819,9 +875,14 @@ __global__ void __launch_bounds__((A::kWpgWarps + 1) * 32, 1)
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t S = L.stages;
 
-    const uint32_t per = a.units / gridDim.x, rem = a.units % gridDim.x;
-    const uint32_t begin = blockIdx.x * per + min(blockIdx.x, rem);
-    const uint32_t cnt = per + (blockIdx.x < rem ? 1u : 0u);
+    const uint32_t ncol = FU ? T->ncol : 1u;
+    // this CTA's units of colour col: [begin, begin + cnt), as a launch of that colour alone would split them
+    auto share = [&](uint32_t col, uint32_t& begin, uint32_t& cnt) {
+        const uint32_t units = FU ? T->units[col] : a.units;
+        const uint32_t per = units / gridDim.x, rem = units % gridDim.x;
+        begin = blockIdx.x * per + min(blockIdx.x, rem);
+        cnt = per + (blockIdx.x < rem ? 1u : 0u);
+    };
 
     if (threadIdx.x == 0) {
         for (uint32_t s = 0; s < S; s++) {
@@ -838,21 +899,32 @@ __global__ void __launch_bounds__((A::kWpgWarps + 1) * 32, 1)
     // copies of small element units are issue-bound one by one); chunk c goes
     // to group c % ng, which takes its elements in order
     const uint32_t E = CH ? L.chunk : 1u;
-    const uint32_t nch = (cnt + E - 1) / E;
     if (warp == G.ng * G.g) {  // producer
         if (lane == 0) {
             const uint64_t pol = l2_evict_first_policy();
-            uint32_t issued = 0;
-            for (uint32_t c = 0; c < nch; c++) {
-                const uint32_t s = c % S;
-                if (c >= S && !mbar_wait_abortable(&empty[s], ((c / S) - 1) & 1, abort, a.wait_ns)) break;
-                const uint32_t e0 = c * E, ne = min(E, cnt - e0);
-                tag[s] = c;
-                // E > 1 only for whole units (copy_bytes == unit_bytes), so the chunk is contiguous
-                mbar_arrive_expect_tx(&full[s], ne * a.copy_bytes);
-                bulk_load(smem + (size_t)s * L.slot_bytes, a.ke + (size_t)(begin + e0) * a.unit_bytes,
-                          ne * a.copy_bytes, &full[s], pol);
-                issued = c + 1;
+            // ring index g runs on across colours: the copies of a colour start while the previous one drains
+            uint32_t issued = 0, gbase = 0;
+            bool stop = false;
+            for (uint32_t col = 0; col < ncol && !stop; col++) {
+                uint32_t begin, cnt;
+                share(col, begin, cnt);
+                const unsigned char* ke = FU ? a.ke + T->ke_off[col] : a.ke;
+                const uint32_t nch = (cnt + E - 1) / E;
+                for (uint32_t c = 0; c < nch; c++) {
+                    const uint32_t g = gbase + c, s = g % S;
+                    if (g >= S && !mbar_wait_abortable(&empty[s], ((g / S) - 1) & 1, abort, a.wait_ns)) {
+                        stop = true;
+                        break;
+                    }
+                    const uint32_t e0 = c * E, ne = min(E, cnt - e0);
+                    tag[s] = g;
+                    // E > 1 only for whole units (copy_bytes == unit_bytes), so the chunk is contiguous
+                    mbar_arrive_expect_tx(&full[s], ne * a.copy_bytes);
+                    bulk_load(smem + (size_t)s * L.slot_bytes, ke + (size_t)(begin + e0) * a.unit_bytes,
+                              ne * a.copy_bytes, &full[s], pol);
+                    issued = g + 1;
+                }
+                gbase += nch;
             }
             allow_dependent_launch();
             if (*abort) atomicOr(a.err, kErrTimeout);
@@ -880,12 +952,20 @@ __global__ void __launch_bounds__((A::kWpgWarps + 1) * 32, 1)
     auto ubuf = [&](uint32_t p) { return reinterpret_cast<UT*>(ubuf0 + (size_t)p * ub); };
     auto pbuf = [&](uint32_t p) { return pbuf0 + (size_t)p * pstride; };
 
+    const uint64_t keep = l2_evict_last_policy(), stream_pol = l2_evict_first_policy();
+    // v written by other CTAs in an earlier colour of a fused launch is read past L1
+    auto v_load = [&](const VO* pv) { return FU ? ld_cg_hint(pv, keep) : ld_hint(pv, keep); };
+    const uint32_t consumer_threads = G.ng * G.g * 32;
+    uint32_t gbase = 0;  // ring index of the colour's first chunk
+    for (uint32_t col = 0; col < ncol; col++) {
+    uint32_t begin, cnt;
+    share(col, begin, cnt);
+    const uint32_t* __restrict__ mapc = FU ? a.map + T->map_off[col] : a.map;
     uint32_t dof_c = 0, dof_n = 0, dof_nn = 0;
     VO vold_c = VO(0), vold_n = VO(0);
     VT u_n = VT(0);
-    const uint64_t keep = l2_evict_last_policy(), stream_pol = l2_evict_first_policy();
     auto map_at = [&](uint32_t i) {
-        return rvalid ? ld_nc_hint(a.map + (size_t)(begin + i) * n + r, stream_pol) : 0u;
+        return rvalid ? ld_nc_hint(mapc + (size_t)(begin + i) * n + r, stream_pol) : 0u;
     };
 
     // The group's elements in order: element ch E + jc of chunk ch, the chunks
@@ -909,8 +989,11 @@ __global__ void __launch_bounds__((A::kWpgWarps + 1) * 32, 1)
         }
         if (inext < cnt) dof_n = map_at(inext);
     }
-    wait_prior_grid();
-    if (gatherer && i < cnt && rvalid) vold_c = ld_hint(v + (dof_c & kDofMask), keep);
+    if (!FU || col == 0)
+        wait_prior_grid();
+    else  // every CTA has written the previous colour's sums to v
+        grid_barrier(T->gbar + (col - 1), consumer_threads, abort, a.wait_ns);
+    if (gatherer && i < cnt && rvalid) vold_c = v_load(v + (dof_c & kDofMask));
     group_sync(bar_id, bar_threads);
     bool ok = false;  // the current chunk's slot has landed (one verdict per warp and chunk)
     uint32_t s = 0;   // the current chunk's ring slot
@@ -922,15 +1005,16 @@ __global__ void __launch_bounds__((A::kWpgWarps + 1) * 32, 1)
         if (gatherer && rvalid) {
             if (inext < cnt) {
                 u_n = load_u_hint(u, dof_n, a.bc_mode, keep);
-                vold_n = ld_hint(v + (dof_n & kDofMask), keep);
+                vold_n = v_load(v + (dof_n & kDofMask));
             }
             if (inn < cnt) dof_nn = map_at(inn);
         }
         Acc acc = A::zero();
         // one verdict per warp and chunk: the block below synchronises the warp, so no lane may skip it alone
         if (jc == 0) {
-            s = ch % S;
-            ok = __all_sync(0xffffffffu, ring_wait(&full[s], &tag[s], ch, (ch / S) & 1, abort, a.wait_ns));
+            const uint32_t g = gbase + ch;
+            s = g % S;
+            ok = __all_sync(0xffffffffu, ring_wait(&full[s], &tag[s], g, (g / S) & 1, abort, a.wait_ns));
         }
         if (ok) {
             const unsigned char* ks = smem + (size_t)s * L.slot_bytes + (size_t)jc * a.unit_bytes;
@@ -1022,7 +1106,23 @@ __global__ void __launch_bounds__((A::kWpgWarps + 1) * 32, 1)
         jn = jnn;
         inext = inn;
     }
+    gbase += (cnt + E - 1) / E;
+    }  // colours
     if (lane == 0 && *abort) atomicOr(a.err, kErrTimeout);
+}
+
+template <int NT, typename A, bool CH>
+__global__ void __launch_bounds__((A::kWpgWarps + 1) * 32, 1)
+    afm_wpg_kernel(SegArgs a, RingLayout L, GroupGeom G, uint32_t n_rt) {
+    wpg_run<NT, A, CH, false>(a, L, G, n_rt, nullptr);
+}
+
+// All colours of a segment plan with one element size in one cooperative
+// launch (one CTA per SM, all resident), a grid barrier between colours.
+template <int NT, typename A, bool CH>
+__global__ void __launch_bounds__((A::kWpgWarps + 1) * 32, 1)
+    afm_wpg_fused_kernel(SegArgs a, RingLayout L, GroupGeom G, uint32_t n_rt, const __grid_constant__ ColourTable T) {
+    wpg_run<NT, A, CH, true>(a, L, G, n_rt, &T);
 }
 
 // ---- thread per element (n <= 16) ------------------------------------------

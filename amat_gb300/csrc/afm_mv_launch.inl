@@ -82,7 +82,7 @@ constexpr uint32_t kChunkBytes = 16384;
 // Ring layout and (for the warp-group kernel) group geometry of a segment;
 // unit_bytes: the stride between units (chunks need whole units copied).
 static RingLayout ring_layout(const Segment& s, uint64_t copy_bytes, uint64_t unit_bytes, bool dup,
-                              GroupGeom* geom) {
+                              GroupGeom* geom, bool fused = false) {
     RingLayout L;
     const size_t ut = sizeof(typename ARITH::UT), acc = sizeof(typename ARITH::Acc);
     L.slot_bytes = (uint32_t)((copy_bytes + kSlotAlign - 1) / kSlotAlign * kSlotAlign);
@@ -96,8 +96,10 @@ static RingLayout ring_layout(const Segment& s, uint64_t copy_bytes, uint64_t un
         G.g = G.gr * G.gc;
         const uint32_t ub = wpg_ubuf_bytes(ARITH::kSym ? 2 * s.n : s.n, (uint32_t)ut);  // u staged twice (symmetric)
         const uint32_t pstride = (G.gc > 1 ? G.gc - 1 : 1) * s.n;
-        // groups of one warp synchronise with __syncwarp; larger groups take one named barrier each (15 ids)
-        const uint32_t ng_max = G.g == 1 ? ARITH::kWpgWarps : std::min<uint32_t>(ARITH::kWpgWarps / G.g, 15u);
+        // groups of one warp synchronise with __syncwarp; larger groups take one named barrier each (ids 1..15;
+        // a fused launch keeps id 15 for its grid barrier)
+        const uint32_t ng_max =
+            G.g == 1 ? ARITH::kWpgWarps : std::min<uint32_t>(ARITH::kWpgWarps / G.g, fused ? 14u : 15u);
         const uint32_t emax = copy_bytes == unit_bytes
                                   ? std::max<uint32_t>(1u, std::min<uint32_t>(kMaxChunk, (uint32_t)(kChunkBytes / copy_bytes)))
                                   : 1u;
@@ -309,6 +311,68 @@ size_t PATCH_SMEM_FN(const PatchPlanGeom& pg, uint32_t copy_bytes) {
 
 size_t SMEM_FN(const Segment& s) { return ring_layout(s, s.unit_bytes, s.unit_bytes, false, nullptr).total(); }
 
+#ifdef FUSED_FN
+namespace {
+template <int NT, bool CH>
+void* fused_ptr() {
+    return (void*)afm_wpg_fused_kernel<NT, ARITH, CH>;
+}
+void* pick_fused_kernel(uint32_t n, bool chunked) {
+    if (chunked) {
+        switch (n) {
+            case 24: return fused_ptr<24, true>();
+            case 30: return fused_ptr<30, true>();
+            default: return fused_ptr<0, true>();
+        }
+    }
+    switch (n) {
+        case 24: return fused_ptr<24, false>();
+        case 30: return fused_ptr<30, false>();
+        case 60: return fused_ptr<60, false>();
+        default: return fused_ptr<0, false>();
+    }
+}
+}  // namespace
+
+// The colours segs[0 .. ncol) of a segment plan whose elements share one size
+// (warp-group regime) in one cooperative launch: one CTA per SM, each taking
+// the share of every colour that a launch of that colour alone would give it,
+// a grid barrier between colours (gbar: ncol - 1 counters, zero at launch).
+// a.ke and a.map: the arena and map bases; the colours' offsets come from segs.
+cudaError_t FUSED_FN(const Segment* segs, uint32_t ncol, const SegArgs& a, unsigned* gbar, int sm_count,
+                     cudaStream_t stream) {
+    if (ncol == 0 || ncol > kMaxFusedColours || segs[0].regime != REG_WPE) return cudaErrorInvalidValue;
+    GroupGeom G{1, 1, 1, 1};
+    const RingLayout L = ring_layout(segs[0], a.copy_bytes, a.unit_bytes, false, &G, true);
+    if (L.stages < 2) return cudaErrorInvalidConfiguration;
+    void* fn = pick_fused_kernel(segs[0].n, L.chunk > 1);
+    ColourTable T{};
+    T.ncol = ncol;
+    T.gbar = gbar;
+    for (uint32_t c = 0; c < ncol; c++) {
+        if (segs[c].n != segs[0].n || segs[c].regime != REG_WPE) return cudaErrorInvalidValue;
+        T.ke_off[c] = segs[c].ke_offset;
+        T.map_off[c] = segs[c].map_offset;
+        T.units[c] = segs[c].units;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((uint32_t)sm_count);
+    cfg.blockDim = dim3((L.warps + 1) * 32);
+    cfg.dynamicSmemBytes = L.total();
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    SegArgs args = a;
+    RingLayout Lc = L;
+    uint32_t n_rt = segs[0].n;
+    void* params[] = {&args, &Lc, &G, &n_rt, &T};
+    return cudaLaunchKernelExC(&cfg, fn, params);
+}
+#endif  // FUSED_FN
+
 #define AFM_CAT2(a, b) a##b
 #define AFM_CAT(a, b) AFM_CAT2(a, b)
 // Launch geometry of a warp-group segment (host checks): out = chunk,
@@ -344,6 +408,14 @@ cudaError_t CONFIG_FN() {
                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kSmemBudget + 1024));
             if (e != cudaSuccess) return e;
         }
+#ifdef FUSED_FN
+    for (uint32_t nn : {24u, 30u, 60u, 7u})
+        for (int ch = 0; ch < 2; ch++) {
+            cudaError_t e = cudaFuncSetAttribute(pick_fused_kernel(nn, ch != 0),
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kSmemBudget + 1024));
+            if (e != cudaSuccess) return e;
+        }
+#endif
 #ifdef BATCH_FN
     const int tiles[4][2] = {{2, 8}, {4, 4}, {4, 8}, {6, 8}};
     for (const auto& t : tiles)

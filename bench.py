@@ -398,6 +398,7 @@ def run_ours(args, w, rank, world, local_rank):
         m, dmap, A, ke_host = build_problem(w, prec, dev, keep_ke=True)
     else:
         (m, dmap, A), ke_host = build_problem(w, prec, dev), None
+    A.set_fused_colours(bool(args.fused))
     n = m.n_dofs
     info, ms, u_host, v, clk = measure_device(A, n, args.steps, args.warmup, world, dev, rank, True)
     ms_step = ms / args.steps
@@ -1000,6 +1001,8 @@ def main():
     ap.add_argument("--precision", default="auto", choices=sorted(PREC_NAMES))
     ap.add_argument("--also-native", type=int, default=1, help="also time native FP64 when the split path runs")
     ap.add_argument("--cpu-sample-elems", type=int, default=65536)
+    ap.add_argument("--fused", type=int, default=1, choices=[0, 1],
+                    help="every colour of a split product in one cooperative launch")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU time the baseline sample is timed for")
     ap.add_argument("--mode", default="matvec", choices=["matvec", "solve", "batched", "product", "serve",
                                                          "assembled", "free"])

@@ -197,6 +197,12 @@ int afm_set_patch_mode(afm_operator* op, int mode);
  * mixed-precision solve after a change (outside any stream capture). FP64
  * products never use it. */
 int afm_set_symmetric_inner(afm_operator* op, int format);
+/* 1 (default): the FP64-split product of a segment plan whose elements share
+ * one size (warp-group regime, up to 48 colours) runs every colour in one
+ * cooperative launch, a grid barrier between colours, outside stream capture
+ * (captured solve iterations keep one launch per colour); same results bit for
+ * bit. 0: one launch per colour. */
+int afm_set_fused_colours(afm_operator* op, int enable);
 /* Limit of each wait inside the operator's element kernels (no counterpart
  * in the reference, which ends the process on a device error:
  * include/aMatGpu.hpp:303-306). The kernels' producer and consumer warps meet
