@@ -185,7 +185,7 @@ class aMatFree:
         check(self._lib.afm_set_symmetric_inner(self._h, int(fmt)), "afm_set_symmetric_inner")
 
     def set_fused_colours(self, enable):
-        """Every colour of a split product in one cooperative launch (default) or one launch per colour."""
+        """Every colour of a split product in one cooperative launch, or one launch per colour (default)."""
         check(self._lib.afm_set_fused_colours(self._h, int(bool(enable))), "afm_set_fused_colours")
 
     def set_wait_limit(self, seconds):

@@ -309,7 +309,7 @@ struct afm_operator {
     uint8_t* d_bcmask = nullptr;     // 1 per constrained DoF (null without constraints)
     // one cooperative launch for every colour of a split product (segment plans of one element size)
     bool fused_ok = false;           // the plan allows it (decided at finalize)
-    bool fused = true;               // afm_set_fused_colours
+    bool fused = false;              // afm_set_fused_colours (off: measured slower than the colour launches)
     unsigned* d_gbar = nullptr;      // grid-barrier counters of the fused launch
     std::vector<int> trace_iters;    // the last mixed solve: inner iterations at each FP64 residual
     std::vector<double> trace_res;   // ... and that residual over ||b||

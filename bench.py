@@ -1001,8 +1001,8 @@ def main():
     ap.add_argument("--precision", default="auto", choices=sorted(PREC_NAMES))
     ap.add_argument("--also-native", type=int, default=1, help="also time native FP64 when the split path runs")
     ap.add_argument("--cpu-sample-elems", type=int, default=65536)
-    ap.add_argument("--fused", type=int, default=1, choices=[0, 1],
-                    help="every colour of a split product in one cooperative launch")
+    ap.add_argument("--fused", type=int, default=0, choices=[0, 1],
+                    help="every colour of a split product in one cooperative launch (slower; off by default)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU time the baseline sample is timed for")
     ap.add_argument("--mode", default="matvec", choices=["matvec", "solve", "batched", "product", "serve",
                                                          "assembled", "free"])
