@@ -958,156 +958,156 @@ __device__ __forceinline__ void wpg_run(const SegArgs& a, const RingLayout& L, c
     const uint32_t consumer_threads = G.ng * G.g * 32;
     uint32_t gbase = 0;  // ring index of the colour's first chunk
     for (uint32_t col = 0; col < ncol; col++) {
-    uint32_t begin, cnt;
-    share(col, begin, cnt);
-    const uint32_t* __restrict__ mapc = FU ? a.map + T->map_off[col] : a.map;
-    uint32_t dof_c = 0, dof_n = 0, dof_nn = 0;
-    VO vold_c = VO(0), vold_n = VO(0);
-    VT u_n = VT(0);
-    auto map_at = [&](uint32_t i) {
-        return rvalid ? ld_nc_hint(mapc + (size_t)(begin + i) * n + r, stream_pol) : 0u;
-    };
+        uint32_t begin, cnt;
+        share(col, begin, cnt);
+        const uint32_t* __restrict__ mapc = FU ? a.map + T->map_off[col] : a.map;
+        uint32_t dof_c = 0, dof_n = 0, dof_nn = 0;
+        VO vold_c = VO(0), vold_n = VO(0);
+        VT u_n = VT(0);
+        auto map_at = [&](uint32_t i) {
+            return rvalid ? ld_nc_hint(mapc + (size_t)(begin + i) * n + r, stream_pol) : 0u;
+        };
 
-    // The group's elements in order: element ch E + jc of chunk ch, the chunks
-    // grp, grp + ng, ...; positions advance by increments (no division in
-    // the loop but the slot of a new chunk).
-    auto advance = [&](uint32_t& c, uint32_t& j) {
-        if (++j == E) {
-            j = 0;
-            c += G.ng;
-        }
-    };
-    uint32_t ch = grp, jc = 0, chn = grp, jn = 0;
-    advance(chn, jn);
-    uint32_t i = ch * E, inext = chn * E + jn;
-    if (gatherer && i < cnt) {
-        dof_c = map_at(i);
-        if (rvalid) {
-            const UT x = stage_s<A>(load_u_hint(u, dof_c, a.bc_mode, keep), usk);
-            ubuf(0)[r] = x;
-            if constexpr (A::kSym) ubuf(0)[r + n] = x;
-        }
-        if (inext < cnt) dof_n = map_at(inext);
-    }
-    if (!FU || col == 0)
-        wait_prior_grid();
-    else  // every CTA has written the previous colour's sums to v
-        grid_barrier(T->gbar + (col - 1), consumer_threads, abort, a.wait_ns);
-    if (gatherer && i < cnt && rvalid) vold_c = v_load(v + (dof_c & kDofMask));
-    group_sync(bar_id, bar_threads);
-    bool ok = false;  // the current chunk's slot has landed (one verdict per warp and chunk)
-    uint32_t s = 0;   // the current chunk's ring slot
-    for (uint32_t k = 0; i < cnt; k++) {
-        const uint32_t par = k & 1;
-        uint32_t chnn = chn, jnn = jn;
-        advance(chnn, jnn);
-        const uint32_t inn = chnn * E + jnn;
-        if (gatherer && rvalid) {
-            if (inext < cnt) {
-                u_n = load_u_hint(u, dof_n, a.bc_mode, keep);
-                vold_n = v_load(v + (dof_n & kDofMask));
+        // The group's elements in order: element ch E + jc of chunk ch, the chunks
+        // grp, grp + ng, ...; positions advance by increments (no division in
+        // the loop but the slot of a new chunk).
+        auto advance = [&](uint32_t& c, uint32_t& j) {
+            if (++j == E) {
+                j = 0;
+                c += G.ng;
             }
-            if (inn < cnt) dof_nn = map_at(inn);
-        }
-        Acc acc = A::zero();
-        // one verdict per warp and chunk: the block below synchronises the warp, so no lane may skip it alone
-        if (jc == 0) {
-            const uint32_t g = gbase + ch;
-            s = g % S;
-            ok = __all_sync(0xffffffffu, ring_wait(&full[s], &tag[s], g, (g / S) & 1, abort, a.wait_ns));
-        }
-        if (ok) {
-            const unsigned char* ks = smem + (size_t)s * L.slot_bytes + (size_t)jc * a.unit_bytes;
-            const UT* uu = ubuf(par);
+        };
+        uint32_t ch = grp, jc = 0, chn = grp, jn = 0;
+        advance(chn, jn);
+        uint32_t i = ch * E, inext = chn * E + jn;
+        if (gatherer && i < cnt) {
+            dof_c = map_at(i);
             if (rvalid) {
-                if constexpr (A::kSym && NT != 0) {
-                    // the column group's terms, with compile-time bounds
-                    constexpr int GR = (NT + 31) / 32;
-                    constexpr int GC = (int)wpg_gc(GR, sizeof(UT));
-                    const UT* ur = uu + r;
-                    const uint32_t pl = a.plane;
-                    if constexpr (GC == 1) {
-                        sym_terms<A, NT, 0, NT>(acc, ks, pl, ur, r);
-                    } else if constexpr (GC == 2) {
-                        if (cg == 0)
-                            sym_terms<A, NT, 0, NT / 2>(acc, ks, pl, ur, r);
-                        else
-                            sym_terms<A, NT, NT / 2, NT>(acc, ks, pl, ur, r);
-                    } else {
-                        switch (cg) {
-                            case 0: sym_terms<A, NT, 0, NT / 4>(acc, ks, pl, ur, r); break;
-                            case 1: sym_terms<A, NT, NT / 4, 2 * NT / 4>(acc, ks, pl, ur, r); break;
-                            case 2: sym_terms<A, NT, 2 * NT / 4, 3 * NT / 4>(acc, ks, pl, ur, r); break;
-                            default: sym_terms<A, NT, 3 * NT / 4, NT>(acc, ks, pl, ur, r); break;
-                        }
-                    }
-                } else if constexpr (A::kSym) {
-                    // run-time n: term t <= n/2: D[t][r] u[r + t]; term t > n/2, d = t - n/2:
-                    // K(r, r - d) = D[d][(r - d) mod n] times u[r - d + n]
-                    constexpr uint32_t NS = kMaxN;
-                    constexpr uint32_t GR = (NS + 31) / 32;
-                    constexpr uint32_t GC = wpg_gc(GR, sizeof(UT));
-                    constexpr uint32_t TRIP = (NS + GC - 1) / GC;
-                    const uint32_t h = n / 2;
-#pragma unroll 4
-                    for (uint32_t j = 0; j < TRIP; j++) {
-                        const uint32_t t = cb + j;
-                        if (t < ce) {
-                            uint32_t col, k;
-                            if (t <= h) {
-                                col = r + t;
-                                k = t * n + r;
-                            } else {
-                                const uint32_t d = t - h;
-                                col = r + n - d;
-                                k = d * n + (r >= d ? r - d : r + n - d);
-                            }
-                            A::fma(acc, A::kload(ks, k, a.plane), uu[col]);
-                        }
-                    }
-                } else if constexpr (NT != 0) {
-                    constexpr uint32_t GR = (NT + 31) / 32;
-                    constexpr uint32_t GC = wpg_gc(GR, sizeof(UT));
-                    constexpr uint32_t TRIP = (NT + GC - 1) / GC;
-#pragma unroll
-                    for (uint32_t j = 0; j < TRIP; j++) {
-                        const uint32_t c = cb + j;
-                        if (c < ce) A::fma(acc, A::kload(ks, (size_t)c * NT + r, a.plane), uu[c]);
-                    }
-                } else {
-#pragma unroll 4
-                    for (uint32_t c = cb; c < ce; c++) A::fma(acc, A::kload(ks, (size_t)c * n + r, a.plane), uu[c]);
-                }
+                const UT x = stage_s<A>(load_u_hint(u, dof_c, a.bc_mode, keep), usk);
+                ubuf(0)[r] = x;
+                if constexpr (A::kSym) ubuf(0)[r + n] = x;
             }
-            __syncwarp();
-            // the chunk's last element (a CTA's last chunk may be short) releases the slot
-            if (lane == 0 && (jc + 1 == E || i + 1 == cnt)) mbar_arrive(&empty[s]);
+            if (inext < cnt) dof_n = map_at(inext);
         }
-        if (!gatherer && rvalid) pbuf(par)[(cg - 1) * n + r] = acc;
-        if (gatherer && rvalid && inext < cnt) {
-            const UT x = stage_s<A>(u_n, usk);
-            ubuf(par ^ 1)[r] = x;
-            if constexpr (A::kSym) ubuf(par ^ 1)[r + n] = x;
-        }
+        if (!FU || col == 0)
+            wait_prior_grid();
+        else  // every CTA has written the previous colour's sums to v
+            grid_barrier(T->gbar + (col - 1), consumer_threads, abort, a.wait_ns);
+        if (gatherer && i < cnt && rvalid) vold_c = v_load(v + (dof_c & kDofMask));
         group_sync(bar_id, bar_threads);
-        if (gatherer) {
-            for (uint32_t c2 = 1; c2 < G.gc; c2++) {
-                if (rvalid) A::combine(acc, pbuf(par)[(c2 - 1) * n + r]);
+        bool ok = false;  // the current chunk's slot has landed (one verdict per warp and chunk)
+        uint32_t s = 0;   // the current chunk's ring slot
+        for (uint32_t k = 0; i < cnt; k++) {
+            const uint32_t par = k & 1;
+            uint32_t chnn = chn, jnn = jn;
+            advance(chnn, jnn);
+            const uint32_t inn = chnn * E + jnn;
+            if (gatherer && rvalid) {
+                if (inext < cnt) {
+                    u_n = load_u_hint(u, dof_n, a.bc_mode, keep);
+                    vold_n = v_load(v + (dof_n & kDofMask));
+                }
+                if (inn < cnt) dof_nn = map_at(inn);
             }
-            if (rvalid && !*abort) st_hint(v + (dof_c & kDofMask), vold_c + finish_s<A>(acc, usk), keep);
-            dof_c = dof_n;
-            vold_c = vold_n;
-            dof_n = dof_nn;
+            Acc acc = A::zero();
+            // one verdict per warp and chunk: the block below synchronises the warp, so no lane may skip it alone
+            if (jc == 0) {
+                const uint32_t g = gbase + ch;
+                s = g % S;
+                ok = __all_sync(0xffffffffu, ring_wait(&full[s], &tag[s], g, (g / S) & 1, abort, a.wait_ns));
+            }
+            if (ok) {
+                const unsigned char* ks = smem + (size_t)s * L.slot_bytes + (size_t)jc * a.unit_bytes;
+                const UT* uu = ubuf(par);
+                if (rvalid) {
+                    if constexpr (A::kSym && NT != 0) {
+                        // the column group's terms, with compile-time bounds
+                        constexpr int GR = (NT + 31) / 32;
+                        constexpr int GC = (int)wpg_gc(GR, sizeof(UT));
+                        const UT* ur = uu + r;
+                        const uint32_t pl = a.plane;
+                        if constexpr (GC == 1) {
+                            sym_terms<A, NT, 0, NT>(acc, ks, pl, ur, r);
+                        } else if constexpr (GC == 2) {
+                            if (cg == 0)
+                                sym_terms<A, NT, 0, NT / 2>(acc, ks, pl, ur, r);
+                            else
+                                sym_terms<A, NT, NT / 2, NT>(acc, ks, pl, ur, r);
+                        } else {
+                            switch (cg) {
+                                case 0: sym_terms<A, NT, 0, NT / 4>(acc, ks, pl, ur, r); break;
+                                case 1: sym_terms<A, NT, NT / 4, 2 * NT / 4>(acc, ks, pl, ur, r); break;
+                                case 2: sym_terms<A, NT, 2 * NT / 4, 3 * NT / 4>(acc, ks, pl, ur, r); break;
+                                default: sym_terms<A, NT, 3 * NT / 4, NT>(acc, ks, pl, ur, r); break;
+                            }
+                        }
+                    } else if constexpr (A::kSym) {
+                        // run-time n: term t <= n/2: D[t][r] u[r + t]; term t > n/2, d = t - n/2:
+                        // K(r, r - d) = D[d][(r - d) mod n] times u[r - d + n]
+                        constexpr uint32_t NS = kMaxN;
+                        constexpr uint32_t GR = (NS + 31) / 32;
+                        constexpr uint32_t GC = wpg_gc(GR, sizeof(UT));
+                        constexpr uint32_t TRIP = (NS + GC - 1) / GC;
+                        const uint32_t h = n / 2;
+    #pragma unroll 4
+                        for (uint32_t j = 0; j < TRIP; j++) {
+                            const uint32_t t = cb + j;
+                            if (t < ce) {
+                                uint32_t col, k;
+                                if (t <= h) {
+                                    col = r + t;
+                                    k = t * n + r;
+                                } else {
+                                    const uint32_t d = t - h;
+                                    col = r + n - d;
+                                    k = d * n + (r >= d ? r - d : r + n - d);
+                                }
+                                A::fma(acc, A::kload(ks, k, a.plane), uu[col]);
+                            }
+                        }
+                    } else if constexpr (NT != 0) {
+                        constexpr uint32_t GR = (NT + 31) / 32;
+                        constexpr uint32_t GC = wpg_gc(GR, sizeof(UT));
+                        constexpr uint32_t TRIP = (NT + GC - 1) / GC;
+    #pragma unroll
+                        for (uint32_t j = 0; j < TRIP; j++) {
+                            const uint32_t c = cb + j;
+                            if (c < ce) A::fma(acc, A::kload(ks, (size_t)c * NT + r, a.plane), uu[c]);
+                        }
+                    } else {
+    #pragma unroll 4
+                        for (uint32_t c = cb; c < ce; c++) A::fma(acc, A::kload(ks, (size_t)c * n + r, a.plane), uu[c]);
+                    }
+                }
+                __syncwarp();
+                // the chunk's last element (a CTA's last chunk may be short) releases the slot
+                if (lane == 0 && (jc + 1 == E || i + 1 == cnt)) mbar_arrive(&empty[s]);
+            }
+            if (!gatherer && rvalid) pbuf(par)[(cg - 1) * n + r] = acc;
+            if (gatherer && rvalid && inext < cnt) {
+                const UT x = stage_s<A>(u_n, usk);
+                ubuf(par ^ 1)[r] = x;
+                if constexpr (A::kSym) ubuf(par ^ 1)[r + n] = x;
+            }
+            group_sync(bar_id, bar_threads);
+            if (gatherer) {
+                for (uint32_t c2 = 1; c2 < G.gc; c2++) {
+                    if (rvalid) A::combine(acc, pbuf(par)[(c2 - 1) * n + r]);
+                }
+                if (rvalid && !*abort) st_hint(v + (dof_c & kDofMask), vold_c + finish_s<A>(acc, usk), keep);
+                dof_c = dof_n;
+                vold_c = vold_n;
+                dof_n = dof_nn;
+            }
+            ch = chn;
+            jc = jn;
+            i = inext;
+            chn = chnn;
+            jn = jnn;
+            inext = inn;
         }
-        ch = chn;
-        jc = jn;
-        i = inext;
-        chn = chnn;
-        jn = jnn;
-        inext = inn;
+        gbase += (cnt + E - 1) / E;
     }
-    gbase += (cnt + E - 1) / E;
-    }  // colours
     if (lane == 0 && *abort) atomicOr(a.err, kErrTimeout);
 }
 
