@@ -50,3 +50,18 @@ def test_create_validates_arguments():
     h = C.c_void_p()
     assert lib.afm_create(None, 0, 0) == 105
     assert lib.afm_create(C.byref(h), 7, 0) == 10  # UNKNOWN_BC_METH
+
+
+def test_server_calls_reject_null_handles():
+    """The serving calls check their handle before touching a device."""
+    lib = _native.libafm()
+    info = (C.c_uint64 * 6)()
+    assert lib.afm_server_set_lane(None, 1 << 20, 32) == 105
+    assert lib.afm_server_set_inner_format(None, 4) == 105
+    assert lib.afm_server_set_priorities(None, 1) == 105
+    assert lib.afm_server_get_info(None, info) == 105
+    assert lib.afm_server_poll(None, None, None) == 105
+    assert lib.afm_server_destroy(None) == 0
+    assert lib.afm_server_create(None, 0, 0, 0) == 105
+    assert lib.afm_set_fused_colours(None, 1) == 105
+    assert lib.afm_matvec_inner_device(None, None, None, None) == 105
